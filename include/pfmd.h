@@ -1,0 +1,156 @@
+/* pfmd.h -- C ABI of the GB300 (sm_103a) implementation of PFMDS's MD
+ * force-and-integration hot path.
+ *
+ * PFMDS (Fortran 90 + OpenMP) has no plugin or FFI layer: its hot path is the
+ * body of md() in code_source/MOLECULAR_DYNAMICS/md_simulation.f90, reached from
+ * the run_md_simulation command line.  Each entry point below names the reference
+ * subroutine or program it replaces; a Fortran md() calls them through the
+ * ISO_C_BINDING interface module shown in INTEGRATION.md, a C or C++ host calls
+ * them directly, and run_md_simulation (built from this library) is the drop-in
+ * executable.
+ *
+ * Conventions: plain C types only.  Per-atom arrays are xyz-interleaved doubles
+ * (3*N), i.e. the Fortran (3,N) column-major layout of particles%positions.
+ * Neighbour-list and atom indexes are 0-based.  Every call returns PFMD_OK (0) or
+ * one of the PFMD_E_* codes and keeps a message for pfmd_errmsg().  The caller owns
+ * every host array; the library copies in and out and keeps no host pointer after
+ * a call returns.  The library owns its device buffers and one CUDA stream.  One
+ * host thread per context.
+ */
+#ifndef PFMD_H
+#define PFMD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PFMD_OK 0
+#define PFMD_E_NLIST_OVERFLOW 1 /* 'error: too many neighbours' (md_neighbours.f90:80,151) */
+#define PFMD_E_OUT_OF_CELL 2    /* 'particle out of cell' (md_general.f90:342-364) */
+#define PFMD_E_GR_NN 3          /* graphene nearest neighbours != 3 (graphenenorm.f90:26,30) */
+#define PFMD_E_PARAM 4          /* bad settings / parameters ('wrong nhc parameters', ...) */
+#define PFMD_E_CUDA 5           /* CUDA runtime error, or the library built without a device */
+#define PFMD_E_TIMEOUT 6        /* a bounded device wait gave up */
+#define PFMD_E_IO 7             /* unreadable or malformed input file, unwritable output */
+#define PFMD_E_STATE 8          /* call not valid in the context's current state */
+
+/* ---- arithmetic forms -------------------------------------------------- */
+#define PFMD_FORM_PLAIN 0     /* FP64 throughout, as the reference (-fdefault-real-8) */
+#define PFMD_FORM_PRECISION 1 /* FP32 forces with compensated per-atom sums; FP64
+                                 positions, velocities, Nose-Hoover chain, energies */
+
+typedef struct pfmd_ctx pfmd_ctx;
+
+typedef struct pfmd_options {
+  int form;                  /* PFMD_FORM_* */
+  int rand_seed;             /* md()'s rand_seed; run_md_simulation passes 1 */
+  int out_period;            /* -op: period of the output-unit block (default 1) */
+  int out_fd;                /* output unit as a POSIX file descriptor, -1 = none */
+  int all_out_fd;            /* unit for the closing all_out record, -1 = out_fd */
+  int write_files;           /* log, snapshot_*.xyz, traj_*.xyz, final_* files */
+  const char* output_prefix; /* -p / list prefix, prepended to every output file */
+  int num_threads;           /* echoed in 'RUNNING ON n OPENMP THREADS' */
+  int device;                /* CUDA device ordinal */
+  int use_graphs;            /* capture repeated step segments in CUDA graphs */
+} pfmd_options;
+
+/* Defaults of run_md_simulation.f90:10-24 (out_period 1, seed 1, no prefix),
+ * plain form, device 0, graphs on. */
+void pfmd_default_options(pfmd_options* opt);
+
+/* ---- set-up and teardown ----------------------------------------------- */
+
+/* md() set-up, md_simulation.f90:44-113: reads the fixed-order settings file
+ * input_path+settings_filename, the .xyz file and parameter files it names
+ * (read_box_size/read_particles md_read_write.f90:22-61, create_groups and
+ * create_interactions md_interactions.f90:38-136, set_nose_hoover_chain
+ * md_integrators.f90:182, set_new_temperature md_general.f90:328), echoes what md()
+ * echoes to the output unit, and uploads the system to the device. */
+int pfmd_create_from_files(const char* input_path, const char* settings_filename,
+                           const pfmd_options* opt, pfmd_ctx** ctx);
+
+/* Releases the device buffers, stream and graphs (md() returning). */
+void pfmd_destroy(pfmd_ctx* ctx);
+
+/* Message of the last failing call on ctx (the reference's stop message). */
+const char* pfmd_errmsg(const pfmd_ctx* ctx);
+/* Name of a status code, e.g. "PFMD_E_NLIST_OVERFLOW". */
+const char* pfmd_strerror(int code);
+
+/* ---- the step loop ----------------------------------------------------- */
+
+/* Runs up to max_steps passes of md()'s loop body (md_simulation.f90:116-241:
+ * group changes, integrator switches, check_positions, Nose-Hoover chain,
+ * velocity-Verlet, neighbour lists, forces, molecular statics, energies, log /
+ * output block / snapshot / trajectory) on the device.  Host work happens only at
+ * output events.  *finished is set to 1 once the loop has exited (md_step_limit
+ * passed, no more integrators, or nvms converged). */
+int pfmd_advance(pfmd_ctx* ctx, long long max_steps, int* finished);
+
+/* The lines after the loop, md_simulation.f90:245-272: 'steps number', the
+ * PERFOMANCE block, the all_out and final log records and final_<xyz>. */
+int pfmd_finish(pfmd_ctx* ctx);
+
+/* Whole md() call (md_simulation.f90:19): create, advance to the end, finish,
+ * destroy. */
+int pfmd_md(const char* input_path, const char* settings_filename, const pfmd_options* opt);
+
+/* The run_md_simulation program (runners/run_md_simulation.f90:1-77): options
+ * -i -p -op -omp_n -ipath -ilist -opath -ofile, plus -form plain|precision. */
+int pfmd_run_md_simulation(int argc, const char* const* argv);
+
+/* ---- state access -------------------------------------------------------- */
+
+int pfmd_natoms(const pfmd_ctx* ctx, int* n);
+/* The md_step the loop will run next, and dt%simulation_time. */
+int pfmd_md_step(const pfmd_ctx* ctx, long long* md_step, double* simulation_time);
+
+/* particles%positions / velocities / forces (md_general.f90:11-16); any pointer
+ * may be NULL. */
+int pfmd_get_state(pfmd_ctx* ctx, double* pos, double* vel, double* frc);
+/* Overwrites positions and/or velocities (NULL leaves them); the next step checks
+ * the positions as check_positions does. */
+int pfmd_set_state(pfmd_ctx* ctx, const double* pos, const double* vel);
+
+/* Energies of the last energy step: interactions%energy (one per interaction),
+ * potential, kinetic, temperature, Nose-Hoover chain sum, conserved
+ * (md_simulation.f90:190-201).  Any pointer may be NULL. */
+int pfmd_energies(pfmd_ctx* ctx, double* e_inter, double* pe, double* ke, double* temperature,
+                  double* e_nhc, double* e_conserved);
+
+/* update_interactions_neighbour_lists + zero_forces + calculate_forces +
+ * calculate_potential_energies (md_interactions.f90:138,210,263; md_integrators.f90:147)
+ * outside the step loop, with every list rebuilt (rebuild=1) or only refreshed
+ * (rebuild=0).  e_inter may be NULL. */
+int pfmd_compute(pfmd_ctx* ctx, int rebuild, double* e_inter);
+
+/* Number of interactions and the shape of list `list` of interaction `inter`
+ * (interactions(i)%nl(j), md_interactions.f90:26-34). */
+int pfmd_ninteractions(const pfmd_ctx* ctx, int* n);
+int pfmd_nlist_shape(const pfmd_ctx* ctx, int inter, int list, int* n_rows, int* nmax);
+/* The list arrays as the reference holds them (md_general.f90:34-39): nnum,
+ * lessnnum, particle_index and nlist[row*nmax+slot] (group-2 indexes, ascending
+ * within a row).  Any pointer may be NULL. */
+int pfmd_get_nlist(pfmd_ctx* ctx, int inter, int list, int* nnum, int* lessnnum, int* pidx,
+                   int* nlist);
+/* Largest neighbour count of every list, in nlists_load order
+ * (md_interactions.f90:427-444); maxnnum holds one int per list. */
+int pfmd_nlist_load(pfmd_ctx* ctx, int* maxnnum, int* count);
+/* gr_norm of an ljc / morsec interaction (graphenenorm.f90:38-56), 3 per row. */
+int pfmd_get_gr_norm(pfmd_ctx* ctx, int inter, double* norm);
+
+/* change_particle_group_N's effect (md_general.f90:82-95): sets the current size
+ * of group `group` (1-based) to n, clamped to the group's capacity. */
+int pfmd_set_group_n(pfmd_ctx* ctx, int group, int n);
+
+/* The CUDA stream every kernel of ctx is launched on (a cudaStream_t). */
+int pfmd_get_stream(pfmd_ctx* ctx, void** stream);
+/* Number of kernels the library has launched on ctx so far (graph nodes count
+ * once per replay). */
+int pfmd_kernel_launches(const pfmd_ctx* ctx, long long* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFMD_H */

@@ -1,0 +1,258 @@
+"""GB300 (sm_103a) implementation of PFMDS's MD force-and-integration hot path.
+
+The compute path is the CUDA library built in-tree (pfmds_gb300/_build/libpfmd.so,
+C ABI declared in include/pfmd.h).  This module is a thin ctypes mirror of that
+ABI, named after the reference's md() and run_md_simulation: it loads the library
+and fails loudly when it is missing; there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpfmd.so")
+EXE_PATH = os.path.join(HERE, "_build", "run_md_simulation")
+
+PFMD_OK = 0
+PFMD_E_NLIST_OVERFLOW = 1
+PFMD_E_OUT_OF_CELL = 2
+PFMD_E_GR_NN = 3
+PFMD_E_PARAM = 4
+PFMD_E_CUDA = 5
+PFMD_E_TIMEOUT = 6
+PFMD_E_IO = 7
+PFMD_E_STATE = 8
+FORMS = {"plain": 0, "precision": 1}
+
+# every entry point include/pfmd.h declares
+EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pfmd_errmsg", "pfmd_strerror",
+           "pfmd_advance", "pfmd_finish", "pfmd_md", "pfmd_run_md_simulation", "pfmd_natoms", "pfmd_md_step",
+           "pfmd_get_state", "pfmd_set_state", "pfmd_energies", "pfmd_compute", "pfmd_ninteractions",
+           "pfmd_nlist_shape", "pfmd_get_nlist", "pfmd_nlist_load", "pfmd_get_gr_norm", "pfmd_set_group_n",
+           "pfmd_get_stream", "pfmd_kernel_launches")
+
+_LIB = None
+
+
+class PfmdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{strerror(code)}: {msg}")
+        self.code = code
+
+
+class Options(C.Structure):
+    _fields_ = [("form", C.c_int), ("rand_seed", C.c_int), ("out_period", C.c_int), ("out_fd", C.c_int),
+                ("all_out_fd", C.c_int), ("write_files", C.c_int), ("output_prefix", C.c_char_p),
+                ("num_threads", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int)]
+
+
+def load(path=LIB_PATH):
+    """Loads libpfmd.so (build it with pfmds_gb300._build.build() or __graft_entry__.build())."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise ImportError(f"pfmds_gb300: CUDA library {path} is missing; run pfmds_gb300._build.build()")
+    L = C.CDLL(path)
+    vp, ip, dp, llp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_longlong)
+    L.pfmd_default_options.argtypes = [C.POINTER(Options)]
+    L.pfmd_default_options.restype = None
+    L.pfmd_create_from_files.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(Options), C.POINTER(vp)]
+    L.pfmd_destroy.argtypes = [vp]
+    L.pfmd_destroy.restype = None
+    L.pfmd_errmsg.argtypes = [vp]
+    L.pfmd_errmsg.restype = C.c_char_p
+    L.pfmd_strerror.argtypes = [C.c_int]
+    L.pfmd_strerror.restype = C.c_char_p
+    L.pfmd_advance.argtypes = [vp, C.c_longlong, ip]
+    L.pfmd_finish.argtypes = [vp]
+    L.pfmd_md.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(Options)]
+    L.pfmd_run_md_simulation.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    L.pfmd_natoms.argtypes = [vp, ip]
+    L.pfmd_md_step.argtypes = [vp, llp, dp]
+    L.pfmd_get_state.argtypes = [vp, dp, dp, dp]
+    L.pfmd_set_state.argtypes = [vp, dp, dp]
+    L.pfmd_energies.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+    L.pfmd_compute.argtypes = [vp, C.c_int, dp]
+    L.pfmd_ninteractions.argtypes = [vp, ip]
+    L.pfmd_nlist_shape.argtypes = [vp, C.c_int, C.c_int, ip, ip]
+    L.pfmd_get_nlist.argtypes = [vp, C.c_int, C.c_int, ip, ip, ip, ip]
+    L.pfmd_nlist_load.argtypes = [vp, ip, ip]
+    L.pfmd_get_gr_norm.argtypes = [vp, C.c_int, dp]
+    L.pfmd_set_group_n.argtypes = [vp, C.c_int, C.c_int]
+    L.pfmd_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.pfmd_kernel_launches.argtypes = [vp, llp]
+    _LIB = L
+    return L
+
+
+def strerror(code):
+    try:
+        return load().pfmd_strerror(code).decode()
+    except ImportError:
+        return str(code)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def default_options(**kw):
+    o = Options()
+    load().pfmd_default_options(C.byref(o))
+    for k, v in kw.items():
+        if k == "form" and isinstance(v, str):
+            v = FORMS[v]
+        if k == "output_prefix" and isinstance(v, str):
+            v = v.encode()
+        setattr(o, k, v)
+    return o
+
+
+class Simulation:
+    """One md() run on the GPU (md_simulation.f90:19): set-up on construction,
+    then advance() through the loop body and finish() for the closing output."""
+
+    def __init__(self, input_path, settings="md_run_settings.txt", form="plain", out_period=1, write_files=False,
+                 prefix="", use_graphs=True, out_fd=-1, all_out_fd=-1, seed=1, num_threads=1, device=0):
+        L = load()
+        self._prefix = prefix.encode()
+        self.opts = default_options(form=form, out_period=out_period, write_files=1 if write_files else 0,
+                                    output_prefix=self._prefix, use_graphs=1 if use_graphs else 0, out_fd=out_fd,
+                                    all_out_fd=all_out_fd, rand_seed=seed, num_threads=num_threads, device=device)
+        self._h = C.c_void_p()
+        ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
+        rc = L.pfmd_create_from_files(ip.encode(), settings.encode(), C.byref(self.opts), C.byref(self._h))
+        if rc:
+            msg = L.pfmd_errmsg(self._h).decode()
+            L.pfmd_destroy(self._h)
+            self._h = None
+            raise PfmdError(rc, msg)
+        self.finished = False
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pfmd_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def _check(self, rc):
+        if rc:
+            raise PfmdError(rc, load().pfmd_errmsg(self._h).decode())
+
+    def advance(self, n):
+        f = C.c_int(0)
+        self._check(load().pfmd_advance(self._h, int(n), C.byref(f)))
+        self.finished = bool(f.value)
+        return self.finished
+
+    def finish(self):
+        self._check(load().pfmd_finish(self._h))
+
+    @property
+    def natoms(self):
+        n = C.c_int()
+        self._check(load().pfmd_natoms(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def md_step(self):
+        s, t = C.c_longlong(), C.c_double()
+        self._check(load().pfmd_md_step(self._h, C.byref(s), C.byref(t)))
+        return s.value
+
+    @property
+    def sim_time(self):
+        s, t = C.c_longlong(), C.c_double()
+        self._check(load().pfmd_md_step(self._h, C.byref(s), C.byref(t)))
+        return t.value
+
+    def state(self):
+        n = self.natoms
+        p, v, f = (np.zeros((n, 3)) for _ in range(3))
+        self._check(load().pfmd_get_state(self._h, _dp(p), _dp(v), _dp(f)))
+        return p, v, f
+
+    def set_state(self, pos=None, vel=None):
+        p = None if pos is None else np.ascontiguousarray(pos, dtype=np.float64)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
+        self._check(load().pfmd_set_state(self._h, None if p is None else _dp(p), None if v is None else _dp(v)))
+
+    @property
+    def n_interactions(self):
+        n = C.c_int()
+        self._check(load().pfmd_ninteractions(self._h, C.byref(n)))
+        return n.value
+
+    def energies(self):
+        e = np.zeros(max(1, self.n_interactions))
+        vals = [C.c_double() for _ in range(5)]
+        self._check(load().pfmd_energies(self._h, _dp(e), *[C.byref(v) for v in vals]))
+        pe, ke, t, enhc, econs = (v.value for v in vals)
+        return dict(inter=e[:self.n_interactions].copy(), pe=pe, ke=ke, temperature=t, nhc=enhc, conserved=econs)
+
+    def compute(self, rebuild=True):
+        e = np.zeros(max(1, self.n_interactions))
+        self._check(load().pfmd_compute(self._h, 1 if rebuild else 0, _dp(e)))
+        return e[:self.n_interactions].copy()
+
+    def nlist(self, inter, lst):
+        n, m = C.c_int(), C.c_int()
+        self._check(load().pfmd_nlist_shape(self._h, inter, lst, C.byref(n), C.byref(m)))
+        n, m = n.value, m.value
+        nnum = np.zeros(n, np.int32)
+        less = np.zeros(n, np.int32)
+        pidx = np.zeros(n, np.int32)
+        nl = np.zeros((n, m), np.int32)
+        self._check(load().pfmd_get_nlist(self._h, inter, lst, _ip(nnum), _ip(less), _ip(pidx), _ip(nl)))
+        return dict(nnum=nnum, lessnnum=less, pidx=pidx, nlist=nl)
+
+    def gr_norm(self, inter):
+        n, m = C.c_int(), C.c_int()
+        self._check(load().pfmd_nlist_shape(self._h, inter, 2, C.byref(n), C.byref(m)))
+        g = np.zeros((n.value, 3))
+        self._check(load().pfmd_get_gr_norm(self._h, inter, _dp(g)))
+        return g
+
+    def nlist_load(self):
+        buf = np.zeros(64, np.int32)
+        cnt = C.c_int()
+        self._check(load().pfmd_nlist_load(self._h, _ip(buf), C.byref(cnt)))
+        return buf[:cnt.value].copy()
+
+    def set_group_n(self, group, n):
+        self._check(load().pfmd_set_group_n(self._h, group, n))
+
+    @property
+    def stream(self):
+        s = C.c_void_p()
+        self._check(load().pfmd_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    @property
+    def kernel_launches(self):
+        n = C.c_longlong()
+        self._check(load().pfmd_kernel_launches(self._h, C.byref(n)))
+        return n.value
+
+
+def md(input_path, settings="md_run_settings.txt", **kw):
+    """The whole md() call (create, advance to the end, finish)."""
+    L = load()
+    prefix = kw.pop("prefix", "")
+    o = default_options(output_prefix=prefix.encode(), **kw)
+    ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
+    return L.pfmd_md(ip.encode(), settings.encode(), C.byref(o))
+
+
+def run_md_simulation(args):
+    """The run_md_simulation command line, in-process."""
+    L = load()
+    argv = (C.c_char_p * (len(args) + 1))(*([b"run_md_simulation"] + [a.encode() for a in args]))
+    return L.pfmd_run_md_simulation(len(args) + 1, argv)

@@ -1,0 +1,292 @@
+// Device-side building blocks shared by the PFMDS kernels (sm_103a).
+//
+// * Box / minimum image: find_distance of md_general.f90:423-441 in two forms.
+//   mi_exact evaluates the reference expression with round-to-nearest intrinsics
+//   (no FMA contraction), so d r^2 and the list predicate `dr2 < r_cut*r_cut`
+//   (md_neighbours.f90:77) come out bit for bit as in an uncontracted FP64 build.
+//   mi_f32 is the same formula in FP32 for the precision form.
+// * Cut-off switches of cut_off_function.f90 (cosine, truncated pi) and
+//   cut_off_poly.f90 (quintic, f_dfr_cut with its missing 1/(R2-R1)).
+// * Ctl: the device-resident control block (status, step counter, energies,
+//   reduction scratch) that lets a whole step sequence run without the host.
+// * Deterministic grid reductions: per-block partials, the last block to finish
+//   sums them in block order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#ifndef PFMD_MAX_INTER
+#define PFMD_MAX_INTER 16
+#endif
+#define PFMD_MAX_LISTS (3 * PFMD_MAX_INTER)
+#define PFMD_MAX_GROUPS 64
+#define PFMD_MAX_NHC 8
+#define PFMD_MAX_CHAIN 16
+#define PFMD_RED_SLOTS 32
+#define PFMD_PARTIALS (1 << 16)
+
+namespace pfmd {
+
+// status codes (include/pfmd.h)
+enum : int {
+  ST_OK = 0,
+  ST_NLIST_OVERFLOW = 1,
+  ST_OUT_OF_CELL = 2,
+  ST_GR_NN = 3,
+  ST_PARAM = 4,
+  ST_CUDA = 5,
+  ST_TIMEOUT = 6
+};
+
+// Error detail kinds recorded next to the status code.
+enum : int {
+  EK_NONE = 0,
+  EK_OVERFLOW = 1,      // info: list id, row (1-based), count
+  EK_OOB = 2,           // info: atom (1-based)
+  EK_GR_TOO_MANY = 3,   // info: row (1-based)
+  EK_GR_NOT_ENOUGH = 4, // info: row (1-based)
+  EK_L1 = 5,            // 'l1>3'
+  EK_CONVERSE_OVF = 6,  // info: list id, row (1-based), count
+  EK_NMAX_CAP = 7       // nmax above the build kernel's capacity
+};
+
+struct NHCDev {
+  int M, L;
+  double T, s, e;
+  double x[PFMD_MAX_CHAIN], v[PFMD_MAX_CHAIN], q[PFMD_MAX_CHAIN];
+};
+
+// Control block in device memory.  The host reads it back after a segment.
+struct Ctl {
+  // status: `stop` is non-zero once an error or the nvms exit happened; every
+  // kernel returns immediately when it is set.
+  int stop;
+  int error;
+  int err_kind;
+  int err_info[3];
+  long long err_step;
+  int pending_oob;  // an atom left the cell in the last drift; checked at step start
+  int oob_atom;     // smallest offending atom (0-based) of the pending check
+  int converged;    // nvms exit
+  int pad0;
+  long long md_step;  // the step being executed
+  // energies
+  double pe_last, pe_prev;
+  double e_inter[PFMD_MAX_INTER];
+  double ke, temperature, e_nhc, total, conserved;
+  // group sizes (device resident so captured graphs survive group changes)
+  int group_n[PFMD_MAX_GROUPS];
+  // Nose-Hoover chains
+  NHCDev nhc[PFMD_MAX_NHC];
+  // small reduction results
+  double red[PFMD_RED_SLOTS];
+  int maxnnum[PFMD_MAX_LISTS];
+  unsigned int counter[PFMD_RED_SLOTS];
+  double partial[PFMD_PARTIALS];  // per-block partial sums of the grid reductions
+};
+
+struct Box {
+  double L[3], h[3];
+  float Lf[3], hf[3];
+};
+
+// ---------------------------------------------------------------------------
+// minimum image
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double sgn1(double x) { return copysign(1.0, x); }
+__device__ __forceinline__ float sgn1f(float x) { return copysignf(1.0f, x); }
+
+// d - h*(sign(1,d-h)+sign(1,d+h)), rounded exactly as written.
+__device__ __forceinline__ double mi_axis_exact(double d, double h) {
+  double s = __dadd_rn(sgn1(__dsub_rn(d, h)), sgn1(__dadd_rn(d, h)));
+  return __dsub_rn(d, __dmul_rn(h, s));
+}
+// dr = b - a with the minimum image; returns dr.dr evaluated as
+// (dx*dx + dy*dy) + dz*dz without contraction.
+__device__ __forceinline__ double mi_exact(const double4_32a& a, const double4_32a& b, const Box& B, double dr[3]) {
+  dr[0] = mi_axis_exact(__dsub_rn(b.x, a.x), B.h[0]);
+  dr[1] = mi_axis_exact(__dsub_rn(b.y, a.y), B.h[1]);
+  dr[2] = mi_axis_exact(__dsub_rn(b.z, a.z), B.h[2]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dr[0], dr[0]), __dmul_rn(dr[1], dr[1])), __dmul_rn(dr[2], dr[2]));
+}
+__device__ __forceinline__ float mi_axis_f(float d, float h) {
+  float s = sgn1f(d - h) + sgn1f(d + h);
+  return d - h * s;
+}
+__device__ __forceinline__ float mi_f32(const float4& a, const float4& b, const Box& B, float dr[3]) {
+  dr[0] = mi_axis_f(b.x - a.x, B.hf[0]);
+  dr[1] = mi_axis_f(b.y - a.y, B.hf[1]);
+  dr[2] = mi_axis_f(b.z - a.z, B.hf[2]);
+  return dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+}
+
+// ---------------------------------------------------------------------------
+// cut-off switches
+// ---------------------------------------------------------------------------
+#define PFMD_PI_TRUNC 3.14159265358979
+
+// cut_off_function.f90:6-16
+__device__ __forceinline__ double fcut_cos(double r, double R1, double R2) {
+  if (r < R1) return 1.0;
+  if (r < R2) return (1.0 + cos(PFMD_PI_TRUNC * (r - R1) / (R2 - R1))) * 0.5;
+  return 0.0;
+}
+// cut_off_function.f90:18-28 (returns f'/r)
+__device__ __forceinline__ double dfcut_cos(double r, double R1, double R2) {
+  if (r < R1) return 0.0;
+  if (r < R2) return -sin(PFMD_PI_TRUNC * (r - R1) / (R2 - R1)) * PFMD_PI_TRUNC / (R2 - R1) / r * 0.5;
+  return 0.0;
+}
+// both at once: fc and f'/r
+__device__ __forceinline__ void fdfcut_cos(double r, double R1, double R2, double& f, double& df) {
+  if (r < R1) {
+    f = 1.0;
+    df = 0.0;
+  } else if (r < R2) {
+    double s, c;
+    sincos(PFMD_PI_TRUNC * (r - R1) / (R2 - R1), &s, &c);
+    f = (1.0 + c) * 0.5;
+    df = -s * PFMD_PI_TRUNC / (R2 - R1) / r * 0.5;
+  } else {
+    f = 0.0;
+    df = 0.0;
+  }
+}
+__device__ __forceinline__ void fdfcut_cos_f(float r, float R1, float R2, float inv_w, float& f, float& df) {
+  if (r < R1) {
+    f = 1.0f;
+    df = 0.0f;
+  } else if (r < R2) {
+    float s, c;
+    __sincosf(3.14159265358979f * (r - R1) * inv_w, &s, &c);
+    f = (1.0f + c) * 0.5f;
+    df = -s * 3.14159265358979f * inv_w / r * 0.5f;
+  } else {
+    f = 0.0f;
+    df = 0.0f;
+  }
+}
+// cut_off_poly.f90:6-17
+__device__ __forceinline__ double fcut_poly(double r, double R1, double R2) {
+  if (r > R1 && r < R2) {
+    double a = r - R1, w = R2 - R1;
+    double a3 = a * a * a, w2 = w * w;
+    return 1.0 + (-10.0 * a3 * w2 + 15.0 * (a3 * a) * w - 6.0 * (a3 * a * a)) / (w2 * w2 * w);
+  }
+  if (r <= R1) return 1.0;
+  return 0.0;
+}
+// cut_off_poly.f90:30-43 (dfr lacks 1/(R2-R1), as in the reference)
+template <class T>
+__device__ __forceinline__ void f_dfr_cut(T r, T R1, T R2, T& f, T& dfr) {
+  T t = r < R1 ? R1 : r;
+  t = t > R2 ? R2 : t;
+  T x = (t - R1) / (R2 - R1);
+  T x2 = x * x;
+  f = T(1) + x2 * x * (T(-10) + T(15) * x - T(6) * x2);
+  dfr = t * x2 * (T(-30) + T(60) * x - T(30) * x2);
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Sums K values over the block; result valid in thread 0.  blockDim.x <= 1024.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K]) {
+  __shared__ double sh[K][32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][w] = v[k];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double t = lane < nw ? sh[k][lane] : 0.0;
+      v[k] = warp_sum(t);
+    }
+  }
+}
+
+// Grid-wide deterministic sum of K doubles per block.  Every block calls it with
+// its block-partial values; returns true in thread 0 of the last block to arrive,
+// with out[k] holding the grid totals summed in block order.  `slot` selects the
+// arrival counter; the last block resets it, so graphs can replay the kernel.
+template <int K>
+__device__ __forceinline__ bool grid_sum(Ctl* ctl, int slot, double (&v)[K], double (&out)[K]) {
+  block_sum<K>(v);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) ctl->partial[(size_t)blockIdx.x * K + k] = v[k];
+    __threadfence();
+    unsigned int t = atomicAdd(&ctl->counter[slot], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  if (threadIdx.x == 0) {
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double s = 0.0;
+      for (unsigned int b = 0; b < gridDim.x; ++b) s += ((volatile double*)ctl->partial)[(size_t)b * K + k];
+      out[k] = s;
+    }
+    ctl->counter[slot] = 0u;
+  }
+  return threadIdx.x == 0;
+}
+
+__device__ __forceinline__ void set_error(Ctl* ctl, int code, int kind, int a, int b, int c) {
+  if (atomicCAS(&ctl->error, 0, code) == 0) {
+    ctl->err_kind = kind;
+    ctl->err_info[0] = a;
+    ctl->err_info[1] = b;
+    ctl->err_info[2] = c;
+    ctl->err_step = ctl->md_step;
+  }
+  ctl->stop = 1;
+}
+
+// Kahan-compensated accumulation (precision form).
+struct Kahan3 {
+  float s[3], c[3];
+  __device__ __forceinline__ Kahan3() {
+    s[0] = s[1] = s[2] = 0.f;
+    c[0] = c[1] = c[2] = 0.f;
+  }
+  __device__ __forceinline__ void add(float x, float y, float z) {
+    float in[3] = {x, y, z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float yk = in[k] - c[k];
+      float t = s[k] + yk;
+      c[k] = (t - s[k]) - yk;
+      s[k] = t;
+    }
+  }
+  __device__ __forceinline__ double get(int k) const { return (double)s[k] - (double)c[k]; }
+};
+
+}  // namespace pfmd

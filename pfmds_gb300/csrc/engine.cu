@@ -1,0 +1,1437 @@
+// Host engine: md() of PFMDS (md_simulation.f90:19-274) on one GPU.
+//
+// Set-up reads the reference's input files (settings.h), builds the groups
+// (create_particle_group, md_general.f90:57-80), the Nose-Hoover chains, new
+// Maxwell velocities when asked, the interactions and their neighbour lists, and
+// uploads everything.  The step loop then runs on the device: the host plans runs
+// of consecutive steps between host events (log line, output block, snapshot,
+// trajectory frame, integrator switch), launches each step's kernels in the
+// reference's order -- or replays a captured CUDA graph when the same run of
+// steps was seen before -- and synchronises only at the end of a run.  Errors and
+// the nvms exit are raised on the device (Ctl::stop) and reported after the run
+// with the reference's messages.
+#include <unistd.h>
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pfmd.h"
+#include "kernels.h"
+#include "settings.h"
+
+namespace pfmd {
+
+long long g_kernel_launches = 0;
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                                     \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess)                                                                           \
+      throw ::pfmd::Error(PFMD_E_CUDA, std::string("CUDA error ") + cudaGetErrorString(e_) + " at " #call); \
+  } while (0)
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  void alloc(size_t count) {
+    release();
+    n = count;
+    if (count) CK(cudaMalloc(&p, sizeof(T) * count));
+  }
+  void zero(cudaStream_t s) {
+    if (n) CK(cudaMemsetAsync(p, 0, sizeof(T) * n, s));
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    if (count) CK(cudaMemcpyAsync(p, h, sizeof(T) * count, cudaMemcpyHostToDevice, s));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+};
+
+static const double MASS_COEF = 1.6605389217 / 1.6021765654 * 100.0;
+static const double KT_A_DEGREE = 1.3806488 / 1.6021765654 * 1e-4;
+static const double MOMENTA_COEF = 1.3806488 / 1.6605389217 * 1e-6;
+
+static double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct GroupH {
+  std::vector<int> idx;  // 0-based atoms
+  int n0 = 0;            // size at creation
+  DBuf<int> d;
+};
+
+enum ListKind { L_REGULAR = 0, L_CONVERSE = 1, L_NN_TB = 2 };
+
+struct ListH {
+  ListKind kind = L_REGULAR;
+  ListDev d{};
+  CellGrid cg{};
+  DBuf<int> nnum, nlist, pidx, less, bnd, cstart, ccount, ccursor, cjnd, ccell;
+  double rc = 0.0;
+  long long period = 1;
+  int src = -1;  // converse: source list; nn: the tb list
+  bool has_grid = false;
+};
+
+struct InterH {
+  pfmd_io::InteractionSpec spec;
+  int lists[3] = {-1, -1, -1};
+  LJPar lj{};
+  CosPar cp{};
+  RJLPar rjl{};
+  TBPar tb{};
+  bool general = false;  // lj1g weights for a group not in ascending atom order
+  DBuf<double> scratch;  // rjl 1/Eb, tb bond orders
+  DBuf<double4_32a> norm;    // ljc / morsec graphene normals
+  int tb_inter = -1;     // ljc / morsec: the first tb interaction
+  double rc_nn = 0.0;
+};
+
+struct StepPlan {
+  long long step;
+  bool first, energy, out, zero_mom, check_all;
+  std::vector<char> rebuild;  // per list
+};
+
+class Engine {
+ public:
+  pfmd_options opt{};
+  std::string input_path, settings_filename, prefix;
+  pfmd_io::Settings S;
+  int N = 0;
+  Box box{};
+  Atoms A{};
+  DBuf<double4_32a> pos, vel, frc;
+  DBuf<double> mass;
+  DBuf<float4> posf;
+  std::vector<GroupH> groups;
+  std::vector<ListH> lists;
+  std::vector<InterH> inters;
+  std::vector<ChangeSpec> changes;
+  Ctl* ctl = nullptr;
+  Ctl* hctl = nullptr;  // pinned host copy (header part)
+  size_t ctl_head = 0;
+  cudaStream_t st = nullptr;
+  bool prec = false;
+  bool fuse_kick_drift = true;
+  int fused_nhc_chain = -1;  // chain whose scaling folds into the first kick
+  bool need_check_all = true;
+
+  // md() loop state
+  long long md_step = 0;  // next step to execute
+  int integrator_index = 0;
+  std::string integrator_name;
+  int integ = I_NVE;
+  double ts[4] = {0, 0, 0, 0};
+  double sim_time = 0.0;
+  bool finished = false;
+  bool finished_called = false;
+
+  // output
+  std::string obuf;
+  FILE* log = nullptr;
+  double t_start = 0, t_md = 0;
+  std::string err;
+  bool printed = false;  // the failure's message already went to the output unit
+
+  // graphs
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;
+    int seen = 0;
+  };
+  std::map<std::string, GraphEntry> graphs;
+  long long launches = 0;
+
+  ~Engine();
+  void create(const std::string& ip, const std::string& sf, const pfmd_options& o);
+  void advance(long long max_steps, int* fin);
+  void finish();
+  void compute(bool rebuild, double* e_inter);
+
+  // helpers
+  void out(const std::string& s) { obuf += s; }
+  void outln(const std::string& s) { obuf += s + "\n"; }
+  void flush_out();
+  void write_all_out(const std::string& s);
+  GroupRef gref(int g1based) const {
+    const GroupH& g = groups[static_cast<size_t>(g1based - 1)];
+    return GroupRef{g.d.p, g1based - 1, static_cast<int>(g.idx.size())};
+  }
+  int group_checked(int num) const {
+    if (num < 1 || num > static_cast<int>(groups.size()))
+      throw Error(PFMD_E_PARAM, "error: group number " + std::to_string(num) + " out of range");
+    return num;
+  }
+  void read_ctl();
+  void upload_ctl_groups();
+  void raise_device_error();
+  bool switch_needed(long long s) const;
+  bool do_switch();  // false: no more integrators
+  StepPlan plan(long long s) const;
+  bool is_event(const StepPlan& p) const;
+  void enqueue_step(const StepPlan& p);
+  void enqueue_lists(const StepPlan& p);
+  void enqueue_forces(bool energy);
+  void run_plans(const std::vector<StepPlan>& plans);
+  void host_events(const StepPlan& p);
+  void get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f);
+  std::string nlists_load_text();
+};
+
+Engine::~Engine() {
+  for (auto& kv : graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  if (log) std::fclose(log);
+  if (ctl) cudaFree(ctl);
+  if (hctl) cudaFreeHost(hctl);
+  if (st) cudaStreamDestroy(st);
+}
+
+void Engine::flush_out() {
+  if (obuf.empty()) return;
+  if (opt.out_fd >= 0) {
+    size_t off = 0;
+    while (off < obuf.size()) {
+      ssize_t w = ::write(opt.out_fd, obuf.data() + off, obuf.size() - off);
+      if (w <= 0) break;
+      off += static_cast<size_t>(w);
+    }
+  }
+  obuf.clear();
+}
+
+void Engine::write_all_out(const std::string& s) {
+  int fd = opt.all_out_fd >= 0 ? opt.all_out_fd : opt.out_fd;
+  if (fd == opt.out_fd) {
+    out(s);
+    return;
+  }
+  flush_out();
+  if (fd >= 0) {
+    ssize_t w = ::write(fd, s.data(), s.size());
+    (void)w;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// set-up
+// ---------------------------------------------------------------------------
+void Engine::create(const std::string& ip, const std::string& sf, const pfmd_options& o) {
+  opt = o;
+  input_path = ip;
+  settings_filename = sf;
+  prefix = o.output_prefix ? o.output_prefix : "";
+  prec = opt.form == PFMD_FORM_PRECISION;
+  t_start = now_s();
+  try {
+    pfmd_io::read_settings(input_path, settings_filename, S);
+  } catch (const fortio::ReadError& e) {
+    out(S.echo);
+    throw Error(PFMD_E_IO, e.what());
+  } catch (const std::exception& e) {
+    out(S.echo);
+    throw Error(PFMD_E_PARAM, e.what());
+  }
+  out(S.echo);
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    throw Error(PFMD_E_CUDA, "no CUDA device: this library runs its MD step on the GPU only");
+  CK(cudaSetDevice(opt.device));
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+
+  N = S.xyz.N;
+  for (int k = 0; k < 3; ++k) {
+    box.L[k] = S.xyz.box[k];
+    box.h[k] = 0.5 * S.xyz.box[k];
+    box.Lf[k] = static_cast<float>(box.L[k]);
+    box.hf[k] = static_cast<float>(box.h[k]);
+  }
+  // groups: create_particle_group (md_general.f90:57-80)
+  if (S.group_types.size() > PFMD_MAX_GROUPS) throw Error(PFMD_E_PARAM, "error: too many groups");
+  for (const auto& names : S.group_types) {
+    GroupH g;
+    for (const auto& nm : names)
+      for (int i = 0; i < N; ++i)
+        if (S.xyz.types[static_cast<size_t>(i)] == nm) g.idx.push_back(i);
+    g.n0 = static_cast<int>(g.idx.size());
+    groups.push_back(std::move(g));
+  }
+  for (const auto& c : S.changes) {
+    ChangeSpec cs{};
+    cs.from = group_checked(c.from) - 1;
+    cs.to = group_checked(c.to) - 1;
+    cs.ts1 = c.ts1;
+    cs.ts2 = c.ts2;
+    cs.frec = c.frec;
+    if (c.frec < 1) throw Error(PFMD_E_PARAM, "error: group change frequency must be positive");
+    cs.to_cap = static_cast<int>(groups[static_cast<size_t>(cs.to)].idx.size());
+    changes.push_back(cs);
+  }
+  if (changes.size() > 8) throw Error(PFMD_E_PARAM, "error: at most 8 group changes are supported");
+  group_checked(S.all_moving);
+  group_checked(S.xyz_moving);
+  group_checked(S.z_moving);
+  group_checked(S.all_atoms);
+  group_checked(S.traj_group);
+  if (S.period_traj < 1 || S.zero_momentum_period < 1)
+    throw Error(PFMD_E_PARAM, "error: output and momentum periods must be positive");
+  for (const auto& is : S.integrators)
+    if (is.period_log < 1 || is.period_snapshot < 1)
+      throw Error(PFMD_E_PARAM, "error: integrator output periods must be positive");
+  if (S.nhc.size() > PFMD_MAX_NHC) throw Error(PFMD_E_PARAM, "error: too many Nose-Hoover chains");
+  for (const auto& h : S.nhc) {
+    group_checked(h.group);
+    if (h.M < 1 || h.M > PFMD_MAX_CHAIN) throw Error(PFMD_E_PARAM, "error: wrong nhc parameters");
+  }
+
+  // host copies of the state
+  std::vector<double> hp = S.xyz.pos, hv = S.xyz.vel;
+  const std::vector<double>& hm = S.xyz.mass;
+  if (S.new_velocities) {
+    // set_new_temperature (md_general.f90:328-340) with the serial seeded stream
+    const GroupH& g = groups[static_cast<size_t>(S.all_moving - 1)];
+    double t0 = S.initial_temperature < 0.0 ? 0.0 : S.initial_temperature;
+    pfmd_io::MinStd rng(opt.rand_seed);
+    for (int i : g.idx)
+      for (int k = 0; k < 3; ++k) {
+        double a1 = 0, a2 = 0, b = 2.0;
+        while (b >= 1.0) {
+          a1 = 2.0 * rng.next() - 1.0;
+          a2 = 2.0 * rng.next() - 1.0;
+          b = a1 * a1 + a2 * a2;
+        }
+        hv[3 * i + k] = a1 * std::sqrt(-2.0 * std::log(b) / b);
+      }
+    for (int i : g.idx)
+      for (int k = 0; k < 3; ++k) hv[3 * i + k] = hv[3 * i + k] * std::sqrt(MOMENTA_COEF / hm[i]);
+    double mv[3] = {0, 0, 0}, mt = 0;
+    for (int k = 0; k < 3; ++k)
+      for (int i : g.idx) mv[k] = mv[k] + hm[i] * hv[3 * i + k];
+    for (int i : g.idx) mt = mt + hm[i];
+    for (int k = 0; k < 3; ++k) mv[k] = mv[k] / mt;
+    for (int i : g.idx)
+      for (int k = 0; k < 3; ++k) hv[3 * i + k] = hv[3 * i + k] - mv[k];
+    double ke = 0;
+    for (int i : g.idx) {
+      const double* v = &hv[3 * i];
+      ke = ke + hm[i] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / 2 * MASS_COEF;
+    }
+    double temp = 2 * ke / KT_A_DEGREE / static_cast<double>(3 * static_cast<int>(g.idx.size()));
+    double sc = std::sqrt(t0 / temp);
+    for (int i : g.idx)
+      for (int k = 0; k < 3; ++k) hv[3 * i + k] = hv[3 * i + k] * sc;
+  }
+
+  // interactions and their lists (create_interactions, md_interactions.f90:59-136)
+  if (S.interactions.size() > PFMD_MAX_INTER) throw Error(PFMD_E_PARAM, "error: too many interactions");
+  int first_tb = -1;
+  for (size_t k = 0; k < S.interactions.size(); ++k)
+    if (S.interactions[k].kind == pfmd_io::K_TB) {
+      first_tb = static_cast<int>(k);
+      break;
+    }
+  auto new_list = [&](ListKind kind, int row_g, int col_g, int rows, int nmax, double rc, long long period) {
+    ListH L;
+    L.kind = kind;
+    L.rc = rc;
+    L.period = period;
+    L.d.id = static_cast<int>(lists.size());
+    L.d.rows = rows;
+    L.d.nmax = nmax;
+    L.d.stride = ((rows + 31) / 32) * 32;
+    L.d.row_group = row_g - 1;
+    L.d.col_group = col_g - 1;
+    L.d.row_cap = static_cast<int>(groups[static_cast<size_t>(row_g - 1)].idx.size());
+    L.d.col_cap = static_cast<int>(groups[static_cast<size_t>(col_g - 1)].idx.size());
+    if (nmax < 0) throw Error(PFMD_E_PARAM, "error: negative neighb_num_max");
+    if (nmax > 1024) throw Error(PFMD_E_PARAM, "error: neighb_num_max above 1024 is not supported");
+    if (period < 1) throw Error(PFMD_E_PARAM, "error: neighbour list update period must be positive");
+    lists.push_back(std::move(L));
+    if (lists.size() > PFMD_MAX_LISTS) throw Error(PFMD_E_PARAM, "error: too many neighbour lists");
+    return static_cast<int>(lists.size()) - 1;
+  };
+  for (size_t k = 0; k < S.interactions.size(); ++k) {
+    const auto& sp = S.interactions[k];
+    InterH I;
+    I.spec = sp;
+    const auto& p = sp.p;
+    for (const auto& ls : sp.nl) {
+      group_checked(ls.g1);
+      group_checked(ls.g2);
+    }
+    const auto& l1 = sp.nl[0];
+    const int rows1 = static_cast<int>(groups[static_cast<size_t>(l1.g1 - 1)].idx.size());
+    I.lists[0] = new_list(L_REGULAR, l1.g1, l1.g2, rows1, l1.nmax, l1.r_cut, l1.period);
+    switch (sp.kind) {
+      case pfmd_io::K_LJ:
+      case pfmd_io::K_LJ1G:
+        I.lj.eps = p[0];
+        I.lj.sig = p[1];
+        I.lj.R1 = p[2];
+        I.lj.R2 = p[3];
+        {
+          double s6 = p[1] * p[1] * p[1] * p[1] * p[1] * p[1], s12 = s6 * s6;
+          I.lj.c6 = 4.0 * p[0] * s6;
+          I.lj.c12 = 4.0 * p[0] * s12;
+          I.lj.c6t6 = 6.0 * 4.0 * p[0] * s6;
+          I.lj.c12t12 = 12.0 * 4.0 * p[0] * s12;
+        }
+        break;
+      case pfmd_io::K_LJC:
+        I.cp.eps = p[0];
+        I.cp.sig = p[1];
+        I.cp.delt = p[2];
+        I.cp.R1 = p[3];
+        I.cp.R2 = p[4];
+        I.cp.simplified = sp.simplified ? 1 : 0;
+        break;
+      case pfmd_io::K_MORSEC:
+        I.cp.D = p[0];
+        I.cp.r0 = p[1];
+        I.cp.a = p[2];
+        I.cp.delt = p[3];
+        I.cp.R1 = p[4];
+        I.cp.R2 = p[5];
+        I.cp.simplified = sp.simplified ? 1 : 0;
+        break;
+      case pfmd_io::K_RJL:
+        I.rjl = RJLPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6]};
+        break;
+      case pfmd_io::K_TB:
+        I.tb = TBPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[6] * p[6], p[7] * p[7]};
+        break;
+    }
+    if (sp.kind == pfmd_io::K_LJ1G || sp.kind == pfmd_io::K_RJL || sp.kind == pfmd_io::K_TB) {
+      // the reference indexes these lists' partners through the row arrays
+      // (particle_index(nlist), Eb(nlist), nl%nlist(:,j)), which needs g1 == g2
+      if (l1.g1 != l1.g2)
+        throw Error(PFMD_E_PARAM, "error: " + fortio::trim(sp.name) + " needs the same group on both sides of its list");
+      if (sp.kind == pfmd_io::K_LJ1G) {
+        const auto& gi = groups[static_cast<size_t>(l1.g1 - 1)].idx;
+        for (size_t a = 1; a < gi.size(); ++a)
+          if (gi[a] <= gi[a - 1]) I.general = true;
+      }
+    }
+    if (sp.kind == pfmd_io::K_LJ || sp.kind == pfmd_io::K_LJC || sp.kind == pfmd_io::K_MORSEC) {
+      const auto& l2 = sp.nl[1];
+      const int rows2 = static_cast<int>(groups[static_cast<size_t>(l2.g1 - 1)].idx.size());
+      // rows hold nl(1)'s group-2 atoms, entries are nl(1) rows (its group 1)
+      int c = new_list(L_CONVERSE, l1.g2, l1.g1, rows2, l2.nmax, l1.r_cut, l1.period);
+      lists[static_cast<size_t>(c)].src = I.lists[0];
+      I.lists[1] = c;
+    }
+    if (sp.kind == pfmd_io::K_LJC || sp.kind == pfmd_io::K_MORSEC) {
+      const auto& l3 = sp.nl[2];
+      const int rows3 = static_cast<int>(groups[static_cast<size_t>(l3.g1 - 1)].idx.size());
+      I.tb_inter = first_tb;
+      I.rc_nn = l3.r_cut;
+      if (first_tb >= 0) {
+        const auto& tl = S.interactions[static_cast<size_t>(first_tb)].nl[0];
+        int c = new_list(L_NN_TB, tl.g1, tl.g1, rows3, l3.nmax, l3.r_cut, tl.period);
+        I.lists[2] = c;
+      } else {
+        I.lists[2] = new_list(L_REGULAR, l3.g1, l3.g2, rows3, l3.nmax, l3.r_cut, l3.period);
+      }
+      if (rows1 != rows3 && rows1 != 0)
+        throw Error(PFMD_E_PARAM, "error: nl%N/=nl_nn%N " + std::to_string(rows1) + " " + std::to_string(rows3));
+    }
+    inters.push_back(std::move(I));
+  }
+  // the tb list an nn list reads
+  for (auto& I : inters)
+    if (I.tb_inter >= 0) lists[static_cast<size_t>(I.lists[2])].src = inters[static_cast<size_t>(I.tb_inter)].lists[0];
+  for (auto& I : inters)
+    if (I.tb_inter >= 0) {
+      const ListH& tb = lists[static_cast<size_t>(lists[static_cast<size_t>(I.lists[2])].src)];
+      if (tb.d.rows > lists[static_cast<size_t>(I.lists[2])].d.rows)
+        throw Error(PFMD_E_PARAM, "error: the graphene nearest-neighbour list is shorter than the tb list");
+    }
+  // rows of every list must name distinct atoms (forces are added without atomics)
+  {
+    std::vector<char> seen(static_cast<size_t>(N));
+    for (auto& L : lists) {
+      if (L.kind == L_NN_TB) continue;
+      std::fill(seen.begin(), seen.end(), 0);
+      for (int a : groups[static_cast<size_t>(L.d.row_group)].idx) {
+        if (seen[static_cast<size_t>(a)])
+          throw Error(PFMD_E_PARAM, "error: an atom appears twice in a group that rows a neighbour list");
+        seen[static_cast<size_t>(a)] = 1;
+      }
+    }
+  }
+  // kick and drift fuse when the xyz and z groups share no atom
+  {
+    std::vector<char> in_xyz(static_cast<size_t>(N), 0);
+    for (int a : groups[static_cast<size_t>(S.xyz_moving - 1)].idx) in_xyz[static_cast<size_t>(a)] = 1;
+    for (int a : groups[static_cast<size_t>(S.z_moving - 1)].idx)
+      if (in_xyz[static_cast<size_t>(a)]) fuse_kick_drift = false;
+    if (S.xyz_moving == S.z_moving && !groups[static_cast<size_t>(S.xyz_moving - 1)].idx.empty())
+      fuse_kick_drift = false;
+  }
+  // a single chain over exactly the xyz group folds its scaling into the first kick
+  if (S.nhc.size() == 1 && S.nhc[0].group == S.xyz_moving && fuse_kick_drift) fused_nhc_chain = 0;
+
+  // ---- device ----
+  pos.alloc(static_cast<size_t>(std::max(N, 1)));
+  vel.alloc(static_cast<size_t>(std::max(N, 1)));
+  frc.alloc(static_cast<size_t>(std::max(N, 1)));
+  mass.alloc(static_cast<size_t>(std::max(N, 1)));
+  posf.alloc(static_cast<size_t>(std::max(N, 1)));
+  {
+    std::vector<double4_32a> tp(static_cast<size_t>(N)), tv(static_cast<size_t>(N));
+    for (int i = 0; i < N; ++i) {
+      tp[static_cast<size_t>(i)] = make_double4_32a(hp[3 * i], hp[3 * i + 1], hp[3 * i + 2], 0.0);
+      tv[static_cast<size_t>(i)] = make_double4_32a(hv[3 * i], hv[3 * i + 1], hv[3 * i + 2], 0.0);
+    }
+    pos.upload(tp.data(), tp.size(), st);
+    vel.upload(tv.data(), tv.size(), st);
+    frc.zero(st);
+    mass.upload(hm.data(), hm.size(), st);
+    CK(cudaStreamSynchronize(st));
+  }
+  A = Atoms{N, pos.p, vel.p, frc.p, mass.p, posf.p};
+  for (auto& g : groups) {
+    g.d.alloc(std::max<size_t>(g.idx.size(), 1));
+    g.d.upload(g.idx.data(), g.idx.size(), st);
+  }
+  const double maxL = std::max(box.L[0], std::max(box.L[1], box.L[2]));
+  for (auto& L : lists) {
+    const size_t rows = static_cast<size_t>(std::max(L.d.stride, 32));
+    L.nnum.alloc(rows);
+    L.nnum.zero(st);
+    L.nlist.alloc(std::max<size_t>(static_cast<size_t>(L.d.nmax) * rows, 1));
+    L.nlist.zero(st);
+    L.pidx.alloc(rows);
+    L.pidx.zero(st);
+    L.less.alloc(rows);
+    L.less.zero(st);
+    L.bnd.alloc(rows);
+    L.bnd.zero(st);
+    L.d.nnum = L.nnum.p;
+    L.d.nlist = L.nlist.p;
+    L.d.pidx = L.pidx.p;
+    L.d.lessnnum = L.less.p;
+    L.d.bnd = L.bnd.p;
+    L.d.row_idx = groups[static_cast<size_t>(L.d.row_group)].d.p;
+    L.d.col_idx = groups[static_cast<size_t>(L.d.col_group)].d.p;
+    if (L.kind != L_NN_TB) {
+      // cells at least r_cut (+ a margin for FP32 binning) wide
+      const double margin = 1e-3 * L.rc + 2e-3 + 4e-6 * maxL;
+      long long ncell = 1;
+      for (int k = 0; k < 3; ++k) {
+        int nc = static_cast<int>(std::floor(box.L[k] / (L.rc + margin)));
+        L.cg.nc[k] = std::max(1, nc);
+      }
+      const long long cap = 8LL * std::max(L.d.col_cap, 1) + 64;
+      for (;;) {
+        ncell = 1LL * L.cg.nc[0] * L.cg.nc[1] * L.cg.nc[2];
+        if (ncell <= cap) break;
+        int k = 0;
+        for (int a = 1; a < 3; ++a)
+          if (L.cg.nc[a] > L.cg.nc[k]) k = a;
+        L.cg.nc[k] = std::max(1, L.cg.nc[k] / 2);
+      }
+      L.cg.ncell = static_cast<int>(ncell);
+      for (int k = 0; k < 3; ++k) L.cg.inv_cs[k] = static_cast<float>(L.cg.nc[k] / box.L[k]);
+      L.cstart.alloc(static_cast<size_t>(ncell) + 1);
+      L.ccount.alloc(static_cast<size_t>(ncell));
+      L.ccursor.alloc(static_cast<size_t>(ncell));
+      L.cjnd.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+      L.ccell.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+      L.cg.start = L.cstart.p;
+      L.cg.count = L.ccount.p;
+      L.cg.cursor = L.ccursor.p;
+      L.cg.jnd = L.cjnd.p;
+      L.cg.cell_of = L.ccell.p;
+      L.has_grid = true;
+    }
+  }
+  for (auto& I : inters) {
+    const ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
+    if (I.spec.kind == pfmd_io::K_RJL) I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.stride), 32));
+    if (I.spec.kind == pfmd_io::K_TB)
+      I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 32));
+    if (I.lists[2] >= 0) {
+      const ListH& L3 = lists[static_cast<size_t>(I.lists[2])];
+      I.norm.alloc(std::max<size_t>(static_cast<size_t>(L3.d.rows), 1));
+      I.norm.zero(st);
+    }
+  }
+  // control block
+  CK(cudaMalloc(&ctl, sizeof(Ctl)));
+  CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+  ctl_head = offsetof(Ctl, partial);
+  CK(cudaMallocHost(&hctl, ctl_head));
+  std::memset(hctl, 0, ctl_head);
+  hctl->md_step = -1;
+  hctl->oob_atom = INT_MAX;
+  for (size_t g = 0; g < groups.size(); ++g) hctl->group_n[g] = static_cast<int>(groups[g].idx.size());
+  for (size_t c = 0; c < S.nhc.size(); ++c) {
+    const auto& h = S.nhc[c];
+    NHCDev& d = hctl->nhc[c];
+    d.M = h.M;
+    d.L = static_cast<int>(groups[static_cast<size_t>(h.group - 1)].idx.size());
+    d.T = h.temperature;
+    d.s = 1.0;
+    d.e = 0.0;
+    d.q[0] = h.q1;
+    for (int i = 1; i < d.M; ++i) d.q[i] = d.q[0] / (3.0 * d.L);
+  }
+  CK(cudaMemcpyAsync(ctl, hctl, ctl_head, cudaMemcpyHostToDevice, st));
+  launch_pack_posf(A, ctl, st);
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+
+  if (opt.write_files) {
+    std::string ln = prefix + fortio::trim(S.logfilename);
+    log = std::fopen(ln.c_str(), "w");
+    if (!log) throw Error(PFMD_E_IO, "cannot open log file " + ln);
+  }
+  outln(fortio::Rec().a("PREPARATIONS TIME: ", 24).f(now_s() - t_start, 10, 2).a(" S ").s);
+  outln(fortio::Rec().a("RUNNING ON ", 24).i(opt.num_threads, 6).a(" OPENMP THREADS").s);
+  outln("");
+  flush_out();
+  t_md = now_s();
+  md_step = 0;
+  integrator_index = 0;
+  sim_time = 0.0;
+}
+
+void Engine::read_ctl() {
+  CK(cudaMemcpyAsync(hctl, ctl, ctl_head, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+}
+
+void Engine::upload_ctl_groups() {
+  CK(cudaMemcpyAsync(ctl->group_n, hctl->group_n, sizeof(hctl->group_n), cudaMemcpyHostToDevice, st));
+}
+
+// Reports a device-side stop with the reference's messages and throws.
+void Engine::raise_device_error() {
+  const Ctl& c = *hctl;
+  std::string msg;
+  switch (c.err_kind) {
+    case EK_OVERFLOW:
+    case EK_CONVERSE_OVF:
+      msg = "error: too many neighbours" + fortio::list_int(c.err_info[1]) + fortio::list_int(c.err_info[2]);
+      break;
+    case EK_OOB: {
+      std::vector<double> p, v;
+      get_state_host(p, v, nullptr);
+      for (int i = 0; i < N; ++i)
+        for (int k = 0; k < 3; ++k) {
+          double x = p[3 * i + k];
+          if (!(x > (0.0 - 0.0000001) && x < (box.L[k] + 0.0000001)))
+            outln(fortio::list_int(i + 1) + " particle out of cell " + fortio::list_real(p[3 * i]) +
+                  fortio::list_real(p[3 * i + 1]) + fortio::list_real(p[3 * i + 2]));
+        }
+      msg = "particle out of cell";
+      break;
+    }
+    case EK_GR_TOO_MANY:
+      msg = "error: too many gr nearest neibs" + fortio::list_int(c.err_info[0]);
+      break;
+    case EK_GR_NOT_ENOUGH:
+      msg = "error: not enough gr nearest neibs" + fortio::list_int(c.err_info[0]);
+      break;
+    case EK_L1:
+      msg = "l1>3";
+      break;
+    default:
+      if (c.error == PFMD_E_PARAM)
+        msg = "error: group1%N>nl%N" + fortio::list_int(c.err_info[1]) + fortio::list_int(c.err_info[2]);
+      else
+        msg = "device error";
+  }
+  if (c.err_kind != EK_OOB) outln(" " + msg);
+  flush_out();
+  printed = true;
+  throw Error(c.error ? c.error : PFMD_E_STATE, msg + " (md_step " + std::to_string(c.err_step) + ")");
+}
+
+// ---------------------------------------------------------------------------
+// step planning
+// ---------------------------------------------------------------------------
+bool Engine::switch_needed(long long s) const {
+  if (integrator_index == 0) return true;
+  long long sum = 0;
+  for (int k = 1; k <= integrator_index && k <= static_cast<int>(S.integrators.size()); ++k)
+    sum += S.integrators[static_cast<size_t>(k - 1)].l;
+  return s - 1 == sum;
+}
+
+// md_simulation.f90:121-136
+bool Engine::do_switch() {
+  const int n = static_cast<int>(S.integrators.size());
+  integrator_index = integrator_index + 1;
+  int i = integrator_index;
+  for (; i <= n; ++i) {
+    const auto& is = S.integrators[static_cast<size_t>(i - 1)];
+    if (is.l > 0) {
+      integrator_name = is.name;
+      for (int k = 0; k < 4; ++k) ts[k] = is.dt / static_cast<double>(1 << k);
+      integ = (fortio::trim(is.name) == "nvt") ? I_NVT : (fortio::trim(is.name) == "nvms") ? I_NVMS : I_NVE;
+      break;
+    }
+  }
+  if (i > n) return false;
+  integrator_index = i;
+  return true;
+}
+
+StepPlan Engine::plan(long long s) const {
+  StepPlan p;
+  p.step = s;
+  p.first = (s == 0);
+  const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
+  p.energy = (s % I.period_log == 0) || (s % opt.out_period == 0) || integ == I_NVMS;
+  p.out = (s % opt.out_period == 0) && opt.out_fd >= 0;
+  p.zero_mom = (s % S.zero_momentum_period == 0);
+  p.check_all = need_check_all;
+  p.rebuild.resize(lists.size());
+  for (size_t k = 0; k < lists.size(); ++k) {
+    const ListH& L = lists[k];
+    long long per = L.period;
+    if (L.kind == L_CONVERSE) per = lists[static_cast<size_t>(L.src)].period;
+    p.rebuild[k] = (s % per == 0) ? 1 : 0;
+  }
+  return p;
+}
+
+bool Engine::is_event(const StepPlan& p) const {
+  const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
+  if (log && p.step % I.period_log == 0) return true;
+  if (p.out) return true;
+  if (opt.write_files && p.step % I.period_snapshot == 0 && p.step != 0) return true;
+  if (opt.write_files && p.step % S.period_traj == 0) return true;
+  return false;
+}
+
+void Engine::enqueue_lists(const StepPlan& p) {
+  for (auto& I : inters) {
+    ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
+    if (p.rebuild[static_cast<size_t>(I.lists[0])]) {
+      launch_bin(L1.d, L1.cg, A, ctl, st);
+      launch_build_list(prec, L1.d, L1.cg, A, box, L1.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
+                        0, 0, ctl, st);
+    }
+    if (I.lists[1] >= 0 && p.rebuild[static_cast<size_t>(I.lists[1])]) {
+      ListH& L2 = lists[static_cast<size_t>(I.lists[1])];
+      launch_bin(L2.d, L2.cg, A, ctl, st);
+      launch_build_list(prec, L2.d, L2.cg, A, box, L2.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
+                        1, L1.d.rows, ctl, st);
+    }
+    if (I.lists[2] >= 0 && p.rebuild[static_cast<size_t>(I.lists[2])]) {
+      ListH& L3 = lists[static_cast<size_t>(I.lists[2])];
+      if (L3.kind == L_NN_TB) {
+        if (L3.d.nmax != 3) {
+          // find_gr_nearest_neighbors checks this on every selection (graphenenorm.f90:13)
+          throw Error(PFMD_E_GR_NN, "error: nl_nn%neighb_num_max/=nnum_nn");
+        }
+        launch_nn_select(prec, lists[static_cast<size_t>(L3.src)].d, L3.d, I.rc_nn, A, box, ctl, st);
+      } else {
+        launch_bin(L3.d, L3.cg, A, ctl, st);
+        launch_build_list(prec, L3.d, L3.cg, A, box, L3.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
+                          0, 0, ctl, st);
+      }
+    }
+  }
+  for (auto& I : inters)
+    if (I.lists[2] >= 0)
+      launch_normals(prec, lists[static_cast<size_t>(I.lists[2])].d, I.norm.p, I.cp.simplified, A, box, ctl, st);
+}
+
+void Engine::enqueue_forces(bool energy) {
+  for (size_t k = 0; k < inters.size(); ++k) {
+    InterH& I = inters[k];
+    const int key = static_cast<int>(k);
+    const int eslot = 4 + static_cast<int>(k % 16);
+    const ListDev& L1 = lists[static_cast<size_t>(I.lists[0])].d;
+    switch (I.spec.kind) {
+      case pfmd_io::K_LJ:
+        launch_lj(prec, energy, L1, I.lj, A, box, ctl, eslot, key, st);
+        launch_lj(prec, false, lists[static_cast<size_t>(I.lists[1])].d, I.lj, A, box, ctl, eslot, key, st);
+        break;
+      case pfmd_io::K_LJ1G:
+        launch_lj1g(prec, energy, I.general, L1, I.lj, A, box, ctl, eslot, key, st);
+        break;
+      case pfmd_io::K_RJL:
+        launch_rjl(prec, energy, L1, I.rjl, A, box, I.scratch.p, ctl, eslot, key, st);
+        break;
+      case pfmd_io::K_TB:
+        launch_tb(prec, energy, L1, I.tb, A, box, I.scratch.p, ctl, eslot, key, st);
+        break;
+      case pfmd_io::K_LJC:
+      case pfmd_io::K_MORSEC:
+        launch_cos(prec, energy, I.spec.kind == pfmd_io::K_MORSEC, L1, lists[static_cast<size_t>(I.lists[1])].d,
+                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, A, box, ctl, eslot, key, st);
+        break;
+    }
+  }
+}
+
+// One pass of md()'s loop body on the device (md_simulation.f90:116-231).
+void Engine::enqueue_step(const StepPlan& p) {
+  const bool nvms = integ == I_NVMS, nvt = integ == I_NVT;
+  if (p.check_all) launch_check_all(A, box, ctl, st);
+  if (S.invert_z_vel) {
+    launch_step_begin(0, static_cast<int>(changes.size()), changes.data(), 0, S.ms_de, ctl, st);
+    launch_invert_z(A, box, ctl, st);
+    launch_step_begin(1, 0, nullptr, nvms ? 1 : 0, S.ms_de, ctl, st);
+  } else {
+    launch_step_begin(2, static_cast<int>(changes.size()), changes.data(), nvms ? 1 : 0, S.ms_de, ctl, st);
+  }
+  const GroupRef gx = gref(S.xyz_moving), gz = gref(S.z_moving);
+  if (!p.first) {
+    int scale_chain = 0;
+    if (nvt)
+      for (size_t c = 0; c < S.nhc.size(); ++c) {
+        const GroupRef gc = gref(S.nhc[c].group);
+        launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st);
+        if (static_cast<int>(c) == fused_nhc_chain)
+          scale_chain = static_cast<int>(c) + 1;
+        else
+          launch_scale(static_cast<int>(c), gc, A, ctl, st);
+      }
+    if (fuse_kick_drift) {
+      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, A, box, ctl, st);
+      if (gz.cap > 0) {
+        launch_kick(gz, false, ts[1], A, ctl, st);
+        launch_drift(gz, false, ts[0], true, A, box, ctl, st);
+      }
+    } else {
+      launch_kick(gx, true, ts[1], A, ctl, st);
+      launch_kick(gz, false, ts[1], A, ctl, st);
+      launch_drift(gx, true, ts[0], true, A, box, ctl, st);
+      launch_drift(gz, false, ts[0], true, A, box, ctl, st);
+    }
+  }
+  enqueue_lists(p);
+  const GroupRef gall = gref(S.all_atoms);
+  if (p.zero_mom) launch_zero_momentum(gall, A, ctl, st);
+  launch_zero_forces(gall, A, ctl, st);
+  enqueue_forces(p.energy);
+  if (!p.first) {
+    launch_kick(gx, true, ts[1], A, ctl, st);
+    if (gz.cap > 0) launch_kick(gz, false, ts[1], A, ctl, st);
+    if (nvt)
+      for (size_t c = 0; c < S.nhc.size(); ++c) {
+        const GroupRef gc = gref(S.nhc[c].group);
+        launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st);
+        launch_scale(static_cast<int>(c), gc, A, ctl, st);
+      }
+    if (nvms) {
+      launch_ms(gx, true, A, ctl, st);
+      if (gz.cap > 0) launch_ms(gz, false, A, ctl, st);
+    }
+  }
+  if (p.energy)
+    launch_energy_finalize(gref(S.all_moving), static_cast<int>(inters.size()), static_cast<int>(S.nhc.size()),
+                           nvt ? 1 : 0, A, ctl, st);
+  if (p.out) {
+    launch_out_reduce(gall, A, ctl, st);
+    CK(cudaMemsetAsync(ctl->maxnnum, 0, sizeof(int) * PFMD_MAX_LISTS, st));
+    for (auto& L : lists) launch_nnum_max(L.d, ctl, st);
+  }
+}
+
+static std::string plan_key(const StepPlan& p) {
+  std::string k;
+  k.reserve(8 + p.rebuild.size());
+  k.push_back(static_cast<char>('A' + (p.first ? 1 : 0) + 2 * (p.energy ? 1 : 0) + 4 * (p.out ? 1 : 0) +
+                                8 * (p.zero_mom ? 1 : 0) + 16 * (p.check_all ? 1 : 0)));
+  for (char r : p.rebuild) k.push_back(r ? '1' : '0');
+  k.push_back('|');
+  return k;
+}
+
+void Engine::run_plans(const std::vector<StepPlan>& plans) {
+  std::string key = std::to_string(integrator_index) + ":";
+  for (const auto& p : plans) key += plan_key(p);
+  GraphEntry* ge = nullptr;
+  if (opt.use_graphs && plans.size() >= 2) {
+    ge = &graphs[key];
+    ge->seen++;
+  }
+  if (ge && ge->exec) {
+    CK(cudaGraphLaunch(ge->exec, st));
+    launches += ge->kernels;
+  } else if (ge && ge->seen >= 2) {
+    if (graphs.size() > 64) {  // keep the cache bounded
+      for (auto it = graphs.begin(); it != graphs.end();) {
+        if (it->second.exec && it->first != key) {
+          cudaGraphExecDestroy(it->second.exec);
+          it = graphs.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      ge = &graphs[key];
+    }
+    cudaGraph_t g = nullptr;
+    const long long before = g_kernel_launches;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (const auto& p : plans) enqueue_step(p);
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    CK(cudaStreamEndCapture(st, &g));
+    ge->kernels = g_kernel_launches - before;
+    CK(cudaGraphInstantiate(&ge->exec, g, 0));
+    cudaGraphDestroy(g);
+    CK(cudaGraphLaunch(ge->exec, st));
+    launches += ge->kernels;
+  } else {
+    const long long before = g_kernel_launches;
+    for (const auto& p : plans) enqueue_step(p);
+    launches += g_kernel_launches - before;
+  }
+  need_check_all = false;
+}
+
+void Engine::get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f) {
+  std::vector<double4_32a> tp(static_cast<size_t>(N)), tv(static_cast<size_t>(N)), tf;
+  if (N) {
+    CK(cudaMemcpyAsync(tp.data(), pos.p, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(tv.data(), vel.p, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, st));
+    if (f) {
+      tf.resize(static_cast<size_t>(N));
+      CK(cudaMemcpyAsync(tf.data(), frc.p, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, st));
+    }
+  }
+  CK(cudaStreamSynchronize(st));
+  p.resize(3 * static_cast<size_t>(N));
+  v.resize(3 * static_cast<size_t>(N));
+  if (f) f->resize(3 * static_cast<size_t>(N));
+  for (int i = 0; i < N; ++i) {
+    p[3 * i] = tp[i].x;
+    p[3 * i + 1] = tp[i].y;
+    p[3 * i + 2] = tp[i].z;
+    v[3 * i] = tv[i].x;
+    v[3 * i + 1] = tv[i].y;
+    v[3 * i + 2] = tv[i].z;
+    if (f) {
+      (*f)[3 * i] = tf[i].x;
+      (*f)[3 * i + 1] = tf[i].y;
+      (*f)[3 * i + 2] = tf[i].z;
+    }
+  }
+}
+
+std::string Engine::nlists_load_text() {  // md_interactions.f90:427-444
+  std::string s;
+  if (!inters.empty()) s += "neib lists load:\n";
+  for (auto& I : inters) {
+    const int nl_n = I.spec.nl_n;
+    for (int j = 0; j < nl_n; ++j) {
+      const ListH& L = lists[static_cast<size_t>(I.lists[j])];
+      int mx = L.d.rows > 0 ? hctl->maxnnum[L.d.id] : 0;
+      s += fortio::Rec().a(fortio::trim(I.spec.name), 8).i(j + 1, 3).i(mx, 6).a(" /").i(L.d.nmax, 6).s + "\n";
+    }
+  }
+  return s;
+}
+
+// Host work after an event step: log line, output block, snapshot, trajectory
+// (md_simulation.f90:204-241).
+void Engine::host_events(const StepPlan& p) {
+  const long long s = p.step;
+  const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
+  const Ctl& c = *hctl;
+  if (log && s % I.period_log == 0) {
+    fortio::Rec r;
+    r.a(fortio::trim(integrator_name), 6).i(s, 9);
+    r.f(sim_time, 24, 6).f(c.conserved, 24, 6).f(c.e_nhc, 24, 6).f(c.total, 24, 6).f(c.pe_last, 24, 6);
+    r.f(c.ke, 24, 6).f(c.temperature, 24, 6);
+    for (size_t k = 0; k < inters.size(); ++k) r.f(c.e_inter[k], 20, 9);
+    for (size_t k = 0; k < S.nhc.size(); ++k) r.f(c.nhc[k].e, 20, 9);
+    std::string line = r.s + "\n";
+    std::fputs(line.c_str(), log);
+  }
+  if (p.out) {
+    const double fs = std::sqrt(c.red[0] * c.red[0] + c.red[1] * c.red[1] + c.red[2] * c.red[2]);
+    const double mv[3] = {c.red[6] / c.red[9], c.red[7] / c.red[9], c.red[8] / c.red[9]};
+    const double mcv = std::sqrt(mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]);
+    outln(fortio::Rec().a("exe time (s) = ").f(now_s() - t_start, 10, 2).s);
+    outln(fortio::Rec().a("step = ").i(s, 12).a(" integrator = ").a(fortio::trim(integrator_name), 6).s);
+    outln(fortio::Rec().a("conserved energy (eV) = ").es(c.conserved, 21, 9).s);
+    outln(fortio::Rec().a("forces sum (eV/A) = ").es(fs, 16, 6).s);
+    outln(fortio::Rec().a("c.o.m. velocity (A/fs) = ").es(mcv, 16, 6).s);
+    outln(fortio::Rec()
+              .a("c.o.m. position (A) = ")
+              .f(c.red[3] / c.red[9], 12, 6)
+              .f(c.red[4] / c.red[9], 12, 6)
+              .f(c.red[5] / c.red[9], 12, 6)
+              .s);
+    outln(fortio::Rec().a("maximum velocity (A/fs) = ").f(std::sqrt(c.red[10]), 12, 6).s);
+    out(nlists_load_text());
+    if (integ != I_NVMS && fs > 1e-14) outln(" WARNING: forces sum is too big");
+    if (integ == I_NVT && S.xyz_moving == S.all_atoms && mcv > 1e-14)
+      outln(" WARNING: center of mass velocity is too big");
+    outln("");
+  }
+  const bool snap = opt.write_files && s % I.period_snapshot == 0 && s != 0;
+  const bool traj = opt.write_files && s % S.period_traj == 0;
+  if (snap || traj) {
+    std::vector<double> hp, hv;
+    get_state_host(hp, hv, nullptr);
+    if (snap) {
+      std::string fn = prefix + "snapshot_" + fortio::fmt_i0pad(s, 6, 6) + ".xyz";
+      const auto& g = groups[static_cast<size_t>(S.all_atoms - 1)];
+      const int gn = hctl->group_n[S.all_atoms - 1];
+      std::string text = pfmd_io::xyz_snapshot_text(box.L, gn, g.idx.data(), hp.data(), hv.data(),
+                                                    S.xyz.mass.data(), S.xyz.types);
+      FILE* f = std::fopen(fn.c_str(), "w");
+      if (!f) throw Error(PFMD_E_IO, "cannot open " + fn);
+      std::fputs(text.c_str(), f);
+      std::fclose(f);
+    }
+    if (traj) {
+      std::string fn = prefix + "traj_" + fortio::fmt_i0pad(S.traj_group, 2, 2) + ".xyz";
+      const auto& g = groups[static_cast<size_t>(S.traj_group - 1)];
+      const int gn = hctl->group_n[S.traj_group - 1];
+      std::string text = pfmd_io::xyz_traj_frame_text(box.L, gn, g.idx.data(), hp.data(), hv.data(),
+                                                      S.xyz.mass.data(), S.xyz.types, s);
+      if (!text.empty()) {
+        FILE* f = std::fopen(fn.c_str(), "a");
+        if (!f) throw Error(PFMD_E_IO, "cannot open " + fn);
+        std::fputs(text.c_str(), f);
+        std::fclose(f);
+      }
+    }
+  }
+}
+
+void Engine::advance(long long max_steps, int* fin) {
+  long long done = 0;
+  const size_t seg_cap = 4096;
+  while (!finished && done < max_steps) {
+    const long long s = md_step;
+    if (s > S.md_step_limit) {
+      finished = true;
+      break;
+    }
+    if (switch_needed(s)) {
+      if (!do_switch()) {
+        outln(" no more integrators");
+        finished = true;
+        break;
+      }
+    }
+    std::vector<StepPlan> plans;
+    for (long long t = s; t <= S.md_step_limit; ++t) {
+      if (t != s && switch_needed(t)) break;
+      plans.push_back(plan(t));
+      need_check_all = false;  // only the first planned step runs the full check
+      if (is_event(plans.back()) || plans.size() >= seg_cap || done + static_cast<long long>(plans.size()) >= max_steps)
+        break;
+    }
+    need_check_all = plans.front().check_all;
+    run_plans(plans);
+    read_ctl();
+    if (hctl->error) raise_device_error();
+    const long long executed_to = hctl->converged ? hctl->err_step : plans.back().step + 1;
+    for (long long t = s; t < executed_to; ++t)
+      if (t != 0) sim_time = sim_time + ts[0];
+    if (hctl->converged) {
+      outln(" potential energy diffrence is small enough");
+      md_step = hctl->err_step;
+      finished = true;
+      done += md_step - s;
+      break;
+    }
+    md_step = plans.back().step + 1;
+    done += static_cast<long long>(plans.size());
+    if (is_event(plans.back())) host_events(plans.back());
+    flush_out();
+  }
+  if (md_step > S.md_step_limit) finished = true;
+  flush_out();
+  if (log) std::fflush(log);
+  if (fin) *fin = finished ? 1 : 0;
+}
+
+// md_simulation.f90:245-272
+void Engine::finish() {
+  if (finished_called) throw Error(PFMD_E_STATE, "pfmd_finish was already called");
+  finished_called = true;
+  read_ctl();
+  const double exe = now_s() - t_md;
+  const Ctl& c = *hctl;
+  if (integ == I_NVMS) outln(" potential energy difference: " + fortio::list_real(c.pe_last - c.pe_prev));
+  outln(" steps number:" + fortio::list_int(md_step - 1));
+  outln("");
+  outln(" PERFOMANCE:");
+  auto perf = [&](const char* name, double t) {
+    outln(fortio::Rec().a(name, 24).f(t, 10, 2).a(" S ").f(t / exe * 100, 10, 2).a("%").s);
+  };
+  // phases run back to back on the device inside one stream; only the loop's
+  // wall time is measured
+  perf("MD:", exe);
+  perf("POSITION AND VELOCITY:", 0.0);
+  perf("NEIGHBOURS:", 0.0);
+  perf("NEIGHBOURS SEARCH:", 0.0);
+  perf("NEIGHBOURS DISTANCE:", 0.0);
+  perf("FORCES:", 0.0);
+  perf("ENERGY:", 0.0);
+  perf("REST:", exe);
+  outln(fortio::Rec().a("TIME STEPS PER HOUR:", 24).f(static_cast<double>(md_step) / exe * 3600, 16, 2).s);
+  outln("");
+  fortio::Rec r;
+  r.a(fortio::trim(prefix), 32).i(md_step - 1, 9).f(sim_time, 20, 9);
+  r.f(c.total, 20, 9).f(c.pe_last, 20, 9).f(c.ke, 20, 9).f(c.temperature, 20, 9);
+  for (size_t k = 0; k < inters.size(); ++k) r.f(c.e_inter[k], 20, 9);
+  write_all_out(r.s);
+  if (log) std::fputs((r.s + "\n").c_str(), log);
+  if (md_step != 0 && opt.write_files) {
+    std::vector<double> hp, hv;
+    get_state_host(hp, hv, nullptr);
+    std::string fn = prefix + "final_" + fortio::trim(S.init_xyz_filename);
+    const auto& g = groups[static_cast<size_t>(S.all_atoms - 1)];
+    std::string text = pfmd_io::xyz_snapshot_text(box.L, hctl->group_n[S.all_atoms - 1], g.idx.data(), hp.data(),
+                                                  hv.data(), S.xyz.mass.data(), S.xyz.types);
+    FILE* f = std::fopen(fn.c_str(), "w");
+    if (!f) throw Error(PFMD_E_IO, "cannot open " + fn);
+    std::fputs(text.c_str(), f);
+    std::fclose(f);
+  }
+  if (log) {
+    std::fclose(log);
+    log = nullptr;
+  }
+  flush_out();
+}
+
+void Engine::compute(bool rebuild, double* e_inter) {
+  StepPlan p;
+  p.step = 0;
+  p.first = true;
+  p.energy = true;
+  p.out = false;
+  p.zero_mom = false;
+  p.check_all = false;
+  p.rebuild.assign(lists.size(), rebuild ? 1 : 0);
+  enqueue_lists(p);
+  launch_zero_forces(gref(S.all_atoms), A, ctl, st);
+  enqueue_forces(true);
+  read_ctl();
+  if (hctl->error) raise_device_error();
+  if (e_inter)
+    for (size_t k = 0; k < inters.size(); ++k) e_inter[k] = hctl->e_inter[k];
+}
+
+}  // namespace pfmd
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct pfmd_ctx {
+  std::unique_ptr<pfmd::Engine> e;
+  std::string err;
+};
+
+template <class F>
+static int guard(pfmd_ctx* c, F f) {
+  try {
+    f();
+    return PFMD_OK;
+  } catch (const pfmd::Error& e) {
+    if (c) c->err = e.what();
+    return e.code;
+  } catch (const fortio::ReadError& e) {
+    if (c) c->err = e.what();
+    return PFMD_E_IO;
+  } catch (const std::exception& e) {
+    if (c) c->err = e.what();
+    return PFMD_E_PARAM;
+  }
+}
+
+extern "C" {
+
+void pfmd_default_options(pfmd_options* o) {
+  if (!o) return;
+  o->form = PFMD_FORM_PLAIN;
+  o->rand_seed = 1;
+  o->out_period = 1;
+  o->out_fd = -1;
+  o->all_out_fd = -1;
+  o->write_files = 0;
+  o->output_prefix = "";
+  o->num_threads = 1;
+  o->device = 0;
+  o->use_graphs = 1;
+}
+
+int pfmd_create_from_files(const char* input_path, const char* settings_filename, const pfmd_options* opt,
+                           pfmd_ctx** out) {
+  if (!out) return PFMD_E_PARAM;
+  auto* c = new pfmd_ctx();
+  c->e.reset(new pfmd::Engine());
+  *out = c;
+  pfmd_options o;
+  pfmd_default_options(&o);
+  if (opt) o = *opt;
+  if (o.out_period < 1) o.out_period = 1;
+  int rc = guard(c, [&] {
+    c->e->create(input_path ? input_path : "", settings_filename ? settings_filename : "md_run_settings.txt", o);
+  });
+  c->e->flush_out();
+  return rc;
+}
+
+void pfmd_destroy(pfmd_ctx* c) { delete c; }
+const char* pfmd_errmsg(const pfmd_ctx* c) { return c ? c->err.c_str() : "null context"; }
+const char* pfmd_strerror(int code) {
+  switch (code) {
+    case PFMD_OK: return "PFMD_OK";
+    case PFMD_E_NLIST_OVERFLOW: return "PFMD_E_NLIST_OVERFLOW";
+    case PFMD_E_OUT_OF_CELL: return "PFMD_E_OUT_OF_CELL";
+    case PFMD_E_GR_NN: return "PFMD_E_GR_NN";
+    case PFMD_E_PARAM: return "PFMD_E_PARAM";
+    case PFMD_E_CUDA: return "PFMD_E_CUDA";
+    case PFMD_E_TIMEOUT: return "PFMD_E_TIMEOUT";
+    case PFMD_E_IO: return "PFMD_E_IO";
+    case PFMD_E_STATE: return "PFMD_E_STATE";
+  }
+  return "PFMD_E_UNKNOWN";
+}
+
+int pfmd_advance(pfmd_ctx* c, long long max_steps, int* finished) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] { c->e->advance(max_steps, finished); });
+}
+
+int pfmd_finish(pfmd_ctx* c) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] { c->e->finish(); });
+}
+
+int pfmd_md(const char* input_path, const char* settings_filename, const pfmd_options* opt) {
+  pfmd_ctx* c = nullptr;
+  int rc = pfmd_create_from_files(input_path, settings_filename, opt, &c);
+  if (rc == PFMD_OK) {
+    int fin = 0;
+    rc = pfmd_advance(c, LLONG_MAX, &fin);
+    if (rc == PFMD_OK) rc = pfmd_finish(c);
+  }
+  if (rc != PFMD_OK && c && c->e && !c->e->printed) {
+    c->e->outln(" " + c->err);
+    c->e->flush_out();
+  }
+  pfmd_destroy(c);
+  return rc;
+}
+
+int pfmd_natoms(const pfmd_ctx* c, int* n) {
+  if (!c || !c->e || !n) return PFMD_E_STATE;
+  *n = c->e->N;
+  return PFMD_OK;
+}
+
+int pfmd_md_step(const pfmd_ctx* c, long long* s, double* t) {
+  if (!c || !c->e) return PFMD_E_STATE;
+  if (s) *s = c->e->md_step;
+  if (t) *t = c->e->sim_time;
+  return PFMD_OK;
+}
+
+int pfmd_get_state(pfmd_ctx* c, double* pos, double* vel, double* frc) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    std::vector<double> p, v, f;
+    c->e->get_state_host(p, v, &f);
+    size_t n = 3 * static_cast<size_t>(c->e->N);
+    if (pos) std::memcpy(pos, p.data(), n * sizeof(double));
+    if (vel) std::memcpy(vel, v.data(), n * sizeof(double));
+    if (frc) std::memcpy(frc, f.data(), n * sizeof(double));
+  });
+}
+
+int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    pfmd::Engine& e = *c->e;
+    const int N = e.N;
+    std::vector<double4_32a> t(static_cast<size_t>(N));
+    if (pos && N) {
+      for (int i = 0; i < N; ++i) t[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+      e.pos.upload(t.data(), t.size(), e.st);
+      CK(cudaStreamSynchronize(e.st));
+      pfmd::launch_pack_posf(e.A, e.ctl, e.st);
+      e.need_check_all = true;
+    }
+    if (vel && N) {
+      for (int i = 0; i < N; ++i) t[i] = make_double4_32a(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
+      e.vel.upload(t.data(), t.size(), e.st);
+    }
+    CK(cudaStreamSynchronize(e.st));
+  });
+}
+
+int pfmd_energies(pfmd_ctx* c, double* e_inter, double* pe, double* ke, double* temp, double* e_nhc,
+                  double* e_cons) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    pfmd::Engine& e = *c->e;
+    e.read_ctl();
+    if (e_inter)
+      for (size_t k = 0; k < e.inters.size(); ++k) e_inter[k] = e.hctl->e_inter[k];
+    if (pe) *pe = e.hctl->pe_last;
+    if (ke) *ke = e.hctl->ke;
+    if (temp) *temp = e.hctl->temperature;
+    if (e_nhc) *e_nhc = e.hctl->e_nhc;
+    if (e_cons) *e_cons = e.hctl->conserved;
+  });
+}
+
+int pfmd_compute(pfmd_ctx* c, int rebuild, double* e_inter) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] { c->e->compute(rebuild != 0, e_inter); });
+}
+
+int pfmd_ninteractions(const pfmd_ctx* c, int* n) {
+  if (!c || !c->e || !n) return PFMD_E_STATE;
+  *n = static_cast<int>(c->e->inters.size());
+  return PFMD_OK;
+}
+
+static int list_of(const pfmd_ctx* c, int inter, int list) {
+  const auto& e = *c->e;
+  if (inter < 0 || inter >= static_cast<int>(e.inters.size())) return -1;
+  if (list < 0 || list >= 3) return -1;
+  return e.inters[static_cast<size_t>(inter)].lists[list];
+}
+
+int pfmd_nlist_shape(const pfmd_ctx* c, int inter, int list, int* n_rows, int* nmax) {
+  if (!c || !c->e) return PFMD_E_STATE;
+  int l = list_of(c, inter, list);
+  if (l < 0) return PFMD_E_PARAM;
+  const auto& L = c->e->lists[static_cast<size_t>(l)];
+  if (n_rows) *n_rows = L.d.rows;
+  if (nmax) *nmax = L.d.nmax;
+  return PFMD_OK;
+}
+
+int pfmd_get_nlist(pfmd_ctx* c, int inter, int list, int* nnum, int* lessnnum, int* pidx, int* nlist) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  int l = list_of(c, inter, list);
+  if (l < 0) return PFMD_E_PARAM;
+  return guard(c, [&] {
+    auto& e = *c->e;
+    const auto& L = e.lists[static_cast<size_t>(l)];
+    const size_t rows = static_cast<size_t>(L.d.rows), nmax = static_cast<size_t>(L.d.nmax),
+                 stride = static_cast<size_t>(L.d.stride);
+    if (rows == 0) return;
+    if (nnum) CK(cudaMemcpyAsync(nnum, L.nnum.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
+    if (lessnnum) CK(cudaMemcpyAsync(lessnnum, L.less.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
+    if (pidx) CK(cudaMemcpyAsync(pidx, L.pidx.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
+    std::vector<int> t;
+    if (nlist && nmax) {
+      t.resize(nmax * stride);
+      CK(cudaMemcpyAsync(t.data(), L.nlist.p, sizeof(int) * t.size(), cudaMemcpyDeviceToHost, e.st));
+    }
+    CK(cudaStreamSynchronize(e.st));
+    if (nlist && nmax)
+      for (size_t r = 0; r < rows; ++r)
+        for (size_t p = 0; p < nmax; ++p) nlist[r * nmax + p] = t[p * stride + r];
+  });
+}
+
+int pfmd_nlist_load(pfmd_ctx* c, int* maxnnum, int* count) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    auto& e = *c->e;
+    CK(cudaMemsetAsync(e.ctl->maxnnum, 0, sizeof(int) * PFMD_MAX_LISTS, e.st));
+    for (auto& L : e.lists) pfmd::launch_nnum_max(L.d, e.ctl, e.st);
+    e.read_ctl();
+    int k = 0;
+    for (auto& I : e.inters)
+      for (int j = 0; j < I.spec.nl_n; ++j) {
+        const auto& L = e.lists[static_cast<size_t>(I.lists[j])];
+        if (maxnnum) maxnnum[k] = e.hctl->maxnnum[L.d.id];
+        ++k;
+      }
+    if (count) *count = k;
+  });
+}
+
+int pfmd_get_gr_norm(pfmd_ctx* c, int inter, double* norm) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  auto& e = *c->e;
+  if (inter < 0 || inter >= static_cast<int>(e.inters.size())) return PFMD_E_PARAM;
+  auto& I = e.inters[static_cast<size_t>(inter)];
+  if (!I.norm.p) return PFMD_E_PARAM;
+  return guard(c, [&] {
+    const size_t rows = static_cast<size_t>(e.lists[static_cast<size_t>(I.lists[2])].d.rows);
+    std::vector<double4_32a> t(rows);
+    if (rows) CK(cudaMemcpyAsync(t.data(), I.norm.p, sizeof(double4_32a) * rows, cudaMemcpyDeviceToHost, e.st));
+    CK(cudaStreamSynchronize(e.st));
+    for (size_t r = 0; r < rows; ++r) {
+      norm[3 * r] = t[r].x;
+      norm[3 * r + 1] = t[r].y;
+      norm[3 * r + 2] = t[r].z;
+    }
+  });
+}
+
+int pfmd_set_group_n(pfmd_ctx* c, int group, int n) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  auto& e = *c->e;
+  if (group < 1 || group > static_cast<int>(e.groups.size())) return PFMD_E_PARAM;
+  return guard(c, [&] {
+    e.read_ctl();
+    const int cap = static_cast<int>(e.groups[static_cast<size_t>(group - 1)].idx.size());
+    e.hctl->group_n[group - 1] = std::max(0, std::min(n, cap));
+    e.upload_ctl_groups();
+    CK(cudaStreamSynchronize(e.st));
+  });
+}
+
+int pfmd_get_stream(pfmd_ctx* c, void** stream) {
+  if (!c || !c->e || !stream) return PFMD_E_STATE;
+  *stream = c->e->st;
+  return PFMD_OK;
+}
+
+int pfmd_kernel_launches(const pfmd_ctx* c, long long* n) {
+  if (!c || !c->e || !n) return PFMD_E_STATE;
+  *n = c->e->launches;
+  return PFMD_OK;
+}
+
+}  // extern "C"

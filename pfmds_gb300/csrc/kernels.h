@@ -1,0 +1,147 @@
+// Launch interface between the host engine and the CUDA kernels.
+//
+// Layouts in HBM:
+//   atoms      double4_32a pos/vel/frc [N] (w unused), double mass [N],
+//              float4 posf [N] (FP32 copy for the precision form and for the
+//              list-build prefilter)
+//   groups     int idx[cap] (0-based atom indexes); current sizes live in
+//              Ctl::group_n so captured graphs survive change_particle_group_N
+//   lists      slot-major: nlist[slot*stride + row] holds the group-2 index (jnd)
+//              of a row's neighbour, rows padded to `stride` (multiple of 32) so
+//              that a warp reading one slot of 32 consecutive rows is coalesced;
+//              nnum/pidx/lessnnum/bnd [rows]
+//   cells      per list: cell_start[ncell+1], cell_jnd[cap2] (group-2 indexes
+//              grouped by cell), cell_of[cap2], cell_count/cursor[ncell]
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dev.cuh"
+
+namespace pfmd {
+
+// Kernels launched by this library (incremented by every launcher, also while a
+// stream is being captured into a graph).
+extern long long g_kernel_launches;
+
+struct Atoms {
+  int N;
+  double4_32a* pos;
+  double4_32a* vel;
+  double4_32a* frc;
+  double* mass;
+  float4* posf;
+};
+
+struct ListDev {
+  int id;            // index into Ctl::maxnnum
+  int rows;          // nl%N
+  int nmax, stride;
+  int* nnum;
+  int* nlist;
+  int* pidx;
+  int* lessnnum;
+  int* bnd;          // first group-2 index whose atom index exceeds the row's atom
+  const int* row_idx;  // row group indexes (particle_index source)
+  const int* col_idx;  // column group indexes
+  int row_group, col_group;  // 0-based group numbers (sizes in Ctl::group_n)
+  int row_cap, col_cap;
+};
+
+struct CellGrid {
+  int nc[3];
+  int ncell;
+  float inv_cs[3];
+  int* start;   // [ncell+1]
+  int* count;   // [ncell]
+  int* cursor;  // [ncell]
+  int* jnd;     // [col_cap]
+  int* cell_of; // [col_cap]
+};
+
+struct GroupRef {
+  const int* idx;
+  int g;    // 0-based group number
+  int cap;  // capacity (launch size)
+};
+
+// potential parameters (plain FP64 copies; FP32 forms derived in the kernels)
+struct LJPar {
+  double eps, sig, R1, R2;
+  double c6, c12, c6t6, c12t12;  // lj1g
+};
+struct CosPar {  // ljc: eps sig delt; morsec: D r0 a delt
+  double eps, sig, delt, D, r0, a, R1, R2;
+  int simplified;
+};
+struct RJLPar {
+  double A0, xi, p, q, r0, R1, R2;
+};
+struct TBPar {
+  double d, s, b, r0, delt, a0, c0, d0, R1, R2, c02, d02;
+};
+
+struct ChangeSpec {
+  int from, to;  // 0-based groups
+  long long ts1, ts2, frec;
+  int to_cap;
+};
+
+enum Integ { I_NVE = 0, I_NVT = 1, I_NVMS = 2 };
+
+// ---------------- neighbour lists (nlist.cu) ----------------
+void launch_pack_posf(const Atoms& A, Ctl* ctl, cudaStream_t s);
+void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s);
+// Regular list (converse=0), or the converse of a list with src_rows rows
+// (converse=1, built at the source list's rebuild steps).  The plain form tests
+// candidates with an FP32 prefilter at r_cut + prefilter_margin, then exactly.
+void launch_build_list(bool prec, const ListDev& L, const CellGrid& cg, const Atoms& A, const Box& B, double rc,
+                       double prefilter_margin, int converse, int src_rows, Ctl* ctl, cudaStream_t s);
+// graphene nearest neighbours picked from a tb list (graphenenorm.f90:8-36)
+void launch_nn_select(bool prec, const ListDev& tb, const ListDev& nn, double rc_nn, const Atoms& A,
+                      const Box& B, Ctl* ctl, cudaStream_t s);
+// graphene normals (graphenenorm.f90:38-56); norm is double4_32a[rows]
+void launch_normals(bool prec, const ListDev& nn, double4_32a* norm, int simplified, const Atoms& A,
+                    const Box& B, Ctl* ctl, cudaStream_t s);
+void launch_nnum_max(const ListDev& L, Ctl* ctl, cudaStream_t s);
+
+// ---------------- forces and energies (forces.cu) ----------------
+void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const Atoms& A, const Box& B,
+               Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const LJPar& P, const Atoms& A,
+                 const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+// inv_eb: per-row 1/Eb scratch (double[rows] for plain, float[rows] for precision)
+void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const Atoms& A, const Box& B,
+                void* inv_eb, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B,
+               double* Bbuf, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
+                const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot,
+                int ekey, cudaStream_t s);
+
+// ---------------- integration and reductions (integrate.cu) ----------------
+// phase: 0 = group changes + out-of-cell check, 1 = nvms exit test, 2 = both
+void launch_step_begin(int phase, int n_changes, const ChangeSpec* changes, int nvms, double ms_de,
+                       Ctl* ctl, cudaStream_t s);
+void launch_check_all(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
+void launch_invert_z(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
+void launch_kick(const GroupRef& g, bool xyz, double ts2, const Atoms& A, Ctl* ctl, cudaStream_t s);
+void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posf, const Atoms& A, const Box& B,
+                  Ctl* ctl, cudaStream_t s);
+void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posf, int nhc_scale,
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
+void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
+                cudaStream_t s);
+void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
+void launch_ms(const GroupRef& g, bool xyz, const Atoms& A, Ctl* ctl, cudaStream_t s);
+void launch_zero_forces(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
+void launch_zero_momentum(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
+// energies at log/out/nvms steps: KE and temperature of the all-moving group,
+// Nose-Hoover energies (when nvt), potential/total/conserved sums
+void launch_energy_finalize(const GroupRef& moving, int n_inter, int n_nhc, int nvt, const Atoms& A,
+                            Ctl* ctl, cudaStream_t s);
+// output-block sums: force sum, mass-weighted position and velocity sums and the
+// mass of the all-atoms group; largest |v|^2 over every atom (red[0..8])
+void launch_out_reduce(const GroupRef& all, const Atoms& A, Ctl* ctl, cudaStream_t s);
+
+}  // namespace pfmd

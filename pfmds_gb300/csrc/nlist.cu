@@ -1,0 +1,377 @@
+// Neighbour lists on the device: cell binning, list build, graphene nearest
+// neighbours and normals.
+//
+// Reference: find_neighbours (md_neighbours.f90:56-100) tests every pair of the two
+// groups; converce_neighbour_list (md_neighbours.f90:128-160) transposes a list every
+// step; find_gr_nearest_neighbors / find_norm_in_graphene (graphenenorm.f90:8-56).
+//
+// Here the candidates come from a cell grid over the column group (cells at least
+// r_cut wide, so the 27 surrounding cells hold every partner), one warp per row
+// tests them, and the row is sorted by group-2 index before it is written, so a
+// row holds exactly the reference's entries in the reference's order.  In the
+// plain form an FP32 prefilter with a safety margin discards far candidates and
+// the survivors are tested with the exact FP64 predicate (mi_exact); the
+// precision form uses the FP32 predicate alone.  The converse list is built the
+// same way with the groups swapped at the source list's rebuild steps: its
+// membership equals the transpose because dr.dr is symmetric bit for bit.
+// Distances are not stored: every force kernel recomputes them from positions.
+#include <climits>
+
+#include "kernels.h"
+
+namespace pfmd {
+
+static constexpr int kBuildWarps = 8;
+
+__global__ void k_pack_posf(Atoms A) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.N) {
+    double4_32a p = A.pos[i];
+    A.posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+  }
+}
+
+__device__ __forceinline__ int cell_axis(float x, float inv, int nc) {
+  int c = (int)floorf(x * inv);
+  return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+__global__ void k_bin_count(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
+  if (ctl->stop) return;
+  int n2 = ctl->group_n[L.col_group];
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n2) return;
+  float4 p = A.posf[L.col_idx[j]];
+  int c = (cell_axis(p.z, cg.inv_cs[2], cg.nc[2]) * cg.nc[1] + cell_axis(p.y, cg.inv_cs[1], cg.nc[1])) * cg.nc[0] +
+          cell_axis(p.x, cg.inv_cs[0], cg.nc[0]);
+  cg.cell_of[j] = c;
+  atomicAdd(&cg.count[c], 1);
+}
+
+__global__ void k_bin_scan(CellGrid cg, Ctl* ctl) {
+  if (ctl->stop) return;
+  __shared__ int sh[1024];
+  const int n = cg.ncell, t = threadIdx.x, nt = blockDim.x;
+  const int chunk = (n + nt - 1) / nt;
+  const int b = t * chunk, e = min(n, b + chunk);
+  int s = 0;
+  for (int c = b; c < e; ++c) s += cg.count[c];
+  sh[t] = s;
+  __syncthreads();
+  for (int o = 1; o < nt; o <<= 1) {  // inclusive Hillis-Steele scan
+    int v = t >= o ? sh[t - o] : 0;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  int run = sh[t] - s;
+  for (int c = b; c < e; ++c) {
+    cg.start[c] = run;
+    cg.cursor[c] = run;
+    run += cg.count[c];
+  }
+  if (t == nt - 1) cg.start[n] = sh[t];
+}
+
+__global__ void k_bin_scatter(ListDev L, CellGrid cg, Ctl* ctl) {
+  if (ctl->stop) return;
+  int n2 = ctl->group_n[L.col_group];
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n2) return;
+  int slot = atomicAdd(&cg.cursor[cg.cell_of[j]], 1);
+  cg.jnd[slot] = j;
+}
+
+// One warp per row.  CAP >= nmax rounded up to a power of two.
+template <bool PREC, int CAP>
+__global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid cg, Atoms A, Box B, double rc2,
+                                                             float rcp2, int converse, int src_rows, Ctl* ctl) {
+  __shared__ int sbuf[kBuildWarps][CAP];
+  if (ctl->stop) return;
+  const int n1 = ctl->group_n[L.row_group];
+  const int n2 = ctl->group_n[L.col_group];
+  if (!converse) {
+    // update_neighbour_list only acts when both groups and the list are non-empty
+    if (n1 == 0 || n2 == 0 || L.rows == 0) return;
+  } else {
+    // converce_neighbour_list acts when group 2, the source list and itself are
+    if (n1 == 0 || src_rows == 0 || L.rows == 0) return;
+  }
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int row = blockIdx.x * kBuildWarps + wib;
+  if (row == 0 && lane == 0 && n1 > L.rows) set_error(ctl, ST_PARAM, EK_NONE, L.id, n1, L.rows);
+  if (row >= L.rows) return;
+  if (row >= n1) {
+    // rows past the group: the converse list clears them, a regular list keeps them
+    if (converse && lane == 0) L.nnum[row] = 0;
+    return;
+  }
+  int* buf = sbuf[wib];
+  const int ai = L.row_idx[row];
+  const float4 pif = A.posf[ai];
+  double4_32a pi = make_double4_32a(0, 0, 0, 0);
+  if (!PREC) pi = A.pos[ai];
+  const int c0[3] = {cell_axis(pif.x, cg.inv_cs[0], cg.nc[0]), cell_axis(pif.y, cg.inv_cs[1], cg.nc[1]),
+                     cell_axis(pif.z, cg.inv_cs[2], cg.nc[2])};
+  int lo[3], hi[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (cg.nc[k] < 3) {
+      lo[k] = 0;
+      hi[k] = cg.nc[k] - 1;
+    } else {
+      lo[k] = c0[k] - 1;
+      hi[k] = c0[k] + 1;
+    }
+  }
+  int cnt = 0;
+  for (int z = lo[2]; z <= hi[2]; ++z) {
+    const int cz = (z + cg.nc[2]) % cg.nc[2];
+    for (int y = lo[1]; y <= hi[1]; ++y) {
+      const int cy = (y + cg.nc[1]) % cg.nc[1];
+      for (int x = lo[0]; x <= hi[0]; ++x) {
+        const int cx = (x + cg.nc[0]) % cg.nc[0];
+        const int c = (cz * cg.nc[1] + cy) * cg.nc[0] + cx;
+        const int s = cg.start[c], e = cg.start[c + 1];
+        for (int k0 = s; k0 < e; k0 += 32) {
+          const int k = k0 + lane;
+          bool hit = false;
+          int jnd = 0;
+          if (k < e) {
+            jnd = cg.jnd[k];
+            const int aj = L.col_idx[jnd];
+            if (aj != ai) {
+              float d[3];
+              float r2f = mi_f32(pif, A.posf[aj], B, d);
+              if (PREC) {
+                hit = r2f < rcp2;
+              } else if (r2f < rcp2) {
+                double dd[3];
+                hit = mi_exact(pi, A.pos[aj], B, dd) < rc2;
+              }
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, hit);
+          if (hit) {
+            const int p = cnt + __popc(m & ((1u << lane) - 1u));
+            if (p < CAP) buf[p] = jnd;
+          }
+          cnt += __popc(m);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (cnt > L.nmax) {
+    // 'error: too many neighbours', ind, nnumind  (md_neighbours.f90:80, :151)
+    if (lane == 0) set_error(ctl, ST_NLIST_OVERFLOW, converse ? EK_CONVERSE_OVF : EK_OVERFLOW, L.id, row + 1, L.nmax + 1);
+    return;
+  }
+  // bitonic sort of buf[0..n) ascending, padded with INT_MAX
+  int n = 1;
+  while (n < cnt) n <<= 1;
+  for (int p = cnt + lane; p < n; p += 32) buf[p] = INT_MAX;
+  __syncwarp();
+  for (int k = 2; k <= n; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const int a = buf[i], b = buf[ixj];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            buf[i] = b;
+            buf[ixj] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // lessnnum: entries before the first neighbour with a larger atom index
+  // (md_neighbours.f90:78); the converse list leaves it at zero as the reference does
+  int less = cnt;
+  if (!converse) {
+    for (int p0 = 0; p0 < cnt; p0 += 32) {
+      const int p = p0 + lane;
+      const bool gt = p < cnt && ai < L.col_idx[buf[p]];
+      const unsigned m = __ballot_sync(0xffffffffu, gt);
+      if (m) {
+        less = p0 + __ffs(m) - 1;
+        break;
+      }
+    }
+  }
+  for (int p = lane; p < cnt; p += 32) L.nlist[(size_t)p * L.stride + row] = buf[p];
+  if (lane == 0) {
+    L.nnum[row] = cnt;
+    L.pidx[row] = ai;
+    L.lessnnum[row] = converse ? 0 : less;
+    L.bnd[row] = (less < cnt) ? buf[less] : INT_MAX;
+  }
+}
+
+template <bool PREC>
+__global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= tb.rows) return;
+  const int ai = tb.row_idx[i];
+  const int n = tb.nnum[i];
+  int k = 0;
+  bool bad = false;
+  for (int p = 0; p < n; ++p) {
+    const int jnd = tb.nlist[(size_t)p * tb.stride + i];
+    const int aj = tb.col_idx[jnd];
+    bool in;
+    if (PREC) {
+      float d[3];
+      float r2 = mi_f32(A.posf[ai], A.posf[aj], B, d);
+      in = sqrtf(r2) < (float)rcnn;
+    } else {
+      double d[3];
+      double r2 = mi_exact(A.pos[ai], A.pos[aj], B, d);
+      in = sqrt(r2) < rcnn;
+    }
+    if (in) {
+      k = k + 1;
+      if (k <= 3) {
+        nn.nlist[(size_t)(k - 1) * nn.stride + i] = jnd;
+      } else {
+        set_error(ctl, ST_GR_NN, EK_GR_TOO_MANY, i + 1, 0, 0);
+        bad = true;
+        break;
+      }
+    }
+  }
+  if (!bad && k != 3) set_error(ctl, ST_GR_NN, EK_GR_NOT_ENOUGH, i + 1, k, 0);
+  nn.nnum[i] = 3;
+}
+
+template <bool PREC>
+__global__ void k_normals(ListDev nn, double4_32a* norm, int simplified, Atoms A, Box B, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn.rows) return;
+  if (simplified) {
+    norm[i] = make_double4_32a(0.0, 0.0, 1.0, 0.0);
+    return;
+  }
+  // rows past the row group keep zero vectors (the reference normalises a zero
+  // vector there too)
+  const bool has_row = i < nn.row_cap;
+  const int ai = has_row ? nn.row_idx[i] : 0;
+  const int cnt = has_row ? nn.nnum[i] : 0;
+  double d[3][3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    d[q][0] = d[q][1] = d[q][2] = 0.0;
+    if (q < cnt) {
+      const int aj = nn.col_idx[nn.nlist[(size_t)q * nn.stride + i]];
+      if (PREC) {
+        float df[3];
+        mi_f32(A.posf[ai], A.posf[aj], B, df);
+        d[q][0] = df[0];
+        d[q][1] = df[1];
+        d[q][2] = df[2];
+      } else {
+        mi_exact(A.pos[ai], A.pos[aj], B, d[q]);
+      }
+    }
+  }
+  double d12[3], d31[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    d12[k] = d[1][k] - d[0][k];
+    d31[k] = d[0][k] - d[2][k];
+  }
+  double g0 = d12[1] * d31[2] - d12[2] * d31[1];
+  double g1 = d12[2] * d31[0] - d12[0] * d31[2];
+  double g2 = d12[0] * d31[1] - d12[1] * d31[0];
+  if (g2 < 0.0) {
+    g0 = -g0;
+    g1 = -g1;
+    g2 = -g2;
+  }
+  const double nr = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+  norm[i] = make_double4_32a(g0 / nr, g1 / nr, g2 / nr, 0.0);
+}
+
+__global__ void k_nnum_max(ListDev L, Ctl* ctl) {
+  int m = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.rows; i += gridDim.x * blockDim.x) m = max(m, L.nnum[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(&ctl->maxnnum[L.id], m);
+}
+
+// ---------------- launchers ----------------
+static inline int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+void launch_pack_posf(const Atoms& A, Ctl* ctl, cudaStream_t s) {
+  (void)ctl;
+  if (A.N > 0) { k_pack_posf<<<blocks_for(A.N, 256), 256, 0, s>>>(A); ++g_kernel_launches; }
+}
+
+void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s) {
+  cudaMemsetAsync(cg.count, 0, sizeof(int) * (size_t)cg.ncell, s);
+  if (L.col_cap > 0) { k_bin_count<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, A, ctl); ++g_kernel_launches; }
+  { k_bin_scan<<<1, 1024, 0, s>>>(cg, ctl); ++g_kernel_launches; }
+  if (L.col_cap > 0) { k_bin_scatter<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, ctl); ++g_kernel_launches; }
+}
+
+template <bool PREC>
+static void build_dispatch(const ListDev& L, const CellGrid& cg, const Atoms& A, const Box& B, double rc2,
+                           float rcp2, int converse, int src_rows, Ctl* ctl, cudaStream_t s) {
+  const int grid = blocks_for(L.rows, kBuildWarps);
+  const int bs = kBuildWarps * 32;
+  if (grid == 0) return;
+  if (L.nmax <= 64)
+    { k_build<PREC, 64><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+  else if (L.nmax <= 128)
+    { k_build<PREC, 128><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+  else if (L.nmax <= 256)
+    { k_build<PREC, 256><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+  else if (L.nmax <= 512)
+    { k_build<PREC, 512><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+  else
+    { k_build<PREC, 1024><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+}
+
+void launch_build_list(bool prec, const ListDev& L, const CellGrid& cg, const Atoms& A, const Box& B, double rc,
+                       double prefilter_margin, int converse, int src_rows, Ctl* ctl, cudaStream_t s) {
+  const double rc2 = rc * rc;
+  if (prec) {
+    build_dispatch<true>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
+  } else {
+    const double rp = rc + prefilter_margin;
+    build_dispatch<false>(L, cg, A, B, rc2, (float)(rp * rp), converse, src_rows, ctl, s);
+  }
+}
+
+void launch_nn_select(bool prec, const ListDev& tb, const ListDev& nn, double rc_nn, const Atoms& A,
+                      const Box& B, Ctl* ctl, cudaStream_t s) {
+  if (tb.rows == 0) return;
+  if (prec)
+    { k_nn_select<true><<<blocks_for(tb.rows, 128), 128, 0, s>>>(tb, nn, rc_nn, A, B, ctl); ++g_kernel_launches; }
+  else
+    { k_nn_select<false><<<blocks_for(tb.rows, 128), 128, 0, s>>>(tb, nn, rc_nn, A, B, ctl); ++g_kernel_launches; }
+}
+
+void launch_normals(bool prec, const ListDev& nn, double4_32a* norm, int simplified, const Atoms& A, const Box& B,
+                    Ctl* ctl, cudaStream_t s) {
+  if (nn.rows == 0) return;
+  if (prec)
+    { k_normals<true><<<blocks_for(nn.rows, 128), 128, 0, s>>>(nn, norm, simplified, A, B, ctl); ++g_kernel_launches; }
+  else
+    { k_normals<false><<<blocks_for(nn.rows, 128), 128, 0, s>>>(nn, norm, simplified, A, B, ctl); ++g_kernel_launches; }
+}
+
+void launch_nnum_max(const ListDev& L, Ctl* ctl, cudaStream_t s) {
+  if (L.rows == 0) return;
+  int g = blocks_for(L.rows, 256);
+  if (g > 256) g = 256;
+  { k_nnum_max<<<g, 256, 0, s>>>(L, ctl); ++g_kernel_launches; }
+}
+
+}  // namespace pfmd
