@@ -1,0 +1,330 @@
+"""Benchmark: atom-steps/s of PFMDS's MD hot path on one GB300.
+
+Workload (the configuration the metric is quoted on): Cu fcc (001) slab of
+32x32x16 cubic cells = 65,536 atoms under rjl (A 0.0855 eV, xi 1.224 eV,
+p 10.96, q 2.278, r0 2.556 A, switch 4.5-5.0 A), list r_cut 5.5 A rebuilt every
+10 steps, bottom two (001) layers fixed, random 0.05 A displacements, 300 K,
+NVE with dt 1 fs.  Synthetic seeded input in PFMDS's own file formats.
+
+One benchmark step = 10 MD steps (one list-rebuild period, ending with an energy
+evaluation), run on the device from inputs already in HBM; L2 is flushed between
+timed steps.  `value` is the precision form (FP32 forces with compensated sums,
+FP64 integration and energies); the plain FP64 form is reported beside it with
+the precision form's force RMSE against it.  `e2e` runs the same steps through the
+C ABI with host buffers: set positions and velocities, advance, read positions,
+velocities, forces and energies back.
+
+--impl reference times the CPU oracle (the FP64 restatement of the reference's
+Fortran/OpenMP algorithm, O(N^2) list search included) on all host cores.
+Several GPUs: independent replicas, one per rank ("replicas only").
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "atom-steps/s on 1 GB300: plain vs chosen form at stated force RMSE and NVE drift"
+WORKLOAD = ("Cu fcc (001) slab 32x32x16 cells = 65,536 atoms, rjl (r_cut 5.0 A, list 5.5 A every 10 steps), "
+            "bottom 2 layers fixed, 300 K, NVE dt 1 fs")
+MD_PER_STEP = 10
+DT_FS = 1.0
+
+
+def make_workload(d, seed=2024):
+    from pfmds_gb300 import configs
+    return configs.cu_slab(d, nx=32, ny=32, nz=16, seed=seed, temperature=300.0, dt=DT_FS, steps=10 ** 8,
+                           log_period=MD_PER_STEP, integrator="nve")
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while running."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_rate(d, threads, md_steps):
+    """Atom-steps/s of the CPU oracle on the workload (set-up excluded)."""
+    from oracle.pyoracle import Oracle
+    o = Oracle(d, out_period=10 ** 9, threads=threads)
+    n = o.natoms
+    t0 = time.perf_counter()
+    o.run(md_steps)
+    t = time.perf_counter() - t0
+    return n * md_steps / t, t
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    dist.init_process_group(backend)
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def traffic_from_profiles(kernel, form):
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        j = json.load(f)
+    e = j.get(f"{form}:{kernel}")
+    return None if e is None else float(e)
+
+
+def run_ours(args):
+    import pfmds_gb300 as pf
+    rank, world, dist = dist_init()
+    if world > 1:
+        os.environ.setdefault("LOCAL_RANK", str(rank))
+    device = int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0
+    K, W, S = args.steps, args.warmup, MD_PER_STEP
+    hbm_peak, peak_kind = peaks()
+    with tempfile.TemporaryDirectory() as d:
+        make_workload(d, seed=2024 + rank)
+        sim = pf.Simulation(d, form="precision", out_period=10 ** 9, device=device)
+        n = sim.natoms
+        for _ in range(W):
+            sim.advance_timed(S)
+        e0 = sim.energies()["conserved"]
+        barrier(dist)
+        launches0 = sim.kernel_launches
+        total_ms = 0.0
+        with ClockSampler() as clk:
+            for _ in range(K):
+                sim.flush_l2()
+                total_ms += sim.advance_timed(S)
+        launches = sim.kernel_launches - launches0
+        e1 = sim.energies()["conserved"]
+        total_ms = dist_max(dist, total_ms)
+        atoms_all = dist_sum(dist, float(n))
+        value = atoms_all * S * K / (total_ms / 1e3)
+        drift = (e1 - e0) / n / (K * S * DT_FS * 1e-6)  # eV/atom/ns over the timed window
+
+        # roofline of the dominant kernel: time shares per MD step
+        cands = {}
+        for name, per_md in (("rjl_force", 1.0), ("rjl_density", 1.0), ("lists", 1.0 / 10)):
+            ms, b = sim.time_kernel(name, reps=50)
+            cands[name] = (ms, b, ms * per_md)
+        dom = max(cands, key=lambda k: cands[k][2])
+        ms, b, _ = cands[dom]
+        achieved = b / (ms * 1e-3) / 1e9
+        traffic = traffic_from_profiles(dom, "precision")
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
+                    "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                    "traffic": traffic, "alg_bytes_per_launch": int(b), "ms_per_launch": ms,
+                    "kernel_ms_per_md_step": {k: round(v[2], 5) for k, v in cands.items()}}
+
+        # end to end through the C ABI with host buffers
+        p0, v0, _ = sim.state()
+        t_e2e = 0.0
+        for _ in range(max(1, K)):
+            t0 = time.perf_counter()
+            sim.set_state(p0, v0)
+            sim.advance(S)
+            p, v, f = sim.state()
+            sim.energies()
+            t_e2e += time.perf_counter() - t0
+        t_e2e = dist_max(dist, t_e2e)
+        e2e = {"value": atoms_all * S * max(1, K) / t_e2e, "unit": "atom-steps/s",
+               "h2d_bytes_per_step": 2 * 24 * n, "d2h_bytes_per_step": 3 * 24 * n + 8 * 6,
+               "api": "pfmd_set_state + pfmd_advance + pfmd_get_state + pfmd_energies"}
+
+        # plain FP64 form beside it, and the precision form's force error against it
+        plain = pf.Simulation(d, form="plain", out_period=10 ** 9, device=device)
+        for _ in range(max(1, W // 2)):
+            plain.advance(S)
+        pms = 0.0
+        Kp = max(2, K // 2)
+        for _ in range(Kp):
+            plain.flush_l2()
+            pms += plain.advance_timed(S)
+        pms = dist_max(dist, pms)
+        plain_rate = atoms_all * S * Kp / (pms / 1e3)
+        ref_p = pf.Simulation(d, form="plain", out_period=10 ** 9, device=device)
+        pre_p = pf.Simulation(d, form="precision", out_period=10 ** 9, device=device)
+        ref_p.advance(1)
+        pre_p.advance(1)
+        _, _, fp = ref_p.state()
+        _, _, fq = pre_p.state()
+        import numpy as np
+        rmse = float(np.sqrt(((fq - fp) ** 2).mean()))
+        frms = float(np.sqrt((fp ** 2).mean()))
+        plain_line = {"value": plain_rate, "ms_per_step": pms / Kp, "dtype": "f64",
+                      "speedup_of_precision_form": value / plain_rate}
+
+        cpu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            rate, t = cpu_oracle_rate(d, threads, args.cpu_md_steps)
+            cpu = {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                   "sample": f"{args.cpu_md_steps} MD steps of the same 65,536-atom workload "
+                             f"({t:.1f} s, O(N^2) list search at step 0 as the reference), FP64 oracle, OpenMP"}
+        clocks = clk.summary()
+        for s in (sim, plain, ref_p, pre_p):
+            s.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": total_ms / K, "ms_per_md_step": total_ms / K / S, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "dtype_detail": "precision form: FP32 pair forces with Kahan sums; FP64 positions, velocities, energies",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "precision", "md_steps_per_step": S,
+                   "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}",
+                   "atoms_per_replica": n},
+        "force_rmse": {"value": rmse, "rel": rmse / frms, "unit": "eV/A", "against": "plain FP64 form"},
+        "nve_drift": {"value": drift, "unit": "eV/atom/ns", "window_fs": K * S * DT_FS},
+        "plain": plain_line,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    K, W, S = args.steps, args.warmup, MD_PER_STEP
+    from oracle.pyoracle import Oracle
+    with tempfile.TemporaryDirectory() as d:
+        make_workload(d)
+        o = Oracle(d, out_period=10 ** 9, threads=threads)
+        n = o.natoms
+        for _ in range(W):
+            o.run(S)
+        t0 = time.perf_counter()
+        for _ in range(K):
+            o.run(S)
+        t = time.perf_counter() - t0
+    value = n * S * K / t
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "atom-steps/s", "n_gpus": 0,
+            "steps": K, "warmup": W, "ms_per_step": t / K * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "reference FP64 algorithm (CPU oracle)",
+                       "md_steps_per_step": S},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{K} timed steps of {S} MD steps after {W} warm-up steps"},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-md-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    import __graft_entry__
+    __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -150,6 +150,30 @@ int pfmd_get_stream(pfmd_ctx* ctx, void** stream);
  * once per replay). */
 int pfmd_kernel_launches(const pfmd_ctx* ctx, long long* n);
 
+/* ---- measurement ----------------------------------------------------------
+ * No reference counterpart (PFMDS times phases with omp_get_wtime,
+ * md_simulation.f90:104-202); these support the benchmark. */
+
+/* pfmd_advance with CUDA events recorded on the context's stream right before
+ * the first and right after the last kernel of the call; *device_ms is the
+ * elapsed device time between them. */
+int pfmd_advance_timed(pfmd_ctx* ctx, long long max_steps, int* finished, double* device_ms);
+
+/* Times `reps` back-to-back launches of one kernel group on the context's
+ * stream with CUDA events and restores the forces afterwards.  name: "forces"
+ * (zero_forces + every interaction's force kernels), "lists" (every list
+ * rebuild), or one kernel: "lj", "lj1g", "rjl_density", "rjl_force",
+ * "tb_bond", "tb_force", "cos_graphene", "cos_metal" (first interaction of that
+ * kind).  *ms = average per launch; *bytes = the kernel's algorithmic HBM bytes
+ * per launch (list entries, per-row data and force updates; neighbour positions
+ * counted as cache-resident). */
+int pfmd_time_kernel(pfmd_ctx* ctx, const char* name, int reps, double* ms, double* bytes);
+
+/* Writes `bytes` bytes of a scratch buffer on the context's stream, evicting the
+ * step's working set from L2 between timed runs.  The buffer is allocated on the
+ * first call and kept. */
+int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,7 +30,8 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_advance", "pfmd_finish", "pfmd_md", "pfmd_run_md_simulation", "pfmd_natoms", "pfmd_md_step",
            "pfmd_get_state", "pfmd_set_state", "pfmd_energies", "pfmd_compute", "pfmd_ninteractions",
            "pfmd_nlist_shape", "pfmd_get_nlist", "pfmd_nlist_load", "pfmd_get_gr_norm", "pfmd_set_group_n",
-           "pfmd_get_stream", "pfmd_kernel_launches")
+           "pfmd_get_stream", "pfmd_kernel_launches", "pfmd_advance_timed", "pfmd_time_kernel",
+           "pfmd_flush_l2")
 
 _LIB = None
 
@@ -83,6 +84,9 @@ def load(path=LIB_PATH):
     L.pfmd_set_group_n.argtypes = [vp, C.c_int, C.c_int]
     L.pfmd_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.pfmd_kernel_launches.argtypes = [vp, llp]
+    L.pfmd_advance_timed.argtypes = [vp, C.c_longlong, ip, dp]
+    L.pfmd_time_kernel.argtypes = [vp, C.c_char_p, C.c_int, dp, dp]
+    L.pfmd_flush_l2.argtypes = [vp, C.c_longlong]
     _LIB = L
     return L
 
@@ -234,6 +238,22 @@ class Simulation:
         s = C.c_void_p()
         self._check(load().pfmd_get_stream(self._h, C.byref(s)))
         return s.value or 0
+
+    def advance_timed(self, n):
+        """advance(n) and the device milliseconds between its first and last kernel."""
+        f, ms = C.c_int(0), C.c_double(0.0)
+        self._check(load().pfmd_advance_timed(self._h, int(n), C.byref(f), C.byref(ms)))
+        self.finished = bool(f.value)
+        return ms.value
+
+    def time_kernel(self, name, reps=20):
+        """(average ms per launch, algorithmic bytes per launch) of one kernel group."""
+        ms, b = C.c_double(), C.c_double()
+        self._check(load().pfmd_time_kernel(self._h, name.encode(), int(reps), C.byref(ms), C.byref(b)))
+        return ms.value, b.value
+
+    def flush_l2(self, nbytes=256 << 20):
+        self._check(load().pfmd_flush_l2(self._h, int(nbytes)))
 
     @property
     def kernel_launches(self):

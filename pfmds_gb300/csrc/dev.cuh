@@ -86,16 +86,20 @@ struct Ctl {
   double partial[PFMD_PARTIALS];  // per-block partial sums of the grid reductions
 };
 
+// Box lengths, halves, and the fixed-point scales of the force-side positions:
+// a coordinate is stored as round(x * 2^32 / L) modulo 2^32 (posq), so the
+// difference of two stored coordinates, taken modulo 2^32 as a signed 32-bit
+// integer, is the minimum-image separation in units of L / 2^32.
 struct Box {
   double L[3], h[3];
-  float Lf[3], hf[3];
+  double qinv[3];  // 2^32 / L
+  float qs[3];     // L / 2^32
 };
 
 // ---------------------------------------------------------------------------
 // minimum image
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double sgn1(double x) { return copysign(1.0, x); }
-__device__ __forceinline__ float sgn1f(float x) { return copysignf(1.0f, x); }
 
 // d - h*(sign(1,d-h)+sign(1,d+h)), rounded exactly as written.
 __device__ __forceinline__ double mi_axis_exact(double d, double h) {
@@ -110,15 +114,22 @@ __device__ __forceinline__ double mi_exact(const double4_32a& a, const double4_3
   dr[2] = mi_axis_exact(__dsub_rn(b.z, a.z), B.h[2]);
   return __dadd_rn(__dadd_rn(__dmul_rn(dr[0], dr[0]), __dmul_rn(dr[1], dr[1])), __dmul_rn(dr[2], dr[2]));
 }
-__device__ __forceinline__ float mi_axis_f(float d, float h) {
-  float s = sgn1f(d - h) + sgn1f(d + h);
-  return d - h * s;
+// Fixed-point coordinate of x (wraps modulo 2^32, i.e. periodically).
+__device__ __forceinline__ int quantize(double x, double qinv) {
+  return (int)(unsigned int)(unsigned long long)__double2ll_rn(x * qinv);
 }
-__device__ __forceinline__ float mi_f32(const float4& a, const float4& b, const Box& B, float dr[3]) {
-  dr[0] = mi_axis_f(b.x - a.x, B.hf[0]);
-  dr[1] = mi_axis_f(b.y - a.y, B.hf[1]);
-  dr[2] = mi_axis_f(b.z - a.z, B.hf[2]);
+// Minimum-image b - a from fixed-point coordinates, in FP32 (precision form and
+// the list-build prefilter).  Resolution L / 2^32; the relative error of dr is
+// that of one int->float conversion and one multiply.
+__device__ __forceinline__ float mi_q(const int4& a, const int4& b, const Box& B, float dr[3]) {
+  dr[0] = (float)(int)((unsigned int)b.x - (unsigned int)a.x) * B.qs[0];
+  dr[1] = (float)(int)((unsigned int)b.y - (unsigned int)a.y) * B.qs[1];
+  dr[2] = (float)(int)((unsigned int)b.z - (unsigned int)a.z) * B.qs[2];
   return dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+}
+// Cell of a fixed-point coordinate on a grid of nc cells: floor(frac * nc), exact.
+__device__ __forceinline__ int cell_q(int xq, int nc) {
+  return (int)(((unsigned long long)(unsigned int)xq * (unsigned long long)nc) >> 32);
 }
 
 // ---------------------------------------------------------------------------

@@ -133,7 +133,7 @@ class Engine {
   Atoms A{};
   DBuf<double4_32a> pos, vel, frc;
   DBuf<double> mass;
-  DBuf<float4> posf;
+  DBuf<int4> posq;
   std::vector<GroupH> groups;
   std::vector<ListH> lists;
   std::vector<InterH> inters;
@@ -172,12 +172,19 @@ class Engine {
   };
   std::map<std::string, GraphEntry> graphs;
   long long launches = 0;
+  // device timing of advance (events recorded on st around the enqueued work)
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timing = false, timing_started = false;
+  DBuf<unsigned char> flush_buf;
+  int flush_seq = 0;
 
   ~Engine();
   void create(const std::string& ip, const std::string& sf, const pfmd_options& o);
   void advance(long long max_steps, int* fin);
   void finish();
   void compute(bool rebuild, double* e_inter);
+  double time_kernel(const std::string& name, int reps, double* bytes);
+  double kernel_bytes(const std::string& name);
 
   // helpers
   void out(const std::string& s) { obuf += s; }
@@ -210,6 +217,8 @@ class Engine {
 };
 
 Engine::~Engine() {
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
   for (auto& kv : graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   if (log) std::fclose(log);
@@ -274,8 +283,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   for (int k = 0; k < 3; ++k) {
     box.L[k] = S.xyz.box[k];
     box.h[k] = 0.5 * S.xyz.box[k];
-    box.Lf[k] = static_cast<float>(box.L[k]);
-    box.hf[k] = static_cast<float>(box.h[k]);
+    box.qinv[k] = 4294967296.0 / box.L[k];
+    box.qs[k] = static_cast<float>(box.L[k] / 4294967296.0);
   }
   // groups: create_particle_group (md_general.f90:57-80)
   if (S.group_types.size() > PFMD_MAX_GROUPS) throw Error(PFMD_E_PARAM, "error: too many groups");
@@ -507,7 +516,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   vel.alloc(static_cast<size_t>(std::max(N, 1)));
   frc.alloc(static_cast<size_t>(std::max(N, 1)));
   mass.alloc(static_cast<size_t>(std::max(N, 1)));
-  posf.alloc(static_cast<size_t>(std::max(N, 1)));
+  posq.alloc(static_cast<size_t>(std::max(N, 1)));
   {
     std::vector<double4_32a> tp(static_cast<size_t>(N)), tv(static_cast<size_t>(N));
     for (int i = 0; i < N; ++i) {
@@ -520,7 +529,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     mass.upload(hm.data(), hm.size(), st);
     CK(cudaStreamSynchronize(st));
   }
-  A = Atoms{N, pos.p, vel.p, frc.p, mass.p, posf.p};
+  A = Atoms{N, pos.p, vel.p, frc.p, mass.p, posq.p};
   for (auto& g : groups) {
     g.d.alloc(std::max<size_t>(g.idx.size(), 1));
     g.d.upload(g.idx.data(), g.idx.size(), st);
@@ -563,7 +572,6 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
         L.cg.nc[k] = std::max(1, L.cg.nc[k] / 2);
       }
       L.cg.ncell = static_cast<int>(ncell);
-      for (int k = 0; k < 3; ++k) L.cg.inv_cs[k] = static_cast<float>(L.cg.nc[k] / box.L[k]);
       L.cstart.alloc(static_cast<size_t>(ncell) + 1);
       L.ccount.alloc(static_cast<size_t>(ncell));
       L.ccursor.alloc(static_cast<size_t>(ncell));
@@ -609,7 +617,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     for (int i = 1; i < d.M; ++i) d.q[i] = d.q[0] / (3.0 * d.L);
   }
   CK(cudaMemcpyAsync(ctl, hctl, ctl_head, cudaMemcpyHostToDevice, st));
-  launch_pack_posf(A, ctl, st);
+  launch_pack_posq(A, box, ctl, st);
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
 
@@ -877,6 +885,16 @@ static std::string plan_key(const StepPlan& p) {
 }
 
 void Engine::run_plans(const std::vector<StepPlan>& plans) {
+  if (timing && !timing_started) {
+    CK(cudaEventRecord(ev0, st));
+    timing_started = true;
+  }
+  struct RecordEnd {
+    Engine* e;
+    ~RecordEnd() {
+      if (e->timing) cudaEventRecord(e->ev1, e->st);
+    }
+  } record_end{this};
   std::string key = std::to_string(integrator_index) + ":";
   for (const auto& p : plans) key += plan_key(p);
   GraphEntry* ge = nullptr;
@@ -1154,6 +1172,141 @@ void Engine::compute(bool rebuild, double* e_inter) {
     for (size_t k = 0; k < inters.size(); ++k) e_inter[k] = hctl->e_inter[k];
 }
 
+static long long host_nnz(const ListH& L, cudaStream_t st) {
+  std::vector<int> n(static_cast<size_t>(L.d.rows));
+  if (!n.empty()) CK(cudaMemcpyAsync(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  long long t = 0;
+  for (int v : n) t += v;
+  return t;
+}
+
+// Algorithmic HBM bytes of one launch: list entries (4 B each), per-row list data
+// (nnum, pidx: 8 B), the row atom's position (32 B plain, 16 B fixed-point), its
+// force update (read + write of a double4: 64 B) and kernel-specific per-row
+// arrays.  Neighbour positions and neighbour per-row data are counted as cache
+// resident (they are re-read by many rows).
+double Engine::kernel_bytes(const std::string& name) {
+  const double P = prec ? 16.0 : 32.0, F = 64.0, IE = prec ? 4.0 : 8.0;
+  auto row_bytes = [&](const ListH& L, double extra_row, double extra_entry) {
+    const double R = L.d.rows, nnz = static_cast<double>(host_nnz(L, st));
+    return 8.0 * R + 4.0 * nnz + P * R + extra_row * R + extra_entry * nnz;
+  };
+  double b = 0.0;
+  for (auto& I : inters) {
+    const ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
+    const int k = I.spec.kind;
+    if (k == pfmd_io::K_LJ && (name == "lj" || name == "forces")) {
+      b += row_bytes(L1, F, 0) + row_bytes(lists[static_cast<size_t>(I.lists[1])], F, 0);
+      if (name == "lj") return b;
+    }
+    if (k == pfmd_io::K_LJ1G && (name == "lj1g" || name == "forces")) {
+      b += row_bytes(L1, F + 4.0, 0);
+      if (name == "lj1g") return b;
+    }
+    if (k == pfmd_io::K_RJL) {
+      if (name == "rjl_density") return row_bytes(L1, IE, 0);
+      if (name == "rjl_force") return row_bytes(L1, IE + F, 0);
+      if (name == "forces") b += row_bytes(L1, IE, 0) + row_bytes(L1, IE + F, 0);
+    }
+    if (k == pfmd_io::K_TB) {
+      if (name == "tb_bond") return row_bytes(L1, 0, 8.0);
+      if (name == "tb_force") return row_bytes(L1, F, 8.0);
+      if (name == "forces") b += row_bytes(L1, 0, 8.0) + row_bytes(L1, F, 8.0);
+    }
+    if (k == pfmd_io::K_LJC || k == pfmd_io::K_MORSEC) {
+      const ListH& L2 = lists[static_cast<size_t>(I.lists[1])];
+      if (name == "cos_graphene") return row_bytes(L1, F + 32.0, 0);
+      if (name == "cos_metal") return row_bytes(L2, F, 0);
+      if (name == "forces") b += row_bytes(L1, F + 32.0, 0) + row_bytes(L2, F, 0);
+    }
+  }
+  if (name == "forces") {
+    b += 32.0 * static_cast<double>(groups[static_cast<size_t>(S.all_atoms - 1)].idx.size());  // zero_forces
+    return b;
+  }
+  if (name == "lists") {
+    for (auto& L : lists) {
+      if (L.kind == L_NN_TB) continue;
+      const double C = L.d.col_cap, R = L.d.rows, nnz = static_cast<double>(host_nnz(L, st));
+      // binning: posq + cell id + count + scatter; build: posq, list entries, row data
+      b += 28.0 * C + P * R + 4.0 * nnz + 16.0 * R;
+    }
+    return b;
+  }
+  return b;
+}
+
+// Launches `reps` times one kernel group between two events on st.
+double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
+  if (reps < 1) reps = 1;
+  if (!ev0) {
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+  }
+  auto once = [&]() -> bool {
+    if (name == "forces") {
+      launch_zero_forces(gref(S.all_atoms), A, ctl, st);
+      enqueue_forces(false);
+      return true;
+    }
+    if (name == "lists") {
+      StepPlan p;
+      p.step = 0;
+      p.first = true;
+      p.energy = p.out = p.zero_mom = p.check_all = false;
+      p.rebuild.assign(lists.size(), 1);
+      enqueue_lists(p);
+      return true;
+    }
+    for (size_t k = 0; k < inters.size(); ++k) {
+      InterH& I = inters[k];
+      const ListDev& L1 = lists[static_cast<size_t>(I.lists[0])].d;
+      const int kind = I.spec.kind;
+      const int eslot = 4;
+      if (kind == pfmd_io::K_LJ && name == "lj") {
+        launch_lj(prec, false, L1, I.lj, A, box, ctl, eslot, 0, st);
+        launch_lj(prec, false, lists[static_cast<size_t>(I.lists[1])].d, I.lj, A, box, ctl, eslot, 0, st);
+        return true;
+      }
+      if (kind == pfmd_io::K_LJ1G && name == "lj1g") {
+        launch_lj1g(prec, false, I.general, L1, I.lj, A, box, ctl, eslot, 0, st);
+        return true;
+      }
+      if (kind == pfmd_io::K_RJL && (name == "rjl_density" || name == "rjl_force")) {
+        launch_rjl(prec, false, L1, I.rjl, A, box, I.scratch.p, ctl, eslot, 0, st, name == "rjl_density" ? 1 : 2);
+        return true;
+      }
+      if (kind == pfmd_io::K_TB && (name == "tb_bond" || name == "tb_force")) {
+        launch_tb(prec, false, L1, I.tb, A, box, I.scratch.p, ctl, eslot, 0, st, name == "tb_bond" ? 1 : 2);
+        return true;
+      }
+      if ((kind == pfmd_io::K_LJC || kind == pfmd_io::K_MORSEC) && (name == "cos_graphene" || name == "cos_metal")) {
+        launch_cos(prec, false, kind == pfmd_io::K_MORSEC, L1, lists[static_cast<size_t>(I.lists[1])].d,
+                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, A, box, ctl, eslot, 0, st,
+                   name == "cos_graphene" ? 1 : 2);
+        return true;
+      }
+    }
+    return false;
+  };
+  if (!once()) throw Error(PFMD_E_PARAM, "no kernel named '" + name + "' in this system");
+  CK(cudaStreamSynchronize(st));
+  CK(cudaEventRecord(ev0, st));
+  for (int r = 0; r < reps; ++r) once();
+  CK(cudaEventRecord(ev1, st));
+  CK(cudaEventSynchronize(ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  // restore the forces of the current positions
+  launch_zero_forces(gref(S.all_atoms), A, ctl, st);
+  enqueue_forces(false);
+  read_ctl();
+  if (hctl->error) raise_device_error();
+  if (bytes) *bytes = kernel_bytes(name);
+  return static_cast<double>(ms) / reps;
+}
+
 }  // namespace pfmd
 
 // ---------------------------------------------------------------------------
@@ -1292,7 +1445,7 @@ int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
       for (int i = 0; i < N; ++i) t[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
       e.pos.upload(t.data(), t.size(), e.st);
       CK(cudaStreamSynchronize(e.st));
-      pfmd::launch_pack_posf(e.A, e.ctl, e.st);
+      pfmd::launch_pack_posq(e.A, e.box, e.ctl, e.st);
       e.need_check_all = true;
     }
     if (vel && N) {
@@ -1426,6 +1579,49 @@ int pfmd_get_stream(pfmd_ctx* c, void** stream) {
   if (!c || !c->e || !stream) return PFMD_E_STATE;
   *stream = c->e->st;
   return PFMD_OK;
+}
+
+int pfmd_advance_timed(pfmd_ctx* c, long long max_steps, int* finished, double* device_ms) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    pfmd::Engine& e = *c->e;
+    if (!e.ev0) {
+      CK(cudaEventCreate(&e.ev0));
+      CK(cudaEventCreate(&e.ev1));
+    }
+    e.timing = true;
+    e.timing_started = false;
+    try {
+      e.advance(max_steps, finished);
+    } catch (...) {
+      e.timing = false;
+      throw;
+    }
+    e.timing = false;
+    float ms = 0.f;
+    if (e.timing_started) {
+      CK(cudaEventSynchronize(e.ev1));
+      CK(cudaEventElapsedTime(&ms, e.ev0, e.ev1));
+    }
+    if (device_ms) *device_ms = ms;
+  });
+}
+
+int pfmd_time_kernel(pfmd_ctx* c, const char* name, int reps, double* ms, double* bytes) {
+  if (!c || !c->e || !c->e->ctl || !name) return PFMD_E_STATE;
+  return guard(c, [&] {
+    double t = c->e->time_kernel(name, reps, bytes);
+    if (ms) *ms = t;
+  });
+}
+
+int pfmd_flush_l2(pfmd_ctx* c, long long bytes) {
+  if (!c || !c->e || !c->e->ctl || bytes <= 0) return PFMD_E_STATE;
+  return guard(c, [&] {
+    pfmd::Engine& e = *c->e;
+    if (e.flush_buf.n < static_cast<size_t>(bytes)) e.flush_buf.alloc(static_cast<size_t>(bytes));
+    CK(cudaMemsetAsync(e.flush_buf.p, (++e.flush_seq) & 0xff, static_cast<size_t>(bytes), e.st));
+  });
 }
 
 int pfmd_kernel_launches(const pfmd_ctx* c, long long* n) {

@@ -11,8 +11,9 @@
 //
 // PREC=false: FP64 throughout; the `r < R2` style tests use the exact FP64
 // distance, so the set of interacting pairs equals the reference's.
-// PREC=true : the precision form -- FP32 pair terms, per-row Kahan sums in FP32,
-// FP64 per-atom force update and FP64 energy reduction.
+// PREC=true : the precision form -- separations from the fixed-point positions,
+// FP32 pair terms, per-row Kahan sums in FP32, FP64 per-atom force update and
+// FP64 energy reduction.
 #include <type_traits>
 
 #include "kernels.h"
@@ -33,10 +34,10 @@ struct RT<false> {
 template <>
 struct RT<true> {
   using R = float;
-  using P4 = float4;
-  static __device__ __forceinline__ P4 load(const Atoms& A, int i) { return A.posf[i]; }
+  using P4 = int4;
+  static __device__ __forceinline__ P4 load(const Atoms& A, int i) { return A.posq[i]; }
   static __device__ __forceinline__ R d2(const P4& a, const P4& b, const Box& B, R dr[3]) {
-    return mi_f32(a, b, B, dr);
+    return mi_q(a, b, B, dr);
   }
 };
 
@@ -693,42 +694,49 @@ void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const L
 }
 
 void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const Atoms& A, const Box& B, void* Eb,
-                Ctl* ctl, int eslot, int ekey, cudaStream_t s) {
+                Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts) {
   if (L.rows == 0) {
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
   }
   const int g = nblk(L.rows, 256);
+  if (!(parts & 1)) {
+    if (prec) { k_rjl_force<true><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl); ++g_kernel_launches; }
+    else { k_rjl_force<false><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl); ++g_kernel_launches; }
+    return;
+  }
   if (prec) {
     if (energy)
       { k_rjl_density<true, true><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl, eslot, ekey); ++g_kernel_launches; }
     else
       { k_rjl_density<true, false><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl, eslot, ekey); ++g_kernel_launches; }
-    { k_rjl_force<true><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl); ++g_kernel_launches; }
+    if (parts & 2) { k_rjl_force<true><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl); ++g_kernel_launches; }
   } else {
     if (energy)
       { k_rjl_density<false, true><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl, eslot, ekey); ++g_kernel_launches; }
     else
       { k_rjl_density<false, false><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl, eslot, ekey); ++g_kernel_launches; }
-    { k_rjl_force<false><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl); ++g_kernel_launches; }
+    if (parts & 2) { k_rjl_force<false><<<g, 256, 0, s>>>(L, P, A, B, Eb, ctl); ++g_kernel_launches; }
   }
 }
 
 void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B, double* Bb,
-               Ctl* ctl, int eslot, int ekey, cudaStream_t s) {
+               Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts) {
   if (L.rows == 0) {
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
   }
   const int g = nblk(L.rows, 128);
   if (prec) {
-    { k_tb_bond<true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl); ++g_kernel_launches; }
+    if (parts & 1) { k_tb_bond<true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl); ++g_kernel_launches; }
+    if (!(parts & 2)) return;
     if (energy)
       { k_tb_force<true, true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey); ++g_kernel_launches; }
     else
       { k_tb_force<true, false><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey); ++g_kernel_launches; }
   } else {
-    { k_tb_bond<false><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl); ++g_kernel_launches; }
+    if (parts & 1) { k_tb_bond<false><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl); ++g_kernel_launches; }
+    if (!(parts & 2)) return;
     if (energy)
       { k_tb_force<false, true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey); ++g_kernel_launches; }
     else
@@ -738,8 +746,8 @@ void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const A
 
 void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
                 const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey,
-                cudaStream_t s) {
-  if (nl1.rows > 0) {
+                cudaStream_t s, int parts) {
+  if (nl1.rows > 0 && (parts & 1)) {
     const int g = nblk(nl1.rows, 128);
 #define PFMD_COSG(PR, EN, MO) \
   (k_cos_graphene<PR, EN, MO><<<g, 128, 0, s>>>(nl1, nn, P, norm, A, B, ctl, eslot, ekey), ++g_kernel_launches)
@@ -757,10 +765,10 @@ void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const Li
       }
     }
 #undef PFMD_COSG
-  } else if (energy) {
+  } else if (energy && (parts & 1)) {
     cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
   }
-  if (nl2.rows > 0) {
+  if (nl2.rows > 0 && (parts & 2)) {
     const int g = nblk(nl2.rows, 128);
     if (prec) {
       if (morse)

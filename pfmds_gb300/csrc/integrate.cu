@@ -122,7 +122,7 @@ __global__ void k_kick(GroupRef g, int xyz, double ts2, Atoms A, Ctl* ctl) {
   A.vel[i] = v;
 }
 
-__global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posf, Atoms A, Box B, Ctl* ctl) {
+__global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A, Box B, Ctl* ctl) {
   if (ctl->stop) return;
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   if (ind >= ctl->group_n[g.g]) return;
@@ -135,12 +135,12 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posf, Atoms A
   }
   p.z = drift1(p.z, v.z, ts1, B.L[2]);
   A.pos[i] = p;
-  if (write_posf) A.posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+  if (write_posq) A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
   if (out_of_cell(p.x, B.L[0]) || out_of_cell(p.y, B.L[1]) || out_of_cell(p.z, B.L[2])) flag_oob(ctl, i);
 }
 
 // Nose-Hoover scaling (optional), half kick and drift of the xyz group in one pass.
-__global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posf, int nhc_scale, Atoms A, Box B,
+__global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, Atoms A, Box B,
                              Ctl* ctl) {
   if (ctl->stop) return;
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
@@ -164,7 +164,7 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posf,
   p.y = drift1(p.y, v.y, ts1, B.L[1]);
   p.z = drift1(p.z, v.z, ts1, B.L[2]);
   A.pos[i] = p;
-  if (write_posf) A.posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+  if (write_posq) A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
   if (out_of_cell(p.x, B.L[0]) || out_of_cell(p.y, B.L[1]) || out_of_cell(p.z, B.L[2])) flag_oob(ctl, i);
 }
 
@@ -386,14 +386,14 @@ void launch_invert_z(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
 void launch_kick(const GroupRef& g, bool xyz, double ts2, const Atoms& A, Ctl* ctl, cudaStream_t s) {
   if (g.cap > 0) { k_kick<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts2, A, ctl); ++g_kernel_launches; }
 }
-void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posf, const Atoms& A, const Box& B, Ctl* ctl,
+void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, const Atoms& A, const Box& B, Ctl* ctl,
                   cudaStream_t s) {
-  if (g.cap > 0) { k_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts1, write_posf ? 1 : 0, A, B, ctl); ++g_kernel_launches; }
+  if (g.cap > 0) { k_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts1, write_posq ? 1 : 0, A, B, ctl); ++g_kernel_launches; }
 }
-void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posf, int nhc_scale, const Atoms& A,
+void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, const Atoms& A,
                        const Box& B, Ctl* ctl, cudaStream_t s) {
   if (g.cap > 0)
-    { k_kick_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posf ? 1 : 0, nhc_scale, A, B, ctl); ++g_kernel_launches; }
+    { k_kick_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, A, B, ctl); ++g_kernel_launches; }
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s) {

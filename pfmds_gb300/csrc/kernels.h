@@ -2,8 +2,9 @@
 //
 // Layouts in HBM:
 //   atoms      double4_32a pos/vel/frc [N] (w unused), double mass [N],
-//              float4 posf [N] (FP32 copy for the precision form and for the
-//              list-build prefilter)
+//              int4 posq [N]: fixed-point box fractions (x*2^32/L mod 2^32) used
+//              by the precision form's forces, the list-build prefilter and the
+//              cell binning
 //   groups     int idx[cap] (0-based atom indexes); current sizes live in
 //              Ctl::group_n so captured graphs survive change_particle_group_N
 //   lists      slot-major: nlist[slot*stride + row] holds the group-2 index (jnd)
@@ -30,7 +31,7 @@ struct Atoms {
   double4_32a* vel;
   double4_32a* frc;
   double* mass;
-  float4* posf;
+  int4* posq;
 };
 
 struct ListDev {
@@ -51,7 +52,6 @@ struct ListDev {
 struct CellGrid {
   int nc[3];
   int ncell;
-  float inv_cs[3];
   int* start;   // [ncell+1]
   int* count;   // [ncell]
   int* cursor;  // [ncell]
@@ -90,7 +90,7 @@ struct ChangeSpec {
 enum Integ { I_NVE = 0, I_NVT = 1, I_NVMS = 2 };
 
 // ---------------- neighbour lists (nlist.cu) ----------------
-void launch_pack_posf(const Atoms& A, Ctl* ctl, cudaStream_t s);
+void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s);
 // Regular list (converse=0), or the converse of a list with src_rows rows
 // (converse=1, built at the source list's rebuild steps).  The plain form tests
@@ -110,14 +110,19 @@ void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const A
                Ctl* ctl, int eslot, int ekey, cudaStream_t s);
 void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const LJPar& P, const Atoms& A,
                  const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+// Multi-kernel interactions take `parts`, a bit mask of their kernels (all by
+// default; single kernels are launched alone only for timing).
 // inv_eb: per-row 1/Eb scratch (double[rows] for plain, float[rows] for precision)
+// parts: 1 density, 2 force
 void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const Atoms& A, const Box& B,
-                void* inv_eb, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+                void* inv_eb, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3);
+// parts: 1 bond orders, 2 force
 void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B,
-               double* Bbuf, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+               double* Bbuf, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3);
+// parts: 1 graphene side, 2 metal side
 void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
                 const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot,
-                int ekey, cudaStream_t s);
+                int ekey, cudaStream_t s, int parts = 3);
 
 // ---------------- integration and reductions (integrate.cu) ----------------
 // phase: 0 = group changes + out-of-cell check, 1 = nvms exit test, 2 = both
@@ -126,9 +131,9 @@ void launch_step_begin(int phase, int n_changes, const ChangeSpec* changes, int 
 void launch_check_all(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_invert_z(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_kick(const GroupRef& g, bool xyz, double ts2, const Atoms& A, Ctl* ctl, cudaStream_t s);
-void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posf, const Atoms& A, const Box& B,
+void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, const Atoms& A, const Box& B,
                   Ctl* ctl, cudaStream_t s);
-void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posf, int nhc_scale,
+void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale,
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s);

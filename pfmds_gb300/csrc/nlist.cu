@@ -23,17 +23,12 @@ namespace pfmd {
 
 static constexpr int kBuildWarps = 8;
 
-__global__ void k_pack_posf(Atoms A) {
+__global__ void k_pack_posq(Atoms A, Box B) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < A.N) {
     double4_32a p = A.pos[i];
-    A.posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+    A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
   }
-}
-
-__device__ __forceinline__ int cell_axis(float x, float inv, int nc) {
-  int c = (int)floorf(x * inv);
-  return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
 __global__ void k_bin_count(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
@@ -41,9 +36,8 @@ __global__ void k_bin_count(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
   int n2 = ctl->group_n[L.col_group];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n2) return;
-  float4 p = A.posf[L.col_idx[j]];
-  int c = (cell_axis(p.z, cg.inv_cs[2], cg.nc[2]) * cg.nc[1] + cell_axis(p.y, cg.inv_cs[1], cg.nc[1])) * cg.nc[0] +
-          cell_axis(p.x, cg.inv_cs[0], cg.nc[0]);
+  int4 p = A.posq[L.col_idx[j]];
+  int c = (cell_q(p.z, cg.nc[2]) * cg.nc[1] + cell_q(p.y, cg.nc[1])) * cg.nc[0] + cell_q(p.x, cg.nc[0]);
   cg.cell_of[j] = c;
   atomicAdd(&cg.count[c], 1);
 }
@@ -108,11 +102,10 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   }
   int* buf = sbuf[wib];
   const int ai = L.row_idx[row];
-  const float4 pif = A.posf[ai];
+  const int4 piq = A.posq[ai];
   double4_32a pi = make_double4_32a(0, 0, 0, 0);
   if (!PREC) pi = A.pos[ai];
-  const int c0[3] = {cell_axis(pif.x, cg.inv_cs[0], cg.nc[0]), cell_axis(pif.y, cg.inv_cs[1], cg.nc[1]),
-                     cell_axis(pif.z, cg.inv_cs[2], cg.nc[2])};
+  const int c0[3] = {cell_q(piq.x, cg.nc[0]), cell_q(piq.y, cg.nc[1]), cell_q(piq.z, cg.nc[2])};
   int lo[3], hi[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -142,7 +135,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
             const int aj = L.col_idx[jnd];
             if (aj != ai) {
               float d[3];
-              float r2f = mi_f32(pif, A.posf[aj], B, d);
+              float r2f = mi_q(piq, A.posq[aj], B, d);
               if (PREC) {
                 hit = r2f < rcp2;
               } else if (r2f < rcp2) {
@@ -226,7 +219,7 @@ __global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B,
     bool in;
     if (PREC) {
       float d[3];
-      float r2 = mi_f32(A.posf[ai], A.posf[aj], B, d);
+      float r2 = mi_q(A.posq[ai], A.posq[aj], B, d);
       in = sqrtf(r2) < (float)rcnn;
     } else {
       double d[3];
@@ -270,7 +263,7 @@ __global__ void k_normals(ListDev nn, double4_32a* norm, int simplified, Atoms A
       const int aj = nn.col_idx[nn.nlist[(size_t)q * nn.stride + i]];
       if (PREC) {
         float df[3];
-        mi_f32(A.posf[ai], A.posf[aj], B, df);
+        mi_q(A.posq[ai], A.posq[aj], B, df);
         d[q][0] = df[0];
         d[q][1] = df[1];
         d[q][2] = df[2];
@@ -308,9 +301,9 @@ __global__ void k_nnum_max(ListDev L, Ctl* ctl) {
 // ---------------- launchers ----------------
 static inline int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
-void launch_pack_posf(const Atoms& A, Ctl* ctl, cudaStream_t s) {
+void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
   (void)ctl;
-  if (A.N > 0) { k_pack_posf<<<blocks_for(A.N, 256), 256, 0, s>>>(A); ++g_kernel_launches; }
+  if (A.N > 0) { k_pack_posq<<<blocks_for(A.N, 256), 256, 0, s>>>(A, B); ++g_kernel_launches; }
 }
 
 void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s) {
