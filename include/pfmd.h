@@ -53,6 +53,7 @@ typedef struct pfmd_options {
   int num_threads;           /* echoed in 'RUNNING ON n OPENMP THREADS' */
   int device;                /* CUDA device ordinal */
   int use_graphs;            /* capture repeated step segments in CUDA graphs */
+  int threads_per_row;       /* force-kernel threads per list row: 1,2,4,...,32, 0 = automatic */
 } pfmd_options;
 
 /* Defaults of run_md_simulation.f90:10-24 (out_period 1, seed 1, no prefix),

@@ -79,6 +79,17 @@ static const double MASS_COEF = 1.6605389217 / 1.6021765654 * 100.0;
 static const double KT_A_DEGREE = 1.3806488 / 1.6021765654 * 1e-4;
 static const double MOMENTA_COEF = 1.3806488 / 1.6605389217 * 1e-6;
 
+// Threads per list row: enough threads to fill the GPU (~152 SMs x 32 resident
+// warps) when rows are few, but at least ~2 entries per thread, and one thread
+// per row for large lists so that a warp reads 32 consecutive rows' slots.
+static int auto_tpa(int rows, double mean_entries) {
+  const double want = 152.0 * 32 * 32 / std::max(rows, 1);
+  int t = 1;
+  while (t < want && t < 32) t <<= 1;
+  while (t > 1 && t > mean_entries / 2.0) t >>= 1;
+  return t;
+}
+
 static double now_s() {
   using namespace std::chrono;
   return duration<double>(steady_clock::now().time_since_epoch()).count();
@@ -96,7 +107,9 @@ struct ListH {
   ListKind kind = L_REGULAR;
   ListDev d{};
   CellGrid cg{};
-  DBuf<int> nnum, nlist, pidx, less, bnd, cstart, ccount, ccursor, cjnd, ccell;
+  DBuf<int> nnum, nlist, pidx, less, bnd, row_of, cstart, ccount, ccursor, cjnd, catom, ccell;
+  DBuf<int4> cposq;
+  std::vector<int> col_inv;  // host: atom -> column-group index (reading lists back)
   double rc = 0.0;
   long long period = 1;
   int src = -1;  // converse: source list; nn: the tb list
@@ -132,7 +145,7 @@ class Engine {
   Box box{};
   Atoms A{};
   DBuf<double4_32a> pos, vel, frc;
-  DBuf<double> mass;
+  DBuf<double> mass, kc;
   DBuf<int4> posq;
   std::vector<GroupH> groups;
   std::vector<ListH> lists;
@@ -156,6 +169,7 @@ class Engine {
   double sim_time = 0.0;
   bool finished = false;
   bool finished_called = false;
+  bool tpa_tuned = false;
 
   // output
   std::string obuf;
@@ -201,6 +215,7 @@ class Engine {
     return num;
   }
   void read_ctl();
+  void tune_tpa();
   void upload_ctl_groups();
   void raise_device_error();
   bool switch_needed(long long s) const;
@@ -263,6 +278,11 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   prefix = o.output_prefix ? o.output_prefix : "";
   prec = opt.form == PFMD_FORM_PRECISION;
   t_start = now_s();
+  {
+    const int t = opt.threads_per_row;
+    if (t < 0 || t > 32 || (t & (t - 1)) != 0)
+      throw Error(PFMD_E_PARAM, "threads_per_row must be 0 (automatic) or a power of two up to 32");
+  }
   try {
     pfmd_io::read_settings(input_path, settings_filename, S);
   } catch (const fortio::ReadError& e) {
@@ -378,7 +398,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     L.d.id = static_cast<int>(lists.size());
     L.d.rows = rows;
     L.d.nmax = nmax;
-    L.d.stride = ((rows + 31) / 32) * 32;
+    L.d.stride = ((std::max(rows, 1) + 31) / 32) * 32;
+    L.d.tpa = opt.threads_per_row > 0 ? opt.threads_per_row : auto_tpa(rows, std::max(nmax, 2) / 2.0);
     L.d.row_group = row_g - 1;
     L.d.col_group = col_g - 1;
     L.d.row_cap = static_cast<int>(groups[static_cast<size_t>(row_g - 1)].idx.size());
@@ -527,19 +548,23 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     vel.upload(tv.data(), tv.size(), st);
     frc.zero(st);
     mass.upload(hm.data(), hm.size(), st);
+    std::vector<double> hk(hm.size());
+    for (size_t i = 0; i < hm.size(); ++i) hk[i] = 1.0 / (hm[i] * MASS_COEF);
+    kc.alloc(std::max<size_t>(hk.size(), 1));
+    kc.upload(hk.data(), hk.size(), st);
     CK(cudaStreamSynchronize(st));
   }
-  A = Atoms{N, pos.p, vel.p, frc.p, mass.p, posq.p};
+  A = Atoms{N, pos.p, vel.p, frc.p, mass.p, posq.p, kc.p};
   for (auto& g : groups) {
     g.d.alloc(std::max<size_t>(g.idx.size(), 1));
     g.d.upload(g.idx.data(), g.idx.size(), st);
   }
   const double maxL = std::max(box.L[0], std::max(box.L[1], box.L[2]));
   for (auto& L : lists) {
-    const size_t rows = static_cast<size_t>(std::max(L.d.stride, 32));
+    const size_t rows = static_cast<size_t>(std::max(L.d.rows, 1));
     L.nnum.alloc(rows);
     L.nnum.zero(st);
-    L.nlist.alloc(std::max<size_t>(static_cast<size_t>(L.d.nmax) * rows, 1));
+    L.nlist.alloc(std::max<size_t>(static_cast<size_t>(L.d.nmax), 1) * static_cast<size_t>(L.d.stride));
     L.nlist.zero(st);
     L.pidx.alloc(rows);
     L.pidx.zero(st);
@@ -554,6 +579,12 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     L.d.bnd = L.bnd.p;
     L.d.row_idx = groups[static_cast<size_t>(L.d.row_group)].d.p;
     L.d.col_idx = groups[static_cast<size_t>(L.d.col_group)].d.p;
+    L.d.row_of = nullptr;
+    {
+      const auto& cg = groups[static_cast<size_t>(L.d.col_group)].idx;
+      L.col_inv.assign(static_cast<size_t>(N), -1);
+      for (size_t k = 0; k < cg.size(); ++k) L.col_inv[static_cast<size_t>(cg[k])] = static_cast<int>(k);
+    }
     if (L.kind != L_NN_TB) {
       // cells at least r_cut (+ a margin for FP32 binning) wide
       const double margin = 1e-3 * L.rc + 2e-3 + 4e-6 * maxL;
@@ -576,24 +607,41 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
       L.ccount.alloc(static_cast<size_t>(ncell));
       L.ccursor.alloc(static_cast<size_t>(ncell));
       L.cjnd.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+      L.catom.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+      L.cposq.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
       L.ccell.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
       L.cg.start = L.cstart.p;
       L.cg.count = L.ccount.p;
       L.cg.cursor = L.ccursor.p;
       L.cg.jnd = L.cjnd.p;
+      L.cg.atom = L.catom.p;
+      L.cg.posq = L.cposq.p;
       L.cg.cell_of = L.ccell.p;
       L.has_grid = true;
     }
   }
   for (auto& I : inters) {
     const ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
-    if (I.spec.kind == pfmd_io::K_RJL) I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.stride), 32));
+    if (I.spec.kind == pfmd_io::K_RJL) I.scratch.alloc(static_cast<size_t>(std::max(N, 1)));  // 1/Eb per atom
     if (I.spec.kind == pfmd_io::K_TB)
-      I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 32));
+      I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));  // B per list slot
     if (I.lists[2] >= 0) {
-      const ListH& L3 = lists[static_cast<size_t>(I.lists[2])];
-      I.norm.alloc(std::max<size_t>(static_cast<size_t>(L3.d.rows), 1));
+      I.norm.alloc(static_cast<size_t>(std::max(N, 1)));  // normals per atom
       I.norm.zero(st);
+    }
+    // lists whose kernels address a partner's row: tb (and the nn selection that
+    // reads it), lj1g in a group that is not in ascending atom order
+    std::vector<int> need;
+    if (I.spec.kind == pfmd_io::K_TB || (I.spec.kind == pfmd_io::K_LJ1G && I.general)) need.push_back(I.lists[0]);
+    for (int li : need) {
+      ListH& L = lists[static_cast<size_t>(li)];
+      if (L.row_of.p) continue;
+      std::vector<int> ro(static_cast<size_t>(N), -1);
+      const auto& rg = groups[static_cast<size_t>(L.d.row_group)].idx;
+      for (size_t k = 0; k < rg.size(); ++k) ro[static_cast<size_t>(rg[k])] = static_cast<int>(k);
+      L.row_of.alloc(ro.size());
+      L.row_of.upload(ro.data(), ro.size(), st);
+      L.d.row_of = L.row_of.p;
     }
   }
   // control block
@@ -634,6 +682,32 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   md_step = 0;
   integrator_index = 0;
   sim_time = 0.0;
+}
+
+// Threads per row of each list's force kernels once the first build's mean
+// neighbour count is known (a deterministic choice, so repeated runs stay
+// bit-identical).
+void Engine::tune_tpa() {
+  tpa_tuned = true;
+  if (opt.threads_per_row > 0) return;
+  bool changed = false;
+  for (auto& L : lists) {
+    if (L.kind == L_NN_TB || L.d.rows == 0) continue;
+    std::vector<int> n(static_cast<size_t>(L.d.rows));
+    CK(cudaMemcpy(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost));
+    double tot = 0;
+    for (int v : n) tot += v;
+    const int t = auto_tpa(L.d.rows, tot / static_cast<double>(n.size()));
+    if (t != L.d.tpa) {
+      L.d.tpa = t;
+      changed = true;
+    }
+  }
+  if (changed) {
+    for (auto& kv : graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    graphs.clear();
+  }
 }
 
 void Engine::read_ctl() {
@@ -833,14 +907,14 @@ void Engine::enqueue_step(const StepPlan& p) {
           launch_scale(static_cast<int>(c), gc, A, ctl, st);
       }
     if (fuse_kick_drift) {
-      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, A, box, ctl, st);
+      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st);
       if (gz.cap > 0) {
-        launch_kick(gz, false, ts[1], A, ctl, st);
+        launch_kick(gz, false, ts[1], !prec, A, ctl, st);
         launch_drift(gz, false, ts[0], true, A, box, ctl, st);
       }
     } else {
-      launch_kick(gx, true, ts[1], A, ctl, st);
-      launch_kick(gz, false, ts[1], A, ctl, st);
+      launch_kick(gx, true, ts[1], !prec, A, ctl, st);
+      launch_kick(gz, false, ts[1], !prec, A, ctl, st);
       launch_drift(gx, true, ts[0], true, A, box, ctl, st);
       launch_drift(gz, false, ts[0], true, A, box, ctl, st);
     }
@@ -851,8 +925,8 @@ void Engine::enqueue_step(const StepPlan& p) {
   launch_zero_forces(gall, A, ctl, st);
   enqueue_forces(p.energy);
   if (!p.first) {
-    launch_kick(gx, true, ts[1], A, ctl, st);
-    if (gz.cap > 0) launch_kick(gz, false, ts[1], A, ctl, st);
+    launch_kick(gx, true, ts[1], !prec, A, ctl, st);
+    if (gz.cap > 0) launch_kick(gz, false, ts[1], !prec, A, ctl, st);
     if (nvt)
       for (size_t c = 0; c < S.nhc.size(); ++c) {
         const GroupRef gc = gref(S.nhc[c].group);
@@ -1082,6 +1156,7 @@ void Engine::advance(long long max_steps, int* fin) {
     run_plans(plans);
     read_ctl();
     if (hctl->error) raise_device_error();
+    if (!tpa_tuned) tune_tpa();
     const long long executed_to = hctl->converged ? hctl->err_step : plans.back().step + 1;
     for (long long t = s; t < executed_to; ++t)
       if (t != 0) sim_time = sim_time + ts[0];
@@ -1348,6 +1423,7 @@ void pfmd_default_options(pfmd_options* o) {
   o->num_threads = 1;
   o->device = 0;
   o->use_graphs = 1;
+  o->threads_per_row = 0;
 }
 
 int pfmd_create_from_files(const char* input_path, const char* settings_filename, const pfmd_options* opt,
@@ -1519,9 +1595,14 @@ int pfmd_get_nlist(pfmd_ctx* c, int inter, int list, int* nnum, int* lessnnum, i
       CK(cudaMemcpyAsync(t.data(), L.nlist.p, sizeof(int) * t.size(), cudaMemcpyDeviceToHost, e.st));
     }
     CK(cudaStreamSynchronize(e.st));
+    // main lists hold partner atoms: report the reference's group-2 indexes
+    const bool atoms = L.kind != pfmd::L_NN_TB;
     if (nlist && nmax)
       for (size_t r = 0; r < rows; ++r)
-        for (size_t p = 0; p < nmax; ++p) nlist[r * nmax + p] = t[p * stride + r];
+        for (size_t p = 0; p < nmax; ++p) {
+          const int v = t[p * stride + r];
+          nlist[r * nmax + p] = (atoms && v >= 0 && v < e.N) ? L.col_inv[static_cast<size_t>(v)] : v;
+        }
   });
 }
 
@@ -1550,14 +1631,19 @@ int pfmd_get_gr_norm(pfmd_ctx* c, int inter, double* norm) {
   auto& I = e.inters[static_cast<size_t>(inter)];
   if (!I.norm.p) return PFMD_E_PARAM;
   return guard(c, [&] {
-    const size_t rows = static_cast<size_t>(e.lists[static_cast<size_t>(I.lists[2])].d.rows);
-    std::vector<double4_32a> t(rows);
-    if (rows) CK(cudaMemcpyAsync(t.data(), I.norm.p, sizeof(double4_32a) * rows, cudaMemcpyDeviceToHost, e.st));
+    // normals are kept per atom; gr_norm is indexed by the nn list's rows
+    const auto& L3 = e.lists[static_cast<size_t>(I.lists[2])];
+    const size_t rows = static_cast<size_t>(L3.d.rows);
+    const auto& rg = e.groups[static_cast<size_t>(L3.d.row_group)].idx;
+    std::vector<double4_32a> t(static_cast<size_t>(std::max(e.N, 1)));
+    if (e.N) CK(cudaMemcpyAsync(t.data(), I.norm.p, sizeof(double4_32a) * e.N, cudaMemcpyDeviceToHost, e.st));
     CK(cudaStreamSynchronize(e.st));
     for (size_t r = 0; r < rows; ++r) {
-      norm[3 * r] = t[r].x;
-      norm[3 * r + 1] = t[r].y;
-      norm[3 * r + 2] = t[r].z;
+      const double nan = std::nan("");
+      const bool has = r < rg.size();
+      norm[3 * r] = has ? t[static_cast<size_t>(rg[r])].x : nan;
+      norm[3 * r + 1] = has ? t[static_cast<size_t>(rg[r])].y : nan;
+      norm[3 * r + 2] = has ? t[static_cast<size_t>(rg[r])].z : nan;
     }
   });
 }

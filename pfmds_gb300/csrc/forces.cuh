@@ -1,0 +1,225 @@
+// Shared pieces of the force kernels (forces_*.cu).
+//
+// Every force kernel is a full-list gather: TPA threads own one list row (one
+// thread per row for large systems), split its entries, recompute the
+// minimum-image vector to each partner from positions (the reference stores it
+// per entry and refreshes it every step, md_neighbours.f90:104-124), reduce the
+// row's force across the group and add it to the row's atom once.  No atomics.
+// Energies are folded into the force pass at energy steps and reduced
+// deterministically.
+//
+// PREC=false: FP64 throughout; tests like `r < R2` use the exact FP64 distance,
+// so the set of interacting pairs equals the reference's.
+// PREC=true : the precision form -- separations from the fixed-point positions,
+// FP32 pair terms, per-thread Kahan sums merged across the group with an
+// error-free TwoSum, FP64 per-atom force update and FP64 energy reduction.
+#pragma once
+
+#include <type_traits>
+
+#include "kernels.h"
+
+namespace pfmd {
+
+template <bool PREC>
+struct RT;
+template <>
+struct RT<false> {
+  using R = double;
+  using P4 = double4_32a;
+  static __device__ __forceinline__ P4 load(const Atoms& A, int i) { return A.pos[i]; }
+  static __device__ __forceinline__ R d2(const P4& a, const P4& b, const Box& B, R dr[3]) {
+    return mi_exact(a, b, B, dr);
+  }
+};
+template <>
+struct RT<true> {
+  using R = float;
+  using P4 = int4;
+  static __device__ __forceinline__ P4 load(const Atoms& A, int i) { return A.posq[i]; }
+  static __device__ __forceinline__ R d2(const P4& a, const P4& b, const Box& B, R dr[3]) {
+    return mi_q(a, b, B, dr);
+  }
+};
+
+// Rows are spread over the lanes of a warp so that consecutive rows sit on
+// consecutive lanes: a warp holds 32/TPA rows, and the TPA threads of a row are
+// lanes r, r + 32/TPA, r + 2*32/TPA, ...  Thread `sub` of a row takes slots
+// sub, sub + TPA, ...; its partial sums are combined by xor-shuffles over
+// offsets 16, 8, ..., 32/TPA.
+template <int TPA>
+struct Grp {
+  int row, sub;
+  __device__ __forceinline__ Grp() {
+    constexpr int RPW = 32 / TPA;  // rows per warp
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = g & 31;
+    row = (g >> 5) * RPW + (lane % RPW);
+    sub = lane / RPW;
+  }
+};
+template <int TPA>
+__device__ __forceinline__ double gsum(double v) {
+#pragma unroll
+  for (int o = 16; o >= 32 / TPA; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// Compensated merge of per-lane Kahan pairs (value = s - c) across the group:
+// TwoSum(s1, s2) = t + e exactly, so (s1 - c1) + (s2 - c2) = t - (c1 + c2 - e).
+template <int TPA>
+__device__ __forceinline__ void gmerge(float& s, float& c) {
+#pragma unroll
+  for (int o = 16; o >= 32 / TPA; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+    const float t = s + s2;
+    const float bb = t - s;
+    const float e = (s - (t - bb)) + (s2 - bb);
+    c = (c + c2) - e;
+    s = t;
+  }
+}
+
+// Per-thread accumulators: plain FP64, or FP32 with Kahan compensation.
+template <bool PREC>
+struct Acc3;
+template <>
+struct Acc3<false> {
+  double s[3] = {0.0, 0.0, 0.0};
+  __device__ __forceinline__ void add(double x, double y, double z) {
+    s[0] += x;
+    s[1] += y;
+    s[2] += z;
+  }
+  template <int TPA>
+  __device__ __forceinline__ void reduce() {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s[k] = gsum<TPA>(s[k]);
+  }
+  __device__ __forceinline__ double get(int k) const { return s[k]; }
+};
+template <>
+struct Acc3<true> {
+  Kahan3 k;
+  __device__ __forceinline__ void add(float x, float y, float z) { k.add(x, y, z); }
+  template <int TPA>
+  __device__ __forceinline__ void reduce() {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gmerge<TPA>(k.s[c], k.c[c]);
+  }
+  __device__ __forceinline__ double get(int c) const { return k.get(c); }
+};
+template <bool PREC>
+struct Acc1;
+template <>
+struct Acc1<false> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  template <int TPA>
+  __device__ __forceinline__ void reduce() {
+    s = gsum<TPA>(s);
+  }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <>
+struct Acc1<true> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  template <int TPA>
+  __device__ __forceinline__ void reduce() {
+    gmerge<TPA>(s, c);
+  }
+  __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
+template <bool PREC>
+__device__ __forceinline__ void fdfc(typename RT<PREC>::R r, typename RT<PREC>::R R1, typename RT<PREC>::R R2,
+                                     typename RT<PREC>::R inv_w, typename RT<PREC>::R& f,
+                                     typename RT<PREC>::R& df) {
+  if constexpr (PREC)
+    fdfcut_cos_f(r, R1, R2, inv_w, f, df);
+  else
+    fdfcut_cos(r, R1, R2, f, df);
+}
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R fc_only(typename RT<PREC>::R r, typename RT<PREC>::R R1,
+                                                        typename RT<PREC>::R R2, typename RT<PREC>::R inv_w) {
+  if constexpr (PREC) {
+    if (r < R1) return 1.0f;
+    if (r < R2) return (1.0f + __cosf(3.14159265358979f * (r - R1) * inv_w)) * 0.5f;
+    return 0.0f;
+  } else {
+    return fcut_cos(r, R1, R2);
+  }
+}
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R xexp(typename RT<PREC>::R x) {
+  if constexpr (PREC)
+    return __expf(x);
+  else
+    return exp(x);
+}
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R xpow(typename RT<PREC>::R x, typename RT<PREC>::R y) {
+  if constexpr (PREC)
+    return x > 0.0f ? exp2f(y * __log2f(x)) : 0.0f;
+  else
+    return pow(x, y);
+}
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R xsqrt(typename RT<PREC>::R x) {
+  if constexpr (PREC)
+    return sqrtf(x);
+  else
+    return sqrt(x);
+}
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R dot3(const typename RT<PREC>::R* a, const typename RT<PREC>::R* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+__device__ __forceinline__ void add_force(const Atoms& A, int ai, double fx, double fy, double fz) {
+  double4_32a f = A.frc[ai];
+  f.x += fx;
+  f.y += fy;
+  f.z += fz;
+  A.frc[ai] = f;
+}
+
+// Energy of one row into the interaction's total (every thread of the grid calls it).
+__device__ __forceinline__ void energy_reduce(Ctl* ctl, int eslot, int ekey, double erow) {
+  double v[1] = {erow}, out[1];
+  if (grid_sum<1>(ctl, eslot, v, out)) ctl->e_inter[ekey] = out[0];
+}
+
+static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+// Entry `p` of list row `row` (slot-major storage).
+__device__ __forceinline__ int ent(const ListDev& L, int row, int p) { return L.nlist[(size_t)p * L.stride + row]; }
+
+// Calls F with an integral_constant for the list's threads-per-row.
+template <class F>
+static inline void with_tpa(int tpa, F f) {
+  switch (tpa) {
+    case 1: f(std::integral_constant<int, 1>()); break;
+    case 2: f(std::integral_constant<int, 2>()); break;
+    case 4: f(std::integral_constant<int, 4>()); break;
+    case 8: f(std::integral_constant<int, 8>()); break;
+    case 16: f(std::integral_constant<int, 16>()); break;
+    default: f(std::integral_constant<int, 32>()); break;
+  }
+}
+template <class F>
+static inline void with_bool(bool b, F f) {
+  if (b)
+    f(std::true_type());
+  else
+    f(std::false_type());
+}
+
+}  // namespace pfmd

@@ -1,0 +1,196 @@
+// ljc / morsec: LennardJonesCosine.f90 and MorseCosine.f90 (26-139).
+// Graphene side (rows of nl(1)): the pair term with the row's normal plus, unless
+// `simplified`, the term through the normals of its three nearest neighbours j
+// (dn_j/dr_i).  Metal side (rows of nl(2)): the pair term with the neighbour's
+// normal; morsec divides that cosine by |n| (MorseCosine.f90:127), ljc does not.
+// Normals are stored per atom.  See forces.cuh for the execution scheme.
+#include "forces.cuh"
+
+namespace pfmd {
+
+template <bool PREC, bool MORSE>
+__device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r, const typename RT<PREC>::R* dr,
+                                         const typename RT<PREC>::R* nv, typename RT<PREC>::R nnorm, bool metal,
+                                         typename RT<PREC>::R& X, typename RT<PREC>::R& Y, typename RT<PREC>::R& E) {
+  using R = typename RT<PREC>::R;
+  const R R1 = (R)P.R1, R2 = (R)P.R2, delt = (R)P.delt, inv_w = (R)(1.0 / (P.R2 - P.R1));
+  const R nd = nv[0] * dr[0] + nv[1] * dr[1] + nv[2] * dr[2];
+  R fc, dfc;
+  fdfc<PREC>(r, R1, R2, inv_w, fc, dfc);
+  if (!MORSE) {
+    const R x = (R)P.sig / r, x2 = x * x, V2 = x2 * x2 * x2, V1 = V2 * V2;
+    const R V3 = xpow<PREC>(fabs(nd) / r, delt);
+    X = (R(12) * V1 - (R(6) + delt) * V2 * V3) / (r * r) * fc - (V1 - V2 * V3) * dfc;
+    Y = delt * V2 * V3 / nd * fc;
+    E = (V1 - V2 * V3) * fc;
+  } else {
+    const R a = (R)P.a;
+    const R V2 = xexp<PREC>(-a * (r - (R)P.r0)), V1 = V2 * V2;
+    const R V3 = xpow<PREC>(metal ? fabs(nd) / (nnorm * r) : fabs(nd) / r, delt);
+    X = R(2) * (a * V1 - (a + delt / r) * V2 * V3) / r * fc - (V1 - R(2) * V2 * V3) * dfc;
+    Y = R(2) * delt * V2 * V3 / nd * fc;
+    E = (V1 - R(2) * V2 * V3) * fc;
+  }
+}
+
+template <bool PREC, bool ENERGY, bool MORSE, int TPA>
+__global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, CosPar P, const double4_32a* norm,
+                                                      Atoms A, Box B, Ctl* ctl, int eslot, int ekey) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+  if (ctl->stop) return;
+  const Grp<TPA> g;
+  const bool valid = g.row < nl.rows;
+  const int i = g.row;
+  Acc3<PREC> acc;
+  Acc1<PREC> e;
+  const int ai = valid ? nl.pidx[i] : 0;
+  const R pref = MORSE ? (R)P.D : (R)(4.0 * P.eps);
+  if (valid) {
+    const auto pi = T::load(A, ai);
+    const R R2 = (R)P.R2;
+    const double4_32a ni = norm[ai];
+    const R nv[3] = {(R)ni.x, (R)ni.y, (R)ni.z};
+    const int n = nl.nnum[i];
+    for (int p = g.sub; p < n; p += TPA) {
+      R dr[3];
+      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(nl, i, p)), B, dr));
+      if (r < R2) {
+        R X, Y, E;
+        cos_pair<PREC, MORSE>(P, r, dr, nv, R(1), false, X, Y, E);
+        acc.add(-pref * (X * dr[0] + Y * nv[0]), -pref * (X * dr[1] + Y * nv[1]), -pref * (X * dr[2] + Y * nv[2]));
+        if (ENERGY) e.add(pref * E);
+      }
+    }
+    if (!P.simplified) {
+      const R R1 = (R)P.R1, delt = (R)P.delt, inv_w = (R)(1.0 / (P.R2 - P.R1));
+      for (int q = 0; q < 3; ++q) {
+        const int j = ent(nn, i, q);
+        if (j < 0 || j >= nn.rows || j >= nl.rows || j >= nn.row_cap) {
+          // a neighbour outside the graphene rows (groups 5/6 of the list differ)
+          if (g.sub == 0) set_error(ctl, ST_PARAM, EK_NONE, i + 1, j + 1, 0);
+          break;
+        }
+        int l1 = 0;
+        for (; l1 < 3; ++l1)
+          if (ent(nn, j, l1) == i) break;
+        if (l1 >= 3) {
+          if (g.sub == 0) set_error(ctl, ST_GR_NN, EK_L1, i + 1, j + 1, 0);
+          break;
+        }
+        const int l2 = (l1 + 1) % 3, l3 = (l1 + 2) % 3;
+        const int aj = nn.row_idx[j];
+        const auto pj = T::load(A, aj);
+        R dl[3][3];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) T::d2(pj, T::load(A, nn.col_idx[ent(nn, j, l)]), B, dl[l]);
+        R d12[3], d31[3], d23[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          d12[k] = dl[l2][k] - dl[l1][k];
+          d31[k] = dl[l1][k] - dl[l3][k];
+          d23[k] = dl[l3][k] - dl[l2][k];
+        }
+        const R Aa = dot3<PREC>(d12, d12) * dot3<PREC>(d31, d31) - dot3<PREC>(d12, d31) * dot3<PREC>(d12, d31);
+        const R s2331 = dot3<PREC>(d23, d31), s2312 = dot3<PREC>(d23, d12);
+        R w[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) w[k] = d12[k] * s2331 - d31[k] * s2312;
+        const int ag = nl.pidx[j];
+        const double4_32a nj4 = norm[ag];
+        const R nj[3] = {(R)nj4.x, (R)nj4.y, (R)nj4.z};
+        const auto pg = T::load(A, ag);
+        const int m = nl.nnum[j];
+        for (int p = g.sub; p < m; p += TPA) {
+          R dr[3];
+          const R r = xsqrt<PREC>(T::d2(pg, T::load(A, ent(nl, j, p)), B, dr));
+          if (r < R2) {
+            const R nd = nj[0] * dr[0] + nj[1] * dr[1] + nj[2] * dr[2];
+            const R V3 = xpow<PREC>(fabs(nd) / r, delt);
+            const R fc = fc_only<PREC>(r, R1, R2, inv_w);
+            R V2;
+            if (MORSE)
+              V2 = xexp<PREC>(-(R)P.a * (r - (R)P.r0));
+            else {
+              const R x = (R)P.sig / r, x2 = x * x;
+              V2 = x2 * x2 * x2;
+            }
+            const R C = dr[0] * w[0] + dr[1] * w[1] + dr[2] * w[2];
+            const R coef = (MORSE ? R(2) * pref : pref) * delt * V2 * V3 * fc / Aa / nd;
+            acc.add(-coef * nj[0] * C, -coef * nj[1] * C, -coef * nj[2] * C);
+          }
+        }
+      }
+    }
+  }
+  acc.template reduce<TPA>();
+  if (ENERGY) e.template reduce<TPA>();
+  if (valid && g.sub == 0) add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+  if (ENERGY) energy_reduce(ctl, eslot, ekey, (valid && g.sub == 0) ? e.get() : 0.0);
+}
+
+template <bool PREC, bool MORSE, int TPA>
+__global__ void __launch_bounds__(256) k_cos_metal(ListDev nl, CosPar P, const double4_32a* norm, Atoms A, Box B,
+                                                   Ctl* ctl) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+  if (ctl->stop) return;
+  const Grp<TPA> g;
+  const int n = g.row < nl.rows ? nl.nnum[g.row] : 0;
+  const int ai = n > 0 ? nl.pidx[g.row] : 0;
+  Acc3<PREC> acc;
+  if (n > 0) {
+    const auto pi = T::load(A, ai);
+    const R R2 = (R)P.R2;
+    const R pref = MORSE ? (R)P.D : (R)(4.0 * P.eps);
+    for (int p = g.sub; p < n; p += TPA) {
+      const int aj = ent(nl, g.row, p);
+      R dr[3];
+      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dr));
+      if (r < R2) {
+        const double4_32a gn = norm[aj];
+        const R nv[3] = {(R)gn.x, (R)gn.y, (R)gn.z};
+        const R nn = xsqrt<PREC>(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        R X, Y, E;
+        cos_pair<PREC, MORSE>(P, r, dr, nv, nn, true, X, Y, E);
+        acc.add(-pref * (X * dr[0] + Y * nv[0]), -pref * (X * dr[1] + Y * nv[1]), -pref * (X * dr[2] + Y * nv[2]));
+      }
+    }
+  }
+  acc.template reduce<TPA>();
+  if (n > 0 && g.sub == 0) add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+}
+
+void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
+                const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey,
+                cudaStream_t s, int parts) {
+  with_bool(prec, [&](auto pr) {
+    with_bool(morse, [&](auto mo) {
+      constexpr bool PR = decltype(pr)::value, MO = decltype(mo)::value;
+      if (parts & 1) {
+        if (nl1.rows > 0) {
+          const int grid = nblk((long long)nl1.rows * nl1.tpa, 256);
+          with_tpa(nl1.tpa, [&](auto t) {
+            constexpr int TP = decltype(t)::value;
+            if (energy)
+              k_cos_graphene<PR, true, MO, TP><<<grid, 256, 0, s>>>(nl1, nn, P, norm, A, B, ctl, eslot, ekey);
+            else
+              k_cos_graphene<PR, false, MO, TP><<<grid, 256, 0, s>>>(nl1, nn, P, norm, A, B, ctl, eslot, ekey);
+            ++g_kernel_launches;
+          });
+        } else if (energy) {
+          cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
+        }
+      }
+      if ((parts & 2) && nl2.rows > 0) {
+        const int grid = nblk((long long)nl2.rows * nl2.tpa, 256);
+        with_tpa(nl2.tpa, [&](auto t) {
+          k_cos_metal<PR, MO, decltype(t)::value><<<grid, 256, 0, s>>>(nl2, P, norm, A, B, ctl);
+          ++g_kernel_launches;
+        });
+      }
+    });
+  });
+}
+
+}  // namespace pfmd

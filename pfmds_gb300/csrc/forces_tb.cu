@@ -1,0 +1,178 @@
+// tb (Tersoff-Brenner bond order) forces and energy, TersoffBrenner.f90:26-150.
+// Pass 1: bond orders B(p,i) per list slot; pass 2: forces with the angular terms
+// of i's and of each neighbour j's environment and, at energy steps, the bond
+// energies for j > i.  Lists hold ~3 partners, so one thread owns a row.
+// Requires g1 == g2: a partner's row is row_of[atom].
+#include "forces.cuh"
+
+namespace pfmd {
+
+template <bool PREC>
+__global__ void __launch_bounds__(128) k_tb_bond(ListDev L, TBPar P, Atoms A, Box B, double* Bb, Ctl* ctl) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+  if (ctl->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.rows) return;
+  const int n = L.nnum[i];
+  const int ai = L.pidx[i];
+  const auto pi = T::load(A, ai);
+  const R R1 = (R)P.R1, R2 = (R)P.R2, a0 = (R)P.a0, c02 = (R)P.c02, d02 = (R)P.d02, delt = (R)P.delt,
+          inv_w = (R)(1.0 / (P.R2 - P.R1));
+  for (int p = 0; p < n; ++p) {
+    R dp[3];
+    const R rp = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, p)), B, dp));
+    R b = R(0);
+    if (rp < R2) {
+      for (int q = 0; q < n; ++q) {
+        if (q == p) continue;
+        R dq[3];
+        const R rq = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, q)), B, dq));
+        if (rq < R2) {
+          const R cs = dot3<PREC>(dp, dq) / (rp * rq);
+          b += fc_only<PREC>(rq, R1, R2, inv_w) * (R(1) + c02 / d02 - c02 / (d02 + (R(1) + cs) * (R(1) + cs)));
+        }
+      }
+      b = xpow<PREC>(R(1) + a0 * b, -delt);
+    }
+    Bb[(size_t)p * L.stride + i] = (double)b;
+  }
+}
+
+template <bool PREC, bool ENERGY>
+__global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, Box B, const double* Bb, Ctl* ctl,
+                                                  int eslot, int ekey) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+  if (ctl->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double erow = 0.0;
+  if (i < L.rows && L.nnum[i] > 0) {
+    const int n = L.nnum[i];
+    const int ai = L.pidx[i];
+    const auto pi = T::load(A, ai);
+    const R R1 = (R)P.R1, R2 = (R)P.R2, a0 = (R)P.a0, c02 = (R)P.c02, d02 = (R)P.d02, delt = (R)P.delt,
+            d = (R)P.d, s = (R)P.s, bb = (R)P.b, r0 = (R)P.r0, inv_w = (R)(1.0 / (P.R2 - P.R1));
+    const R ex = (R)(1.0 / P.delt + 1.0);
+    const R sq2s = (R)sqrt(2.0 * P.s), sq2os = (R)sqrt(2.0 / P.s);
+    const R pre_e = d / (s - R(1));
+    Acc3<PREC> acc;
+    Acc1<PREC> e;
+    for (int p = 0; p < n; ++p) {
+      const int aj = ent(L, i, p);
+      const int j = L.row_of[aj];
+      R dp[3];
+      const R rp = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dp));
+      R dB[3] = {R(0), R(0), R(0)};
+      for (int q = 0; q < n; ++q) {
+        if (q == p) continue;
+        R dq[3];
+        const R rq = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, q)), B, dq));
+        const R rr = R(1) / rp / rq;
+        const R cosi = dot3<PREC>(dp, dq) * rr;
+        const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
+        R fq, dfq;
+        fdfc<PREC>(rq, R1, R2, inv_w, fq, dfq);
+        const R g1 = fq * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
+        const R g2 = dfq * a0 * (R(1) + c02 / d02 - c02 / t);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          dB[k] += g1 * ((dp[k] + dq[k]) * rr - cosi * (dp[k] / (rp * rp) + dq[k] / (rq * rq))) + g2 * dq[k];
+      }
+      const R Bpi = (R)Bb[(size_t)p * L.stride + i];
+      const R bpe = xpow<PREC>(Bpi, ex);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dB[k] *= bpe;
+      // i's slot l in j's row, and j's environment
+      const int nj = L.nnum[j];
+      const auto pj = T::load(A, aj);
+      int l = 0;
+      for (; l < nj; ++l)
+        if (ent(L, j, l) == ai) break;
+      R dl[3] = {R(0), R(0), R(0)};
+      R rl = R(0), Blj = R(0);
+      if (l < nj) {
+        rl = xsqrt<PREC>(T::d2(pj, pi, B, dl));
+        Blj = (R)Bb[(size_t)l * L.stride + j];
+      }
+      const R blpe = xpow<PREC>(Blj, ex);
+      for (int q = 0; q < nj && l < nj; ++q) {
+        if (q == l) continue;
+        R dq[3];
+        const R rq = xsqrt<PREC>(T::d2(pj, T::load(A, ent(L, j, q)), B, dq));
+        const R rr = R(1) / rl / rq;
+        const R cosi = dot3<PREC>(dl, dq) * rr;
+        const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
+        const R g = blpe * fc_only<PREC>(rq, R1, R2, inv_w) * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dB[k] += g * (-dq[k] * rr + cosi * dl[k] / (rl * rl));
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dB[k] = dB[k] * (-delt) * R(0.5);
+      if (rp < R2) {
+        R fc, dfc;
+        fdfc<PREC>(rp, R1, R2, inv_w, fc, dfc);
+        const R dff = dfc / fc;
+        const R a = -sq2s * bb * (rp - r0);
+        const R ea = xexp<PREC>(a), eas = xexp<PREC>(a / s);
+        const R c1 = sq2s * bb / rp, c2 = sq2os * bb / rp;
+        const R pre = fc * d / (s - R(1));
+        const R bavg = (Bpi + Blj) * R(0.5);
+        R f[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          f[k] = pre * ((dp[k] * dff - c1 * dp[k]) * ea - (dB[k] + bavg * (dp[k] * dff - c2 * dp[k])) * s * eas);
+        acc.add(f[0], f[1], f[2]);
+        if (ENERGY && j > i) e.add(fc * pre_e * (ea - bavg * s * eas));
+      }
+      if (l < nj) {
+        R fl, dfl;
+        fdfc<PREC>(rl, R1, R2, inv_w, fl, dfl);
+        for (int q = 0; q < nj; ++q) {
+          if (q == l) continue;
+          R dq[3];
+          const R rq = xsqrt<PREC>(T::d2(pj, T::load(A, ent(L, j, q)), B, dq));
+          const R rr = R(1) / rl / rq;
+          const R cosi = dot3<PREC>(dl, dq) * rr;
+          const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
+          const R t1 = fl * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
+          const R t2 = dfl * a0 * (R(1) + c02 / d02 - c02 / t);
+          const R pre = delt * R(0.5) * xpow<PREC>((R)Bb[(size_t)q * L.stride + j], ex);
+          const R post = fc_only<PREC>(rq, R1, R2, inv_w) * d / (s - R(1)) * s * xexp<PREC>(-sq2s * bb * (rq - r0) / s);
+          R f[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) f[k] = pre * (t1 * (-dq[k] * rr + cosi * dl[k] / (rl * rl)) + dp[k] * t2) * post;
+          acc.add(f[0], f[1], f[2]);
+        }
+      }
+    }
+    add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+    erow = e.get();
+  }
+  if (ENERGY) energy_reduce(ctl, eslot, ekey, erow);
+}
+
+void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B, double* Bb,
+               Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts) {
+  if (L.rows == 0) {
+    if (energy && (parts & 2)) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
+    return;
+  }
+  const int g = nblk(L.rows, 128);
+  with_bool(prec, [&](auto pr) {
+    constexpr bool PR = decltype(pr)::value;
+    if (parts & 1) {
+      k_tb_bond<PR><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl);
+      ++g_kernel_launches;
+    }
+    if (parts & 2) {
+      if (energy)
+        k_tb_force<PR, true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey);
+      else
+        k_tb_force<PR, false><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey);
+      ++g_kernel_launches;
+    }
+  });
+}
+
+}  // namespace pfmd

@@ -96,6 +96,8 @@ __global__ void k_invert_z(Atoms A, Box B, Ctl* ctl) {
 __device__ __forceinline__ double kick1(double v, double f, double m, double ts2) {
   return __dadd_rn(v, __dmul_rn(__ddiv_rn(__ddiv_rn(f, m), c_mass_coef), ts2));
 }
+// the same with a precomputed 1/(m*mass_coef): no FP64 divide on the step
+__device__ __forceinline__ double kick1_fast(double v, double f, double kc, double ts2) { return v + f * kc * ts2; }
 // x = x + v*ts(1) then one shift back into [0, L] (md_integrators.f90:19-24)
 __device__ __forceinline__ double drift1(double x, double v, double ts1, double L) {
   x = __dadd_rn(x, __dmul_rn(v, ts1));
@@ -106,19 +108,29 @@ __device__ __forceinline__ double drift1(double x, double v, double ts1, double 
   return x;
 }
 
+template <bool EXACT>
 __global__ void k_kick(GroupRef g, int xyz, double ts2, Atoms A, Ctl* ctl) {
   if (ctl->stop) return;
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   if (ind >= ctl->group_n[g.g]) return;
   const int i = g.idx[ind];
   const double4_32a f = A.frc[i];
-  const double m = A.mass[i];
   double4_32a v = A.vel[i];
-  if (xyz) {
-    v.x = kick1(v.x, f.x, m, ts2);
-    v.y = kick1(v.y, f.y, m, ts2);
+  if (EXACT) {
+    const double m = A.mass[i];
+    if (xyz) {
+      v.x = kick1(v.x, f.x, m, ts2);
+      v.y = kick1(v.y, f.y, m, ts2);
+    }
+    v.z = kick1(v.z, f.z, m, ts2);
+  } else {
+    const double kc = A.kc[i];
+    if (xyz) {
+      v.x = kick1_fast(v.x, f.x, kc, ts2);
+      v.y = kick1_fast(v.y, f.y, kc, ts2);
+    }
+    v.z = kick1_fast(v.z, f.z, kc, ts2);
   }
-  v.z = kick1(v.z, f.z, m, ts2);
   A.vel[i] = v;
 }
 
@@ -140,6 +152,7 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
 }
 
 // Nose-Hoover scaling (optional), half kick and drift of the xyz group in one pass.
+template <bool EXACT>
 __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, Atoms A, Box B,
                              Ctl* ctl) {
   if (ctl->stop) return;
@@ -147,7 +160,6 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   if (ind >= ctl->group_n[g.g]) return;
   const int i = g.idx[ind];
   const double4_32a f = A.frc[i];
-  const double m = A.mass[i];
   double4_32a v = A.vel[i];
   if (nhc_scale) {
     const double s = ctl->nhc[nhc_scale - 1].s;
@@ -155,9 +167,17 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
     v.y *= s;
     v.z *= s;
   }
-  v.x = kick1(v.x, f.x, m, ts2);
-  v.y = kick1(v.y, f.y, m, ts2);
-  v.z = kick1(v.z, f.z, m, ts2);
+  if (EXACT) {
+    const double m = A.mass[i];
+    v.x = kick1(v.x, f.x, m, ts2);
+    v.y = kick1(v.y, f.y, m, ts2);
+    v.z = kick1(v.z, f.z, m, ts2);
+  } else {
+    const double kc = A.kc[i];
+    v.x = kick1_fast(v.x, f.x, kc, ts2);
+    v.y = kick1_fast(v.y, f.y, kc, ts2);
+    v.z = kick1_fast(v.z, f.z, kc, ts2);
+  }
   A.vel[i] = v;
   double4_32a p = A.pos[i];
   p.x = drift1(p.x, v.x, ts1, B.L[0]);
@@ -383,17 +403,26 @@ void launch_check_all(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
 void launch_invert_z(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
   if (A.N > 0) { k_invert_z<<<nb(A.N, 256), 256, 0, s>>>(A, B, ctl); ++g_kernel_launches; }
 }
-void launch_kick(const GroupRef& g, bool xyz, double ts2, const Atoms& A, Ctl* ctl, cudaStream_t s) {
-  if (g.cap > 0) { k_kick<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts2, A, ctl); ++g_kernel_launches; }
+void launch_kick(const GroupRef& g, bool xyz, double ts2, bool exact, const Atoms& A, Ctl* ctl, cudaStream_t s) {
+  if (g.cap <= 0) return;
+  if (exact)
+    k_kick<true><<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts2, A, ctl);
+  else
+    k_kick<false><<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts2, A, ctl);
+  ++g_kernel_launches;
 }
 void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, const Atoms& A, const Box& B, Ctl* ctl,
                   cudaStream_t s) {
   if (g.cap > 0) { k_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts1, write_posq ? 1 : 0, A, B, ctl); ++g_kernel_launches; }
 }
-void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, const Atoms& A,
-                       const Box& B, Ctl* ctl, cudaStream_t s) {
-  if (g.cap > 0)
-    { k_kick_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, A, B, ctl); ++g_kernel_launches; }
+void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
+  if (g.cap <= 0) return;
+  if (exact)
+    k_kick_drift<true><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, A, B, ctl);
+  else
+    k_kick_drift<false><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, A, B, ctl);
+  ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s) {

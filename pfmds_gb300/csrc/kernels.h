@@ -7,12 +7,17 @@
 //              cell binning
 //   groups     int idx[cap] (0-based atom indexes); current sizes live in
 //              Ctl::group_n so captured graphs survive change_particle_group_N
-//   lists      slot-major: nlist[slot*stride + row] holds the group-2 index (jnd)
-//              of a row's neighbour, rows padded to `stride` (multiple of 32) so
-//              that a warp reading one slot of 32 consecutive rows is coalesced;
-//              nnum/pidx/lessnnum/bnd [rows]
-//   cells      per list: cell_start[ncell+1], cell_jnd[cap2] (group-2 indexes
-//              grouped by cell), cell_of[cap2], cell_count/cursor[ncell]
+//   lists      slot-major: nlist[slot*stride + row] (stride = rows rounded up to
+//              32), a row's entries in the reference's order (ascending group-2
+//              index).  Main lists store the partner's atom index; the graphene
+//              nearest-neighbour list stores tb row indexes.  Consecutive rows sit
+//              on consecutive lanes, so a warp reading one slot of its rows is
+//              coalesced, and in an ordered crystal slot p of neighbouring rows
+//              points at neighbouring atoms (a near-coalesced position gather).
+//              nnum/pidx/lessnnum/bnd [rows]; row_of[N]: row of an atom (-1 if
+//              none) for lists whose kernels address the partner's row
+//   cells      per list: cell_start[ncell+1]; cell-ordered jnd/atom/posq copies of
+//              the column group [cap2]; cell_of[cap2]; cell_count/cursor[ncell]
 #pragma once
 
 #include <cuda_runtime.h>
@@ -32,12 +37,14 @@ struct Atoms {
   double4_32a* frc;
   double* mass;
   int4* posq;
+  double* kc;  // 1/(m*mass_coef) per atom: the precision form's kick factor
 };
 
 struct ListDev {
   int id;            // index into Ctl::maxnnum
   int rows;          // nl%N
-  int nmax, stride;
+  int nmax, stride;  // nlist[slot*stride + row]
+  int tpa;           // threads per row in the force kernels (1..32, power of two)
   int* nnum;
   int* nlist;
   int* pidx;
@@ -45,6 +52,7 @@ struct ListDev {
   int* bnd;          // first group-2 index whose atom index exceeds the row's atom
   const int* row_idx;  // row group indexes (particle_index source)
   const int* col_idx;  // column group indexes
+  const int* row_of;   // atom -> row (g1 == g2 lists that need it), else null
   int row_group, col_group;  // 0-based group numbers (sizes in Ctl::group_n)
   int row_cap, col_cap;
 };
@@ -55,7 +63,9 @@ struct CellGrid {
   int* start;   // [ncell+1]
   int* count;   // [ncell]
   int* cursor;  // [ncell]
-  int* jnd;     // [col_cap]
+  int* jnd;     // [col_cap] group-2 index, cell order
+  int* atom;    // [col_cap] atom index, cell order
+  int4* posq;   // [col_cap] fixed-point position, cell order
   int* cell_of; // [col_cap]
 };
 
@@ -130,10 +140,12 @@ void launch_step_begin(int phase, int n_changes, const ChangeSpec* changes, int 
                        Ctl* ctl, cudaStream_t s);
 void launch_check_all(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_invert_z(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
-void launch_kick(const GroupRef& g, bool xyz, double ts2, const Atoms& A, Ctl* ctl, cudaStream_t s);
+// exact: the reference's f/m/mass_coef*dt/2 with round-to-nearest divides (plain form);
+// otherwise f*kc*dt/2 (precision form)
+void launch_kick(const GroupRef& g, bool xyz, double ts2, bool exact, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, const Atoms& A, const Box& B,
                   Ctl* ctl, cudaStream_t s);
-void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale,
+void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s);

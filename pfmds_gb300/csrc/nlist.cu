@@ -6,15 +6,19 @@
 // step; find_gr_nearest_neighbors / find_norm_in_graphene (graphenenorm.f90:8-56).
 //
 // Here the candidates come from a cell grid over the column group (cells at least
-// r_cut wide, so the 27 surrounding cells hold every partner), one warp per row
-// tests them, and the row is sorted by group-2 index before it is written, so a
-// row holds exactly the reference's entries in the reference's order.  In the
-// plain form an FP32 prefilter with a safety margin discards far candidates and
-// the survivors are tested with the exact FP64 predicate (mi_exact); the
-// precision form uses the FP32 predicate alone.  The converse list is built the
-// same way with the groups swapped at the source list's rebuild steps: its
-// membership equals the transpose because dr.dr is symmetric bit for bit.
-// Distances are not stored: every force kernel recomputes them from positions.
+// r_cut wide, so the 27 surrounding cells hold every partner).  Binning writes
+// cell-ordered copies of each candidate's group-2 index, atom index and
+// fixed-point position, so one warp per row streams its candidates contiguously.
+// The row is sorted by group-2 index before it is written, so it holds exactly the
+// reference's entries in the reference's order; the entries stored are the atom
+// indexes of those partners (the force kernels need nothing else) and the
+// reference's group-2 indexes are recovered on read-back.  In the plain form an
+// FP32 prefilter with a safety margin discards far candidates and the survivors
+// are tested with the exact FP64 predicate (mi_exact); the precision form uses the
+// fixed-point separation alone.  The converse list is built the same way with the
+// groups swapped at the source list's rebuild steps: its membership equals the
+// transpose because dr.dr is symmetric bit for bit.  Distances are not stored:
+// every force kernel recomputes them from positions.
 #include <climits>
 
 #include "kernels.h"
@@ -67,13 +71,16 @@ __global__ void k_bin_scan(CellGrid cg, Ctl* ctl) {
   if (t == nt - 1) cg.start[n] = sh[t];
 }
 
-__global__ void k_bin_scatter(ListDev L, CellGrid cg, Ctl* ctl) {
+__global__ void k_bin_scatter(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
   if (ctl->stop) return;
   int n2 = ctl->group_n[L.col_group];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n2) return;
   int slot = atomicAdd(&cg.cursor[cg.cell_of[j]], 1);
+  const int a = L.col_idx[j];
   cg.jnd[slot] = j;
+  cg.atom[slot] = a;
+  cg.posq[slot] = A.posq[a];
 }
 
 // One warp per row.  CAP >= nmax rounded up to a power of two.
@@ -131,17 +138,17 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
           bool hit = false;
           int jnd = 0;
           if (k < e) {
-            jnd = cg.jnd[k];
-            const int aj = L.col_idx[jnd];
+            const int aj = cg.atom[k];
             if (aj != ai) {
               float d[3];
-              float r2f = mi_q(piq, A.posq[aj], B, d);
+              const float r2f = mi_q(piq, cg.posq[k], B, d);
               if (PREC) {
                 hit = r2f < rcp2;
               } else if (r2f < rcp2) {
                 double dd[3];
                 hit = mi_exact(pi, A.pos[aj], B, dd) < rc2;
               }
+              if (hit) jnd = cg.jnd[k];
             }
           }
           const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -184,18 +191,16 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   // lessnnum: entries before the first neighbour with a larger atom index
   // (md_neighbours.f90:78); the converse list leaves it at zero as the reference does
   int less = cnt;
-  if (!converse) {
-    for (int p0 = 0; p0 < cnt; p0 += 32) {
-      const int p = p0 + lane;
-      const bool gt = p < cnt && ai < L.col_idx[buf[p]];
-      const unsigned m = __ballot_sync(0xffffffffu, gt);
-      if (m) {
-        less = p0 + __ffs(m) - 1;
-        break;
-      }
+  
+  for (int p0 = 0; p0 < cnt; p0 += 32) {
+    const int p = p0 + lane;
+    const int aj = p < cnt ? L.col_idx[buf[p]] : 0;
+    if (p < cnt) L.nlist[(size_t)p * L.stride + row] = aj;
+    if (!converse && less == cnt) {
+      const unsigned m = __ballot_sync(0xffffffffu, p < cnt && ai < aj);
+      if (m) less = p0 + __ffs(m) - 1;
     }
   }
-  for (int p = lane; p < cnt; p += 32) L.nlist[(size_t)p * L.stride + row] = buf[p];
   if (lane == 0) {
     L.nnum[row] = cnt;
     L.pidx[row] = ai;
@@ -204,6 +209,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   }
 }
 
+// tb entries are atoms; the nn list keeps tb row indexes (tb lists have g1 == g2)
 template <bool PREC>
 __global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B, Ctl* ctl) {
   if (ctl->stop) return;
@@ -211,11 +217,11 @@ __global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B,
   if (i >= tb.rows) return;
   const int ai = tb.row_idx[i];
   const int n = tb.nnum[i];
+
   int k = 0;
   bool bad = false;
   for (int p = 0; p < n; ++p) {
-    const int jnd = tb.nlist[(size_t)p * tb.stride + i];
-    const int aj = tb.col_idx[jnd];
+    const int aj = tb.nlist[(size_t)p * tb.stride + i];
     bool in;
     if (PREC) {
       float d[3];
@@ -229,7 +235,7 @@ __global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B,
     if (in) {
       k = k + 1;
       if (k <= 3) {
-        nn.nlist[(size_t)(k - 1) * nn.stride + i] = jnd;
+        nn.nlist[(size_t)(k - 1) * nn.stride + i] = tb.row_of[aj];
       } else {
         set_error(ctl, ST_GR_NN, EK_GR_TOO_MANY, i + 1, 0, 0);
         bad = true;
@@ -241,20 +247,19 @@ __global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B,
   nn.nnum[i] = 3;
 }
 
+// Normals of the nn rows, stored per atom (norm[atom]); nn entries are group
+// indexes of nn.col_idx (tb rows, or group 6 of the list without tb).
 template <bool PREC>
 __global__ void k_normals(ListDev nn, double4_32a* norm, int simplified, Atoms A, Box B, Ctl* ctl) {
   if (ctl->stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nn.rows) return;
+  if (i >= nn.rows || i >= nn.row_cap) return;  // rows past the row group have no atom
+  const int ai = nn.row_idx[i];
   if (simplified) {
-    norm[i] = make_double4_32a(0.0, 0.0, 1.0, 0.0);
+    norm[ai] = make_double4_32a(0.0, 0.0, 1.0, 0.0);
     return;
   }
-  // rows past the row group keep zero vectors (the reference normalises a zero
-  // vector there too)
-  const bool has_row = i < nn.row_cap;
-  const int ai = has_row ? nn.row_idx[i] : 0;
-  const int cnt = has_row ? nn.nnum[i] : 0;
+  const int cnt = nn.nnum[i];
   double d[3][3];
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
@@ -287,7 +292,7 @@ __global__ void k_normals(ListDev nn, double4_32a* norm, int simplified, Atoms A
     g2 = -g2;
   }
   const double nr = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
-  norm[i] = make_double4_32a(g0 / nr, g1 / nr, g2 / nr, 0.0);
+  norm[ai] = make_double4_32a(g0 / nr, g1 / nr, g2 / nr, 0.0);
 }
 
 __global__ void k_nnum_max(ListDev L, Ctl* ctl) {
@@ -310,7 +315,7 @@ void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, 
   cudaMemsetAsync(cg.count, 0, sizeof(int) * (size_t)cg.ncell, s);
   if (L.col_cap > 0) { k_bin_count<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, A, ctl); ++g_kernel_launches; }
   { k_bin_scan<<<1, 1024, 0, s>>>(cg, ctl); ++g_kernel_launches; }
-  if (L.col_cap > 0) { k_bin_scatter<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, ctl); ++g_kernel_launches; }
+  if (L.col_cap > 0) { k_bin_scatter<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, A, ctl); ++g_kernel_launches; }
 }
 
 template <bool PREC>
