@@ -188,6 +188,12 @@ def run_ours(args):
                 total_ms += sim.advance_timed(S)
         launches = sim.kernel_launches - launches0
         e1 = sim.energies()["conserved"]
+        if args.quick:
+            if rank == 0:
+                print(json.dumps({"metric": METRIC, "value": n * S * K / (total_ms / 1e3), "unit": "atom-steps/s",
+                                  "ms_per_md_step": total_ms / K / S, "quick": True, "gpu_launches": launches}))
+            sim.close()
+            return
         total_ms = dist_max(dist, total_ms)
         atoms_all = dist_sum(dist, float(n))
         value = atoms_all * S * K / (total_ms / 1e3)
@@ -315,6 +321,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-md-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline timing loop only (no plain form, e2e, roofline or CPU legs), for profiling")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -82,12 +82,90 @@ static const double MOMENTA_COEF = 1.3806488 / 1.6605389217 * 1e-6;
 // Threads per list row: enough threads to fill the GPU (~152 SMs x 32 resident
 // warps) when rows are few, but at least ~2 entries per thread, and one thread
 // per row for large lists so that a warp reads 32 consecutive rows' slots.
-static int auto_tpa(int rows, double mean_entries) {
+static int auto_tpa(int rows, double mean_entries, bool prec) {
   const double want = 152.0 * 32 * 32 / std::max(rows, 1);
   int t = 1;
-  while (t < want && t < 32) t <<= 1;
+  // FP32 kernels are latency bound: the largest power of two within the target;
+  // FP64 kernels hide pipe latency with more threads: the smallest above it
+  if (prec)
+    while (2 * t <= want && t < 32) t <<= 1;
+  else
+    while (t < want && t < 32) t <<= 1;
   while (t > 1 && t > mean_entries / 2.0) t >>= 1;
   return t;
+}
+
+template <class R>
+static void fill_lj(LJc<R>& c, const LJPar& P) {
+  c.eps4 = (R)(4.0 * P.eps);
+  c.sig = (R)P.sig;
+  c.R1 = (R)P.R1;
+  c.R2 = (R)P.R2;
+  c.inv_w = (R)(1.0 / (P.R2 - P.R1));
+  c.c6 = (R)P.c6;
+  c.c12 = (R)P.c12;
+  c.c6t6 = (R)P.c6t6;
+  c.c12t12 = (R)P.c12t12;
+}
+void derive(LJPar& P) {
+  fill_lj(P.d, P);
+  fill_lj(P.f, P);
+}
+template <class R>
+static void fill_cos(Cosc<R>& c, const CosPar& P, bool morse) {
+  c.sig = (R)P.sig;
+  c.delt = (R)P.delt;
+  c.a = (R)P.a;
+  c.r0 = (R)P.r0;
+  c.R1 = (R)P.R1;
+  c.R2 = (R)P.R2;
+  c.inv_w = (R)(1.0 / (P.R2 - P.R1));
+  c.pref = (R)(morse ? P.D : 4.0 * P.eps);
+}
+void derive(CosPar& P, bool morse) {
+  fill_cos(P.d, P, morse);
+  fill_cos(P.f, P, morse);
+}
+template <class R>
+static void fill_rjl(RJLc<R>& c, const RJLPar& P) {
+  c.A0 = (R)P.A0;
+  c.xi = (R)P.xi;
+  c.R1 = (R)P.R1;
+  c.R2 = (R)P.R2;
+  c.inv_w = (R)(1.0 / (P.R2 - P.R1));
+  c.inv_r0 = (R)(1.0 / P.r0);
+  c.m2q = (R)(-2.0 * P.q);
+  c.mp = (R)(-P.p);
+  c.a2 = (R)(2.0 * P.A0);
+  c.pr0 = (R)(P.p / P.r0);
+  c.qr0 = (R)(P.q / P.r0);
+}
+void derive(RJLPar& P) {
+  fill_rjl(P.d, P);
+  fill_rjl(P.f, P);
+}
+template <class R>
+static void fill_tb(TBc<R>& c, const TBPar& P) {
+  c.d = (R)P.d;
+  c.s = (R)P.s;
+  c.b = (R)P.b;
+  c.r0 = (R)P.r0;
+  c.delt = (R)P.delt;
+  c.a0 = (R)P.a0;
+  c.c02 = (R)P.c02;
+  c.d02 = (R)P.d02;
+  c.R1 = (R)P.R1;
+  c.R2 = (R)P.R2;
+  c.inv_w = (R)(1.0 / (P.R2 - P.R1));
+  c.ex = (R)(1.0 / P.delt + 1.0);
+  c.sq2s = (R)std::sqrt(2.0 * P.s);
+  c.sq2os = (R)std::sqrt(2.0 / P.s);
+  c.pre_e = (R)(P.d / (P.s - 1.0));
+  c.c02d02 = (R)(P.c02 / P.d02);
+}
+void derive(TBPar& P) {
+  fill_tb(P.dd, P);
+  fill_tb(P.f, P);
 }
 
 static double now_s() {
@@ -125,6 +203,7 @@ struct InterH {
   TBPar tb{};
   bool general = false;  // lj1g weights for a group not in ascending atom order
   DBuf<double> scratch;  // rjl 1/Eb, tb bond orders
+  DBuf<double2> pair;    // rjl plain form: per-slot force coefficients
   DBuf<double4_32a> norm;    // ljc / morsec graphene normals
   int tb_inter = -1;     // ljc / morsec: the first tb interaction
   double rc_nn = 0.0;
@@ -158,6 +237,10 @@ class Engine {
   bool prec = false;
   bool fuse_kick_drift = true;
   int fused_nhc_chain = -1;  // chain whose scaling folds into the first kick
+  // force-phase fusion (Epi): the first force kernel stores instead of adding,
+  // the last one applies the second half-kick
+  bool store_first = false, kick_last = false;
+  DBuf<unsigned char> mflag;  // per atom: bit 0 in the xyz group, bit 1 in the z group
   bool need_check_all = true;
 
   // md() loop state
@@ -224,7 +307,8 @@ class Engine {
   bool is_event(const StepPlan& p) const;
   void enqueue_step(const StepPlan& p);
   void enqueue_lists(const StepPlan& p);
-  void enqueue_forces(bool energy);
+  void enqueue_forces(bool energy, bool kick = false);
+  void plan_fusion();
   void run_plans(const std::vector<StepPlan>& plans);
   void host_events(const StepPlan& p);
   void get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f);
@@ -399,7 +483,10 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     L.d.rows = rows;
     L.d.nmax = nmax;
     L.d.stride = ((std::max(rows, 1) + 31) / 32) * 32;
-    L.d.tpa = opt.threads_per_row > 0 ? opt.threads_per_row : auto_tpa(rows, std::max(nmax, 2) / 2.0);
+    // the plain form keeps the reference's row order (bit-exact lists); the
+    // precision form keeps the deterministic cell-scan order
+    L.d.sorted = prec ? 0 : 1;
+    L.d.tpa = opt.threads_per_row > 0 ? opt.threads_per_row : auto_tpa(rows, std::max(nmax, 2) / 2.0, opt.form == PFMD_FORM_PRECISION);
     L.d.row_group = row_g - 1;
     L.d.col_group = col_g - 1;
     L.d.row_cap = static_cast<int>(groups[static_cast<size_t>(row_g - 1)].idx.size());
@@ -456,12 +543,16 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
         I.cp.simplified = sp.simplified ? 1 : 0;
         break;
       case pfmd_io::K_RJL:
-        I.rjl = RJLPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6]};
+        I.rjl = RJLPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6], {}, {}};
+        derive(I.rjl);
         break;
       case pfmd_io::K_TB:
-        I.tb = TBPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[6] * p[6], p[7] * p[7]};
+        I.tb = TBPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[6] * p[6], p[7] * p[7], {}, {}};
+        derive(I.tb);
         break;
     }
+    if (sp.kind == pfmd_io::K_LJ || sp.kind == pfmd_io::K_LJ1G) derive(I.lj);
+    if (sp.kind == pfmd_io::K_LJC || sp.kind == pfmd_io::K_MORSEC) derive(I.cp, sp.kind == pfmd_io::K_MORSEC);
     if (sp.kind == pfmd_io::K_LJ1G || sp.kind == pfmd_io::K_RJL || sp.kind == pfmd_io::K_TB) {
       // the reference indexes these lists' partners through the row arrays
       // (particle_index(nlist), Eb(nlist), nl%nlist(:,j)), which needs g1 == g2
@@ -622,13 +713,18 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   }
   for (auto& I : inters) {
     const ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
-    if (I.spec.kind == pfmd_io::K_RJL) I.scratch.alloc(static_cast<size_t>(std::max(N, 1)));  // 1/Eb per atom
+    if (I.spec.kind == pfmd_io::K_RJL) {
+      I.scratch.alloc(static_cast<size_t>(std::max(N, 1)));  // 1/Eb per atom
+      if (!prec) I.pair.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));
+    }
     if (I.spec.kind == pfmd_io::K_TB)
       I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));  // B per list slot
     if (I.lists[2] >= 0) {
       I.norm.alloc(static_cast<size_t>(std::max(N, 1)));  // normals per atom
       I.norm.zero(st);
     }
+    // lj1g in a group that is not in atom order needs lessnnum in the reference's order
+    if (I.spec.kind == pfmd_io::K_LJ1G && I.general) lists[static_cast<size_t>(I.lists[0])].d.sorted = 1;
     // lists whose kernels address a partner's row: tb (and the nn selection that
     // reads it), lj1g in a group that is not in ascending atom order
     std::vector<int> need;
@@ -644,6 +740,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
       L.d.row_of = L.row_of.p;
     }
   }
+  plan_fusion();
   // control block
   CK(cudaMalloc(&ctl, sizeof(Ctl)));
   CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
@@ -697,7 +794,7 @@ void Engine::tune_tpa() {
     CK(cudaMemcpy(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost));
     double tot = 0;
     for (int v : n) tot += v;
-    const int t = auto_tpa(L.d.rows, tot / static_cast<double>(n.size()));
+    const int t = auto_tpa(L.d.rows, tot / static_cast<double>(n.size()), prec);
     if (t != L.d.tpa) {
       L.d.tpa = t;
       changed = true;
@@ -854,25 +951,92 @@ void Engine::enqueue_lists(const StepPlan& p) {
       launch_normals(prec, lists[static_cast<size_t>(I.lists[2])].d, I.norm.p, I.cp.simplified, A, box, ctl, st);
 }
 
-void Engine::enqueue_forces(bool energy) {
-  for (size_t k = 0; k < inters.size(); ++k) {
-    InterH& I = inters[k];
-    const int key = static_cast<int>(k);
-    const int eslot = 4 + static_cast<int>(k % 16);
+// The force kernels that write forces, in launch order, and whether the first
+// may store (its rows are exactly the all-atoms group, the only group zero_forces
+// clears) and the last may kick (its rows hold every xyz and z atom).
+void Engine::plan_fusion() {
+  struct W {
+    int list;
+    bool epi;
+  };
+  std::vector<W> w;
+  for (auto& I : inters) {
+    switch (I.spec.kind) {
+      case pfmd_io::K_LJ:
+        w.push_back({I.lists[0], true});
+        w.push_back({I.lists[1], true});
+        break;
+      case pfmd_io::K_LJC:
+      case pfmd_io::K_MORSEC:
+        w.push_back({I.lists[0], false});
+        w.push_back({I.lists[1], false});
+        break;
+      default:
+        w.push_back({I.lists[0], true});
+    }
+  }
+  if (w.empty() || !changes.empty()) return;
+  auto rows_set = [&](int li) {
+    const ListH& L = lists[static_cast<size_t>(li)];
+    std::vector<char> s(static_cast<size_t>(N), 0);
+    const auto& g = groups[static_cast<size_t>(L.d.row_group)].idx;
+    for (size_t r = 0; r < g.size() && r < static_cast<size_t>(L.d.rows); ++r) s[static_cast<size_t>(g[r])] = 1;
+    return s;
+  };
+  const auto& all = groups[static_cast<size_t>(S.all_atoms - 1)].idx;
+  {
+    const ListH& L0 = lists[static_cast<size_t>(w.front().list)];
+    const auto& g0 = groups[static_cast<size_t>(L0.d.row_group)].idx;
+    std::vector<char> sa(static_cast<size_t>(N), 0);
+    for (int a : all) sa[static_cast<size_t>(a)] = 1;
+    store_first = w.front().epi && L0.d.rows == static_cast<int>(g0.size()) && rows_set(w.front().list) == sa;
+  }
+  if (fuse_kick_drift && w.back().epi) {
+    const auto s = rows_set(w.back().list);
+    bool cover = true;
+    std::vector<unsigned char> fl(static_cast<size_t>(N), 0);
+    for (int a : groups[static_cast<size_t>(S.xyz_moving - 1)].idx) fl[static_cast<size_t>(a)] |= 1;
+    for (int a : groups[static_cast<size_t>(S.z_moving - 1)].idx) fl[static_cast<size_t>(a)] |= 2;
+    for (int a = 0; a < N; ++a)
+      if (fl[static_cast<size_t>(a)] && !s[static_cast<size_t>(a)]) cover = false;
+    if (cover) {
+      kick_last = true;
+      mflag.alloc(static_cast<size_t>(std::max(N, 1)));
+      mflag.upload(fl.data(), fl.size(), st);
+    }
+  }
+}
+
+void Engine::enqueue_forces(bool energy, bool kick) {
+  // which launch is the first / last force writer
+  const int nint = static_cast<int>(inters.size());
+  auto epi = [&](bool first, bool last) {
+    Epi e{0, 0, prec ? 0 : 1, ts[1], mflag.p};
+    e.store = (first && store_first) ? 1 : 0;
+    e.kick = (last && kick && kick_last) ? 1 : 0;
+    return e;
+  };
+  for (int k = 0; k < nint; ++k) {
+    InterH& I = inters[static_cast<size_t>(k)];
+    const int key = k;
+    const int eslot = 4 + (k % 16);
+    const bool first = k == 0, last = k == nint - 1;
     const ListDev& L1 = lists[static_cast<size_t>(I.lists[0])].d;
     switch (I.spec.kind) {
       case pfmd_io::K_LJ:
-        launch_lj(prec, energy, L1, I.lj, A, box, ctl, eslot, key, st);
-        launch_lj(prec, false, lists[static_cast<size_t>(I.lists[1])].d, I.lj, A, box, ctl, eslot, key, st);
+        launch_lj(prec, energy, L1, I.lj, A, box, ctl, eslot, key, st, epi(first, false));
+        launch_lj(prec, false, lists[static_cast<size_t>(I.lists[1])].d, I.lj, A, box, ctl, eslot, key, st,
+                  epi(false, last));
         break;
       case pfmd_io::K_LJ1G:
-        launch_lj1g(prec, energy, I.general, L1, I.lj, A, box, ctl, eslot, key, st);
+        launch_lj1g(prec, energy, I.general, L1, I.lj, A, box, ctl, eslot, key, st, epi(first, last));
         break;
       case pfmd_io::K_RJL:
-        launch_rjl(prec, energy, L1, I.rjl, A, box, I.scratch.p, ctl, eslot, key, st);
+        launch_rjl(prec, energy, L1, I.rjl, A, box, I.scratch.p, I.pair.p, ctl, eslot, key, st, 3,
+                   epi(first, last));
         break;
       case pfmd_io::K_TB:
-        launch_tb(prec, energy, L1, I.tb, A, box, I.scratch.p, ctl, eslot, key, st);
+        launch_tb(prec, energy, L1, I.tb, A, box, I.scratch.p, ctl, eslot, key, st, 3, epi(first, last));
         break;
       case pfmd_io::K_LJC:
       case pfmd_io::K_MORSEC:
@@ -887,7 +1051,12 @@ void Engine::enqueue_forces(bool energy) {
 void Engine::enqueue_step(const StepPlan& p) {
   const bool nvms = integ == I_NVMS, nvt = integ == I_NVT;
   if (p.check_all) launch_check_all(A, box, ctl, st);
-  if (S.invert_z_vel) {
+  // an nve step without group changes lets the kick-drift kernel open the step
+  const bool fused_begin = !p.first && integ == I_NVE && changes.empty() && !S.invert_z_vel && fuse_kick_drift &&
+                           groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size() > 0;
+  if (fused_begin) {
+    // (nothing: k_kick_drift below)
+  } else if (S.invert_z_vel) {
     launch_step_begin(0, static_cast<int>(changes.size()), changes.data(), 0, S.ms_de, ctl, st);
     launch_invert_z(A, box, ctl, st);
     launch_step_begin(1, 0, nullptr, nvms ? 1 : 0, S.ms_de, ctl, st);
@@ -907,7 +1076,7 @@ void Engine::enqueue_step(const StepPlan& p) {
           launch_scale(static_cast<int>(c), gc, A, ctl, st);
       }
     if (fuse_kick_drift) {
-      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st);
+      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st, fused_begin);
       if (gz.cap > 0) {
         launch_kick(gz, false, ts[1], !prec, A, ctl, st);
         launch_drift(gz, false, ts[0], true, A, box, ctl, st);
@@ -922,11 +1091,13 @@ void Engine::enqueue_step(const StepPlan& p) {
   enqueue_lists(p);
   const GroupRef gall = gref(S.all_atoms);
   if (p.zero_mom) launch_zero_momentum(gall, A, ctl, st);
-  launch_zero_forces(gall, A, ctl, st);
-  enqueue_forces(p.energy);
+  if (!store_first) launch_zero_forces(gall, A, ctl, st);
+  enqueue_forces(p.energy, !p.first);
   if (!p.first) {
-    launch_kick(gx, true, ts[1], !prec, A, ctl, st);
-    if (gz.cap > 0) launch_kick(gz, false, ts[1], !prec, A, ctl, st);
+    if (!kick_last) {
+      launch_kick(gx, true, ts[1], !prec, A, ctl, st);
+      if (gz.cap > 0) launch_kick(gz, false, ts[1], !prec, A, ctl, st);
+    }
     if (nvt)
       for (size_t c = 0; c < S.nhc.size(); ++c) {
         const GroupRef gc = gref(S.nhc[c].group);
@@ -1280,9 +1451,12 @@ double Engine::kernel_bytes(const std::string& name) {
       if (name == "lj1g") return b;
     }
     if (k == pfmd_io::K_RJL) {
-      if (name == "rjl_density") return row_bytes(L1, IE, 0);
-      if (name == "rjl_force") return row_bytes(L1, IE + F, 0);
-      if (name == "forces") b += row_bytes(L1, IE, 0) + row_bytes(L1, IE + F, 0);
+      // the plain form writes two FP64 pair coefficients per entry in the density
+      // pass and reads them back in the force pass
+      const double PC = prec ? 0.0 : 16.0;
+      if (name == "rjl_density") return row_bytes(L1, IE, PC);
+      if (name == "rjl_force") return row_bytes(L1, IE + F, PC);
+      if (name == "forces") b += row_bytes(L1, IE, PC) + row_bytes(L1, IE + F, PC);
     }
     if (k == pfmd_io::K_TB) {
       if (name == "tb_bond") return row_bytes(L1, 0, 8.0);
@@ -1349,7 +1523,8 @@ double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
         return true;
       }
       if (kind == pfmd_io::K_RJL && (name == "rjl_density" || name == "rjl_force")) {
-        launch_rjl(prec, false, L1, I.rjl, A, box, I.scratch.p, ctl, eslot, 0, st, name == "rjl_density" ? 1 : 2);
+        launch_rjl(prec, false, L1, I.rjl, A, box, I.scratch.p, I.pair.p, ctl, eslot, 0, st,
+                   name == "rjl_density" ? 1 : 2);
         return true;
       }
       if (kind == pfmd_io::K_TB && (name == "tb_bond" || name == "tb_force")) {

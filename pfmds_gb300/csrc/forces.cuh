@@ -191,10 +191,65 @@ __device__ __forceinline__ void add_force(const Atoms& A, int ai, double fx, dou
   A.frc[ai] = f;
 }
 
+__device__ __forceinline__ double kick_component(double v, double f, double m, double kc, double ts2, int exact) {
+  // the plain form keeps the reference's f/m/mass_coef*dt/2 (md_integrators.f90:70)
+  return exact ? __dadd_rn(v, __dmul_rn(__ddiv_rn(__ddiv_rn(f, m), 1.6605389217 / 1.6021765654 * 100.0), ts2))
+               : v + f * kc * ts2;
+}
+// Stores or adds the row's force, then (Epi::kick) applies the second half-kick.
+__device__ __forceinline__ void finish_force(const Atoms& A, const Epi& E, int ai, double fx, double fy, double fz) {
+  double4_32a f;
+  if (E.store) {
+    f = make_double4_32a(fx, fy, fz, 0.0);
+  } else {
+    f = A.frc[ai];
+    f.x += fx;
+    f.y += fy;
+    f.z += fz;
+  }
+  A.frc[ai] = f;
+  if (E.kick) {
+    const unsigned char m = E.mflag[ai];
+    if (m) {
+      double4_32a v = A.vel[ai];
+      const double ms = A.mass[ai], kc = A.kc[ai];
+      if (m & 1) {
+        v.x = kick_component(v.x, f.x, ms, kc, E.ts2, E.exact);
+        v.y = kick_component(v.y, f.y, ms, kc, E.ts2, E.exact);
+      }
+      v.z = kick_component(v.z, f.z, ms, kc, E.ts2, E.exact);
+      A.vel[ai] = v;
+    }
+  }
+}
+
 // Energy of one row into the interaction's total (every thread of the grid calls it).
 __device__ __forceinline__ void energy_reduce(Ctl* ctl, int eslot, int ekey, double erow) {
   double v[1] = {erow}, out[1];
   if (grid_sum<1>(ctl, eslot, v, out)) ctl->e_inter[ekey] = out[0];
+}
+
+// The constants of a parameter set in the kernel's precision.
+template <bool PREC>
+__device__ __forceinline__ const LJc<typename RT<PREC>::R>& cst(const LJPar& p) {
+  if constexpr (PREC) return p.f; else return p.d;
+}
+template <bool PREC>
+__device__ __forceinline__ const Cosc<typename RT<PREC>::R>& cst(const CosPar& p) {
+  if constexpr (PREC) return p.f; else return p.d;
+}
+template <bool PREC>
+__device__ __forceinline__ const RJLc<typename RT<PREC>::R>& cst(const RJLPar& p) {
+  if constexpr (PREC) return p.f; else return p.d;
+}
+template <bool PREC>
+__device__ __forceinline__ const TBc<typename RT<PREC>::R>& cst(const TBPar& p) {
+  if constexpr (PREC) return p.f; else return p.dd;
+}
+// 1/x: one divide per pair in FP64 (the plain form), the fast reciprocal in FP32
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R xrcp(typename RT<PREC>::R x) {
+  if constexpr (PREC) return __frcp_rn(x); else return 1.0 / x;
 }
 
 static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }

@@ -13,19 +13,21 @@ __device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r
                                          const typename RT<PREC>::R* nv, typename RT<PREC>::R nnorm, bool metal,
                                          typename RT<PREC>::R& X, typename RT<PREC>::R& Y, typename RT<PREC>::R& E) {
   using R = typename RT<PREC>::R;
-  const R R1 = (R)P.R1, R2 = (R)P.R2, delt = (R)P.delt, inv_w = (R)(1.0 / (P.R2 - P.R1));
+  const auto& c = cst<PREC>(P);
+  const R R1 = c.R1, R2 = c.R2, delt = c.delt, inv_w = c.inv_w;
   const R nd = nv[0] * dr[0] + nv[1] * dr[1] + nv[2] * dr[2];
   R fc, dfc;
   fdfc<PREC>(r, R1, R2, inv_w, fc, dfc);
   if (!MORSE) {
-    const R x = (R)P.sig / r, x2 = x * x, V2 = x2 * x2 * x2, V1 = V2 * V2;
-    const R V3 = xpow<PREC>(fabs(nd) / r, delt);
-    X = (R(12) * V1 - (R(6) + delt) * V2 * V3) / (r * r) * fc - (V1 - V2 * V3) * dfc;
+    const R ir = xrcp<PREC>(r);
+    const R x = c.sig * ir, x2 = x * x, V2 = x2 * x2 * x2, V1 = V2 * V2;
+    const R V3 = xpow<PREC>(fabs(nd) * ir, delt);
+    X = (R(12) * V1 - (R(6) + delt) * V2 * V3) * (ir * ir) * fc - (V1 - V2 * V3) * dfc;
     Y = delt * V2 * V3 / nd * fc;
     E = (V1 - V2 * V3) * fc;
   } else {
-    const R a = (R)P.a;
-    const R V2 = xexp<PREC>(-a * (r - (R)P.r0)), V1 = V2 * V2;
+    const R a = c.a;
+    const R V2 = xexp<PREC>(-a * (r - c.r0)), V1 = V2 * V2;
     const R V3 = xpow<PREC>(metal ? fabs(nd) / (nnorm * r) : fabs(nd) / r, delt);
     X = R(2) * (a * V1 - (a + delt / r) * V2 * V3) / r * fc - (V1 - R(2) * V2 * V3) * dfc;
     Y = R(2) * delt * V2 * V3 / nd * fc;
@@ -45,10 +47,11 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
   Acc3<PREC> acc;
   Acc1<PREC> e;
   const int ai = valid ? nl.pidx[i] : 0;
-  const R pref = MORSE ? (R)P.D : (R)(4.0 * P.eps);
+  const auto& c = cst<PREC>(P);
+  const R pref = c.pref;
   if (valid) {
     const auto pi = T::load(A, ai);
-    const R R2 = (R)P.R2;
+    const R R2 = c.R2;
     const double4_32a ni = norm[ai];
     const R nv[3] = {(R)ni.x, (R)ni.y, (R)ni.z};
     const int n = nl.nnum[i];
@@ -63,7 +66,7 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
       }
     }
     if (!P.simplified) {
-      const R R1 = (R)P.R1, delt = (R)P.delt, inv_w = (R)(1.0 / (P.R2 - P.R1));
+      const R R1 = c.R1, delt = c.delt, inv_w = c.inv_w;
       for (int q = 0; q < 3; ++q) {
         const int j = ent(nn, i, q);
         if (j < 0 || j >= nn.rows || j >= nl.rows || j >= nn.row_cap) {
@@ -110,9 +113,9 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
             const R fc = fc_only<PREC>(r, R1, R2, inv_w);
             R V2;
             if (MORSE)
-              V2 = xexp<PREC>(-(R)P.a * (r - (R)P.r0));
+              V2 = xexp<PREC>(-c.a * (r - c.r0));
             else {
-              const R x = (R)P.sig / r, x2 = x * x;
+              const R x = c.sig / r, x2 = x * x;
               V2 = x2 * x2 * x2;
             }
             const R C = dr[0] * w[0] + dr[1] * w[1] + dr[2] * w[2];
@@ -141,8 +144,9 @@ __global__ void __launch_bounds__(256) k_cos_metal(ListDev nl, CosPar P, const d
   Acc3<PREC> acc;
   if (n > 0) {
     const auto pi = T::load(A, ai);
-    const R R2 = (R)P.R2;
-    const R pref = MORSE ? (R)P.D : (R)(4.0 * P.eps);
+    const auto& c = cst<PREC>(P);
+    const R R2 = c.R2;
+    const R pref = c.pref;
     for (int p = g.sub; p < n; p += TPA) {
       const int aj = ent(nl, g.row, p);
       R dr[3];

@@ -5,34 +5,38 @@ namespace pfmd {
 
 // lj: LennardJones.f90:23-69 (cosine switch, full list, force on the row atom)
 template <bool PREC, bool ENERGY, int TPA>
-__global__ void __launch_bounds__(256) k_lj(ListDev L, LJPar P, Atoms A, Box B, Ctl* ctl, int eslot, int ekey) {
+__global__ void __launch_bounds__(256) k_lj(ListDev L, LJPar P, Atoms A, Box B, Ctl* ctl, int eslot, int ekey,
+                                            Epi E) {
   using T = RT<PREC>;
   using R = typename T::R;
   if (ctl->stop) return;
   const Grp<TPA> g;
-  const int n = g.row < L.rows ? L.nnum[g.row] : 0;
-  const int ai = n > 0 ? L.pidx[g.row] : 0;
+  const bool valid = g.row < L.rows;
+  const int n = valid ? L.nnum[g.row] : 0;
+  const int ai = valid ? L.pidx[g.row] : 0;
+  const auto& c = cst<PREC>(P);
   Acc3<PREC> acc;
   Acc1<PREC> e;
   if (n > 0) {
     const auto pi = T::load(A, ai);
-    const R sig = (R)P.sig, R1 = (R)P.R1, R2 = (R)P.R2, eps4 = (R)(4.0 * P.eps), inv_w = (R)(1.0 / (P.R2 - P.R1));
+#pragma unroll 4
     for (int p = g.sub; p < n; p += TPA) {
       R dr[3];
       const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, g.row, p)), B, dr));
-      if (r < R2) {
-        const R x = sig / r, x2 = x * x, V = x2 * x2 * x2;
+      if (r < c.R2) {
+        const R ir = xrcp<PREC>(r);
+        const R x = c.sig * ir, x2 = x * x, V = x2 * x2 * x2;
         R fc, dfc;
-        fdfc<PREC>(r, R1, R2, inv_w, fc, dfc);
-        const R c = eps4 * (V * (R(12) * V - R(6)) / (r * r) * fc - V * (V - R(1)) * dfc);
-        acc.add(-c * dr[0], -c * dr[1], -c * dr[2]);
-        if (ENERGY) e.add(eps4 * V * (V - R(1)) * fc);
+        fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
+        const R k = c.eps4 * (V * (R(12) * V - R(6)) * (ir * ir) * fc - V * (V - R(1)) * dfc);
+        acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
+        if (ENERGY) e.add(c.eps4 * V * (V - R(1)) * fc);
       }
     }
   }
   acc.template reduce<TPA>();
   if (ENERGY) e.template reduce<TPA>();
-  if (n > 0 && g.sub == 0) add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+  if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
   if (ENERGY) energy_reduce(ctl, eslot, ekey, (n > 0 && g.sub == 0) ? e.get() : 0.0);
 }
 
@@ -44,55 +48,59 @@ __global__ void __launch_bounds__(256) k_lj(ListDev L, LJPar P, Atoms A, Box B, 
 // weights for any group order: w = [p < lessnnum(i)] + [i < bnd(j)].
 // Requires list groups g1 == g2, as the reference's particle_index(nlist(p,i)) does.
 template <bool PREC, bool ENERGY, bool GENERAL, int TPA>
-__global__ void __launch_bounds__(256) k_lj1g(ListDev L, LJPar P, Atoms A, Box B, Ctl* ctl, int eslot, int ekey) {
+__global__ void __launch_bounds__(256) k_lj1g(ListDev L, LJPar P, Atoms A, Box B, Ctl* ctl, int eslot, int ekey,
+                                              Epi E) {
   using T = RT<PREC>;
   using R = typename T::R;
   if (ctl->stop) return;
   const Grp<TPA> g;
-  const int n = g.row < L.rows ? L.nnum[g.row] : 0;
-  const int ai = n > 0 ? L.pidx[g.row] : 0;
+  const bool valid = g.row < L.rows;
+  const int n = valid ? L.nnum[g.row] : 0;
+  const int ai = valid ? L.pidx[g.row] : 0;
+  const auto& c = cst<PREC>(P);
   Acc3<PREC> acc;
   Acc1<PREC> e;
   if (n > 0) {
     const int less = L.lessnnum[g.row];
     const auto pi = T::load(A, ai);
-    const R R1 = (R)P.R1, R2 = (R)P.R2, c6 = (R)P.c6, c12 = (R)P.c12, c6t6 = (R)P.c6t6, c12t12 = (R)P.c12t12;
+#pragma unroll 4
     for (int p = g.sub; p < n; p += TPA) {
       const int aj = ent(L, g.row, p);
       R dr[3];
-      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dr));
-      if (r < R2) {  // beyond R2 the clamped switch makes force and energy exactly zero
+      const R r2 = T::d2(pi, T::load(A, aj), B, dr);
+      const R r = xsqrt<PREC>(r2);
+      if (r < c.R2) {  // beyond R2 the clamped switch makes force and energy exactly zero
         R w = R(1);
         if (GENERAL) w = R((p < less ? 1 : 0) + (g.row < L.bnd[L.row_of[aj]] ? 1 : 0));
-        const R invr2 = R(1) / (r * r);
+        const R invr2 = xrcp<PREC>(r2);
         const R U = invr2 * invr2 * invr2;
         R fcut, dfr;
-        f_dfr_cut<R>(r, R1, R2, fcut, dfr);
-        const R F = w * (U * invr2 * ((c12t12 * U - c6t6) * fcut - (c12 * U - c6) * dfr));
+        f_dfr_cut<R>(r, c.R1, c.R2, fcut, dfr);
+        const R F = w * (U * invr2 * ((c.c12t12 * U - c.c6t6) * fcut - (c.c12 * U - c.c6) * dfr));
         acc.add(-F * dr[0], -F * dr[1], -F * dr[2]);
-        if (ENERGY && p < less) {
-          R Ue, fp;
+        // the half list p <= lessnnum(i); in a row kept in cell order (groups in
+        // atom order only) that is the partners with a smaller atom index
+        if (ENERGY && (L.sorted ? p < less : aj < ai)) {
+          R fp;
           if constexpr (PREC) {
-            Ue = U;
-            const R x = (r - R1) / (R2 - R1);
-            fp = r <= R1 ? R(1) : R(1) + x * x * x * (R(-10) + R(15) * x - R(6) * x * x);
+            const R x = (r - c.R1) * c.inv_w;
+            fp = r <= c.R1 ? R(1) : R(1) + x * x * x * (R(-10) + R(15) * x - R(6) * x * x);
           } else {
-            Ue = 1.0 / (r * r * r * r * r * r);
-            fp = fcut_poly(r, R1, R2);
+            fp = fcut_poly(r, c.R1, c.R2);
           }
-          e.add(Ue * (c12 * Ue - c6) * fp);
+          e.add(U * (c.c12 * U - c.c6) * fp);
         }
       }
     }
   }
   acc.template reduce<TPA>();
   if (ENERGY) e.template reduce<TPA>();
-  if (n > 0 && g.sub == 0) add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+  if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
   if (ENERGY) energy_reduce(ctl, eslot, ekey, (n > 0 && g.sub == 0) ? e.get() : 0.0);
 }
 
 void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const Atoms& A, const Box& B, Ctl* ctl,
-               int eslot, int ekey, cudaStream_t s) {
+               int eslot, int ekey, cudaStream_t s, const Epi& E) {
   if (L.rows == 0) {
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
@@ -102,7 +110,7 @@ void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const A
     with_bool(energy, [&](auto en) {
       with_tpa(L.tpa, [&](auto t) {
         k_lj<decltype(pr)::value, decltype(en)::value, decltype(t)::value>
-            <<<grid, 256, 0, s>>>(L, P, A, B, ctl, eslot, ekey);
+            <<<grid, 256, 0, s>>>(L, P, A, B, ctl, eslot, ekey, E);
         ++g_kernel_launches;
       });
     });
@@ -110,7 +118,7 @@ void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const A
 }
 
 void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const LJPar& P, const Atoms& A,
-                 const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s) {
+                 const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s, const Epi& E) {
   if (L.rows == 0) {
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
@@ -121,7 +129,7 @@ void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const L
       with_bool(general, [&](auto ge) {
         with_tpa(L.tpa, [&](auto t) {
           k_lj1g<decltype(pr)::value, decltype(en)::value, decltype(ge)::value, decltype(t)::value>
-              <<<grid, 256, 0, s>>>(L, P, A, B, ctl, eslot, ekey);
+              <<<grid, 256, 0, s>>>(L, P, A, B, ctl, eslot, ekey, E);
           ++g_kernel_launches;
         });
       });

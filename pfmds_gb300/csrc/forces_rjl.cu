@@ -3,14 +3,21 @@
 // Eb_i = sqrt(sum exp(-2q(r/r0-1)) fc), stores 1/Eb per atom and, at energy steps,
 // the row energy A0*Er - xi*Eb; pass 2 gathers the pair forces with
 // 1/Eb_i + 1/Eb_j.  See forces.cuh for the execution scheme.
+//
+// The plain (FP64) form keeps the pair terms of pass 1 per list slot,
+//   a = 2 A0 (p/r0 fc - f' ) e_p / r,   b = xi (q/r0 fc - f'/2) e_q / r,
+// so pass 2 only needs the separation vector: F_i -= (a - b (1/Eb_i + 1/Eb_j)) dr.
+// That replaces two FP64 exponentials, a square root and a divide per pair with a
+// 16-byte load (GB300's FP64 rate is a small fraction of its FP32 rate).  The
+// precision form recomputes its FP32 terms instead.
 #include "forces.cuh"
 
 namespace pfmd {
 
 // inv_eb holds 1/Eb per atom: double for the plain form, float for the precision form.
 template <bool PREC, bool ENERGY, int TPA>
-__global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb, Ctl* ctl,
-                                                     int eslot, int ekey) {
+__global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb,
+                                                     double2* pair, Ctl* ctl, int eslot, int ekey) {
   using T = RT<PREC>;
   using R = typename T::R;
   if (ctl->stop) return;
@@ -18,23 +25,35 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   const bool valid = g.row < L.rows;
   const int n = valid ? L.nnum[g.row] : 0;
   const int ai = valid ? L.pidx[g.row] : 0;
+  const auto& c = cst<PREC>(P);
   Acc1<PREC> eb2, er;
   if (n > 0) {
     const auto pi = T::load(A, ai);
-    const R R1 = (R)P.R1, R2 = (R)P.R2, inv_r0 = (R)(1.0 / P.r0), m2q = (R)(-2.0 * P.q), mp = (R)(-P.p),
-            inv_w = (R)(1.0 / (P.R2 - P.R1));
+#pragma unroll 4
     for (int p = g.sub; p < n; p += TPA) {
       R dr[3];
       const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, g.row, p)), B, dr));
-      if (r <= R2) {
-        const R fc = fc_only<PREC>(r, R1, R2, inv_w);
-        R x;
-        if constexpr (PREC)
-          x = r * inv_r0 - 1.0f;
-        else
-          x = r / P.r0 - 1.0;
-        eb2.add(xexp<PREC>(m2q * x) * fc);
-        if (ENERGY) er.add(xexp<PREC>(mp * x) * fc);
+      if constexpr (PREC) {
+        if (r <= c.R2) {
+          const R fc = fc_only<PREC>(r, c.R1, c.R2, c.inv_w);
+          const R x = r * c.inv_r0 - R(1);
+          eb2.add(xexp<PREC>(c.m2q * x) * fc);
+          if (ENERGY) er.add(xexp<PREC>(c.mp * x) * fc);
+        }
+      } else {
+        double2 ab = make_double2(0.0, 0.0);
+        if (r <= c.R2) {
+          R fc, dfc;
+          fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
+          const R x = r * c.inv_r0 - R(1);
+          const R eq = xexp<PREC>(c.m2q * x), ep = xexp<PREC>(c.mp * x);
+          eb2.add(eq * fc);
+          if (ENERGY) er.add(ep * fc);
+          const R ir = xrcp<PREC>(r);
+          ab.x = c.a2 * (c.pr0 * fc - dfc * r) * ep * ir;
+          ab.y = c.xi * (c.qr0 * fc - dfc * R(0.5) * r) * eq * ir;
+        }
+        pair[(size_t)p * L.stride + g.row] = ab;
       }
     }
   }
@@ -44,7 +63,7 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   if (valid && g.sub == 0) {
     const double eb = sqrt(eb2.get());
     if constexpr (PREC)
-      static_cast<float*>(inv_eb)[ai] = (float)(1.0 / eb);
+      static_cast<float*>(inv_eb)[ai] = __frcp_rn((float)eb);
     else
       static_cast<double*>(inv_eb)[ai] = 1.0 / eb;
     if (ENERGY) erow = P.A0 * er.get() - P.xi * eb;
@@ -54,48 +73,51 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
 
 template <bool PREC, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A, Box B, const void* inv_eb,
-                                                   Ctl* ctl) {
+                                                   const double2* pair, Ctl* ctl, Epi E) {
   using T = RT<PREC>;
   using R = typename T::R;
   using IE = typename std::conditional<PREC, float, double>::type;
   const IE* ieb = static_cast<const IE*>(inv_eb);
   if (ctl->stop) return;
   const Grp<TPA> g;
-  const int n = g.row < L.rows ? L.nnum[g.row] : 0;
-  const int ai = n > 0 ? L.pidx[g.row] : 0;
+  const bool valid = g.row < L.rows;
+  const int n = valid ? L.nnum[g.row] : 0;
+  const int ai = valid ? L.pidx[g.row] : 0;
+  const auto& c = cst<PREC>(P);
   Acc3<PREC> acc;
   if (n > 0) {
     const auto pi = T::load(A, ai);
-    const R R1 = (R)P.R1, R2 = (R)P.R2, inv_r0 = (R)(1.0 / P.r0), m2q = (R)(-2.0 * P.q), mp = (R)(-P.p),
-            inv_w = (R)(1.0 / (P.R2 - P.R1));
-    const R a2 = (R)(2.0 * P.A0), pr0 = (R)(P.p / P.r0), qr0 = (R)(P.q / P.r0), xi = (R)P.xi;
     const R ieb_i = ieb[ai];
+#pragma unroll 4
     for (int p = g.sub; p < n; p += TPA) {
       const int aj = ent(L, g.row, p);
       R dr[3];
-      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dr));
-      if (r <= R2) {
-        R fc, dfc;
-        fdfc<PREC>(r, R1, R2, inv_w, fc, dfc);
-        R x;
-        if constexpr (PREC)
-          x = r * inv_r0 - 1.0f;
-        else
-          x = r / P.r0 - 1.0;
-        const R ep = xexp<PREC>(mp * x), eq = xexp<PREC>(m2q * x);
-        const R T1 = a2 * (pr0 * fc - dfc * r) * ep;
-        const R T2 = xi * (qr0 * fc - dfc * R(0.5) * r) * (ieb_i + (R)ieb[aj]) * eq;
-        const R c = (T1 - T2) / r;
-        acc.add(-c * dr[0], -c * dr[1], -c * dr[2]);
+      if constexpr (PREC) {
+        const R r = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dr));
+        if (r <= c.R2) {
+          R fc, dfc;
+          fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
+          const R x = r * c.inv_r0 - R(1);
+          const R ep = xexp<PREC>(c.mp * x), eq = xexp<PREC>(c.m2q * x);
+          const R T1 = c.a2 * (c.pr0 * fc - dfc * r) * ep;
+          const R T2 = c.xi * (c.qr0 * fc - dfc * R(0.5) * r) * (ieb_i + ieb[aj]) * eq;
+          const R k = (T1 - T2) * xrcp<PREC>(r);
+          acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
+        }
+      } else {
+        const double2 ab = pair[(size_t)p * L.stride + g.row];
+        T::d2(pi, T::load(A, aj), B, dr);
+        const R k = ab.x - ab.y * (ieb_i + ieb[aj]);
+        acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
       }
     }
   }
   acc.template reduce<TPA>();
-  if (n > 0 && g.sub == 0) add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+  if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
 }
 
 void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const Atoms& A, const Box& B, void* Eb,
-                Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts) {
+                double2* pair, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts, const Epi& E) {
   if (L.rows == 0) {
     if (energy && (parts & 1)) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
@@ -107,13 +129,13 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
       constexpr int TP = decltype(t)::value;
       if (parts & 1) {
         if (energy)
-          k_rjl_density<PR, true, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, ctl, eslot, ekey);
+          k_rjl_density<PR, true, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey);
         else
-          k_rjl_density<PR, false, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, ctl, eslot, ekey);
+          k_rjl_density<PR, false, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey);
         ++g_kernel_launches;
       }
       if (parts & 2) {
-        k_rjl_force<PR, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, ctl);
+        k_rjl_force<PR, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, E);
         ++g_kernel_launches;
       }
     });

@@ -17,8 +17,8 @@ __global__ void __launch_bounds__(128) k_tb_bond(ListDev L, TBPar P, Atoms A, Bo
   const int n = L.nnum[i];
   const int ai = L.pidx[i];
   const auto pi = T::load(A, ai);
-  const R R1 = (R)P.R1, R2 = (R)P.R2, a0 = (R)P.a0, c02 = (R)P.c02, d02 = (R)P.d02, delt = (R)P.delt,
-          inv_w = (R)(1.0 / (P.R2 - P.R1));
+  const auto& c = cst<PREC>(P);
+  const R R1 = c.R1, R2 = c.R2, a0 = c.a0, c02 = c.c02, d02 = c.d02, delt = c.delt, inv_w = c.inv_w;
   for (int p = 0; p < n; ++p) {
     R dp[3];
     const R rp = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, p)), B, dp));
@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(128) k_tb_bond(ListDev L, TBPar P, Atoms A, Bo
         const R rq = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, q)), B, dq));
         if (rq < R2) {
           const R cs = dot3<PREC>(dp, dq) / (rp * rq);
-          b += fc_only<PREC>(rq, R1, R2, inv_w) * (R(1) + c02 / d02 - c02 / (d02 + (R(1) + cs) * (R(1) + cs)));
+          b += fc_only<PREC>(rq, R1, R2, inv_w) * (R(1) + c.c02d02 - c02 / (d02 + (R(1) + cs) * (R(1) + cs)));
         }
       }
       b = xpow<PREC>(R(1) + a0 * b, -delt);
@@ -41,21 +41,19 @@ __global__ void __launch_bounds__(128) k_tb_bond(ListDev L, TBPar P, Atoms A, Bo
 
 template <bool PREC, bool ENERGY>
 __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, Box B, const double* Bb, Ctl* ctl,
-                                                  int eslot, int ekey) {
+                                                  int eslot, int ekey, Epi E) {
   using T = RT<PREC>;
   using R = typename T::R;
   if (ctl->stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double erow = 0.0;
-  if (i < L.rows && L.nnum[i] > 0) {
+  if (i < L.rows && (L.nnum[i] > 0 || E.store || E.kick)) {
     const int n = L.nnum[i];
     const int ai = L.pidx[i];
     const auto pi = T::load(A, ai);
-    const R R1 = (R)P.R1, R2 = (R)P.R2, a0 = (R)P.a0, c02 = (R)P.c02, d02 = (R)P.d02, delt = (R)P.delt,
-            d = (R)P.d, s = (R)P.s, bb = (R)P.b, r0 = (R)P.r0, inv_w = (R)(1.0 / (P.R2 - P.R1));
-    const R ex = (R)(1.0 / P.delt + 1.0);
-    const R sq2s = (R)sqrt(2.0 * P.s), sq2os = (R)sqrt(2.0 / P.s);
-    const R pre_e = d / (s - R(1));
+    const auto& c = cst<PREC>(P);
+    const R R1 = c.R1, R2 = c.R2, a0 = c.a0, c02 = c.c02, d02 = c.d02, delt = c.delt, d = c.d, s = c.s, bb = c.b,
+            r0 = c.r0, inv_w = c.inv_w, ex = c.ex, sq2s = c.sq2s, sq2os = c.sq2os, pre_e = c.pre_e;
     Acc3<PREC> acc;
     Acc1<PREC> e;
     for (int p = 0; p < n; ++p) {
@@ -74,7 +72,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
         R fq, dfq;
         fdfc<PREC>(rq, R1, R2, inv_w, fq, dfq);
         const R g1 = fq * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
-        const R g2 = dfq * a0 * (R(1) + c02 / d02 - c02 / t);
+        const R g2 = dfq * a0 * (R(1) + c.c02d02 - c02 / t);
 #pragma unroll
         for (int k = 0; k < 3; ++k)
           dB[k] += g1 * ((dp[k] + dq[k]) * rr - cosi * (dp[k] / (rp * rp) + dq[k] / (rq * rq))) + g2 * dq[k];
@@ -136,7 +134,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
           const R cosi = dot3<PREC>(dl, dq) * rr;
           const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
           const R t1 = fl * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
-          const R t2 = dfl * a0 * (R(1) + c02 / d02 - c02 / t);
+          const R t2 = dfl * a0 * (R(1) + c.c02d02 - c02 / t);
           const R pre = delt * R(0.5) * xpow<PREC>((R)Bb[(size_t)q * L.stride + j], ex);
           const R post = fc_only<PREC>(rq, R1, R2, inv_w) * d / (s - R(1)) * s * xexp<PREC>(-sq2s * bb * (rq - r0) / s);
           R f[3];
@@ -146,14 +144,14 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
         }
       }
     }
-    add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+    finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
     erow = e.get();
   }
   if (ENERGY) energy_reduce(ctl, eslot, ekey, erow);
 }
 
 void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B, double* Bb,
-               Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts) {
+               Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts, const Epi& E) {
   if (L.rows == 0) {
     if (energy && (parts & 2)) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
@@ -167,9 +165,9 @@ void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const A
     }
     if (parts & 2) {
       if (energy)
-        k_tb_force<PR, true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey);
+        k_tb_force<PR, true><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey, E);
       else
-        k_tb_force<PR, false><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey);
+        k_tb_force<PR, false><<<g, 128, 0, s>>>(L, P, A, B, Bb, ctl, eslot, ekey, E);
       ++g_kernel_launches;
     }
   });

@@ -152,10 +152,23 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
 }
 
 // Nose-Hoover scaling (optional), half kick and drift of the xyz group in one pass.
+// begin: also do k_step_begin's work for an nve step without group changes: every
+// thread checks the previous drift's out-of-cell verdict, one thread advances the
+// step counter and the previous-step potential energy.
 template <bool EXACT>
-__global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, Atoms A, Box B,
-                             Ctl* ctl) {
+__global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, int begin, Atoms A,
+                             Box B, Ctl* ctl) {
   if (ctl->stop) return;
+  if (begin) {
+    if (ctl->pending_oob) {
+      set_error(ctl, ST_OUT_OF_CELL, EK_OOB, ctl->oob_atom + 1, 0, 0);
+      return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ctl->md_step = ctl->md_step + 1;
+      ctl->pe_prev = ctl->pe_last;
+    }
+  }
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   if (ind >= ctl->group_n[g.g]) return;
   const int i = g.idx[ind];
@@ -416,12 +429,14 @@ void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, cons
   if (g.cap > 0) { k_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts1, write_posq ? 1 : 0, A, B, ctl); ++g_kernel_launches; }
 }
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
-                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin) {
   if (g.cap <= 0) return;
   if (exact)
-    k_kick_drift<true><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, A, B, ctl);
+    k_kick_drift<true><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0, A,
+                                                      B, ctl);
   else
-    k_kick_drift<false><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, A, B, ctl);
+    k_kick_drift<false><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0,
+                                                       A, B, ctl);
   ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,

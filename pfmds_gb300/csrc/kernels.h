@@ -45,6 +45,7 @@ struct ListDev {
   int rows;          // nl%N
   int nmax, stride;  // nlist[slot*stride + row]
   int tpa;           // threads per row in the force kernels (1..32, power of two)
+  int sorted;        // rows kept in the reference's order (ascending group-2 index)
   int* nnum;
   int* nlist;
   int* pidx;
@@ -75,21 +76,52 @@ struct GroupRef {
   int cap;  // capacity (launch size)
 };
 
-// potential parameters (plain FP64 copies; FP32 forms derived in the kernels)
+// Potential parameters.  Every constant a kernel needs is derived on the host
+// (both precisions), so no thread spends FP64 divides on parameter algebra.
+template <class R>
+struct LJc {
+  R eps4, sig, R1, R2, inv_w;     // lj (cosine switch)
+  R c6, c12, c6t6, c12t12;        // lj1g (LennardJones_1g.f90:21-24)
+};
 struct LJPar {
-  double eps, sig, R1, R2;
-  double c6, c12, c6t6, c12t12;  // lj1g
+  double eps, sig, R1, R2, c6, c12, c6t6, c12t12;
+  LJc<double> d;
+  LJc<float> f;
+};
+template <class R>
+struct Cosc {
+  R sig, delt, a, r0, R1, R2, inv_w;
+  R pref;  // 4 eps (ljc) or D (morsec)
 };
 struct CosPar {  // ljc: eps sig delt; morsec: D r0 a delt
   double eps, sig, delt, D, r0, a, R1, R2;
   int simplified;
+  Cosc<double> d;
+  Cosc<float> f;
+};
+template <class R>
+struct RJLc {
+  R A0, xi, R1, R2, inv_w, inv_r0, m2q, mp, a2, pr0, qr0;
 };
 struct RJLPar {
   double A0, xi, p, q, r0, R1, R2;
+  RJLc<double> d;
+  RJLc<float> f;
+};
+template <class R>
+struct TBc {
+  R d, s, b, r0, delt, a0, c02, d02, R1, R2, inv_w, ex, sq2s, sq2os, pre_e, c02d02;
 };
 struct TBPar {
   double d, s, b, r0, delt, a0, c0, d0, R1, R2, c02, d02;
+  TBc<double> dd;
+  TBc<float> f;
 };
+// Fill the derived constants of a parameter set.
+void derive(LJPar& P);
+void derive(CosPar& P, bool morse);
+void derive(RJLPar& P);
+void derive(TBPar& P);
 
 struct ChangeSpec {
   int from, to;  // 0-based groups
@@ -98,6 +130,17 @@ struct ChangeSpec {
 };
 
 enum Integ { I_NVE = 0, I_NVT = 1, I_NVMS = 2 };
+
+// How a force kernel finishes an atom's force.  store: the kernel is the first
+// and only writer of every atom of the all-atoms group, so it stores instead of
+// adding (zero_forces is skipped).  kick: it is the last writer of every moving
+// atom, so it also applies the second half-kick (v += f/m/mass_coef*dt/2 for the
+// xyz group, z only for the z group; flags bit 0 / bit 1).
+struct Epi {
+  int store, kick, exact;
+  double ts2;
+  const unsigned char* mflag;
+};
 
 // ---------------- neighbour lists (nlist.cu) ----------------
 void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
@@ -117,18 +160,22 @@ void launch_nnum_max(const ListDev& L, Ctl* ctl, cudaStream_t s);
 
 // ---------------- forces and energies (forces.cu) ----------------
 void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const Atoms& A, const Box& B,
-               Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+               Ctl* ctl, int eslot, int ekey, cudaStream_t s, const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
 void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const LJPar& P, const Atoms& A,
-                 const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s);
+                 const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s,
+                 const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
 // Multi-kernel interactions take `parts`, a bit mask of their kernels (all by
 // default; single kernels are launched alone only for timing).
-// inv_eb: per-row 1/Eb scratch (double[rows] for plain, float[rows] for precision)
-// parts: 1 density, 2 force
+// inv_eb: 1/Eb per atom (double[N] plain, float[N] precision); pair: the plain
+// form's per-slot force coefficients (double2[nmax*stride]) written by the density
+// pass.  parts: 1 density, 2 force
 void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const Atoms& A, const Box& B,
-                void* inv_eb, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3);
+                void* inv_eb, double2* pair, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3,
+                const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
 // parts: 1 bond orders, 2 force
 void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B,
-               double* Bbuf, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3);
+               double* Bbuf, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3,
+               const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
 // parts: 1 graphene side, 2 metal side
 void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
                 const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot,
@@ -146,7 +193,7 @@ void launch_kick(const GroupRef& g, bool xyz, double ts2, bool exact, const Atom
 void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, const Atoms& A, const Box& B,
                   Ctl* ctl, cudaStream_t s);
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
-                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s);
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);

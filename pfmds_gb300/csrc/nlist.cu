@@ -83,8 +83,68 @@ __global__ void k_bin_scatter(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
   cg.posq[slot] = A.posq[a];
 }
 
-// One warp per row.  CAP >= nmax rounded up to a power of two.
-template <bool PREC, int CAP>
+// Puts every cell's atoms in ascending group-2 order, so rows built from the
+// cell order (no per-row sort) are the same on every run.  One warp per cell;
+// cells of more than 32 atoms (rare: large or sparse cells) use an insertion
+// sort by one lane.
+__global__ void k_cell_sort(CellGrid cg, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= cg.ncell) return;
+  const int s = cg.start[c], e = cg.start[c + 1], len = e - s;
+  if (len <= 1) return;
+  if (len <= 32) {
+    int key = lane < len ? cg.jnd[s + lane] : INT_MAX;
+    int src = lane;
+    const int atom = lane < len ? cg.atom[s + lane] : 0;
+    const int4 pq = lane < len ? cg.posq[s + lane] : make_int4(0, 0, 0, 0);
+    for (int k = 2; k <= 32; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const int ok = __shfl_xor_sync(0xffffffffu, key, j);
+        const int os = __shfl_xor_sync(0xffffffffu, src, j);
+        const bool lower = (lane & j) == 0, up = (lane & k) == 0;
+        const bool take = lower ? ((key > ok) == up) : ((key < ok) == up);
+        if (take) {
+          key = ok;
+          src = os;
+        }
+      }
+    }
+    const int a = __shfl_sync(0xffffffffu, atom, src);
+    int4 q;
+    q.x = __shfl_sync(0xffffffffu, pq.x, src);
+    q.y = __shfl_sync(0xffffffffu, pq.y, src);
+    q.z = __shfl_sync(0xffffffffu, pq.z, src);
+    q.w = 0;
+    if (lane < len) {
+      cg.jnd[s + lane] = key;
+      cg.atom[s + lane] = a;
+      cg.posq[s + lane] = q;
+    }
+  } else if (lane == 0) {
+    for (int i = s + 1; i < e; ++i) {
+      const int k = cg.jnd[i], a = cg.atom[i];
+      const int4 q = cg.posq[i];
+      int j = i - 1;
+      while (j >= s && cg.jnd[j] > k) {
+        cg.jnd[j + 1] = cg.jnd[j];
+        cg.atom[j + 1] = cg.atom[j];
+        cg.posq[j + 1] = cg.posq[j];
+        --j;
+      }
+      cg.jnd[j + 1] = k;
+      cg.atom[j + 1] = a;
+      cg.posq[j + 1] = q;
+    }
+  }
+}
+
+// One warp per row.  CAP >= nmax rounded up to a power of two.  SORT: sort the
+// row by group-2 index (the reference's order; needed for bit-exact lists and for
+// lessnnum in groups that are not in atom order).  Without SORT the row keeps the
+// cell-scan order, which the per-cell sort makes deterministic.
+template <bool PREC, int CAP, bool SORT>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid cg, Atoms A, Box B, double rc2,
                                                              float rcp2, int converse, int src_rows, Ctl* ctl) {
   __shared__ int sbuf[kBuildWarps][CAP];
@@ -125,20 +185,40 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
     }
   }
   int cnt = 0;
+  int nless = 0;  // entries with a smaller atom index (lessnnum of an unsorted row)
+  const int nx = cg.nc[0];
   for (int z = lo[2]; z <= hi[2]; ++z) {
     const int cz = (z + cg.nc[2]) % cg.nc[2];
     for (int y = lo[1]; y <= hi[1]; ++y) {
       const int cy = (y + cg.nc[1]) % cg.nc[1];
-      for (int x = lo[0]; x <= hi[0]; ++x) {
-        const int cx = (x + cg.nc[0]) % cg.nc[0];
-        const int c = (cz * cg.nc[1] + cy) * cg.nc[0] + cx;
-        const int s = cg.start[c], e = cg.start[c + 1];
-        for (int k0 = s; k0 < e; k0 += 32) {
+      const int base = (cz * cg.nc[1] + cy) * nx;
+      // the x-cells of this (y,z) row as at most two contiguous candidate runs
+      int r0s, r0e, r1s = 0, r1e = 0;
+      if (nx < 3) {
+        r0s = cg.start[base];
+        r0e = cg.start[base + nx];
+      } else if (c0[0] >= 1 && c0[0] + 1 < nx) {
+        r0s = cg.start[base + c0[0] - 1];
+        r0e = cg.start[base + c0[0] + 2];
+      } else if (c0[0] == 0) {
+        r0s = cg.start[base];
+        r0e = cg.start[base + 2];
+        r1s = cg.start[base + nx - 1];
+        r1e = cg.start[base + nx];
+      } else {
+        r0s = cg.start[base + nx - 2];
+        r0e = cg.start[base + nx];
+        r1s = cg.start[base];
+        r1e = cg.start[base + 1];
+      }
+      for (int run = 0; run < 2; ++run) {
+        const int s0 = run ? r1s : r0s, e0 = run ? r1e : r0e;
+        for (int k0 = s0; k0 < e0; k0 += 32) {
           const int k = k0 + lane;
           bool hit = false;
-          int jnd = 0;
-          if (k < e) {
-            const int aj = cg.atom[k];
+          int jnd = 0, aj = 0;
+          if (k < e0) {
+            aj = cg.atom[k];
             if (aj != ai) {
               float d[3];
               const float r2f = mi_q(piq, cg.posq[k], B, d);
@@ -154,8 +234,13 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
           const unsigned m = __ballot_sync(0xffffffffu, hit);
           if (hit) {
             const int p = cnt + __popc(m & ((1u << lane) - 1u));
-            if (p < CAP) buf[p] = jnd;
+            if (SORT) {
+              if (p < CAP) buf[p] = jnd;
+            } else if (p < L.nmax) {
+              L.nlist[(size_t)p * L.stride + row] = aj;
+            }
           }
+          if (!SORT) nless += __popc(__ballot_sync(0xffffffffu, hit && aj < ai));
           cnt += __popc(m);
         }
       }
@@ -165,6 +250,15 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   if (cnt > L.nmax) {
     // 'error: too many neighbours', ind, nnumind  (md_neighbours.f90:80, :151)
     if (lane == 0) set_error(ctl, ST_NLIST_OVERFLOW, converse ? EK_CONVERSE_OVF : EK_OVERFLOW, L.id, row + 1, L.nmax + 1);
+    return;
+  }
+  if (!SORT) {
+    if (lane == 0) {
+      L.nnum[row] = cnt;
+      L.pidx[row] = ai;
+      L.lessnnum[row] = converse ? 0 : nless;
+      L.bnd[row] = INT_MAX;
+    }
     return;
   }
   // bitonic sort of buf[0..n) ascending, padded with INT_MAX
@@ -191,7 +285,6 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   // lessnnum: entries before the first neighbour with a larger atom index
   // (md_neighbours.f90:78); the converse list leaves it at zero as the reference does
   int less = cnt;
-  
   for (int p0 = 0; p0 < cnt; p0 += 32) {
     const int p = p0 + lane;
     const int aj = p < cnt ? L.col_idx[buf[p]] : 0;
@@ -318,32 +411,42 @@ void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, 
   if (L.col_cap > 0) { k_bin_scatter<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, A, ctl); ++g_kernel_launches; }
 }
 
-template <bool PREC>
+template <bool PREC, bool SORT>
 static void build_dispatch(const ListDev& L, const CellGrid& cg, const Atoms& A, const Box& B, double rc2,
                            float rcp2, int converse, int src_rows, Ctl* ctl, cudaStream_t s) {
   const int grid = blocks_for(L.rows, kBuildWarps);
   const int bs = kBuildWarps * 32;
   if (grid == 0) return;
   if (L.nmax <= 64)
-    { k_build<PREC, 64><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+    k_build<PREC, 64, SORT><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl);
   else if (L.nmax <= 128)
-    { k_build<PREC, 128><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+    k_build<PREC, 128, SORT><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl);
   else if (L.nmax <= 256)
-    { k_build<PREC, 256><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+    k_build<PREC, 256, SORT><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl);
   else if (L.nmax <= 512)
-    { k_build<PREC, 512><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+    k_build<PREC, 512, SORT><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl);
   else
-    { k_build<PREC, 1024><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl); ++g_kernel_launches; }
+    k_build<PREC, 1024, SORT><<<grid, bs, 0, s>>>(L, cg, A, B, rc2, rcp2, converse, src_rows, ctl);
+  ++g_kernel_launches;
 }
 
 void launch_build_list(bool prec, const ListDev& L, const CellGrid& cg, const Atoms& A, const Box& B, double rc,
                        double prefilter_margin, int converse, int src_rows, Ctl* ctl, cudaStream_t s) {
   const double rc2 = rc * rc;
+  if (!L.sorted) {
+    { k_cell_sort<<<blocks_for((long long)cg.ncell * 32, 256), 256, 0, s>>>(cg, ctl); ++g_kernel_launches; }
+  }
   if (prec) {
-    build_dispatch<true>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
+    if (L.sorted)
+      build_dispatch<true, true>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
+    else
+      build_dispatch<true, false>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
   } else {
     const double rp = rc + prefilter_margin;
-    build_dispatch<false>(L, cg, A, B, rc2, (float)(rp * rp), converse, src_rows, ctl, s);
+    if (L.sorted)
+      build_dispatch<false, true>(L, cg, A, B, rc2, (float)(rp * rp), converse, src_rows, ctl, s);
+    else
+      build_dispatch<false, false>(L, cg, A, B, rc2, (float)(rp * rp), converse, src_rows, ctl, s);
   }
 }
 
