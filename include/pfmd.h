@@ -175,6 +175,41 @@ int pfmd_time_kernel(pfmd_ctx* ctx, const char* name, int reps, double* ms, doub
  * first call and kept. */
 int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
 
+/* ---- rjl forces without device allocation ----------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * host codes whose device memory is all reserved up front by their own pool
+ * allocator, and loops that cannot take the device-wide synchronisation that
+ * cudaMalloc and cudaFree imply.  It allocates nothing; the caller passes every
+ * input and output as device memory it owns.
+ *
+ * Computes the plain (FP64) rjl forces and total energy of n_atoms atoms that
+ * all belong to one rjl interaction (rows = atoms 0..n_atoms-1, a full list):
+ *   pos     device, n_atoms x 3 doubles (x, y, z of atom i at pos[3i..3i+2])
+ *   box     host, the three periodic box lengths
+ *   params  host, the parameter file's seven values: A0 xi p q r0 R1 R2
+ *   nnum    device, n_atoms ints: entries of each row
+ *   nbr     device, n_atoms x max_nbr ints, row i at nbr[i*max_nbr]: 0-based
+ *           partner atoms (counts above max_nbr are cut, entries outside
+ *           0..n_atoms-1 skipped)
+ *   frc     device, n_atoms x 3 doubles, written (not added to)
+ *   energy  device, one double, or NULL to skip the energy
+ *   stream  cudaStream_t to launch on (NULL: the default stream); the call
+ *           returns once its three kernels are queued
+ *   err     optional host buffer of err_len bytes for a message on failure
+ * Returns PFMD_OK, PFMD_E_PARAM (sizes or parameters out of range, including
+ * n_atoms above 1048576, the capacity of its fixed scratch) or PFMD_E_CUDA.
+ *
+ * Its scratch (1/Eb per atom, per-block energy partials; about 8 MiB) is a
+ * fixed array inside the library, held by every device that loads it until the
+ * process exits.  The first call on each device looks up that array's device
+ * address with that device current; make that first call before any stream
+ * capture.  All calls share the one array, so calls whose kernels overlap on
+ * the GPU (other streams, other host threads) race: order them on one stream
+ * or with events. */
+int pfmd_rjl_forces_noalloc(int n_atoms, const double* pos, const double box[3], const double params[7],
+                            const int* nnum, const int* nbr, int max_nbr, double* frc, double* energy,
+                            void* stream, char* err, int err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,7 +31,7 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_get_state", "pfmd_set_state", "pfmd_energies", "pfmd_compute", "pfmd_ninteractions",
            "pfmd_nlist_shape", "pfmd_get_nlist", "pfmd_nlist_load", "pfmd_get_gr_norm", "pfmd_set_group_n",
            "pfmd_get_stream", "pfmd_kernel_launches", "pfmd_advance_timed", "pfmd_time_kernel",
-           "pfmd_flush_l2")
+           "pfmd_flush_l2", "pfmd_rjl_forces_noalloc")
 
 _LIB = None
 
@@ -88,6 +88,8 @@ def load(path=LIB_PATH):
     L.pfmd_advance_timed.argtypes = [vp, C.c_longlong, ip, dp]
     L.pfmd_time_kernel.argtypes = [vp, C.c_char_p, C.c_int, dp, dp]
     L.pfmd_flush_l2.argtypes = [vp, C.c_longlong]
+    # device buffers are passed as integer addresses (c_void_p)
+    L.pfmd_rjl_forces_noalloc.argtypes = [C.c_int, vp, dp, dp, vp, vp, C.c_int, vp, vp, vp, C.c_char_p, C.c_int]
     _LIB = L
     return L
 
