@@ -94,6 +94,7 @@ struct Box {
   double L[3], h[3];
   double qinv[3];  // 2^32 / L
   float qs[3];     // L / 2^32
+  double Ltol[3];  // L + 1e-7, the upper bound of the out-of-cell test (md_general.f90:346)
 };
 
 // ---------------------------------------------------------------------------
@@ -241,8 +242,11 @@ __device__ __forceinline__ void block_sum(double (&v)[K]) {
 
 // Grid-wide deterministic sum of K doubles per block.  Every block calls it with
 // its block-partial values; returns true in thread 0 of the last block to arrive,
-// with out[k] holding the grid totals summed in block order.  `slot` selects the
-// arrival counter; the last block resets it, so graphs can replay the kernel.
+// with out[k] holding the grid totals.  The last block sums the partials with all
+// its threads: thread t takes partials t, t + blockDim.x, ... in order, then the
+// block tree sums those -- a fixed order, so the result does not depend on which
+// block arrived last.  `slot` selects the arrival counter; the last block resets
+// it, so graphs can replay the kernel.
 template <int K>
 __device__ __forceinline__ bool grid_sum(Ctl* ctl, int slot, double (&v)[K], double (&out)[K]) {
   block_sum<K>(v);
@@ -256,14 +260,18 @@ __device__ __forceinline__ bool grid_sum(Ctl* ctl, int slot, double (&v)[K], dou
   }
   __syncthreads();
   if (!last) return false;
-  if (threadIdx.x == 0) {
-    __threadfence();
+  __threadfence();
+  double w[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double s = 0.0;
-      for (unsigned int b = 0; b < gridDim.x; ++b) s += ((volatile double*)ctl->partial)[(size_t)b * K + k];
-      out[k] = s;
-    }
+  for (int k = 0; k < K; ++k) w[k] = 0.0;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < K; ++k) w[k] += ((volatile double*)ctl->partial)[(size_t)b * K + k];
+  __syncthreads();  // block_sum's shared scratch is reused
+  block_sum<K>(w);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = w[k];
     ctl->counter[slot] = 0u;
   }
   return threadIdx.x == 0;

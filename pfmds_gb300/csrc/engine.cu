@@ -95,6 +95,15 @@ static int auto_tpa(int rows, double mean_entries, bool prec) {
   return t;
 }
 
+// The rjl density pass of the precision form has no force write-back and a short
+// body: twice the force pass's threads per row (measured faster on the Cu slab at
+// 2 -> 4), within the same entries-per-thread floor.
+static int pass1_tpa(int tpa, double mean_entries, bool prec) {
+  if (!prec) return tpa;
+  const int t = std::min(32, 2 * tpa);
+  return t > mean_entries / 4.0 ? tpa : t;
+}
+
 template <class R>
 static void fill_lj(LJc<R>& c, const LJPar& P) {
   c.eps4 = (R)(4.0 * P.eps);
@@ -389,6 +398,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     box.h[k] = 0.5 * S.xyz.box[k];
     box.qinv[k] = 4294967296.0 / box.L[k];
     box.qs[k] = static_cast<float>(box.L[k] / 4294967296.0);
+    box.Ltol[k] = box.L[k] + 0.0000001;
   }
   // groups: create_particle_group (md_general.f90:57-80)
   if (S.group_types.size() > PFMD_MAX_GROUPS) throw Error(PFMD_E_PARAM, "error: too many groups");
@@ -487,6 +497,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     // precision form keeps the deterministic cell-scan order
     L.d.sorted = prec ? 0 : 1;
     L.d.tpa = opt.threads_per_row > 0 ? opt.threads_per_row : auto_tpa(rows, std::max(nmax, 2) / 2.0, opt.form == PFMD_FORM_PRECISION);
+    L.d.tpa1 = opt.threads_per_row > 0 ? opt.threads_per_row
+                                       : pass1_tpa(L.d.tpa, std::max(nmax, 2) / 2.0, opt.form == PFMD_FORM_PRECISION);
     L.d.row_group = row_g - 1;
     L.d.col_group = col_g - 1;
     L.d.row_cap = static_cast<int>(groups[static_cast<size_t>(row_g - 1)].idx.size());
@@ -795,8 +807,10 @@ void Engine::tune_tpa() {
     double tot = 0;
     for (int v : n) tot += v;
     const int t = auto_tpa(L.d.rows, tot / static_cast<double>(n.size()), prec);
-    if (t != L.d.tpa) {
+    const int t1 = pass1_tpa(t, tot / static_cast<double>(n.size()), prec);
+    if (t != L.d.tpa || t1 != L.d.tpa1) {
       L.d.tpa = t;
+      L.d.tpa1 = t1;
       changed = true;
     }
   }

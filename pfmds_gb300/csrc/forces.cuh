@@ -107,7 +107,8 @@ struct Acc3<true> {
 #pragma unroll
     for (int c = 0; c < 3; ++c) gmerge<TPA>(k.s[c], k.c[c]);
   }
-  __device__ __forceinline__ double get(int c) const { return k.get(c); }
+  // the compensated sum rounded to FP32 (one conversion to FP64 per component)
+  __device__ __forceinline__ double get(int c) const { return (double)(k.s[c] - k.c[c]); }
 };
 template <bool PREC>
 struct Acc1;
@@ -196,7 +197,9 @@ __device__ __forceinline__ double kick_component(double v, double f, double m, d
   return exact ? __dadd_rn(v, __dmul_rn(__ddiv_rn(__ddiv_rn(f, m), 1.6605389217 / 1.6021765654 * 100.0), ts2))
                : v + f * kc * ts2;
 }
-// Stores or adds the row's force, then (Epi::kick) applies the second half-kick.
+// Stores or adds the row's force, then (Epi::kick) applies the second half-kick:
+// the reference's expression in the plain form (exact), one FMA per component
+// with kc*dt/2 formed once per atom otherwise.
 __device__ __forceinline__ void finish_force(const Atoms& A, const Epi& E, int ai, double fx, double fy, double fz) {
   double4_32a f;
   if (E.store) {
@@ -212,12 +215,21 @@ __device__ __forceinline__ void finish_force(const Atoms& A, const Epi& E, int a
     const unsigned char m = E.mflag[ai];
     if (m) {
       double4_32a v = A.vel[ai];
-      const double ms = A.mass[ai], kc = A.kc[ai];
-      if (m & 1) {
-        v.x = kick_component(v.x, f.x, ms, kc, E.ts2, E.exact);
-        v.y = kick_component(v.y, f.y, ms, kc, E.ts2, E.exact);
+      if (E.exact) {
+        const double ms = A.mass[ai], kc = A.kc[ai];
+        if (m & 1) {
+          v.x = kick_component(v.x, f.x, ms, kc, E.ts2, 1);
+          v.y = kick_component(v.y, f.y, ms, kc, E.ts2, 1);
+        }
+        v.z = kick_component(v.z, f.z, ms, kc, E.ts2, 1);
+      } else {
+        const double kt = A.kc[ai] * E.ts2;
+        if (m & 1) {
+          v.x = fma(f.x, kt, v.x);
+          v.y = fma(f.y, kt, v.y);
+        }
+        v.z = fma(f.z, kt, v.z);
       }
-      v.z = kick_component(v.z, f.z, ms, kc, E.ts2, E.exact);
       A.vel[ai] = v;
     }
   }

@@ -61,12 +61,15 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   if (ENERGY) er.template reduce<TPA>();
   double erow = 0.0;
   if (valid && g.sub == 0) {
-    const double eb = sqrt(eb2.get());
-    if constexpr (PREC)
-      static_cast<float*>(inv_eb)[ai] = __frcp_rn((float)eb);
-    else
+    if constexpr (PREC) {
+      // 1/Eb from the FP32-rounded sum: no FP64 square root on the step
+      static_cast<float*>(inv_eb)[ai] = rsqrtf(eb2.s - eb2.c);
+      if (ENERGY) erow = P.A0 * er.get() - P.xi * sqrt(eb2.get());
+    } else {
+      const double eb = sqrt(eb2.get());
       static_cast<double*>(inv_eb)[ai] = 1.0 / eb;
-    if (ENERGY) erow = P.A0 * er.get() - P.xi * eb;
+      if (ENERGY) erow = P.A0 * er.get() - P.xi * eb;
+    }
   }
   if (ENERGY) energy_reduce(ctl, eslot, ekey, erow);
 }
@@ -122,23 +125,28 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
     if (energy && (parts & 1)) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
   }
-  const int grid = nblk((long long)L.rows * L.tpa, 256);
   with_bool(prec, [&](auto pr) {
-    with_tpa(L.tpa, [&](auto t) {
-      constexpr bool PR = decltype(pr)::value;
-      constexpr int TP = decltype(t)::value;
-      if (parts & 1) {
+    constexpr bool PR = decltype(pr)::value;
+    if (parts & 1) {
+      const int tpa1 = L.tpa1 > 0 ? L.tpa1 : L.tpa;
+      const int grid = nblk((long long)L.rows * tpa1, 256);
+      with_tpa(tpa1, [&](auto t) {
+        constexpr int TP = decltype(t)::value;
         if (energy)
           k_rjl_density<PR, true, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey);
         else
           k_rjl_density<PR, false, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey);
         ++g_kernel_launches;
-      }
-      if (parts & 2) {
+      });
+    }
+    if (parts & 2) {
+      const int grid = nblk((long long)L.rows * L.tpa, 256);
+      with_tpa(L.tpa, [&](auto t) {
+        constexpr int TP = decltype(t)::value;
         k_rjl_force<PR, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, E);
         ++g_kernel_launches;
-      }
-    });
+      });
+    }
   });
 }
 

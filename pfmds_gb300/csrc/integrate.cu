@@ -62,9 +62,14 @@ __global__ void k_step_begin(int phase, Changes ch, int nvms, double ms_de, Ctl*
   }
 }
 
-__device__ __forceinline__ bool out_of_cell(double x, double L) {
-  const double tol = 0.0000001;  // md_general.f90:346
-  return !(x > (0.0 - tol) && x < (L + tol));
+// !(x > -tol .and. x < L + tol) with tol = 1e-7 (md_general.f90:346), evaluated
+// on the bit patterns with integer compares (GB300's FP64 pipe is narrow).  For
+// x >= +0 the patterns order like the values; a negative x (sign bit set, -0.0
+// included) is inside iff its magnitude is below tol.  NaN is outside either way.
+__device__ __forceinline__ bool out_of_cell(double x, double Ltol) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b >= __double_as_longlong(Ltol)
+                : (unsigned long long)b >= (unsigned long long)__double_as_longlong(-0.0000001);
 }
 __device__ __forceinline__ void flag_oob(Ctl* ctl, int i) {
   atomicMin(&ctl->oob_atom, i);
@@ -75,7 +80,7 @@ __global__ void k_check_all(Atoms A, Box B, Ctl* ctl) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.N) return;
   const double4_32a p = A.pos[i];
-  if (out_of_cell(p.x, B.L[0]) || out_of_cell(p.y, B.L[1]) || out_of_cell(p.z, B.L[2])) flag_oob(ctl, i);
+  if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 
 // invert_z_velocities(atoms, 0.8*Lz, 0.9*Lz), md_general.f90:382-398
@@ -96,16 +101,26 @@ __global__ void k_invert_z(Atoms A, Box B, Ctl* ctl) {
 __device__ __forceinline__ double kick1(double v, double f, double m, double ts2) {
   return __dadd_rn(v, __dmul_rn(__ddiv_rn(__ddiv_rn(f, m), c_mass_coef), ts2));
 }
-// the same with a precomputed 1/(m*mass_coef): no FP64 divide on the step
-__device__ __forceinline__ double kick1_fast(double v, double f, double kc, double ts2) { return v + f * kc * ts2; }
-// x = x + v*ts(1) then one shift back into [0, L] (md_integrators.f90:19-24)
-__device__ __forceinline__ double drift1(double x, double v, double ts1, double L) {
-  x = __dadd_rn(x, __dmul_rn(v, ts1));
-  if (x > L)
+// the same with kt = dt/2/(m*mass_coef) formed once per atom: one FMA
+__device__ __forceinline__ double kick1_fast(double v, double f, double kt) { return fma(f, kt, v); }
+// One shift back into [0, L] (md_integrators.f90:19-24): x > L and x < 0.0 decided
+// on the bit patterns (L > 0; the patterns of x >= +0 order like the values,
+// x < 0.0 is a set sign bit other than -0.0).  NaN stays NaN either way.
+__device__ __forceinline__ double wrap1(double x, double L) {
+  const long long b = __double_as_longlong(x);
+  if (b > __double_as_longlong(L))
     x = x - L;
-  else if (x < 0.0)
+  else if (b < 0 && b != (long long)0x8000000000000000ULL)
     x = x + L;
   return x;
+}
+// x = x + v*ts(1) then the shift, rounded as written
+__device__ __forceinline__ double drift1(double x, double v, double ts1, double L) {
+  return wrap1(__dadd_rn(x, __dmul_rn(v, ts1)), L);
+}
+// the precision form: one FMA
+__device__ __forceinline__ double drift1_fast(double x, double v, double ts1, double L) {
+  return wrap1(fma(v, ts1, x), L);
 }
 
 template <bool EXACT>
@@ -124,12 +139,12 @@ __global__ void k_kick(GroupRef g, int xyz, double ts2, Atoms A, Ctl* ctl) {
     }
     v.z = kick1(v.z, f.z, m, ts2);
   } else {
-    const double kc = A.kc[i];
+    const double kt = A.kc[i] * ts2;
     if (xyz) {
-      v.x = kick1_fast(v.x, f.x, kc, ts2);
-      v.y = kick1_fast(v.y, f.y, kc, ts2);
+      v.x = kick1_fast(v.x, f.x, kt);
+      v.y = kick1_fast(v.y, f.y, kt);
     }
-    v.z = kick1_fast(v.z, f.z, kc, ts2);
+    v.z = kick1_fast(v.z, f.z, kt);
   }
   A.vel[i] = v;
 }
@@ -148,7 +163,7 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
   p.z = drift1(p.z, v.z, ts1, B.L[2]);
   A.pos[i] = p;
   if (write_posq) A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
-  if (out_of_cell(p.x, B.L[0]) || out_of_cell(p.y, B.L[1]) || out_of_cell(p.z, B.L[2])) flag_oob(ctl, i);
+  if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 
 // Nose-Hoover scaling (optional), half kick and drift of the xyz group in one pass.
@@ -186,19 +201,25 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
     v.y = kick1(v.y, f.y, m, ts2);
     v.z = kick1(v.z, f.z, m, ts2);
   } else {
-    const double kc = A.kc[i];
-    v.x = kick1_fast(v.x, f.x, kc, ts2);
-    v.y = kick1_fast(v.y, f.y, kc, ts2);
-    v.z = kick1_fast(v.z, f.z, kc, ts2);
+    const double kt = A.kc[i] * ts2;
+    v.x = kick1_fast(v.x, f.x, kt);
+    v.y = kick1_fast(v.y, f.y, kt);
+    v.z = kick1_fast(v.z, f.z, kt);
   }
   A.vel[i] = v;
   double4_32a p = A.pos[i];
-  p.x = drift1(p.x, v.x, ts1, B.L[0]);
-  p.y = drift1(p.y, v.y, ts1, B.L[1]);
-  p.z = drift1(p.z, v.z, ts1, B.L[2]);
+  if (EXACT) {
+    p.x = drift1(p.x, v.x, ts1, B.L[0]);
+    p.y = drift1(p.y, v.y, ts1, B.L[1]);
+    p.z = drift1(p.z, v.z, ts1, B.L[2]);
+  } else {
+    p.x = drift1_fast(p.x, v.x, ts1, B.L[0]);
+    p.y = drift1_fast(p.y, v.y, ts1, B.L[1]);
+    p.z = drift1_fast(p.z, v.z, ts1, B.L[2]);
+  }
   A.pos[i] = p;
   if (write_posq) A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
-  if (out_of_cell(p.x, B.L[0]) || out_of_cell(p.y, B.L[1]) || out_of_cell(p.z, B.L[2])) flag_oob(ctl, i);
+  if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 
 __device__ __forceinline__ double ke_of(const Atoms& A, int i) {

@@ -45,6 +45,8 @@ struct ListDev {
   int rows;          // nl%N
   int nmax, stride;  // nlist[slot*stride + row]
   int tpa;           // threads per row in the force kernels (1..32, power of two)
+  int tpa1;          // threads per row of the rjl density pass (no force write-back: it
+                     // runs best with more, shorter threads)
   int sorted;        // rows kept in the reference's order (ascending group-2 index)
   int* nnum;
   int* nlist;

@@ -302,6 +302,135 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   }
 }
 
+// Self lists (row group == column group) without sorting: one block per cell.
+// The rows are the cell's own atoms.  The block stages the candidates of the
+// surrounding cells (the same x-runs, in the same order, as k_build) in shared
+// memory once, and its warps scan them for each of the cell's rows, so a
+// candidate is read from global memory once per cell instead of once per row.
+// Rows and entries come out exactly as k_build<PREC, CAP, false> writes them.
+static constexpr int kCellWarps = 4;
+static constexpr int kCellCand = 1024;  // candidates staged per pass
+static constexpr int kCellRows = 64;    // rows per pass
+
+__global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, CellGrid cg, Box B, float rcp2, Ctl* ctl) {
+  __shared__ int s_atom[kCellCand];
+  __shared__ int4 s_posq[kCellCand];
+  __shared__ int s_off[19];  // prefix offsets of up to 18 candidate runs
+  __shared__ int s_beg[18];  // run starts in the cell-ordered arrays
+  __shared__ int s_cnt[kCellRows], s_less[kCellRows];
+  if (ctl->stop) return;
+  const int n1 = ctl->group_n[L.row_group];
+  // update_neighbour_list only acts when the group and the list are non-empty
+  if (n1 == 0 || L.rows == 0) return;
+  if (n1 > L.rows) {  // rows are indexed by group index: nothing is written past L.rows
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_error(ctl, ST_PARAM, EK_NONE, L.id, n1, L.rows);
+    return;
+  }
+  const int c = blockIdx.x;
+  const int r0 = cg.start[c], nr = cg.start[c + 1] - r0;
+  if (nr == 0) return;
+  const int nx = cg.nc[0], ny = cg.nc[1], nz = cg.nc[2];
+  const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+  if (threadIdx.x < 18) {
+    // run t: (y, z) row t/2 of the 3x3 (fewer when a dimension has < 3 cells),
+    // z outer, y inner; x-run t&1
+    const int t = threadIdx.x, which = t & 1, yz = t >> 1;
+    const int my = ny < 3 ? ny : 3, mz = nz < 3 ? nz : 3;
+    int b = 0, e = 0;
+    if (yz < my * mz) {
+      const int iy = yz % my, iz = yz / my;
+      const int y = ny < 3 ? iy : (cy - 1 + iy + ny) % ny;
+      const int z = nz < 3 ? iz : (cz - 1 + iz + nz) % nz;
+      const int base = (z * ny + y) * nx;
+      if (nx < 3) {
+        if (!which) { b = cg.start[base]; e = cg.start[base + nx]; }
+      } else if (cx >= 1 && cx + 1 < nx) {
+        if (!which) { b = cg.start[base + cx - 1]; e = cg.start[base + cx + 2]; }
+      } else if (cx == 0) {
+        if (!which) { b = cg.start[base]; e = cg.start[base + 2]; }
+        else { b = cg.start[base + nx - 1]; e = cg.start[base + nx]; }
+      } else {
+        if (!which) { b = cg.start[base + nx - 2]; e = cg.start[base + nx]; }
+        else { b = cg.start[base]; e = cg.start[base + 1]; }
+      }
+    }
+    s_beg[t] = b;
+    s_off[t + 1] = e - b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_off[0] = 0;
+    for (int t = 0; t < 18; ++t) s_off[t + 1] += s_off[t];
+  }
+  __syncthreads();
+  const int total = s_off[18];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int rg = 0; rg < nr; rg += kCellRows) {
+    const int nrg = min(kCellRows, nr - rg);
+    for (int i = threadIdx.x; i < nrg; i += blockDim.x) {
+      s_cnt[i] = 0;
+      s_less[i] = 0;
+    }
+    for (int b0 = 0; b0 < total; b0 += kCellCand) {
+      const int nb = min(kCellCand, total - b0);
+      __syncthreads();  // the previous pass is done with the staged candidates
+      for (int v = threadIdx.x; v < nb; v += blockDim.x) {
+        const int g = b0 + v;
+        int r = 0;
+        while (s_off[r + 1] <= g) ++r;  // g < total = s_off[18], so r < 18
+        const int k = s_beg[r] + (g - s_off[r]);
+        s_atom[v] = cg.atom[k];
+        s_posq[v] = cg.posq[k];
+      }
+      __syncthreads();
+      for (int i = w; i < nrg; i += kCellWarps) {
+        const int kr = r0 + rg + i;
+        const int ai = cg.atom[kr], row = cg.jnd[kr];
+        const int4 piq = cg.posq[kr];
+        int cnt = s_cnt[i], nless = s_less[i];
+        for (int k0 = 0; k0 < nb; k0 += 32) {
+          const int k = k0 + lane;
+          bool hit = false;
+          int aj = 0;
+          if (k < nb) {
+            aj = s_atom[k];
+            if (aj != ai) {
+              float d[3];
+              hit = mi_q(piq, s_posq[k], B, d) < rcp2;
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, hit);
+          if (hit) {
+            const int p = cnt + __popc(m & ((1u << lane) - 1u));
+            if (p < L.nmax) L.nlist[(size_t)p * L.stride + row] = aj;
+          }
+          nless += __popc(__ballot_sync(0xffffffffu, hit && aj < ai));
+          cnt += __popc(m);
+        }
+        if (lane == 0) {
+          s_cnt[i] = cnt;
+          s_less[i] = nless;
+        }
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nrg; i += blockDim.x) {
+      const int kr = r0 + rg + i;
+      const int row = cg.jnd[kr], cnt = s_cnt[i];
+      if (cnt > L.nmax) {
+        // 'error: too many neighbours', ind, nnumind  (md_neighbours.f90:80)
+        set_error(ctl, ST_NLIST_OVERFLOW, EK_OVERFLOW, L.id, row + 1, L.nmax + 1);
+      } else {
+        L.nnum[row] = cnt;
+        L.pidx[row] = cg.atom[kr];
+        L.lessnnum[row] = s_less[i];
+        L.bnd[row] = INT_MAX;
+      }
+    }
+    __syncthreads();  // s_cnt is reset for the next group of rows
+  }
+}
+
 // tb entries are atoms; the nn list keeps tb row indexes (tb lists have g1 == g2)
 template <bool PREC>
 __global__ void k_nn_select(ListDev tb, ListDev nn, double rcnn, Atoms A, Box B, Ctl* ctl) {
@@ -439,6 +568,8 @@ void launch_build_list(bool prec, const ListDev& L, const CellGrid& cg, const At
   if (prec) {
     if (L.sorted)
       build_dispatch<true, true>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
+    else if (!converse && L.row_group == L.col_group && cg.ncell > 0)
+      { k_build_cells<<<cg.ncell, kCellWarps * 32, 0, s>>>(L, cg, B, (float)rc2, ctl); ++g_kernel_launches; }
     else
       build_dispatch<true, false>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
   } else {

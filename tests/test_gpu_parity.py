@@ -115,3 +115,40 @@ def test_graphs_match_direct_launches(tmp_path, built):
     pa, va, fa = a.state()
     pb, vb, fb = b.state()
     assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_precision_lists_match_oracle(tmp_path, built, name):
+    """Precision-form rows are in cell-scan order and tested on fixed-point
+    separations: as sets they equal the reference's rows (the inputs put no pair
+    within the fixed-point resolution of a cut-off)."""
+    d = SYSTEMS[name](tmp_path)
+    o = Oracle(d, out_period=1, threads=1)
+    o.step()
+    s = pf.Simulation(d, form="precision", out_period=1)
+    s.advance(1)
+    for i in range(o.n_interactions):
+        for j in range(3):
+            try:
+                ol = o.nlist(i, j)
+            except Exception:
+                break
+            gl = s.nlist(i, j)
+            assert np.array_equal(gl["nnum"], ol["nnum"]), (i, j)
+            for r in range(len(ol["nnum"])):
+                n = ol["nnum"][r]
+                assert np.array_equal(np.sort(gl["nlist"][r, :n]), np.sort(ol["nlist"][r, :n])), (i, j, r)
+
+
+@pytest.mark.parametrize("name", ["cu", "gr_morsec"])
+def test_precision_runs_repeat_bitwise(tmp_path, built, name):
+    d = SYSTEMS[name](tmp_path)
+    runs = []
+    for graphs in (True, False):
+        s = pf.Simulation(d, form="precision", out_period=10 ** 6, use_graphs=graphs)
+        s.advance(30)
+        runs.append(s.state() + (s.energies()["conserved"],))
+        s.close()
+    for a, b in zip(runs[0][:3], runs[1][:3]):
+        assert np.array_equal(a, b)
+    assert runs[0][3] == runs[1][3]
