@@ -179,6 +179,21 @@ __device__ __forceinline__ void fdfcut_cos_f(float r, float R1, float R2, float 
     df = 0.0f;
   }
 }
+// The same switch with r*df in place of df (no divide): f and r*df/dr.
+__device__ __forceinline__ void fdfrcut_cos_f(float r, float R1, float R2, float inv_w, float& f, float& rdf) {
+  if (r < R1) {
+    f = 1.0f;
+    rdf = 0.0f;
+  } else if (r < R2) {
+    float s, c;
+    __sincosf(3.14159265358979f * (r - R1) * inv_w, &s, &c);
+    f = (1.0f + c) * 0.5f;
+    rdf = -s * 3.14159265358979f * inv_w * 0.5f;
+  } else {
+    f = 0.0f;
+    rdf = 0.0f;
+  }
+}
 // cut_off_poly.f90:6-17
 __device__ __forceinline__ double fcut_poly(double r, double R1, double R2) {
   if (r > R1 && r < R2) {

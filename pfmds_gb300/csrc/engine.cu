@@ -726,8 +726,10 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   for (auto& I : inters) {
     const ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
     if (I.spec.kind == pfmd_io::K_RJL) {
-      I.scratch.alloc(static_cast<size_t>(std::max(N, 1)));  // 1/Eb per atom
-      if (!prec) I.pair.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));
+      I.scratch.alloc(static_cast<size_t>(std::max(N, 1)));  // 1/Eb per atom (plain form)
+      // pair terms per list slot: double2 (plain) or float2 (precision)
+      const size_t slots = static_cast<size_t>(L1.d.nmax) * L1.d.stride;
+      I.pair.alloc(std::max<size_t>(prec ? (slots + 1) / 2 : slots, 1));
     }
     if (I.spec.kind == pfmd_io::K_TB)
       I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));  // B per list slot
@@ -1465,9 +1467,9 @@ double Engine::kernel_bytes(const std::string& name) {
       if (name == "lj1g") return b;
     }
     if (k == pfmd_io::K_RJL) {
-      // the plain form writes two FP64 pair coefficients per entry in the density
-      // pass and reads them back in the force pass
-      const double PC = prec ? 0.0 : 16.0;
+      // the density pass writes two pair coefficients per entry (FP64 plain, FP32
+      // precision) and the force pass reads them back
+      const double PC = prec ? 8.0 : 16.0;
       if (name == "rjl_density") return row_bytes(L1, IE, PC);
       if (name == "rjl_force") return row_bytes(L1, IE + F, PC);
       if (name == "forces") b += row_bytes(L1, IE, PC) + row_bytes(L1, IE + F, PC);
@@ -1778,12 +1780,41 @@ int pfmd_get_nlist(pfmd_ctx* c, int inter, int list, int* nnum, int* lessnnum, i
     if (nnum) CK(cudaMemcpyAsync(nnum, L.nnum.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
     if (lessnnum) CK(cudaMemcpyAsync(lessnnum, L.less.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
     if (pidx) CK(cudaMemcpyAsync(pidx, L.pidx.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
-    std::vector<int> t;
-    if (nlist && nmax) {
+    // unsorted (cell-order) rows of a regular list: lessnnum is formed here as the
+    // reference defines it, the position (in ascending group-2 order) of the
+    // first partner with a larger atom index (md_neighbours.f90:78)
+    const bool count_less = lessnnum && !L.d.sorted && L.kind == pfmd::L_REGULAR && nmax;
+    std::vector<int> t, hn, hp;
+    if ((nlist || count_less) && nmax) {
       t.resize(nmax * stride);
       CK(cudaMemcpyAsync(t.data(), L.nlist.p, sizeof(int) * t.size(), cudaMemcpyDeviceToHost, e.st));
     }
+    if (count_less) {
+      hn.resize(rows);
+      hp.resize(rows);
+      CK(cudaMemcpyAsync(hn.data(), L.nnum.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
+      CK(cudaMemcpyAsync(hp.data(), L.pidx.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, e.st));
+    }
     CK(cudaStreamSynchronize(e.st));
+    if (count_less) {
+      std::vector<std::pair<int, int>> row;  // (group-2 index, atom)
+      for (size_t r = 0; r < rows; ++r) {
+        const size_t n = std::min(static_cast<size_t>(std::max(hn[r], 0)), nmax);
+        row.clear();
+        for (size_t p = 0; p < n; ++p) {
+          const int v = t[p * stride + r];
+          row.emplace_back(v >= 0 && v < e.N ? L.col_inv[static_cast<size_t>(v)] : v, v);
+        }
+        std::sort(row.begin(), row.end());
+        int k = static_cast<int>(n);
+        for (size_t p = 0; p < n; ++p)
+          if (hp[r] < row[p].second) {
+            k = static_cast<int>(p);
+            break;
+          }
+        lessnnum[r] = k;
+      }
+    }
     // main lists hold partner atoms: report the reference's group-2 indexes
     const bool atoms = L.kind != pfmd::L_NN_TB;
     if (nlist && nmax)

@@ -4,12 +4,14 @@
 // the row energy A0*Er - xi*Eb; pass 2 gathers the pair forces with
 // 1/Eb_i + 1/Eb_j.  See forces.cuh for the execution scheme.
 //
-// The plain (FP64) form keeps the pair terms of pass 1 per list slot,
+// Pass 1 also keeps the pair terms of each list slot,
 //   a = 2 A0 (p/r0 fc - f' ) e_p / r,   b = xi (q/r0 fc - f'/2) e_q / r,
 // so pass 2 only needs the separation vector: F_i -= (a - b (1/Eb_i + 1/Eb_j)) dr.
-// That replaces two FP64 exponentials, a square root and a divide per pair with a
-// 16-byte load (GB300's FP64 rate is a small fraction of its FP32 rate).  The
-// precision form recomputes its FP32 terms instead.
+// That replaces two exponentials, a sine/cosine, a square root and a reciprocal
+// per pair with one coalesced load: 16 bytes per slot (double2) in the plain form,
+// 8 bytes (float2) in the precision form.  The precision form keeps 1/Eb_i in the
+// spare w word of the atom's fixed-point position, so pass 2 fetches a partner's
+// position and 1/Eb with a single 16-byte gather.
 #include "forces.cuh"
 
 namespace pfmd {
@@ -32,15 +34,24 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
 #pragma unroll 4
     for (int p = g.sub; p < n; p += TPA) {
       R dr[3];
-      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, g.row, p)), B, dr));
+      const R r2 = T::d2(pi, T::load(A, ent(L, g.row, p)), B, dr);
       if constexpr (PREC) {
+        // r and 1/r from one reciprocal square root
+        const float ir = rsqrtf(r2), r = r2 * ir;
+        float2 ab = make_float2(0.f, 0.f);
         if (r <= c.R2) {
-          const R fc = fc_only<PREC>(r, c.R1, c.R2, c.inv_w);
-          const R x = r * c.inv_r0 - R(1);
-          eb2.add(xexp<PREC>(c.m2q * x) * fc);
-          if (ENERGY) er.add(xexp<PREC>(c.mp * x) * fc);
+          float fc, rdfc;
+          fdfrcut_cos_f(r, c.R1, c.R2, c.inv_w, fc, rdfc);
+          const float x = r * c.inv_r0 - 1.f;
+          const float eq = __expf(c.m2q * x), ep = __expf(c.mp * x);
+          eb2.add(eq * fc);
+          if (ENERGY) er.add(ep * fc);
+          ab.x = c.a2 * (c.pr0 * fc - rdfc) * ep * ir;
+          ab.y = c.xi * (c.qr0 * fc - 0.5f * rdfc) * eq * ir;
         }
+        reinterpret_cast<float2*>(pair)[(size_t)p * L.stride + g.row] = ab;
       } else {
+        const R r = sqrt(r2);
         double2 ab = make_double2(0.0, 0.0);
         if (r <= c.R2) {
           R fc, dfc;
@@ -62,8 +73,9 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   double erow = 0.0;
   if (valid && g.sub == 0) {
     if constexpr (PREC) {
-      // 1/Eb from the FP32-rounded sum: no FP64 square root on the step
-      static_cast<float*>(inv_eb)[ai] = rsqrtf(eb2.s - eb2.c);
+      // 1/Eb from the FP32-rounded sum (no FP64 square root on the step), kept in
+      // the w word of the atom's fixed-point position
+      reinterpret_cast<int*>(A.posq + ai)[3] = __float_as_int(rsqrtf(eb2.s - eb2.c));
       if (ENERGY) erow = P.A0 * er.get() - P.xi * sqrt(eb2.get());
     } else {
       const double eb = sqrt(eb2.get());
@@ -90,23 +102,21 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
   Acc3<PREC> acc;
   if (n > 0) {
     const auto pi = T::load(A, ai);
-    const R ieb_i = ieb[ai];
+    R ieb_i;
+    if constexpr (PREC)
+      ieb_i = __int_as_float(pi.w);
+    else
+      ieb_i = ieb[ai];
 #pragma unroll 4
     for (int p = g.sub; p < n; p += TPA) {
       const int aj = ent(L, g.row, p);
       R dr[3];
       if constexpr (PREC) {
-        const R r = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dr));
-        if (r <= c.R2) {
-          R fc, dfc;
-          fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
-          const R x = r * c.inv_r0 - R(1);
-          const R ep = xexp<PREC>(c.mp * x), eq = xexp<PREC>(c.m2q * x);
-          const R T1 = c.a2 * (c.pr0 * fc - dfc * r) * ep;
-          const R T2 = c.xi * (c.qr0 * fc - dfc * R(0.5) * r) * (ieb_i + ieb[aj]) * eq;
-          const R k = (T1 - T2) * xrcp<PREC>(r);
-          acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
-        }
+        const int4 pj = A.posq[aj];
+        T::d2(pi, pj, B, dr);
+        const float2 ab = reinterpret_cast<const float2*>(pair)[(size_t)p * L.stride + g.row];
+        const float k = ab.x - ab.y * (ieb_i + __int_as_float(pj.w));
+        acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
       } else {
         const double2 ab = pair[(size_t)p * L.stride + g.row];
         T::d2(pi, T::load(A, aj), B, dr);

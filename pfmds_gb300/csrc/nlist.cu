@@ -307,7 +307,8 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
 // surrounding cells (the same x-runs, in the same order, as k_build) in shared
 // memory once, and its warps scan them for each of the cell's rows, so a
 // candidate is read from global memory once per cell instead of once per row.
-// Rows and entries come out exactly as k_build<PREC, CAP, false> writes them.
+// Rows and entries come out exactly as k_build<PREC, CAP, false> writes them;
+// lessnnum is not kept (no kernel reads it for unsorted rows).
 static constexpr int kCellWarps = 4;
 static constexpr int kCellCand = 1024;  // candidates staged per pass
 static constexpr int kCellRows = 64;    // rows per pass
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
   __shared__ int4 s_posq[kCellCand];
   __shared__ int s_off[19];  // prefix offsets of up to 18 candidate runs
   __shared__ int s_beg[18];  // run starts in the cell-ordered arrays
-  __shared__ int s_cnt[kCellRows], s_less[kCellRows];
+  __shared__ int s_cnt[kCellRows];
   if (ctl->stop) return;
   const int n1 = ctl->group_n[L.row_group];
   // update_neighbour_list only acts when the group and the list are non-empty
@@ -367,10 +368,7 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int rg = 0; rg < nr; rg += kCellRows) {
     const int nrg = min(kCellRows, nr - rg);
-    for (int i = threadIdx.x; i < nrg; i += blockDim.x) {
-      s_cnt[i] = 0;
-      s_less[i] = 0;
-    }
+    for (int i = threadIdx.x; i < nrg; i += blockDim.x) s_cnt[i] = 0;
     for (int b0 = 0; b0 < total; b0 += kCellCand) {
       const int nb = min(kCellCand, total - b0);
       __syncthreads();  // the previous pass is done with the staged candidates
@@ -387,7 +385,7 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
         const int kr = r0 + rg + i;
         const int ai = cg.atom[kr], row = cg.jnd[kr];
         const int4 piq = cg.posq[kr];
-        int cnt = s_cnt[i], nless = s_less[i];
+        int cnt = s_cnt[i];
         for (int k0 = 0; k0 < nb; k0 += 32) {
           const int k = k0 + lane;
           bool hit = false;
@@ -404,13 +402,9 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
             const int p = cnt + __popc(m & ((1u << lane) - 1u));
             if (p < L.nmax) L.nlist[(size_t)p * L.stride + row] = aj;
           }
-          nless += __popc(__ballot_sync(0xffffffffu, hit && aj < ai));
           cnt += __popc(m);
         }
-        if (lane == 0) {
-          s_cnt[i] = cnt;
-          s_less[i] = nless;
-        }
+        if (lane == 0) s_cnt[i] = cnt;
       }
     }
     __syncthreads();
@@ -423,8 +417,7 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
       } else {
         L.nnum[row] = cnt;
         L.pidx[row] = cg.atom[kr];
-        L.lessnnum[row] = s_less[i];
-        L.bnd[row] = INT_MAX;
+        L.bnd[row] = INT_MAX;  // lessnnum of an unsorted row is formed when it is read back
       }
     }
     __syncthreads();  // s_cnt is reset for the next group of rows

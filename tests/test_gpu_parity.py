@@ -138,6 +138,8 @@ def test_precision_lists_match_oracle(tmp_path, built, name):
             for r in range(len(ol["nnum"])):
                 n = ol["nnum"][r]
                 assert np.array_equal(np.sort(gl["nlist"][r, :n]), np.sort(ol["nlist"][r, :n])), (i, j, r)
+            if j == 0:
+                assert np.array_equal(gl["lessnnum"], ol["lessnnum"]), (i, j)
 
 
 @pytest.mark.parametrize("name", ["cu", "gr_morsec"])
