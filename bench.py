@@ -54,40 +54,86 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons every 200 ms while running."""
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    """SM clocks and clock-event (throttle) reasons sampled during the timed region.
 
-    def __init__(self):
-        self.proc = None
-        self.lines = []
+    Reads NVML directly (libnvidia-ml, read-only queries) every ~1 ms from a
+    thread, so that even a timed region of a few milliseconds gets samples; falls
+    back to `nvidia-smi -lms 200` when NVML cannot be loaded."""
+    # clock-event reason bits (nvml.h): SW power cap, HW slowdown, SW thermal, HW thermal
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index=0, period_s=0.001):
+        self.index, self.period = index, period_s
+        self.sm, self.mask, self.max_mhz = [], 0, None
+        self.proc, self.lines, self.thread = None, [], None
+        self.stop = threading.Event()
+        self.source = None
+
+    def _nvml(self):
+        import ctypes as C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h)) != 0:
+            raise OSError("no NVML handle")
+        mx = C.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, h, reasons
+
+    def _poll_nvml(self, lib, h, reasons):
+        import ctypes as C
+        mhz, mask = C.c_uint(), C.c_ulonglong()
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(mhz)) == 0:
+                self.sm.append(float(mhz.value))
+            if reasons(h, C.byref(mask)) == 0:
+                self.mask |= mask.value
+            time.sleep(self.period)
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            lib, h, reasons = self._nvml()
+            self.thread = threading.Thread(target=self._poll_nvml, args=(lib, h, reasons), daemon=True)
+            self.source = "nvml"
+            self.thread.start()
+            return self
+        except (OSError, AttributeError):
+            pass
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=lambda: self.lines.extend(ln.strip() for ln in self.proc.stdout),
+                                           daemon=True)
+            self.source = "nvidia-smi"
+            self.thread.start()
         except (OSError, ValueError):
             self.proc = None
         return self
 
-    def _read(self):
-        for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
-
     def __exit__(self, *a):
+        self.stop.set()
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, reasons = list(self.sm), set()
+        for bit, name in self.REASONS.items():
+            if self.mask & bit:
+                reasons.add(name)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -95,15 +141,45 @@ class ClockSampler:
                 continue
             try:
                 sm.append(float(f[0]))
-                mx = float(f[1])
+                self.max_mhz = float(f[1])
             except ValueError:
                 continue
             for n, v in zip(names, f[3:7]):
                 if v.lower() == "active":
                     reasons.add(n)
         sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": self.max_mhz, "reasons": sorted(reasons),
+                "samples": len(sm), "source": self.source}
+
+
+def nve_drift(sim, md_steps, chunk=100):
+    """Slope of the conserved energy over `md_steps` NVE steps (least-squares line
+    through one sample every `chunk` steps), in eV/atom/ns, and the RMS of the
+    samples about that line (eV/atom)."""
+    import numpy as np
+    n = sim.natoms
+    t, e = [0.0], [sim.energies()["conserved"]]
+    for k in range(md_steps // chunk):
+        sim.advance(chunk)
+        t.append((k + 1) * chunk * DT_FS)
+        e.append(sim.energies()["conserved"])
+    t, e = np.asarray(t), np.asarray(e) / n
+    slope, icpt = np.polyfit(t, e, 1)
+    rms = float(np.sqrt(np.mean((e - (slope * t + icpt)) ** 2)))
+    return float(slope * 1e6), rms
+
+
+def pinned_arrays(n, k):
+    """k float64 (n, 3) host arrays in page-locked memory (torch's pinned
+    allocator) when a CUDA torch is present, else ordinary numpy arrays."""
+    import numpy as np
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return [torch.zeros((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(k)], True
+    except (ImportError, RuntimeError):
+        pass
+    return [np.zeros((n, 3)) for _ in range(k)], False
 
 
 def cpu_oracle_rate(d, threads, md_steps):
@@ -182,7 +258,9 @@ def run_ours(args):
         barrier(dist)
         launches0 = sim.kernel_launches
         total_ms = 0.0
-        with ClockSampler() as clk:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+        nvml_index = int(vis[device]) if len(vis) > device and vis[device].strip().isdigit() else device
+        with ClockSampler(nvml_index) as clk:
             for _ in range(K):
                 sim.flush_l2()
                 total_ms += sim.advance_timed(S)
@@ -213,20 +291,23 @@ def run_ours(args):
                     "traffic": traffic, "alg_bytes_per_launch": int(b), "ms_per_launch": ms,
                     "kernel_ms_per_md_step": {k: round(v[2], 5) for k, v in cands.items()}}
 
-        # end to end through the C ABI with host buffers
-        p0, v0, _ = sim.state()
+        # end to end through the C ABI with host buffers (pinned when torch can pin)
+        bufs, pinned = pinned_arrays(n, 5)
+        p0, v0 = bufs[0], bufs[1]
+        sim.state(out=(p0, v0, bufs[2]))
         t_e2e = 0.0
         for _ in range(max(1, K)):
             t0 = time.perf_counter()
             sim.set_state(p0, v0)
             sim.advance(S)
-            p, v, f = sim.state()
+            sim.state(out=(bufs[2], bufs[3], bufs[4]))
             sim.energies()
             t_e2e += time.perf_counter() - t0
         t_e2e = dist_max(dist, t_e2e)
         e2e = {"value": atoms_all * S * max(1, K) / t_e2e, "unit": "atom-steps/s",
                "h2d_bytes_per_step": 2 * 24 * n, "d2h_bytes_per_step": 3 * 24 * n + 8 * 6,
-               "api": "pfmd_set_state + pfmd_advance + pfmd_get_state + pfmd_energies"}
+               "api": "pfmd_set_state + pfmd_advance + pfmd_get_state + pfmd_energies",
+               "host_buffers": "pinned" if pinned else "pageable"}
 
         # plain FP64 form beside it, and the precision form's force error against it
         plain = pf.Simulation(d, form="plain", out_period=10 ** 9, device=device)
@@ -248,6 +329,11 @@ def run_ours(args):
         import numpy as np
         rmse = float(np.sqrt(((fq - fp) ** 2).mean()))
         frms = float(np.sqrt((fp ** 2).mean()))
+        # NVE drift: least-squares slope of the conserved energy over a long run of
+        # each form from the same start (the workload's 10,000 steps for the
+        # precision form, 2,000 for the slower plain form)
+        d_pre, rms_pre = nve_drift(pre_p, args.drift_steps)
+        d_pla, rms_pla = nve_drift(ref_p, max(100, args.drift_steps // 5))
         plain_line = {"value": plain_rate, "ms_per_step": pms / Kp, "dtype": "f64",
                       "speedup_of_precision_form": value / plain_rate}
 
@@ -273,7 +359,11 @@ def run_ours(args):
                    "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}",
                    "atoms_per_replica": n},
         "force_rmse": {"value": rmse, "rel": rmse / frms, "unit": "eV/A", "against": "plain FP64 form"},
-        "nve_drift": {"value": drift, "unit": "eV/atom/ns", "window_fs": K * S * DT_FS},
+        "nve_drift": {"value": d_pre, "unit": "eV/atom/ns", "window_fs": args.drift_steps * DT_FS,
+                      "fit": "least-squares slope of the conserved energy, one sample per 100 fs",
+                      "rms_about_fit_eV_per_atom": rms_pre, "timed_window_value": drift,
+                      "plain_fp64": {"value": d_pla, "window_fs": max(100, args.drift_steps // 5) * DT_FS,
+                                     "rms_about_fit_eV_per_atom": rms_pla}},
         "plain": plain_line,
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -321,6 +411,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-md-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--drift-steps", type=int, default=10000,
+                    help="MD steps of the NVE drift measurement (precision form; plain runs a fifth)")
     ap.add_argument("--quick", action="store_true",
                     help="headline timing loop only (no plain form, e2e, roofline or CPU legs), for profiling")
     args = ap.parse_args()

@@ -182,9 +182,14 @@ class Simulation:
         self._check(load().pfmd_md_step(self._h, C.byref(s), C.byref(t)))
         return t.value
 
-    def state(self):
+    def state(self, out=None):
+        """Positions, velocities and forces (n x 3 each); `out` may supply three
+        C-contiguous float64 arrays to fill (pinned host memory, for instance)."""
         n = self.natoms
-        p, v, f = (np.zeros((n, 3)) for _ in range(3))
+        p, v, f = out if out is not None else (np.zeros((n, 3)) for _ in range(3))
+        for a in (p, v, f):
+            if a.shape != (n, 3) or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("state(): out arrays must be C-contiguous float64 of shape (natoms, 3)")
         self._check(load().pfmd_get_state(self._h, _dp(p), _dp(v), _dp(f)))
         return p, v, f
 

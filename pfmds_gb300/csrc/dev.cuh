@@ -263,8 +263,16 @@ __device__ __forceinline__ void block_sum(double (&v)[K]) {
 // block arrived last.  `slot` selects the arrival counter; the last block resets
 // it, so graphs can replay the kernel.
 template <int K>
+__device__ __forceinline__ bool grid_finish(Ctl* ctl, int slot, double (&v)[K], double (&out)[K]);
+template <int K>
 __device__ __forceinline__ bool grid_sum(Ctl* ctl, int slot, double (&v)[K], double (&out)[K]) {
   block_sum<K>(v);
+  return grid_finish<K>(ctl, slot, v, out);
+}
+// grid_sum from block totals already formed (valid in thread 0); every thread of
+// every block calls it.
+template <int K>
+__device__ __forceinline__ bool grid_finish(Ctl* ctl, int slot, double (&v)[K], double (&out)[K]) {
   __shared__ bool last;
   if (threadIdx.x == 0) {
 #pragma unroll

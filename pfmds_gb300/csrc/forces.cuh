@@ -241,6 +241,29 @@ __device__ __forceinline__ void energy_reduce(Ctl* ctl, int eslot, int ekey, dou
   if (grid_sum<1>(ctl, eslot, v, out)) ctl->e_inter[ekey] = out[0];
 }
 
+// The same for a row energy formed in FP32 (precision form): the block's rows are
+// summed in FP32 with error-free TwoSum merges (value = s - c), and the block
+// total goes to FP64 once, so the reduction issues no FP64 shuffles.
+__device__ __forceinline__ void energy_reduce_f(Ctl* ctl, int eslot, int ekey, float erow) {
+  __shared__ float ss[32], sc[32];
+  float s = erow, c = 0.f;
+  gmerge<32>(s, c);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    ss[w] = s;
+    sc[w] = c;
+  }
+  __syncthreads();
+  double v[1] = {0.0}, out[1];
+  if (w == 0) {
+    s = lane < nw ? ss[lane] : 0.f;
+    c = lane < nw ? sc[lane] : 0.f;
+    gmerge<32>(s, c);
+    v[0] = (double)s - (double)c;
+  }
+  if (grid_finish<1>(ctl, eslot, v, out)) ctl->e_inter[ekey] = out[0];
+}
+
 // The constants of a parameter set in the kernel's precision.
 template <bool PREC>
 __device__ __forceinline__ const LJc<typename RT<PREC>::R>& cst(const LJPar& p) {

@@ -71,19 +71,26 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   eb2.template reduce<TPA>();
   if (ENERGY) er.template reduce<TPA>();
   double erow = 0.0;
+  float erowf = 0.f;
   if (valid && g.sub == 0) {
     if constexpr (PREC) {
       // 1/Eb from the FP32-rounded sum (no FP64 square root on the step), kept in
       // the w word of the atom's fixed-point position
-      reinterpret_cast<int*>(A.posq + ai)[3] = __float_as_int(rsqrtf(eb2.s - eb2.c));
-      if (ENERGY) erow = P.A0 * er.get() - P.xi * sqrt(eb2.get());
+      const float e2 = eb2.s - eb2.c, ie = rsqrtf(e2);
+      reinterpret_cast<int*>(A.posq + ai)[3] = __float_as_int(ie);
+      if (ENERGY) erowf = c.A0 * (er.s - er.c) - c.xi * (e2 > 0.f ? e2 * ie : 0.f);
     } else {
       const double eb = sqrt(eb2.get());
       static_cast<double*>(inv_eb)[ai] = 1.0 / eb;
       if (ENERGY) erow = P.A0 * er.get() - P.xi * eb;
     }
   }
-  if (ENERGY) energy_reduce(ctl, eslot, ekey, erow);
+  if constexpr (ENERGY) {
+    if constexpr (PREC)
+      energy_reduce_f(ctl, eslot, ekey, erowf);
+    else
+      energy_reduce(ctl, eslot, ekey, erow);
+  }
 }
 
 template <bool PREC, int TPA>
@@ -150,10 +157,11 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
       });
     }
     if (parts & 2) {
-      const int grid = nblk((long long)L.rows * L.tpa, 256);
+      // 128-thread blocks: 2x as many blocks spread more evenly over the SMs
+      const int grid = nblk((long long)L.rows * L.tpa, 128);
       with_tpa(L.tpa, [&](auto t) {
         constexpr int TP = decltype(t)::value;
-        k_rjl_force<PR, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, E);
+        k_rjl_force<PR, TP><<<grid, 128, 0, s>>>(L, P, A, B, Eb, pair, ctl, E);
         ++g_kernel_launches;
       });
     }
