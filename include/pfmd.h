@@ -67,7 +67,9 @@ void pfmd_default_options(pfmd_options* opt);
  * (read_box_size/read_particles md_read_write.f90:22-61, create_groups and
  * create_interactions md_interactions.f90:38-136, set_nose_hoover_chain
  * md_integrators.f90:182, set_new_temperature md_general.f90:328), echoes what md()
- * echoes to the output unit, and uploads the system to the device. */
+ * echoes to the output unit, and uploads the system to the device.  opt may be
+ * NULL (pfmd_default_options).  *ctx is set even on failure, for pfmd_errmsg; the
+ * caller destroys it. */
 int pfmd_create_from_files(const char* input_path, const char* settings_filename,
                            const pfmd_options* opt, pfmd_ctx** ctx);
 
