@@ -169,6 +169,65 @@ def nve_drift(sim, md_steps, chunk=100):
     return float(slope * 1e6), rms
 
 
+def form_rate(sim, md_steps, reps):
+    """atom-steps/s of `reps` timed segments of `md_steps` MD steps (device time,
+    L2 flushed before each) after one untimed segment."""
+    sim.advance(md_steps)
+    ms = 0.0
+    for _ in range(reps):
+        sim.flush_l2()
+        ms += sim.advance_timed(md_steps)
+    return sim.natoms * md_steps * reps / (ms / 1e3), ms / (md_steps * reps)
+
+
+def other_configs(root, device):
+    """The workload's sibling configurations, measured beside the headline: the
+    binary LJ gas (4,000 atoms, nvt) in both forms with the CPU oracle, and the
+    graphene/Cu(111) moire (tb + rjl + morsec, 500 K nvt) in both forms with the
+    precision form's force error."""
+    import numpy as np
+    import pfmds_gb300 as pf
+    from pfmds_gb300 import configs
+    out = {}
+    d1 = os.path.join(root, "lj_gas")
+    configs.lj_gas(d1, log_period=10)
+    r = {}
+    for form in ("plain", "precision"):
+        s = pf.Simulation(d1, form=form, out_period=10 ** 9, device=device)
+        r[form] = form_rate(s, 10, 10)
+        s.close()
+    rate_cpu, t_cpu = cpu_oracle_rate(d1, os.cpu_count() or 1, 20)
+    out["lj_gas_4000"] = {
+        "workload": "binary LJ gas 2,000 A + 2,000 B in a 60 A cube (lj1g A-A, lj1g B-B, lj A-B, R2 7.5 A, "
+                    "list 8.5 A every 10 steps), nvt 100 K, dt 0.5 fs",
+        "plain": {"value": r["plain"][0], "ms_per_md_step": r["plain"][1]},
+        "precision": {"value": r["precision"][0], "ms_per_md_step": r["precision"][1]},
+        "cpu_oracle": {"value": rate_cpu, "cores": os.cpu_count() or 1, "sample": f"20 MD steps ({t_cpu:.2f} s)"},
+        "unit": "atom-steps/s"}
+    d3 = os.path.join(root, "moire")
+    configs.gr_on_cu(d3, rotation=(49, 3, 2), layers=6, fixed_layers=1, temperature=500.0, integrator="nvt",
+                     dt=0.5, steps=10 ** 8, log_period=10, coupling="morsec")
+    r, f = {}, {}
+    for form in ("plain", "precision"):
+        s = pf.Simulation(d3, form=form, out_period=10 ** 9, device=device)
+        s.advance(1)
+        f[form] = s.state()[2]
+        r[form] = form_rate(s, 10, 5 if form == "plain" else 10)
+        n3 = s.natoms
+        s.close()
+    rmse = float(np.sqrt(((f["precision"] - f["plain"]) ** 2).mean()))
+    frms = float(np.sqrt((f["plain"] ** 2).mean()))
+    n_c = sum(1 for ln in open(os.path.join(d3, "gr_cu.xyz")).read().splitlines()[2:] if ln.split()[-1] == "C")
+    out["graphene_cu_moire"] = {
+        "workload": f"graphene (tb, {n_c} C) rotated 2.945 deg on Cu(111) (rjl, 6 layers), morsec coupling "
+                    f"(D 0.1 eV, r0 2.2 A, alpha 1.7 1/A, cut-off 8 A), 500 K nvt, dt 0.5 fs; {n3} atoms",
+        "plain": {"value": r["plain"][0], "ms_per_md_step": r["plain"][1]},
+        "precision": {"value": r["precision"][0], "ms_per_md_step": r["precision"][1],
+                      "force_rmse_rel": rmse / frms},
+        "unit": "atom-steps/s"}
+    return out
+
+
 def pinned_arrays(n, k):
     """k float64 (n, 3) host arrays in page-locked memory (torch's pinned
     allocator) when a CUDA torch is present, else ordinary numpy arrays."""
@@ -337,6 +396,8 @@ def run_ours(args):
         plain_line = {"value": plain_rate, "ms_per_step": pms / Kp, "dtype": "f64",
                       "speedup_of_precision_form": value / plain_rate}
 
+        extra = other_configs(d, device) if (rank == 0 and not args.no_extra) else None
+
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
@@ -370,6 +431,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clocks,
+        "other_configs": extra,
     }
     print(json.dumps(line), flush=True)
 
@@ -411,6 +473,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-md-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the LJ-gas and moire configurations")
     ap.add_argument("--drift-steps", type=int, default=10000,
                     help="MD steps of the NVE drift measurement (precision form; plain runs a fifth)")
     ap.add_argument("--quick", action="store_true",

@@ -300,15 +300,20 @@ __device__ __forceinline__ bool grid_finish(Ctl* ctl, int slot, double (&v)[K], 
   return threadIdx.x == 0;
 }
 
-__device__ __forceinline__ void set_error(Ctl* ctl, int code, int kind, int a, int b, int c) {
+// Records the first error (later ones are dropped) at md_step `step` and stops
+// the device step loop.
+__device__ __forceinline__ void set_error_at(Ctl* ctl, int code, int kind, int a, int b, int c, long long step) {
   if (atomicCAS(&ctl->error, 0, code) == 0) {
     ctl->err_kind = kind;
     ctl->err_info[0] = a;
     ctl->err_info[1] = b;
     ctl->err_info[2] = c;
-    ctl->err_step = ctl->md_step;
+    ctl->err_step = step;
   }
   ctl->stop = 1;
+}
+__device__ __forceinline__ void set_error(Ctl* ctl, int code, int kind, int a, int b, int c) {
+  set_error_at(ctl, code, kind, a, b, c, ctl->md_step);
 }
 
 // Kahan-compensated accumulation (precision form).

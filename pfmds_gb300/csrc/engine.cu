@@ -835,6 +835,7 @@ void Engine::upload_ctl_groups() {
 // Reports a device-side stop with the reference's messages and throws.
 void Engine::raise_device_error() {
   const Ctl& c = *hctl;
+  md_step = c.err_step;  // the loop stopped inside this step, as the reference's stop does
   std::string msg;
   switch (c.err_kind) {
     case EK_OVERFLOW:

@@ -176,7 +176,8 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   if (ctl->stop) return;
   if (begin) {
     if (ctl->pending_oob) {
-      set_error(ctl, ST_OUT_OF_CELL, EK_OOB, ctl->oob_atom + 1, 0, 0);
+      // the step counter has not advanced yet: the error belongs to the step begun here
+      set_error_at(ctl, ST_OUT_OF_CELL, EK_OOB, ctl->oob_atom + 1, 0, 0, ctl->md_step + 1);
       return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -1,0 +1,90 @@
+"""run_md_simulation, the drop-in executable, against the oracle's build of the
+same program on the same inputs: standard output (timings excepted), the log,
+snapshot, trajectory and final .xyz files, in single-file mode and in list mode
+(-ilist, with the all_out file)."""
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import pfmds_gb300 as pf
+from pfmds_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_EXE = os.path.join(ROOT, "oracle", "_build", "oracle_md")
+TIMING = re.compile(r"TIME|time \(s\)|OPENMP THREADS|PERFOMANCE|:\s+[0-9.]+ S\s")
+NUM = re.compile(r"^[-+]?(\d+\.?\d*|\.\d+)([eEdD][-+]?\d+)?$")
+
+
+def _case(d):
+    configs.lj_gas(str(d), n_a=60, n_b=60, box=18.0, min_sep=2.8,
+                   integrators=[("nvt", 0.5, 20, 10, 5), ("nve", 0.5, 20, 10, 5)])
+
+
+def _run(exe, cwd, args):
+    r = subprocess.run([exe] + args, cwd=cwd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return r.stdout
+
+
+def _same_text(a, b, what, atol=1e-9, rtol=1e-7):
+    la, lb = a.splitlines(), b.splitlines()
+    assert len(la) == len(lb), what
+    for x, y in zip(la, lb):
+        if TIMING.search(x) or TIMING.search(y):
+            mask = lambda t: " ".join(re.sub(r"[0-9.]+", "#", t).split())
+            assert mask(x) == mask(y), (what, x, y)
+            continue
+        tx, ty = x.split(), y.split()
+        assert len(tx) == len(ty), (what, x, y)
+        for u, v in zip(tx, ty):
+            if NUM.match(u) and NUM.match(v) and any(c.isdigit() for c in u):
+                fu, fv = float(u.replace("D", "E")), float(v.replace("D", "E"))
+                assert abs(fu - fv) <= atol + rtol * abs(fv), (what, x, y)
+            else:
+                assert u == v, (what, x, y)
+
+
+def _outputs(d):
+    return sorted(f for f in os.listdir(d) if f.endswith((".log", ".xyz", ".txt")) and not f.startswith(
+        ("md_run_settings", "second_settings", "AB.xyz", "parameters_", "list")))
+
+
+def test_single_file_mode(tmp_path, built):
+    a, b = tmp_path / "gpu", tmp_path / "cpu"
+    _case(a)
+    shutil.copytree(a, b)
+    args = ["-i", "md_run_settings.txt", "-op", "10", "-omp_n", "4"]
+    out_a = _run(pf.EXE_PATH, a, args)
+    out_b = _run(ORACLE_EXE, b, args)
+    _same_text(out_a, out_b, "stdout")
+    files = _outputs(b)
+    assert files == _outputs(a) and "md_run.log" in files and any(f.startswith("snapshot_") for f in files)
+    for f in files:
+        # positions in 16 decimals, energies in 6
+        _same_text(open(a / f).read(), open(b / f).read(), f, atol=2e-6 if f.endswith(".log") else 1e-8, rtol=0)
+
+
+def test_list_mode_with_all_out(tmp_path, built):
+    a, b = tmp_path / "gpu", tmp_path / "cpu"
+    _case(a)
+    s = open(a / "md_run_settings.txt").read()
+    s2 = s.replace("nve     0.50000    20", "nve     0.50000    10")
+    assert s2 != s
+    open(a / "second_settings.txt", "w").write(s2)
+    open(a / "list.txt", "w").write("2\nmd_run_settings.txt first_\nsecond_settings.txt second_\n")
+    shutil.copytree(a, b)
+    args = ["-ilist", "list.txt", "-ofile", "all_out.txt", "-op", "5"]
+    out_a = _run(pf.EXE_PATH, a, args)
+    out_b = _run(ORACLE_EXE, b, args)
+    _same_text(out_a, out_b, "stdout")
+    files = _outputs(b)
+    assert files == _outputs(a) and "all_out.txt" in files
+    assert any(f.startswith("first_") for f in files) and any(f.startswith("second_") for f in files)
+    for f in files:
+        _same_text(open(a / f).read(), open(b / f).read(), f, atol=2e-6 if f.endswith((".log", ".txt")) else 1e-8,
+                   rtol=0)
