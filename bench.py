@@ -228,6 +228,66 @@ def other_configs(root, device):
     return out
 
 
+def batched_config(root, device, steps, n_rep=512):
+    """The batched form on its configuration: n_rep replicas (LJ gases and Cu rjl
+    slabs of 500-20,000 atoms at 100-1,200 K, nve) stepped together by one persistent
+    kernel, after the autotuner picked threads per row per size bucket.  Beside it:
+    the same replicas run one at a time through the single-system library (plain
+    and precision forms, on a sample of 8), the force error against the plain form
+    at the final positions, and each replica's NVE drift from its energy history."""
+    import numpy as np
+    import pfmds_gb300 as pf
+    from pfmds_gb300 import configs
+    d = os.path.join(root, "batch")
+    t0 = time.perf_counter()
+    ln, reps = configs.batch_systems(d, n_rep=n_rep, steps=steps, log_period=100, workers=os.cpu_count() or 1)
+    t_gen = time.perf_counter() - t0
+    b = pf.Batch(d, ln, device=device)
+    R, n_all, _ = b.info()
+    b.run(10)
+    tpa = b.tune(10)
+    ms = b.run(steps - 10)
+    rate = n_all * (steps - 10) / (ms / 1e3)
+    h, per = b.history()
+    ns = np.array([r["n"] for r in reps], float)
+    dts = np.array([0.5 if r["kind"] == "lj" else 1.0 for r in reps])
+    tot = (h[:, :, 0] + h[:, :, 1]) / ns[None, :]
+    rows = np.arange(h.shape[0], dtype=float) * per
+    drift = np.array([np.polyfit(rows * dts[r], tot[:, r], 1)[0] * 1e6 for r in range(R)])
+    rng = np.random.default_rng(1)
+    sample = sorted(rng.choice(R, size=min(8, R), replace=False).tolist())
+    rel, t_one = [], {"plain": [0.0, 0.0], "precision": [0.0, 0.0]}
+    for r in sample:
+        p, v, f = b.state(r)
+        s = pf.Simulation(d, settings=reps[r]["settings"], form="plain", out_period=10 ** 9, device=device)
+        s.set_state(p, v)
+        s.compute()
+        fp = s.state()[2]
+        rel.append(float(np.sqrt(((f - fp) ** 2).mean()) / np.sqrt((fp ** 2).mean())))
+        s.close()
+        for form in ("plain", "precision"):
+            s = pf.Simulation(d, settings=reps[r]["settings"], form=form, out_period=10 ** 9, device=device)
+            s.advance(10)
+            t_one[form][0] += s.natoms * 20
+            t_one[form][1] += s.advance_timed(20) / 1e3
+            s.close()
+    one = {k: v[0] / v[1] for k, v in t_one.items()}
+    b.close()
+    return {
+        "workload": f"{R} replicas (LJ gas or Cu rjl slab, 500-20,000 atoms, 100-1,200 K, nve), {n_all} atoms, "
+                    f"{steps} steps, one persistent cooperative kernel per 100 steps",
+        "value": rate, "unit": "atom-steps/s", "ms_per_md_step": ms / (steps - 10),
+        "tpa_per_bucket": dict(zip(["lj<2k", "lj<8k", "lj>=8k", "rjl<2k", "rjl<8k", "rjl>=8k"], tpa)),
+        "one_at_a_time_sample": {"replicas": len(sample), "plain": one["plain"], "precision": one["precision"]},
+        "speedup_vs_plain": rate / one["plain"], "speedup_vs_precision_one_at_a_time": rate / one["precision"],
+        "force_rmse_rel_vs_plain": {"max": max(rel), "median": float(np.median(rel))},
+        "nve_drift_eV_per_atom_per_ns": {"median_abs": float(np.median(np.abs(drift))),
+                                         "max_abs": float(np.abs(drift).max()),
+                                         "fraction_below_1e-5": float((np.abs(drift) < 1e-5).mean()),
+                                         "window_fs": "steps x dt (0.5 fs LJ, 1 fs Cu), energies every 100 steps"},
+        "input_generation_s": t_gen}
+
+
 def pinned_arrays(n, k):
     """k float64 (n, 3) host arrays in page-locked memory (torch's pinned
     allocator) when a CUDA torch is present, else ordinary numpy arrays."""
@@ -397,6 +457,8 @@ def run_ours(args):
                       "speedup_of_precision_form": value / plain_rate}
 
         extra = other_configs(d, device) if (rank == 0 and not args.no_extra) else None
+        if extra is not None and args.batch_steps > 0:
+            extra["batched_512"] = batched_config(d, device, args.batch_steps)
 
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
@@ -473,7 +535,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-md-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-extra", action="store_true", help="skip the LJ-gas and moire configurations")
+    ap.add_argument("--no-extra", action="store_true", help="skip the LJ-gas, moire and batched configurations")
+    ap.add_argument("--batch-steps", type=int, default=5000, help="MD steps of the batched configuration (0 skips)")
     ap.add_argument("--drift-steps", type=int, default=10000,
                     help="MD steps of the NVE drift measurement (precision form; plain runs a fifth)")
     ap.add_argument("--quick", action="store_true",

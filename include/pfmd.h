@@ -177,6 +177,48 @@ int pfmd_time_kernel(pfmd_ctx* ctx, const char* name, int reps, double* ms, doub
  * first call and kept. */
 int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
 
+/* ---- batched form: many independent replicas -----------------------------
+ * PFMDS runs independent systems one per MPI rank, each rank calling md() on one
+ * entry of a settings list (runners/run_md_simulation_mpi.f90:68-88, the -ilist
+ * format: a count, then settings-file / output-prefix pairs).  These entry points
+ * load every entry of such a list into one device state and advance all replicas
+ * together in one persistent cooperative kernel (precision form).  A replica is a
+ * binary LJ gas (lj1g, lj1g, lj) or an rjl slab integrated with nve; all replicas
+ * share one list period. */
+typedef struct pfmd_batch pfmd_batch;
+
+/* Reads input_path+list_file and every settings file it names (as md() reads
+ * them, md_simulation.f90:44-113) and uploads the replicas.  opt may be NULL.
+ * *batch is set even on failure, for pfmd_batch_errmsg; destroy it. */
+int pfmd_batch_create(const char* input_path, const char* list_file, const pfmd_options* opt,
+                      pfmd_batch** batch);
+void pfmd_batch_destroy(pfmd_batch* batch);
+const char* pfmd_batch_errmsg(const pfmd_batch* batch);
+/* Number of replicas, total atoms, MD steps done. */
+int pfmd_batch_info(const pfmd_batch* batch, int* n_replicas, long long* n_atoms, long long* md_step);
+/* Replica r (0-based, list order): first atom in the concatenated state, atom
+ * count, kind (0 LJ gas, 1 rjl slab). */
+int pfmd_batch_replica(const pfmd_batch* batch, int r, int* atom0, int* n, int* kind);
+/* Advances every replica by nsteps MD steps (md()'s loop body for nve: kick,
+ * drift, lists at the list period, forces, kick; energies at the log period);
+ * *device_ms (may be NULL) is the device time of the launches. */
+int pfmd_batch_run(pfmd_batch* batch, long long nsteps, double* device_ms);
+/* Autotuner: times `steps` MD steps with threads per list row 1, 2, 4 and 8 for
+ * each size bucket (kind x {<2,000, <8,000, larger} atoms) on a saved copy of the
+ * state, keeps the fastest and restores the state; only at a list-period boundary.
+ * tpa (may be NULL) receives the 6 choices. */
+int pfmd_batch_tune(pfmd_batch* batch, int steps, int* tpa);
+/* Sets the 6 bucket choices directly (1, 2, 4 or 8). */
+int pfmd_batch_set_tpa(pfmd_batch* batch, const int* tpa);
+/* Positions, velocities, forces of replica r (3*n doubles each; NULL skips). */
+int pfmd_batch_get_state(pfmd_batch* batch, int r, double* pos, double* vel, double* frc);
+/* Potential and kinetic energy of every replica at the last energy step. */
+int pfmd_batch_energies(pfmd_batch* batch, double* e_pot, double* e_kin);
+/* Energy history: rows x replicas x (potential, kinetic), one row per energy step
+ * from step 0; *rows and *period (steps between rows) are returned; hist may be
+ * NULL to query the size. */
+int pfmd_batch_energy_history(pfmd_batch* batch, double* hist, long long* rows, int* period);
+
 /* ---- rjl forces without device allocation ----------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
  * host codes whose device memory is all reserved up front by their own pool

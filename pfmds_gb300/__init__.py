@@ -31,7 +31,9 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_get_state", "pfmd_set_state", "pfmd_energies", "pfmd_compute", "pfmd_ninteractions",
            "pfmd_nlist_shape", "pfmd_get_nlist", "pfmd_nlist_load", "pfmd_get_gr_norm", "pfmd_set_group_n",
            "pfmd_get_stream", "pfmd_kernel_launches", "pfmd_advance_timed", "pfmd_time_kernel",
-           "pfmd_flush_l2", "pfmd_rjl_forces_noalloc")
+           "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
+           "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
+           "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_rjl_forces_noalloc")
 
 _LIB = None
 
@@ -88,6 +90,19 @@ def load(path=LIB_PATH):
     L.pfmd_advance_timed.argtypes = [vp, C.c_longlong, ip, dp]
     L.pfmd_time_kernel.argtypes = [vp, C.c_char_p, C.c_int, dp, dp]
     L.pfmd_flush_l2.argtypes = [vp, C.c_longlong]
+    L.pfmd_batch_create.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(Options), C.POINTER(vp)]
+    L.pfmd_batch_destroy.argtypes = [vp]
+    L.pfmd_batch_destroy.restype = None
+    L.pfmd_batch_errmsg.argtypes = [vp]
+    L.pfmd_batch_errmsg.restype = C.c_char_p
+    L.pfmd_batch_info.argtypes = [vp, ip, llp, llp]
+    L.pfmd_batch_replica.argtypes = [vp, C.c_int, ip, ip, ip]
+    L.pfmd_batch_run.argtypes = [vp, C.c_longlong, dp]
+    L.pfmd_batch_tune.argtypes = [vp, C.c_int, ip]
+    L.pfmd_batch_set_tpa.argtypes = [vp, ip]
+    L.pfmd_batch_get_state.argtypes = [vp, C.c_int, dp, dp, dp]
+    L.pfmd_batch_energies.argtypes = [vp, dp, dp]
+    L.pfmd_batch_energy_history.argtypes = [vp, dp, llp, ip]
     # device buffers are passed as integer addresses (c_void_p)
     L.pfmd_rjl_forces_noalloc.argtypes = [C.c_int, vp, dp, dp, vp, vp, C.c_int, vp, vp, vp, C.c_char_p, C.c_int]
     _LIB = L
@@ -279,6 +294,85 @@ def md(input_path, settings="md_run_settings.txt", **kw):
     o = default_options(output_prefix=prefix.encode(), **kw)
     ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
     return L.pfmd_md(ip.encode(), settings.encode(), C.byref(o))
+
+
+class Batch:
+    """Batched form: every replica of a settings list (the -ilist format of
+    run_md_simulation_mpi) in one device state, advanced together by one
+    persistent kernel (precision form)."""
+
+    def __init__(self, input_path, list_file, device=0):
+        L = load()
+        self.opts = default_options(form="precision", device=device)
+        self._h = C.c_void_p()
+        ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
+        rc = L.pfmd_batch_create(ip.encode(), list_file.encode(), C.byref(self.opts), C.byref(self._h))
+        if rc:
+            msg = L.pfmd_batch_errmsg(self._h).decode()
+            L.pfmd_batch_destroy(self._h)
+            self._h = None
+            raise PfmdError(rc, msg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pfmd_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def _check(self, rc):
+        if rc:
+            raise PfmdError(rc, load().pfmd_batch_errmsg(self._h).decode())
+
+    def info(self):
+        r, n, s = C.c_int(), C.c_longlong(), C.c_longlong()
+        self._check(load().pfmd_batch_info(self._h, C.byref(r), C.byref(n), C.byref(s)))
+        return r.value, n.value, s.value
+
+    @property
+    def n_replicas(self):
+        return self.info()[0]
+
+    def replica(self, r):
+        a, n, k = C.c_int(), C.c_int(), C.c_int()
+        self._check(load().pfmd_batch_replica(self._h, r, C.byref(a), C.byref(n), C.byref(k)))
+        return dict(atom0=a.value, n=n.value, kind=("lj", "rjl")[k.value])
+
+    def run(self, nsteps):
+        ms = C.c_double()
+        self._check(load().pfmd_batch_run(self._h, nsteps, C.byref(ms)))
+        return ms.value
+
+    def tune(self, steps=10):
+        t = np.zeros(6, np.int32)
+        self._check(load().pfmd_batch_tune(self._h, steps, _ip(t)))
+        return t.tolist()
+
+    def set_tpa(self, tpa):
+        t = np.ascontiguousarray(tpa, dtype=np.int32)
+        self._check(load().pfmd_batch_set_tpa(self._h, _ip(t)))
+
+    def state(self, r):
+        n = self.replica(r)["n"]
+        p, v, f = (np.zeros((n, 3)) for _ in range(3))
+        self._check(load().pfmd_batch_get_state(self._h, r, _dp(p), _dp(v), _dp(f)))
+        return p, v, f
+
+    def energies(self):
+        R = self.n_replicas
+        ep, ek = np.zeros(R), np.zeros(R)
+        self._check(load().pfmd_batch_energies(self._h, _dp(ep), _dp(ek)))
+        return ep, ek
+
+    def history(self):
+        """(rows, replicas, 2) array of (potential, kinetic) per energy step, and
+        the steps between rows."""
+        rows, per = C.c_longlong(), C.c_int()
+        self._check(load().pfmd_batch_energy_history(self._h, None, C.byref(rows), C.byref(per)))
+        h = np.zeros((max(rows.value, 0), self.n_replicas, 2))
+        if rows.value:
+            self._check(load().pfmd_batch_energy_history(self._h, _dp(h), C.byref(rows), C.byref(per)))
+        return h, per.value
 
 
 def run_md_simulation(args):

@@ -30,8 +30,9 @@ def _fmt_xyz(box, pos, vel, mass, types):
              'Lattice="' + "".join(f"{v:16.6f}" for v in
                                    (box[0], 0, 0, 0, box[1], 0, 0, 0, box[2]))
              + ' " Properties=pos:R:3:vel:R:3:mass:R:1:species:S:1']
-    for p, v, m, t in zip(pos, vel, mass, types):
-        lines.append("".join(f"{x:27.16f}" for x in (*p, *v, m)) + "    " + t)
+    fmt = "%27.16f" * 7 + "    %s"
+    rows = np.concatenate([np.asarray(pos, float), np.asarray(vel, float), np.asarray(mass, float)[:, None]], axis=1)
+    lines.extend(fmt % (*r, t) for r, t in zip(rows.tolist(), types))
     return "\n".join(lines) + "\n"
 
 
@@ -146,15 +147,45 @@ def _uniform_min_sep(rng, n, box, dmin, max_tries=200):
     return pts
 
 
+def _uniform_min_sep_batched(rng, n, box, dmin):
+    """Uniform positions with a minimum separation, drawn in vectorised rounds:
+    candidates closer than dmin to an accepted point are dropped, then of each
+    too-close pair among the survivors the later one.  Uses scipy's periodic k-d
+    tree; much faster than the one-at-a-time sampler for tens of thousands of atoms."""
+    from scipy.spatial import cKDTree
+    box = np.asarray(box, float)
+    pts = np.empty((0, 3))
+    for _ in range(10000):
+        need = n - len(pts)
+        if need <= 0:
+            break
+        cand = rng.random((max(64, int(need * 1.5)), 3)) * box
+        if len(pts):
+            dist, _ = cKDTree(pts, boxsize=box).query(cand, k=1)
+            cand = cand[dist >= dmin]
+        if len(cand) > 1:
+            pairs = cKDTree(cand, boxsize=box).query_pairs(dmin, output_type="ndarray")
+            if len(pairs):
+                bad = np.zeros(len(cand), bool)
+                bad[pairs.max(axis=1)] = True
+                cand = cand[~bad]
+        pts = np.concatenate([pts, cand[:need]])
+    if len(pts) < n:
+        raise RuntimeError("could not place atoms with the requested minimum separation")
+    return pts
+
+
 def lj_gas(d, n_a=2000, n_b=2000, box=60.0, seed=12345, temperature=100.0, r1=6.5, r2=7.5,
            rc_list=8.5, period=10, nmax=64, integrators=None, step_limit=None, log_period=100,
-           nhc_tau=100.0, min_sep=2.5, ms_de=1e-8, interleave=True, xyz_name="AB.xyz"):
+           nhc_tau=100.0, min_sep=2.5, ms_de=1e-8, interleave=True, xyz_name="AB.xyz",
+           settings_name="md_run_settings.txt", fast_sampler=False):
     """Binary LJ gas (A-B Lorentz-Berthelot) in a periodic cube; writes AB.xyz, the three
     parameter files and md_run_settings.txt into directory d.  Returns the settings name."""
     os.makedirs(d, exist_ok=True)
     rng = np.random.default_rng(seed)
     n = n_a + n_b
-    pos = _uniform_min_sep(rng, n, (box, box, box), min_sep)
+    sampler = _uniform_min_sep_batched if fast_sampler else _uniform_min_sep
+    pos = sampler(rng, n, (box, box, box), min_sep)
     types = np.array(["A"] * n_a + ["B"] * n_b)
     if interleave:
         types = types[rng.permutation(n)]
@@ -182,8 +213,8 @@ def lj_gas(d, n_a=2000, n_b=2000, box=60.0, seed=12345, temperature=100.0, r1=6.
                                                        (3, 2, nmax, rc_list, period)]),
                       ("lj1g", "parameters_LJ_A-A.txt", [(2, 2, nmax, rc_list, period)]),
                       ("lj1g", "parameters_LJ_B-B.txt", [(3, 3, nmax, rc_list, period)])])
-    _write(d, "md_run_settings.txt", text)
-    return "md_run_settings.txt"
+    _write(d, settings_name, text)
+    return settings_name
 
 
 def fcc_slab(nx, ny, nz, a=3.615, z0=5.0, vacuum=25.0):
@@ -201,7 +232,8 @@ def fcc_slab(nx, ny, nz, a=3.615, z0=5.0, vacuum=25.0):
 
 def cu_slab(d, nx=32, ny=32, nz=16, a=3.615, fixed_layers=2, seed=2024, temperature=300.0,
             disp=0.05, dt=1.0, steps=10000, log_period=100, rc_list=5.5, period=10, nmax=64,
-            r1=4.5, r2=5.0, vacuum=25.0, integrator="nve", nhc_tau=100.0, xyz_name="cu_slab.xyz"):
+            r1=4.5, r2=5.0, vacuum=25.0, integrator="nve", nhc_tau=100.0, xyz_name="cu_slab.xyz",
+            settings_name="md_run_settings.txt"):
     """Cu fcc (001) slab under rjl; the bottom `fixed_layers` (001) layers are CU_fixed
     and excluded from the moving groups."""
     os.makedirs(d, exist_ok=True)
@@ -227,8 +259,8 @@ def cu_slab(d, nx=32, ny=32, nz=16, a=3.615, fixed_layers=2, seed=2024, temperat
         integrators=[(integrator, dt, steps, 100000000, log_period)], ms_de=1e-8,
         nhc=[(2, temperature, 3, q1)], t0=temperature,
         interactions=[("rjl", "parameters_RJL_Cu.txt", [(1, 1, nmax, rc_list, period)])])
-    _write(d, "md_run_settings.txt", text)
-    return "md_run_settings.txt"
+    _write(d, settings_name, text)
+    return settings_name
 
 
 def graphene_sheet(nx, ny, a=2.46, strain=(1.0, 1.0)):
@@ -384,3 +416,51 @@ def gr_on_cu(d, n_gx=10, n_gy=6, n_cx=9, n_cy=5, layers=4, fixed_layers=1, a_cu=
                                                              (1, 1, 3, 1.8, period)])])
     _write(d, "md_run_settings.txt", text)
     return "md_run_settings.txt"
+
+
+def _batch_replica(d, name, kind, n, T, sub, steps, log_period):
+    if kind == "lj":
+        n_a = n // 2
+        box = (n / (4000.0 / 60.0 ** 3)) ** (1.0 / 3.0)
+        sf = lj_gas(d, n_a=n_a, n_b=n - n_a, box=box, seed=sub, temperature=T,
+                    integrators=[("nve", 0.5, steps, 100000000, log_period)], xyz_name=name + ".xyz",
+                    settings_name=name + "_settings.txt", fast_sampler=True)
+    else:
+        nz = max(4, int(round((n / 4.0) ** (1.0 / 3.0))))
+        nxy = max(4, int(round(math.sqrt(n / (4.0 * nz)))))
+        # nmax 96: near 1,200 K the 5.5 A shell of a Cu atom fluctuates past 64
+        sf = cu_slab(d, nx=nxy, ny=nxy, nz=nz, seed=sub, temperature=T, steps=steps, log_period=log_period,
+                     integrator="nve", xyz_name=name + ".xyz", settings_name=name + "_settings.txt", nmax=96)
+        n = 4 * nxy * nxy * nz
+    return dict(name=name, kind=kind, n=n, temperature=T, settings=sf)
+
+
+def batch_systems(d, n_rep=512, seed=4242, n_min=500, n_max=20000, t_min=100.0, t_max=1200.0, steps=5000,
+                  log_period=10, list_name="batch_list.txt", workers=1):
+    """The batched configuration: n_rep independent replicas, each an LJ gas (A-B,
+    as lj_gas, dt 0.5 fs) or a Cu rjl slab (as cu_slab, dt 1 fs) with a 50/50 draw,
+    sizes uniform in [n_min, n_max] atoms and temperatures uniform in [t_min, t_max]
+    K, all nve for `steps` steps.  Writes one settings file and .xyz per replica,
+    the shared parameter files, and the settings list (the -ilist format: count,
+    then settings file and output prefix per line).  All draws come from `seed`
+    first, so `workers` processes (spawned) produce the same files.  Returns the
+    list name and the replica descriptions."""
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(n_rep):
+        n = int(rng.integers(n_min, n_max + 1))
+        T = float(rng.uniform(t_min, t_max))
+        sub = int(rng.integers(0, 2 ** 31 - 1))
+        kind = "lj" if rng.random() < 0.5 else "rjl"
+        jobs.append((d, f"rep{k:04d}", kind, n, T, sub, steps, log_period))
+    if workers > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            reps = list(ex.map(_batch_replica, *zip(*jobs), chunksize=4))
+    else:
+        reps = [_batch_replica(*j) for j in jobs]
+    lines = [f"{r['settings']}\t{r['name']}_" for r in reps]
+    _write(d, list_name, f"{n_rep}\n" + "\n".join(lines) + "\n")
+    return list_name, reps
