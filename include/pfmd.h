@@ -177,6 +177,32 @@ int pfmd_time_kernel(pfmd_ctx* ctx, const char* name, int reps, double* ms, doub
  * first call and kept. */
 int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
 
+/* ---- learned form ----------------------------------------------------------
+ * No reference counterpart: a per-atom network potential (32 radial + 16 angular
+ * Behler-Parrinello symmetry functions, 48-64-64-1 with SiLU) standing in for the
+ * tb and rjl interactions, trained on what the plain kernels compute; the
+ * classical kernels remain its fallback and the judge of its error. */
+
+/* Trains on frames of this context's own run (plain form only): `frames` times it
+ * advances `stride` steps (md()'s loop), records the per-atom tb and rjl energies
+ * of the configuration and takes `iters` Adam steps (learning rate lr) per
+ * network on per-atom energy error.  model_in: a model file to continue from, or
+ * NULL for new networks (normalisation from the first frame); model_out: file to
+ * write (may be NULL).  rmse (per interaction, NaN where no network; may be NULL):
+ * per-atom energy RMSE (eV) on the last frame. */
+int pfmd_learned_train(pfmd_ctx* ctx, const char* model_in, const char* model_out, int frames, int stride,
+                       int iters, double lr, double* rmse);
+/* Switches the context's tb and rjl interactions to the networks in model_path.
+ * Every check_period steps (0: never) the classical kernels recompute the forces
+ * of the same configuration; if the RMSE between the two exceeds max_rmse (eV/A)
+ * the run falls back to the classical kernels for good. */
+int pfmd_learned_use(pfmd_ctx* ctx, const char* model_path, long long check_period, double max_rmse);
+/* RMSE (eV/A) between learned and classical forces at the current positions;
+ * leaves the forces of the active form. */
+int pfmd_learned_check(pfmd_ctx* ctx, double* rmse);
+/* Learned kernels active, checks done, last check's RMSE (-1: none), fell back. */
+int pfmd_learned_status(const pfmd_ctx* ctx, int* active, int* checks, double* last_rmse, int* fallen_back);
+
 /* ---- batched form: many independent replicas -----------------------------
  * PFMDS runs independent systems one per MPI rank, each rank calling md() on one
  * entry of a settings list (runners/run_md_simulation_mpi.f90:68-88, the -ilist

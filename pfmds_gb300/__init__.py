@@ -33,7 +33,8 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_get_stream", "pfmd_kernel_launches", "pfmd_advance_timed", "pfmd_time_kernel",
            "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
            "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
-           "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_rjl_forces_noalloc")
+           "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
+           "pfmd_learned_check", "pfmd_learned_status", "pfmd_rjl_forces_noalloc")
 
 _LIB = None
 
@@ -103,6 +104,10 @@ def load(path=LIB_PATH):
     L.pfmd_batch_get_state.argtypes = [vp, C.c_int, dp, dp, dp]
     L.pfmd_batch_energies.argtypes = [vp, dp, dp]
     L.pfmd_batch_energy_history.argtypes = [vp, dp, llp, ip]
+    L.pfmd_learned_train.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, dp]
+    L.pfmd_learned_use.argtypes = [vp, C.c_char_p, C.c_longlong, C.c_double]
+    L.pfmd_learned_check.argtypes = [vp, dp]
+    L.pfmd_learned_status.argtypes = [vp, ip, ip, dp, ip]
     # device buffers are passed as integer addresses (c_void_p)
     L.pfmd_rjl_forces_noalloc.argtypes = [C.c_int, vp, dp, dp, vp, vp, C.c_int, vp, vp, vp, C.c_char_p, C.c_int]
     _LIB = L
@@ -257,6 +262,29 @@ class Simulation:
 
     def set_group_n(self, group, n):
         self._check(load().pfmd_set_group_n(self._h, group, n))
+
+    def learned_train(self, model_out, frames, stride=10, iters=4, lr=1e-3, model_in=None):
+        """Online training from this plain-form run; returns the per-interaction
+        per-atom energy RMSE (eV) of the last frame (NaN where no network)."""
+        r = np.zeros(max(1, self.n_interactions))
+        self._check(load().pfmd_learned_train(self._h, model_in.encode() if model_in else None,
+                                              model_out.encode() if model_out else None, frames, stride, iters, lr,
+                                              _dp(r)))
+        return r[:self.n_interactions].copy()
+
+    def learned_use(self, model_path, check_period=100, max_rmse=0.05):
+        self._check(load().pfmd_learned_use(self._h, model_path.encode(), check_period, max_rmse))
+
+    def learned_check(self):
+        r = C.c_double()
+        self._check(load().pfmd_learned_check(self._h, C.byref(r)))
+        return r.value
+
+    def learned_status(self):
+        a, n, f = C.c_int(), C.c_int(), C.c_int()
+        r = C.c_double()
+        self._check(load().pfmd_learned_status(self._h, C.byref(a), C.byref(n), C.byref(r), C.byref(f)))
+        return dict(active=bool(a.value), checks=n.value, last_rmse=r.value, fallen_back=bool(f.value))
 
     @property
     def stream(self):

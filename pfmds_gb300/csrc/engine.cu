@@ -27,6 +27,7 @@
 
 #include "../../include/pfmd.h"
 #include "kernels.h"
+#include "learned.h"
 #include "settings.h"
 
 namespace pfmd {
@@ -239,6 +240,32 @@ class Engine {
   std::vector<ListH> lists;
   std::vector<InterH> inters;
   std::vector<ChangeSpec> changes;
+  // learned form: a network per tb / rjl interaction (see learned.h)
+  struct Lrn {
+    bool on = false;
+    learned::Model model;
+    DBuf<learned::DescPar> d;
+    DBuf<learned::Net> net;
+    DBuf<float> G, g, e, part, grad, m, v;
+    DBuf<double> t, lpart, loss;
+    int adam_step = 0;
+  };
+  std::vector<Lrn> lrn;        // per interaction
+  bool learned_active = false;  // learned kernels in place of the classical ones
+  long long check_period = 0;
+  double max_rmse = 0.0, last_rmse = -1.0;
+  int checks = 0;
+  bool fallen_back = false;
+  DBuf<double4_32a> fsave;
+  DBuf<double> fdiff, eatom;
+  double* eatom_out = nullptr;  // set while per-atom energies are recorded
+  void learned_setup(const std::vector<learned::Model>& ms);
+  void learned_upload_desc(Lrn& L);
+  double learned_check(bool switch_on_fail);
+  void learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride, int iters,
+                     double lr, double* rmse_out);
+  void clear_graphs();
+  void ensure_lists();
   Ctl* ctl = nullptr;
   Ctl* hctl = nullptr;  // pinned host copy (header part)
   size_t ctl_head = 0;
@@ -927,6 +954,7 @@ StepPlan Engine::plan(long long s) const {
 
 bool Engine::is_event(const StepPlan& p) const {
   const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
+  if (learned_active && check_period > 0 && p.step > 0 && p.step % check_period == 0) return true;
   if (log && p.step % I.period_log == 0) return true;
   if (p.out) return true;
   if (opt.write_files && p.step % I.period_snapshot == 0 && p.step != 0) return true;
@@ -1028,7 +1056,7 @@ void Engine::enqueue_forces(bool energy, bool kick) {
   // which launch is the first / last force writer
   const int nint = static_cast<int>(inters.size());
   auto epi = [&](bool first, bool last) {
-    Epi e{0, 0, prec ? 0 : 1, ts[1], mflag.p};
+    Epi e{0, 0, prec ? 0 : 1, ts[1], mflag.p, eatom_out};
     e.store = (first && store_first) ? 1 : 0;
     e.kick = (last && kick && kick_last) ? 1 : 0;
     return e;
@@ -1039,6 +1067,13 @@ void Engine::enqueue_forces(bool energy, bool kick) {
     const int eslot = 4 + (k % 16);
     const bool first = k == 0, last = k == nint - 1;
     const ListDev& L1 = lists[static_cast<size_t>(I.lists[0])].d;
+    if (learned_active && k < static_cast<int>(lrn.size()) && lrn[static_cast<size_t>(k)].on) {
+      Lrn& M = lrn[static_cast<size_t>(k)];
+      learned::launch_desc(L1, M.d.p, A, box, M.G.p, ctl, st);
+      learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
+      learned::launch_force(L1, M.d.p, M.g.p, M.e.p, energy, A, box, ctl, eslot, key, st, epi(first, last));
+      continue;
+    }
     switch (I.spec.kind) {
       case pfmd_io::K_LJ:
         launch_lj(prec, energy, L1, I.lj, A, box, ctl, eslot, key, st, epi(first, false));
@@ -1357,7 +1392,11 @@ void Engine::advance(long long max_steps, int* fin) {
     }
     md_step = plans.back().step + 1;
     done += static_cast<long long>(plans.size());
-    if (is_event(plans.back())) host_events(plans.back());
+    if (is_event(plans.back())) {
+      host_events(plans.back());
+      const long long ls = plans.back().step;
+      if (learned_active && check_period > 0 && ls > 0 && ls % check_period == 0) learned_check(true);
+    }
     flush_out();
   }
   if (md_step > S.md_step_limit) finished = true;
@@ -1415,6 +1454,238 @@ void Engine::finish() {
     log = nullptr;
   }
   flush_out();
+}
+
+void Engine::clear_graphs() {
+  for (auto& kv : graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  graphs.clear();
+}
+
+void Engine::learned_setup(const std::vector<learned::Model>& ms) {
+  lrn.clear();
+  lrn.resize(inters.size());
+  int used = 0;
+  for (size_t k = 0; k < inters.size(); ++k) {
+    const int kind = inters[k].spec.kind == pfmd_io::K_TB ? 0 : (inters[k].spec.kind == pfmd_io::K_RJL ? 1 : -1);
+    if (kind < 0) continue;
+    const learned::Model* m = nullptr;
+    for (const auto& x : ms)
+      if (x.kind == kind) {
+        m = &x;
+        break;
+      }
+    if (!m) continue;
+    Lrn& M = lrn[k];
+    M.on = true;
+    M.model = *m;
+    ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
+    if (L.rc < std::max(m->d.rc_rad, m->d.rc_ang))
+      throw Error(PFMD_E_PARAM, "learned form: the " + inters[k].spec.name + " list needs r_cut >= " +
+                                    std::to_string(std::max(m->d.rc_rad, m->d.rc_ang)) + " A for its descriptors");
+    const size_t rows = static_cast<size_t>(std::max(L.d.rows, 1));
+    M.d.alloc(1);
+    M.net.alloc(1);
+    M.G.alloc(rows * learned::NG);
+    M.g.alloc(rows * learned::NG);
+    M.e.alloc(rows);
+    M.t.alloc(rows);
+    M.d.upload(&M.model.d, 1, st);
+    M.net.upload(&M.model.n, 1, st);
+    if (!L.row_of.p) {  // the force gather reads a partner's row
+      std::vector<int> ro(static_cast<size_t>(N), -1);
+      const auto& rg = groups[static_cast<size_t>(L.d.row_group)].idx;
+      for (size_t q = 0; q < rg.size(); ++q) ro[static_cast<size_t>(rg[q])] = static_cast<int>(q);
+      L.row_of.alloc(ro.size());
+      L.row_of.upload(ro.data(), ro.size(), st);
+      L.d.row_of = L.row_of.p;
+    }
+    ++used;
+  }
+  if (!used) throw Error(PFMD_E_PARAM, "learned form: no tb or rjl interaction matches the model file");
+  if (!fsave.p) {
+    fsave.alloc(static_cast<size_t>(std::max(N, 1)));
+    fdiff.alloc(2 * 256 + 2);
+  }
+  clear_graphs();
+  CK(cudaStreamSynchronize(st));
+}
+
+// Learned and classical forces at the current positions: RMSE over all atoms
+// (eV/A).  With switch_on_fail the learned form stays on below max_rmse and falls
+// back to the classical kernels (keeping their forces) above it.
+// A run that has not taken its first step has no lists yet: build them.
+void Engine::ensure_lists() {
+  if (md_step != 0) return;
+  StepPlan p;
+  p.step = 0;
+  p.first = true;
+  p.energy = true;
+  p.out = p.zero_mom = p.check_all = false;
+  p.rebuild.assign(lists.size(), 1);
+  enqueue_lists(p);
+}
+
+double Engine::learned_check(bool switch_on_fail) {
+  const bool was = learned_active;
+  ensure_lists();
+  const GroupRef gall = gref(S.all_atoms);
+  learned_active = true;
+  if (!store_first) launch_zero_forces(gall, A, ctl, st);
+  enqueue_forces(false, false);
+  CK(cudaMemcpyAsync(fsave.p, frc.p, sizeof(double4_32a) * static_cast<size_t>(N), cudaMemcpyDeviceToDevice, st));
+  learned_active = false;
+  if (!store_first) launch_zero_forces(gall, A, ctl, st);
+  enqueue_forces(false, false);
+  learned::launch_force_diff(N, fsave.p, frc.p, fdiff.p, fdiff.p + 512, st);
+  double out[2] = {0.0, 0.0};
+  CK(cudaMemcpyAsync(out, fdiff.p + 512, sizeof(out), cudaMemcpyDeviceToHost, st));
+  read_ctl();
+  if (hctl->error) raise_device_error();
+  const double rmse = std::sqrt(out[0] / (3.0 * std::max(N, 1)));
+  ++checks;
+  last_rmse = rmse;
+  bool keep = was;
+  if (switch_on_fail && was && rmse > max_rmse) {
+    keep = false;
+    fallen_back = true;
+    clear_graphs();
+  }
+  learned_active = keep;
+  if (keep)
+    CK(cudaMemcpyAsync(frc.p, fsave.p, sizeof(double4_32a) * static_cast<size_t>(N), cudaMemcpyDeviceToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  return rmse;
+}
+
+// Online training from this (plain-form) run: every `stride` steps the plain tb and
+// rjl kernels give per-atom energies of the current configuration; each network
+// takes `iters` Adam steps on its atoms' descriptors.  rmse_out[k] (per
+// interaction, NaN where no network) = per-atom energy RMSE of the last frame.
+void Engine::learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride,
+                           int iters, double lr, double* rmse_out) {
+  if (prec) throw Error(PFMD_E_STATE, "learned training runs on the plain form (FP64 targets)");
+  std::vector<learned::Model> ms;
+  const bool fresh = model_in.empty();
+  if (fresh) {
+    for (const auto& I : inters) {
+      if (I.spec.kind == pfmd_io::K_TB) ms.push_back(learned::default_model(0, static_cast<unsigned>(opt.rand_seed)));
+      if (I.spec.kind == pfmd_io::K_RJL) ms.push_back(learned::default_model(1, static_cast<unsigned>(opt.rand_seed)));
+    }
+  } else {
+    ms = learned::load_models(model_in);
+  }
+  iters = std::max(1, iters);
+  learned_setup(ms);
+  learned_active = false;
+  if (!eatom.p) eatom.alloc(static_cast<size_t>(std::max(N, 1)));
+  for (auto& M : lrn) {
+    if (!M.on) continue;
+    const int rows = static_cast<int>(M.e.n);
+    const int blocks = learned::train_blocks(rows);
+    M.part.alloc(static_cast<size_t>(blocks) * learned::NET_FLOATS);
+    M.lpart.alloc(static_cast<size_t>(blocks));
+    M.grad.alloc(learned::NET_FLOATS);
+    M.m.alloc(learned::NET_FLOATS);
+    M.v.alloc(learned::NET_FLOATS);
+    M.m.zero(st);
+    M.v.zero(st);
+    M.loss.alloc(2);
+    M.adam_step = 0;
+  }
+  const GroupRef gall = gref(S.all_atoms);
+  for (int f = 0; f < frames; ++f) {
+    if (stride > 0) {
+      int fin = 0;
+      advance(stride, &fin);
+      if (finished) break;
+    }
+    // per-atom energies of the classical interactions at this configuration
+    ensure_lists();
+    eatom_out = eatom.p;
+    if (!store_first) launch_zero_forces(gall, A, ctl, st);
+    enqueue_forces(true, false);
+    eatom_out = nullptr;
+    for (size_t k = 0; k < lrn.size(); ++k) {
+      Lrn& M = lrn[k];
+      if (!M.on) continue;
+      const ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
+      const int rows = L.d.rows;
+      learned::launch_gather_rows(L.d, eatom.p, M.t.p, st);
+      if (fresh && f == 0) {
+        // descriptor normalisation and the energy offset from the first frame
+        for (int q = 0; q < learned::NG; ++q) {
+          M.model.d.mean[q] = 0.f;
+          M.model.d.inv_std[q] = 1.f;
+        }
+        M.d.upload(&M.model.d, 1, st);
+        learned::launch_desc(L.d, M.d.p, A, box, M.G.p, ctl, st);
+        std::vector<float> G(static_cast<size_t>(rows) * learned::NG);
+        std::vector<double> t(static_cast<size_t>(rows));
+        CK(cudaMemcpyAsync(G.data(), M.G.p, sizeof(float) * G.size(), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(t.data(), M.t.p, sizeof(double) * t.size(), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int q = 0; q < learned::NG; ++q) {
+          double s = 0.0, s2 = 0.0;
+          for (int r = 0; r < rows; ++r) {
+            const double x = G[static_cast<size_t>(r) * learned::NG + q];
+            s += x;
+            s2 += x * x;
+          }
+          const double mu = s / std::max(rows, 1), var = std::max(s2 / std::max(rows, 1) - mu * mu, 0.0);
+          M.model.d.mean[q] = static_cast<float>(mu);
+          // a floor on the spread: a function that is (nearly) constant on the first
+          // frame must not amplify later fluctuations
+          M.model.d.inv_std[q] = static_cast<float>(1.0 / std::max(std::sqrt(var), 0.05));
+        }
+        double tm = 0.0;
+        for (double x : t) tm += x;
+        M.model.n.b3 = static_cast<float>(tm / std::max(rows, 1));
+        M.d.upload(&M.model.d, 1, st);
+        M.net.upload(&M.model.n, 1, st);
+      }
+      learned::launch_desc(L.d, M.d.p, A, box, M.G.p, ctl, st);
+      learned::TrainBuf T;
+      T.part = M.part.p;
+      T.lpart = M.lpart.p;
+      T.part_blocks = learned::train_blocks(rows);
+      T.grad = M.grad.p;
+      T.m = M.m.p;
+      T.v = M.v.p;
+      T.loss = M.loss.p;
+      for (int it = 0; it < iters; ++it) {
+        learned::launch_train_grad(rows, M.G.p, M.t.p, M.net.p, T, st);
+        ++M.adam_step;
+        learned::launch_adam(M.net.p, T, M.adam_step, static_cast<float>(lr), st);
+      }
+    }
+    read_ctl();
+    if (hctl->error) raise_device_error();
+  }
+  // the error of the final networks on the last frame
+  for (size_t k = 0; k < inters.size(); ++k) {
+    if (rmse_out) rmse_out[k] = std::nan("");
+    if (k >= lrn.size() || !lrn[k].on) continue;
+    Lrn& M = lrn[k];
+    const ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
+    learned::TrainBuf T;
+    T.part = M.part.p;
+    T.lpart = M.lpart.p;
+    T.part_blocks = learned::train_blocks(L.d.rows);
+    T.grad = M.grad.p;
+    T.loss = M.loss.p;
+    learned::launch_train_grad(L.d.rows, M.G.p, M.t.p, M.net.p, T, st);
+    double loss[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(loss, M.loss.p, sizeof(loss), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&M.model.n, M.net.p, sizeof(learned::Net), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (rmse_out) rmse_out[k] = std::sqrt(loss[0] / std::max(loss[1], 1.0));
+  }
+  std::vector<learned::Model> out;
+  for (auto& M : lrn)
+    if (M.on) out.push_back(M.model);
+  if (!model_out.empty()) learned::save_models(model_out, out);
+  clear_graphs();
 }
 
 void Engine::compute(bool rebuild, double* e_inter) {
@@ -1929,6 +2200,55 @@ int pfmd_flush_l2(pfmd_ctx* c, long long bytes) {
     if (e.flush_buf.n < static_cast<size_t>(bytes)) e.flush_buf.alloc(static_cast<size_t>(bytes));
     CK(cudaMemsetAsync(e.flush_buf.p, (++e.flush_seq) & 0xff, static_cast<size_t>(bytes), e.st));
   });
+}
+
+int pfmd_learned_train(pfmd_ctx* c, const char* model_in, const char* model_out, int frames, int stride, int iters,
+                       double lr, double* rmse) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  if (frames < 1 || stride < 0 || !(lr > 0.0)) return PFMD_E_PARAM;
+  return guard(c, [&] {
+    c->e->learned_train(model_in ? model_in : "", model_out ? model_out : "", frames, stride, iters, lr, rmse);
+  });
+}
+
+int pfmd_learned_use(pfmd_ctx* c, const char* model_path, long long check_period, double max_rmse) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  if (!model_path || check_period < 0) return PFMD_E_PARAM;
+  return guard(c, [&] {
+    auto& e = *c->e;
+    std::vector<pfmd::learned::Model> ms;
+    try {
+      ms = pfmd::learned::load_models(model_path);
+    } catch (const std::runtime_error& x) {
+      throw ::pfmd::Error(PFMD_E_IO, x.what());
+    }
+    e.learned_setup(ms);
+    e.learned_active = true;
+    e.check_period = check_period;
+    e.max_rmse = max_rmse;
+    e.checks = 0;
+    e.last_rmse = -1.0;
+    e.fallen_back = false;
+  });
+}
+
+int pfmd_learned_check(pfmd_ctx* c, double* rmse) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    if (c->e->lrn.empty()) throw ::pfmd::Error(PFMD_E_STATE, "learned form: no model loaded");
+    const double r = c->e->learned_check(false);
+    if (rmse) *rmse = r;
+  });
+}
+
+int pfmd_learned_status(const pfmd_ctx* c, int* active, int* checks, double* last_rmse, int* fallen_back) {
+  if (!c || !c->e) return PFMD_E_STATE;
+  const auto& e = *c->e;
+  if (active) *active = e.learned_active ? 1 : 0;
+  if (checks) *checks = e.checks;
+  if (last_rmse) *last_rmse = e.last_rmse;
+  if (fallen_back) *fallen_back = e.fallen_back ? 1 : 0;
+  return PFMD_OK;
 }
 
 int pfmd_kernel_launches(const pfmd_ctx* c, long long* n) {

@@ -19,7 +19,7 @@ namespace pfmd {
 // inv_eb holds 1/Eb per atom: double for the plain form, float for the precision form.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb,
-                                                     double2* pair, Ctl* ctl, int eslot, int ekey) {
+                                                     double2* pair, Ctl* ctl, int eslot, int ekey, double* eatom) {
   using T = RT<PREC>;
   using R = typename T::R;
   if (ctl->stop) return;
@@ -86,6 +86,7 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
     }
   }
   if constexpr (ENERGY) {
+    if (eatom && valid && g.sub == 0) eatom[ai] = PREC ? (double)erowf : erow;
     if constexpr (PREC)
       energy_reduce_f(ctl, eslot, ekey, erowf);
     else
@@ -150,9 +151,9 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
       with_tpa(tpa1, [&](auto t) {
         constexpr int TP = decltype(t)::value;
         if (energy)
-          k_rjl_density<PR, true, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey);
+          k_rjl_density<PR, true, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey, E.eatom);
         else
-          k_rjl_density<PR, false, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey);
+          k_rjl_density<PR, false, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey, nullptr);
         ++g_kernel_launches;
       });
     }

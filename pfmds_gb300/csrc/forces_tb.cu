@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
     const R R1 = c.R1, R2 = c.R2, a0 = c.a0, c02 = c.c02, d02 = c.d02, delt = c.delt, d = c.d, s = c.s, bb = c.b,
             r0 = c.r0, inv_w = c.inv_w, ex = c.ex, sq2s = c.sq2s, sq2os = c.sq2os, pre_e = c.pre_e;
     Acc3<PREC> acc;
-    Acc1<PREC> e;
+    Acc1<PREC> e, eh;
     for (int p = 0; p < n; ++p) {
       const int aj = ent(L, i, p);
       const int j = L.row_of[aj];
@@ -122,6 +122,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
           f[k] = pre * ((dp[k] * dff - c1 * dp[k]) * ea - (dB[k] + bavg * (dp[k] * dff - c2 * dp[k])) * s * eas);
         acc.add(f[0], f[1], f[2]);
         if (ENERGY && j > i) e.add(fc * pre_e * (ea - bavg * s * eas));
+        if (ENERGY && E.eatom) eh.add(R(0.5) * fc * pre_e * (ea - bavg * s * eas));
       }
       if (l < nj) {
         R fl, dfl;
@@ -146,6 +147,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
     }
     finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
     erow = e.get();
+    if (ENERGY && E.eatom) E.eatom[ai] = eh.get();
   }
   if (ENERGY) energy_reduce(ctl, eslot, ekey, erow);
 }

@@ -142,6 +142,8 @@ struct Epi {
   int store, kick, exact;
   double ts2;
   const unsigned char* mflag;
+  double* eatom;  // energy steps: per-atom energy of the interaction (rjl: the row energy;
+                  // tb: half of every bond), or null
 };
 
 // ---------------- neighbour lists (nlist.cu) ----------------

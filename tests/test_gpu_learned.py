@@ -1,0 +1,136 @@
+"""Learned form: networks trained on the plain kernels' per-atom energies stand in
+for tb and rjl; the analytic forces are checked against finite differences of the
+library's own energy and of the FP64 CPU reference (oracle/learned_ref.py), and the
+classical kernels judge and replace the networks when they drift."""
+import numpy as np
+import pytest
+
+import pfmds_gb300 as pf
+from pfmds_gb300 import configs
+from oracle import learned_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _gr(d, T=600.0):
+    configs.gr_on_cu(str(d), n_gx=6, n_gy=4, n_cx=6, n_cy=3, layers=3, steps=10 ** 6, log_period=10,
+                     integrator="nve", tb_list=(32, 4.5), temperature=T)
+    return str(d)
+
+
+def _train(d, out, frames=40, stride=5, iters=8, model_in=None):
+    s = pf.Simulation(d, form="plain", out_period=10 ** 9)
+    r = s.learned_train(out, frames=frames, stride=stride, iters=iters, lr=2e-3, model_in=model_in)
+    s.close()
+    return r
+
+
+def test_training_lowers_the_energy_error(tmp_path, built):
+    d = _gr(tmp_path)
+    m0, m1 = str(tmp_path / "m0.bin"), str(tmp_path / "m1.bin")
+    r0 = _train(d, m0, frames=1, stride=0, iters=1)
+    r1 = _train(d, m1, frames=60, stride=5, iters=8, model_in=m0)
+    assert np.isnan(r0[2]) and np.isnan(r1[2])  # the coupling keeps its classical kernel
+    assert (r1[:2] < r0[:2]).all(), (r0, r1)
+    assert (r1[:2] < 0.05).all(), r1  # eV per atom
+    ms = learned_ref.load_models(m1)
+    assert sorted(m["kind"] for m in ms) == [0, 1]
+
+
+def test_energy_matches_cpu_reference_and_forces_its_gradient(tmp_path, built):
+    d = _gr(tmp_path)
+    m = str(tmp_path / "m.bin")
+    _train(d, m, frames=10, stride=5, iters=4)
+    s = pf.Simulation(d, form="precision", out_period=10 ** 9)
+    s.learned_use(m, check_period=0)
+    e = s.compute()
+    p, _, f = s.state()
+    box = np.array([float(x) for x in open(tmp_path / "gr_cu.xyz").read().splitlines()[1].split('"')[1].split()])[[0, 4, 8]]
+    types = [ln.split()[-1] for ln in open(tmp_path / "gr_cu.xyz").read().splitlines()[2:]]
+    models = {mm["kind"]: mm for mm in learned_ref.load_models(m)}
+    c_idx = np.array([i for i, t in enumerate(types) if t == "C"])
+    cu_idx = np.array([i for i, t in enumerate(types) if t.startswith("CU")])
+    e_tb = learned_ref.energy(p, box, c_idx, models[0])
+    e_rjl = learned_ref.energy(p, box, cu_idx, models[1])
+    assert e[0] == pytest.approx(e_tb, abs=2e-5 * len(c_idx))
+    assert e[1] == pytest.approx(e_rjl, abs=2e-5 * len(cu_idx))
+    # forces: central differences of the library's potential energy (all three
+    # interactions) for a few atoms of each kind
+    h = 2e-3
+    for a in list(c_idx[:3]) + list(cu_idx[-3:]):
+        for c in range(3):
+            pp, pm = p.copy(), p.copy()
+            pp[a, c] += h
+            pm[a, c] -= h
+            s.set_state(pp)
+            ep = s.compute().sum()
+            s.set_state(pm)
+            em = s.compute().sum()
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - f[a, c]) < 2e-3 + 2e-2 * abs(f[a, c]), (a, c, fd, f[a, c])
+    s.close()
+
+
+def test_learned_forces_match_cpu_reference_gradient(tmp_path, built):
+    # rjl alone: the library's learned forces against FP64 finite differences of
+    # the CPU reference energy
+    configs.cu_slab(str(tmp_path), nx=3, ny=3, nz=3, steps=10 ** 6, log_period=10, temperature=800.0)
+    m = str(tmp_path / "m.bin")
+    s = pf.Simulation(str(tmp_path), form="plain", out_period=10 ** 9)
+    s.learned_train(m, frames=8, stride=4, iters=4, lr=2e-3)
+    s.close()
+    s = pf.Simulation(str(tmp_path), form="precision", out_period=10 ** 9)
+    s.learned_use(m, check_period=0)
+    s.compute()
+    p, _, f = s.state()
+    box = configs.fcc_slab(3, 3, 3, 3.615, vacuum=25.0)[1]
+    model = learned_ref.load_models(m)[0]
+    idx = np.arange(len(p))
+    atoms = [0, 17, 50, 100]
+    ref = learned_ref.forces_fd(p, box, idx, model, atoms, h=1e-4)
+    scale = np.abs(ref).max()
+    assert np.abs(f[atoms] - ref).max() < 2e-3 * max(scale, 1.0), (f[atoms], ref)
+    s.close()
+
+
+def test_checked_run_stays_within_the_bound(tmp_path, built):
+    # every 10 steps the classical kernels judge the network: the run either stays
+    # learned with the force RMSE under the bound or falls back at the first check
+    # that exceeds it; either way it completes
+    d = _gr(tmp_path)
+    m = str(tmp_path / "m.bin")
+    _train(d, m, frames=60, stride=5, iters=8)
+    s = pf.Simulation(d, form="precision", out_period=10 ** 9)
+    s.learned_use(m, check_period=10, max_rmse=0.5)
+    s.advance(31)
+    st = s.learned_status()
+    assert st["checks"] >= 1 and st["last_rmse"] > 0.0
+    if st["fallen_back"]:
+        assert not st["active"] and st["last_rmse"] > 0.5
+    else:
+        assert st["active"] and st["checks"] == 3 and st["last_rmse"] <= 0.5
+    s.close()
+
+
+def test_fallback_to_classical_kernels(tmp_path, built):
+    d = _gr(tmp_path)
+    m = str(tmp_path / "m.bin")
+    _train(d, m, frames=2, stride=2, iters=1)
+    s = pf.Simulation(d, form="precision", out_period=10 ** 9)
+    s.learned_use(m, check_period=5, max_rmse=1e-9)
+    s.advance(11)
+    st = s.learned_status()
+    assert st["fallen_back"] and not st["active"] and st["checks"] == 1
+    # after the fallback the run uses the classical kernels: same forces as a run
+    # that never loaded a network, from the same state
+    p, v, f = s.state()
+    c = pf.Simulation(d, form="precision", out_period=10 ** 9)
+    c.set_state(p, v)
+    c.compute()
+    s.compute()
+    fs, fc = s.state()[2], c.state()[2]
+    # the same kernels; only the threads per row (tuned after a context's first
+    # steps) and so the FP32 summation order may differ
+    assert np.abs(fs - fc).max() < 1e-6 * np.abs(fc).max()
+    s.close()
+    c.close()
