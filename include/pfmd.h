@@ -184,14 +184,17 @@ int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
  * classical kernels remain its fallback and the judge of its error. */
 
 /* Trains on frames of this context's own run (plain form only): `frames` times it
- * advances `stride` steps (md()'s loop), records the per-atom tb and rjl energies
- * of the configuration and takes `iters` Adam steps (learning rate lr) per
- * network on per-atom energy error.  model_in: a model file to continue from, or
- * NULL for new networks (normalisation from the first frame); model_out: file to
- * write (may be NULL).  rmse (per interaction, NaN where no network; may be NULL):
- * per-atom energy RMSE (eV) on the last frame. */
+ * advances `stride` steps (md()'s loop), takes the per-atom tb and rjl energies and
+ * the forces the plain kernels give for the configuration, and takes `iters` Adam
+ * steps (learning rate lr) on mean squared per-atom energy error plus
+ * force_weight times the mean squared force error (0: energies only).
+ * model_in: a model file to continue from, or NULL for new networks
+ * (normalisation from the first frame); model_out: file to write (may be NULL).
+ * rmse (per interaction, NaN where no network; may be NULL): per-atom energy RMSE
+ * (eV) on the last frame; force_rmse (may be NULL): learned against plain force
+ * RMSE (eV/A) over all atoms on the last frame. */
 int pfmd_learned_train(pfmd_ctx* ctx, const char* model_in, const char* model_out, int frames, int stride,
-                       int iters, double lr, double* rmse);
+                       int iters, double lr, double force_weight, double* rmse, double* force_rmse);
 /* Switches the context's tb and rjl interactions to the networks in model_path.
  * Every check_period steps (0: never) the classical kernels recompute the forces
  * of the same configuration; if the RMSE between the two exceeds max_rmse (eV/A)

@@ -104,7 +104,8 @@ def load(path=LIB_PATH):
     L.pfmd_batch_get_state.argtypes = [vp, C.c_int, dp, dp, dp]
     L.pfmd_batch_energies.argtypes = [vp, dp, dp]
     L.pfmd_batch_energy_history.argtypes = [vp, dp, llp, ip]
-    L.pfmd_learned_train.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, dp]
+    L.pfmd_learned_train.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     dp, dp]
     L.pfmd_learned_use.argtypes = [vp, C.c_char_p, C.c_longlong, C.c_double]
     L.pfmd_learned_check.argtypes = [vp, dp]
     L.pfmd_learned_status.argtypes = [vp, ip, ip, dp, ip]
@@ -263,14 +264,16 @@ class Simulation:
     def set_group_n(self, group, n):
         self._check(load().pfmd_set_group_n(self._h, group, n))
 
-    def learned_train(self, model_out, frames, stride=10, iters=4, lr=1e-3, model_in=None):
+    def learned_train(self, model_out, frames, stride=10, iters=4, lr=1e-3, model_in=None, force_weight=1.0):
         """Online training from this plain-form run; returns the per-interaction
-        per-atom energy RMSE (eV) of the last frame (NaN where no network)."""
+        per-atom energy RMSE (eV) of the last frame (NaN where no network) and the
+        learned-against-plain force RMSE (eV/A) on it."""
         r = np.zeros(max(1, self.n_interactions))
+        fr = C.c_double()
         self._check(load().pfmd_learned_train(self._h, model_in.encode() if model_in else None,
                                               model_out.encode() if model_out else None, frames, stride, iters, lr,
-                                              _dp(r)))
-        return r[:self.n_interactions].copy()
+                                              force_weight, _dp(r), C.byref(fr)))
+        return r[:self.n_interactions].copy(), fr.value
 
     def learned_use(self, model_path, check_period=100, max_rmse=0.05):
         self._check(load().pfmd_learned_use(self._h, model_path.encode(), check_period, max_rmse))

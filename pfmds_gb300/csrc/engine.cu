@@ -263,7 +263,9 @@ class Engine {
   void learned_upload_desc(Lrn& L);
   double learned_check(bool switch_on_fail);
   void learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride, int iters,
-                     double lr, double* rmse_out);
+                     double lr, double force_weight, double* rmse_out, double* force_rmse);
+  DBuf<double4_32a> fref;
+  DBuf<float4> fres;
   void clear_graphs();
   void ensure_lists();
   Ctl* ctl = nullptr;
@@ -1563,7 +1565,7 @@ double Engine::learned_check(bool switch_on_fail) {
 // takes `iters` Adam steps on its atoms' descriptors.  rmse_out[k] (per
 // interaction, NaN where no network) = per-atom energy RMSE of the last frame.
 void Engine::learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride,
-                           int iters, double lr, double* rmse_out) {
+                           int iters, double lr, double force_weight, double* rmse_out, double* force_rmse) {
   if (prec) throw Error(PFMD_E_STATE, "learned training runs on the plain form (FP64 targets)");
   std::vector<learned::Model> ms;
   const bool fresh = model_in.empty();
@@ -1593,7 +1595,28 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
     M.loss.alloc(2);
     M.adam_step = 0;
   }
+  const bool fm = force_weight > 0.0;  // force matching
+  std::vector<DBuf<float>> U(lrn.size());
+  if (fm) {
+    fref.alloc(static_cast<size_t>(std::max(N, 1)));
+    fres.alloc(static_cast<size_t>(std::max(N, 1)));
+    for (size_t k = 0; k < lrn.size(); ++k)
+      if (lrn[k].on) U[k].alloc(lrn[k].G.n);
+  }
   const GroupRef gall = gref(S.all_atoms);
+  // learned forces at this configuration into frc, residuals against fref, and
+  // the force-matching directions of every network
+  auto learned_residuals = [&]() {
+    learned_active = true;
+    if (!store_first) launch_zero_forces(gall, A, ctl, st);
+    enqueue_forces(false, false);
+    learned_active = false;
+    learned::launch_residual(N, frc.p, fref.p, fres.p, st);
+    for (size_t k = 0; k < lrn.size(); ++k)
+      if (lrn[k].on)
+        learned::launch_desc_vjp(lists[static_cast<size_t>(inters[k].lists[0])].d, lrn[k].d.p, A, box, fres.p,
+                                 U[k].p, ctl, st);
+  };
   for (int f = 0; f < frames; ++f) {
     if (stride > 0) {
       int fin = 0;
@@ -1606,6 +1629,8 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
     if (!store_first) launch_zero_forces(gall, A, ctl, st);
     enqueue_forces(true, false);
     eatom_out = nullptr;
+    if (fm)
+      CK(cudaMemcpyAsync(fref.p, frc.p, sizeof(double4_32a) * static_cast<size_t>(N), cudaMemcpyDeviceToDevice, st));
     for (size_t k = 0; k < lrn.size(); ++k) {
       Lrn& M = lrn[k];
       if (!M.on) continue;
@@ -1644,21 +1669,32 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
         M.d.upload(&M.model.d, 1, st);
         M.net.upload(&M.model.n, 1, st);
       }
-      learned::launch_desc(L.d, M.d.p, A, box, M.G.p, ctl, st);
-      learned::TrainBuf T;
-      T.part = M.part.p;
-      T.lpart = M.lpart.p;
-      T.part_blocks = learned::train_blocks(rows);
-      T.grad = M.grad.p;
-      T.m = M.m.p;
-      T.v = M.v.p;
-      T.loss = M.loss.p;
-      for (int it = 0; it < iters; ++it) {
-        learned::launch_train_grad(rows, M.G.p, M.t.p, M.net.p, T, st);
+    }
+    for (int it = 0; it < iters; ++it) {
+      if (fm) learned_residuals();  // also refreshes every network's descriptors
+      for (size_t k = 0; k < lrn.size(); ++k) {
+        Lrn& M = lrn[k];
+        if (!M.on) continue;
+        const ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
+        const int rows = L.d.rows;
+        if (!fm && it == 0) learned::launch_desc(L.d, M.d.p, A, box, M.G.p, ctl, st);
+        learned::TrainBuf T;
+        T.part = M.part.p;
+        T.lpart = M.lpart.p;
+        T.part_blocks = learned::train_blocks(rows);
+        T.grad = M.grad.p;
+        T.m = M.m.p;
+        T.v = M.v.p;
+        T.loss = M.loss.p;
+        learned::launch_train_grad(rows, M.G.p, fm ? U[k].p : nullptr, M.t.p, 1.0f,
+                                   static_cast<float>(force_weight), M.net.p, T, st);
         ++M.adam_step;
         learned::launch_adam(M.net.p, T, M.adam_step, static_cast<float>(lr), st);
       }
     }
+    // the dynamics goes on with the classical forces of this configuration
+    if (fm)
+      CK(cudaMemcpyAsync(frc.p, fref.p, sizeof(double4_32a) * static_cast<size_t>(N), cudaMemcpyDeviceToDevice, st));
     read_ctl();
     if (hctl->error) raise_device_error();
   }
@@ -1674,12 +1710,18 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
     T.part_blocks = learned::train_blocks(L.d.rows);
     T.grad = M.grad.p;
     T.loss = M.loss.p;
-    learned::launch_train_grad(L.d.rows, M.G.p, M.t.p, M.net.p, T, st);
+    learned::launch_desc(L.d, M.d.p, A, box, M.G.p, ctl, st);
+    learned::launch_train_grad(L.d.rows, M.G.p, nullptr, M.t.p, 1.0f, 0.0f, M.net.p, T, st);
     double loss[2] = {0.0, 0.0};
     CK(cudaMemcpyAsync(loss, M.loss.p, sizeof(loss), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&M.model.n, M.net.p, sizeof(learned::Net), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (rmse_out) rmse_out[k] = std::sqrt(loss[0] / std::max(loss[1], 1.0));
+  }
+  if (force_rmse) {
+    // learned against classical forces on the last configuration (all atoms)
+    const double r = learned_check(false);
+    *force_rmse = r;
   }
   std::vector<learned::Model> out;
   for (auto& M : lrn)
@@ -2203,11 +2245,12 @@ int pfmd_flush_l2(pfmd_ctx* c, long long bytes) {
 }
 
 int pfmd_learned_train(pfmd_ctx* c, const char* model_in, const char* model_out, int frames, int stride, int iters,
-                       double lr, double* rmse) {
+                       double lr, double force_weight, double* rmse, double* force_rmse) {
   if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
-  if (frames < 1 || stride < 0 || !(lr > 0.0)) return PFMD_E_PARAM;
+  if (frames < 1 || stride < 0 || !(lr > 0.0) || force_weight < 0.0) return PFMD_E_PARAM;
   return guard(c, [&] {
-    c->e->learned_train(model_in ? model_in : "", model_out ? model_out : "", frames, stride, iters, lr, rmse);
+    c->e->learned_train(model_in ? model_in : "", model_out ? model_out : "", frames, stride, iters, lr,
+                        force_weight, rmse, force_rmse);
   });
 }
 

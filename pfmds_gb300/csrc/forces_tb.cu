@@ -56,16 +56,21 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
             r0 = c.r0, inv_w = c.inv_w, ex = c.ex, sq2s = c.sq2s, sq2os = c.sq2os, pre_e = c.pre_e;
     Acc3<PREC> acc;
     Acc1<PREC> e, eh;
+    // Entries at or beyond R2 contribute exactly zero (every term carries fc or
+    // its derivative of that bond), so they are skipped: a list longer than the
+    // bonds (the learned form's descriptor list) costs little.
     for (int p = 0; p < n; ++p) {
       const int aj = ent(L, i, p);
-      const int j = L.row_of[aj];
       R dp[3];
       const R rp = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dp));
+      if (!(rp < R2)) continue;
+      const int j = L.row_of[aj];
       R dB[3] = {R(0), R(0), R(0)};
       for (int q = 0; q < n; ++q) {
         if (q == p) continue;
         R dq[3];
         const R rq = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, q)), B, dq));
+        if (!(rq < R2)) continue;
         const R rr = R(1) / rp / rq;
         const R cosi = dot3<PREC>(dp, dq) * rr;
         const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
@@ -98,6 +103,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
         if (q == l) continue;
         R dq[3];
         const R rq = xsqrt<PREC>(T::d2(pj, T::load(A, ent(L, j, q)), B, dq));
+        if (!(rq < R2)) continue;
         const R rr = R(1) / rl / rq;
         const R cosi = dot3<PREC>(dl, dq) * rr;
         const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
@@ -131,6 +137,7 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
           if (q == l) continue;
           R dq[3];
           const R rq = xsqrt<PREC>(T::d2(pj, T::load(A, ent(L, j, q)), B, dq));
+          if (!(rq < R2)) continue;
           const R rr = R(1) / rl / rq;
           const R cosi = dot3<PREC>(dl, dq) * rr;
           const R t = d02 + (R(1) + cosi) * (R(1) + cosi);

@@ -416,18 +416,152 @@ void launch_force(const ListDev& L, const DescPar* d, const float* g, const floa
 }
 
 // ---------------------------------------------------------------------------
-// training: per-atom energy regression, fixed-order reductions, Adam
+// force matching: residuals and the descriptor vector-Jacobian product
 // ---------------------------------------------------------------------------
-constexpr int TROWS = 64;
+// res[a] = 2 (f_pred - f_ref) / (3 N): dL_F/dF for L_F = sum |f_pred - f_ref|^2 / (3N)
+__global__ void k_residual(int n, const double4_32a* fp, const double4_32a* fr, float4* res) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  const double s = 2.0 / (3.0 * n);
+  const double4_32a p = fp[a], r = fr[a];
+  res[a] = make_float4((float)(s * (p.x - r.x)), (float)(s * (p.y - r.y)), (float)(s * (p.z - r.z)), 0.f);
+}
+void launch_residual(int n, const double4_32a* fpred, const double4_32a* fref, float4* res, cudaStream_t s) {
+  if (n <= 0) return;
+  k_residual<<<nblk(n, 256), 256, 0, s>>>(n, fpred, fref, res);
+  ++g_kernel_launches;
+}
+
+// U[row] = inv_std * dL_F/dG[row]: for row m,
+//   radial   u_k = -sum_j phi_k'(r) e_mj . (res_j - res_m)
+//   angular  u_a = -sum_{j<k} (res_j - res_m) . dT_a/du + (res_k - res_m) . dT_a/dv
+// which needs only m's own neighbours.
+__global__ void __launch_bounds__(128) k_desc_vjp(ListDev L, const DescPar* __restrict__ Dp, Atoms A, Box B,
+                                                  const float4* __restrict__ res, float* U, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= L.rows) return;
+  const DescPar& d = *Dp;
+  float u[NG];
+#pragma unroll
+  for (int f = 0; f < NG; ++f) u[f] = 0.f;
+  float ux[MAX_ANG], uy[MAX_ANG], uz[MAX_ANG], ur[MAX_ANG], uf[MAX_ANG], udf[MAX_ANG];
+  float qx[MAX_ANG], qy[MAX_ANG], qz[MAX_ANG];
+  int na = 0;
+  const int n = L.nnum[row];
+  if (n > 0) {
+    const int am = L.pidx[row];
+    const int4 pm = A.posq[am];
+    const float4 rm = res[am];
+    for (int p = 0; p < n; ++p) {
+      const int aj = ent(L, row, p);
+      float dr[3];
+      const float r = sqrtf(mi_q(pm, A.posq[aj], B, dr));
+      const float4 rj = res[aj];
+      const float dx = rj.x - rm.x, dy = rj.y - rm.y, dz = rj.z - rm.z;
+      if (r < d.rc_rad) {
+        float fc, dfc;
+        fcut_d(r, d.rc_rad, fc, dfc);
+        const float proj = (dr[0] * dx + dr[1] * dy + dr[2] * dz) / r;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+          const float t = r - d.rs[k];
+          const float ex = __expf(-d.eta_r[k] * t * t);
+          u[k] -= ex * (-2.f * d.eta_r[k] * t * fc + dfc) * proj;
+        }
+      }
+      if (r < d.rc_ang && na < MAX_ANG) {
+        fcut_d(r, d.rc_ang, uf[na], udf[na]);
+        ux[na] = dr[0];
+        uy[na] = dr[1];
+        uz[na] = dr[2];
+        ur[na] = r;
+        qx[na] = dx;
+        qy[na] = dy;
+        qz[na] = dz;
+        ++na;
+      }
+    }
+    for (int j = 0; j < na; ++j)
+      for (int k = j + 1; k < na; ++k) {
+        const float a[3] = {ux[j], uy[j], uz[j]}, b[3] = {ux[k], uy[k], uz[k]};
+        const float ra = ur[j], rb = ur[k];
+        const float cs = (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]) / (ra * rb);
+        // projections of the residual differences on the three vector terms
+        const float qa[3] = {qx[j], qy[j], qz[j]}, qb[3] = {qx[k], qy[k], qz[k]};
+        float pc = 0.f, pe = 0.f, pfa = 0.f, pfb = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float dca = b[c] / (ra * rb) - cs * a[c] / (ra * ra);
+          const float dcb = a[c] / (ra * rb) - cs * b[c] / (rb * rb);
+          pc += qa[c] * dca + qb[c] * dcb;
+          pe += qa[c] * a[c] + qb[c] * b[c];
+          pfa += qa[c] * a[c] / ra;
+          pfb += qb[c] * b[c] / rb;
+        }
+        const float C = uf[j] * uf[k];
+        const float pf = udf[j] * uf[k] * pfa + uf[j] * udf[k] * pfb;
+        float Bq[2];
+#pragma unroll
+        for (int ie = 0; ie < 2; ++ie) Bq[ie] = __expf(-d.eta_a[ie] * (ra * ra + rb * rb));
+#pragma unroll
+        for (int il = 0; il < 2; ++il) {
+          const float lam = d.lambda[il];
+          const float t = fmaxf(1.f + lam * cs, 0.f);
+          const float t2 = t * t, t4 = t2 * t2;
+          const float tz[4] = {t, t2, t4, t4 * t4};
+          const float tzm[4] = {1.f, t, t2 * t, t4 * t2 * t};
+#pragma unroll
+          for (int iz = 0; iz < 4; ++iz) {
+            const float c0 = iz == 0 ? 1.f : (iz == 1 ? 0.5f : (iz == 2 ? 0.125f : 0.0078125f));
+#pragma unroll
+            for (int ie = 0; ie < 2; ++ie) {
+              const float v = c0 * Bq[ie] *
+                              (d.zeta[iz] * lam * tzm[iz] * C * pc + tz[iz] * (-2.f * d.eta_a[ie]) * C * pe + tz[iz] * pf);
+              u[NR + (il * 4 + iz) * 2 + ie] -= v;
+            }
+          }
+        }
+      }
+  }
+  float* out = U + (size_t)row * NG;
+#pragma unroll
+  for (int f = 0; f < NG; ++f) out[f] = u[f] * d.inv_std[f];
+}
+void launch_desc_vjp(const ListDev& L, const DescPar* d, const Atoms& A, const Box& B, const float4* res, float* U,
+                     Ctl* ctl, cudaStream_t s) {
+  if (L.rows == 0) return;
+  k_desc_vjp<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, A, B, res, U, ctl);
+  ++g_kernel_launches;
+}
+
+// ---------------------------------------------------------------------------
+// training: per-atom energy error plus (optionally) force matching, fixed-order
+// reductions, Adam
+// ---------------------------------------------------------------------------
+constexpr int TROWS = 32;
 struct TrainSmem {
   NetSmem S;
-  float x[TROWS][NG], a1[TROWS][NH], a2[TROWS][NH], d1[TROWS][NH], d2[TROWS][NH], de[TROWS];
+  float x[TROWS][NG], ut[TROWS][NG];                       // normalised descriptors, force direction
+  float a1[TROWS][NH], ad1[TROWS][NH];                     // a1 and its tangent
+  float P1[TROWS][NH], Q1[TROWS][NH], P2[TROWS][NH], Q2[TROWS][NH], A3[TROWS][NH];
+  float de[TROWS];
   double se[TROWS];
 };
 
 int train_blocks(int rows) { return (rows + TROWS - 1) / TROWS; }
 
-__global__ void __launch_bounds__(256) k_train(int rows, const float* __restrict__ G, const double* __restrict__ t,
+__device__ __forceinline__ float d2silu(float z) {
+  const float s = sigm(z);
+  return s * (1.f - s) * (2.f + z * (1.f - 2.f * s));
+}
+
+// One tile of TROWS rows.  Energy term: dL_E/dE = 2 (E - t) / rows (times wE).
+// Force term (U given): s = dE/dG . U, the directional derivative of the atom's
+// energy along U in normalised descriptor space; its weight gradient comes from
+// propagating the tangent (z1', a1', z2') forward and both paths backward.
+__global__ void __launch_bounds__(256) k_train(int rows, const float* __restrict__ G, const float* __restrict__ U,
+                                               const double* __restrict__ t, float wE, float wF,
                                                const Net* __restrict__ net, float* part, double* lpart) {
   extern __shared__ __align__(16) unsigned char smem[];
   TrainSmem& T = *reinterpret_cast<TrainSmem*>(smem);
@@ -438,34 +572,78 @@ __global__ void __launch_bounds__(256) k_train(int rows, const float* __restrict
   for (int lr = w; lr < TROWS; lr += 8) {
     const int row = r0 + lr;
     if (row >= rows) {
-      for (int h = lane; h < NH; h += 32) T.a1[lr][h] = T.a2[lr][h] = T.d1[lr][h] = T.d2[lr][h] = 0.f;
-      for (int f = lane; f < NG; f += 32) T.x[lr][f] = 0.f;
+      for (int h = lane; h < NH; h += 32)
+        T.a1[lr][h] = T.ad1[lr][h] = T.P1[lr][h] = T.Q1[lr][h] = T.P2[lr][h] = T.Q2[lr][h] = T.A3[lr][h] = 0.f;
+      for (int f = lane; f < NG; f += 32) T.x[lr][f] = T.ut[lr][f] = 0.f;
       if (lane == 0) {
         T.de[lr] = 0.f;
         T.se[lr] = 0.0;
       }
       continue;
     }
-    for (int f = lane; f < NG; f += 32) T.x[lr][f] = G[(size_t)row * NG + f];
+    for (int f = lane; f < NG; f += 32) {
+      T.x[lr][f] = G[(size_t)row * NG + f];
+      T.ut[lr][f] = U ? U[(size_t)row * NG + f] : 0.f;
+    }
     __syncwarp();
     Fwd F;
     const float E = forward_row(T.S, T.x[lr], T.a1[lr], F);
     const double err = (double)E - t[row];
-    const float de = static_cast<float>(2.0 * err) * inv_rows;
+    const float de = wE * static_cast<float>(2.0 * err) * inv_rows;
+    // tangent: z1' = W1 u, a1' = silu'(z1) z1'
+    float zd1[2], s1[2];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int h = lane + 32 * q;
-      T.a2[lr][h] = F.a2[q];
-      T.d2[lr][h] = de * T.S.w3[h] * dsilu(F.z2[q]);
+      float z = 0.f;
+#pragma unroll 8
+      for (int f = 0; f < NG; ++f) z += T.S.W1[h * NG + f] * T.ut[lr][f];
+      zd1[q] = z;
+      s1[q] = dsilu(F.z1[q]);
+      T.ad1[lr][h] = s1[q] * z;
+    }
+    __syncwarp();
+    // z2' = W2 a1'; energy path d2 = de w3 silu'(z2); force path beta2 = w3 silu'(z2),
+    // gamma2 = w3 silu''(z2) z2'
+    float b2v[2], g2v[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int h = lane + 32 * q;
+      float zd2 = 0.f;
+#pragma unroll 8
+      for (int c = 0; c < NH; ++c) zd2 += T.S.W2[h * NH + c] * T.ad1[lr][c];
+      const float s2 = dsilu(F.z2[q]);
+      const float w3 = T.S.w3[h];
+      b2v[q] = w3 * s2;
+      g2v[q] = w3 * d2silu(F.z2[q]) * zd2;
+      T.P2[lr][h] = de * w3 * s2 + wF * g2v[q];
+      T.Q2[lr][h] = wF * b2v[q];
+      T.A3[lr][h] = de * F.a2[q] + wF * s2 * zd2;
+      // beta2 for the W2^T product below (P1 is overwritten after it)
+      T.P1[lr][h] = b2v[q];
+    }
+    __syncwarp();
+    float wb[2], wd[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int c = lane + 32 * q;
+      float sb = 0.f, sd = 0.f;
+#pragma unroll 8
+      for (int h = 0; h < NH; ++h) {
+        const float w2 = T.S.W2[h * NH + c];
+        sb += w2 * T.P1[lr][h];
+        sd += w2 * T.P2[lr][h];
+      }
+      wb[q] = sb;
+      wd[q] = sd;
     }
     __syncwarp();
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int c = lane + 32 * q;
-      float s = 0.f;
-#pragma unroll 8
-      for (int h = 0; h < NH; ++h) s += T.S.W2[h * NH + c] * T.d2[lr][h];
-      T.d1[lr][c] = s * dsilu(F.z1[q]);
+      // (W2^T P2) already carries de*d2 + wF*gamma2; add the tangent's silu'' term
+      T.P1[lr][c] = s1[q] * wd[q] + wF * d2silu(F.z1[q]) * zd1[q] * wb[q];
+      T.Q1[lr][c] = wF * s1[q] * wb[q];
     }
     if (lane == 0) {
       T.de[lr] = de;
@@ -475,24 +653,24 @@ __global__ void __launch_bounds__(256) k_train(int rows, const float* __restrict
   }
   __syncthreads();
   float* out = part + (size_t)blockIdx.x * NET_FLOATS;
-  const int oW1 = 0, ob1 = NH * NG, oW2 = ob1 + NH, ob2 = oW2 + NH * NH, ow3 = ob2 + NH, ob3 = ow3 + NH;
+  const int ob1 = NH * NG, oW2 = ob1 + NH, ob2 = oW2 + NH * NH, ow3 = ob2 + NH, ob3 = ow3 + NH;
   for (int i = threadIdx.x; i < NET_FLOATS; i += blockDim.x) {
     float s = 0.f;
     if (i < ob1) {
       const int h = i / NG, f = i % NG;
-      for (int r = 0; r < TROWS; ++r) s += T.d1[r][h] * T.x[r][f];
+      for (int r = 0; r < TROWS; ++r) s += T.P1[r][h] * T.x[r][f] + T.Q1[r][h] * T.ut[r][f];
     } else if (i < oW2) {
       const int h = i - ob1;
-      for (int r = 0; r < TROWS; ++r) s += T.d1[r][h];
+      for (int r = 0; r < TROWS; ++r) s += T.P1[r][h];
     } else if (i < ob2) {
       const int h = (i - oW2) / NH, c = (i - oW2) % NH;
-      for (int r = 0; r < TROWS; ++r) s += T.d2[r][h] * T.a1[r][c];
+      for (int r = 0; r < TROWS; ++r) s += T.P2[r][h] * T.a1[r][c] + T.Q2[r][h] * T.ad1[r][c];
     } else if (i < ow3) {
       const int h = i - ob2;
-      for (int r = 0; r < TROWS; ++r) s += T.d2[r][h];
+      for (int r = 0; r < TROWS; ++r) s += T.P2[r][h];
     } else if (i < ob3) {
       const int h = i - ow3;
-      for (int r = 0; r < TROWS; ++r) s += T.de[r] * T.a2[r][h];
+      for (int r = 0; r < TROWS; ++r) s += T.A3[r][h];
     } else {
       for (int r = 0; r < TROWS; ++r) s += T.de[r];
     }
@@ -531,15 +709,16 @@ __global__ void k_adam(float* w, const float* grad, float* m, float* v, float lr
   w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
 }
 
-void launch_train_grad(int rows, const float* G, const double* target_by_row, const Net* net, TrainBuf& T,
-                       cudaStream_t s) {
+void launch_train_grad(int rows, const float* G, const float* U, const double* target_by_row, float wE, float wF,
+                       const Net* net, TrainBuf& T, cudaStream_t s) {
   const int blocks = train_blocks(rows);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(TrainSmem)));
     attr = true;
   }
-  k_train<<<blocks, 256, sizeof(TrainSmem), s>>>(rows, G, target_by_row, net, T.part, T.lpart);
+  k_train<<<blocks, 256, sizeof(TrainSmem), s>>>(rows, G, U, target_by_row, wE, U ? wF : 0.f, net, T.part,
+                                                 T.lpart);
   ++g_kernel_launches;
   k_train_reduce<<<nblk(NET_FLOATS, 256), 256, 0, s>>>(blocks, rows, T.part, T.lpart, T.grad, T.loss);
   ++g_kernel_launches;

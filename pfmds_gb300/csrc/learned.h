@@ -67,8 +67,15 @@ struct TrainBuf {
   float *m = nullptr, *v = nullptr;  // Adam moments
   double* loss = nullptr;            // [0] sum of squared errors, [1] rows
 };
-void launch_train_grad(int rows, const float* G, const double* target_by_row, const Net* net, TrainBuf& T,
-                       cudaStream_t s);
+// U (may be null): rows x NG force-matching directions from launch_desc_vjp;
+// loss = wE * mean (E - t)^2 + wF * sum |F - F_ref|^2 / (3 N).
+void launch_train_grad(int rows, const float* G, const float* U, const double* target_by_row, float wE, float wF,
+                       const Net* net, TrainBuf& T, cudaStream_t s);
+// Force matching: residuals res = 2 (f_pred - f_ref) / (3 N) per atom, and
+// U = inv_std * dL_F/dG per row (needs only the row's own neighbours).
+void launch_residual(int n, const double4_32a* fpred, const double4_32a* fref, float4* res, cudaStream_t s);
+void launch_desc_vjp(const ListDev& L, const DescPar* d, const Atoms& A, const Box& B, const float4* res, float* U,
+                     Ctl* ctl, cudaStream_t s);
 void launch_adam(Net* net, TrainBuf& T, int step, float lr, cudaStream_t s);
 constexpr int NET_FLOATS = static_cast<int>(sizeof(Net) / sizeof(float));
 int train_blocks(int rows);

@@ -18,21 +18,23 @@ def _gr(d, T=600.0):
     return str(d)
 
 
-def _train(d, out, frames=40, stride=5, iters=8, model_in=None):
+def _train(d, out, frames=40, stride=5, iters=8, model_in=None, force_weight=1.0):
     s = pf.Simulation(d, form="plain", out_period=10 ** 9)
-    r = s.learned_train(out, frames=frames, stride=stride, iters=iters, lr=2e-3, model_in=model_in)
+    r, fr = s.learned_train(out, frames=frames, stride=stride, iters=iters, lr=2e-3, model_in=model_in,
+                            force_weight=force_weight)
     s.close()
-    return r
+    return r, fr
 
 
-def test_training_lowers_the_energy_error(tmp_path, built):
+def test_training_lowers_energy_and_force_errors(tmp_path, built):
     d = _gr(tmp_path)
     m0, m1 = str(tmp_path / "m0.bin"), str(tmp_path / "m1.bin")
-    r0 = _train(d, m0, frames=1, stride=0, iters=1)
-    r1 = _train(d, m1, frames=60, stride=5, iters=8, model_in=m0)
+    r0, f0 = _train(d, m0, frames=1, stride=0, iters=1)
+    r1, f1 = _train(d, m1, frames=60, stride=5, iters=8, model_in=m0)
     assert np.isnan(r0[2]) and np.isnan(r1[2])  # the coupling keeps its classical kernel
     assert (r1[:2] < r0[:2]).all(), (r0, r1)
     assert (r1[:2] < 0.05).all(), r1  # eV per atom
+    assert f1 < f0, (f0, f1)  # eV/A, learned against plain forces
     ms = learned_ref.load_models(m1)
     assert sorted(m["kind"] for m in ms) == [0, 1]
 
@@ -79,6 +81,7 @@ def test_learned_forces_match_cpu_reference_gradient(tmp_path, built):
     s = pf.Simulation(str(tmp_path), form="plain", out_period=10 ** 9)
     s.learned_train(m, frames=8, stride=4, iters=4, lr=2e-3)
     s.close()
+    assert np.isfinite(learned_ref.load_models(m)[0]["net"]["W1"]).all()
     s = pf.Simulation(str(tmp_path), form="precision", out_period=10 ** 9)
     s.learned_use(m, check_period=0)
     s.compute()
