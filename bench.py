@@ -253,7 +253,13 @@ def batched_config(root, device, steps, n_rep=512):
     dts = np.array([0.5 if r["kind"] == "lj" else 1.0 for r in reps])
     tot = (h[:, :, 0] + h[:, :, 1]) / ns[None, :]
     rows = np.arange(h.shape[0], dtype=float) * per
-    drift = np.array([np.polyfit(rows * dts[r], tot[:, r], 1)[0] * 1e6 for r in range(R)])
+    half = h.shape[0] // 2
+
+    def slopes(e, t):  # eV/atom/ns over the whole run and over its second half
+        return np.polyfit(t, e, 1)[0] * 1e6, np.polyfit(t[half:], e[half:], 1)[0] * 1e6
+
+    dr = np.array([slopes(tot[:, r], rows * dts[r]) for r in range(R)])
+    drift, drift2 = dr[:, 0], dr[:, 1]
     rng = np.random.default_rng(1)
     sample = sorted(rng.choice(R, size=min(8, R), replace=False).tolist())
     rel, t_one = [], {"plain": [0.0, 0.0], "precision": [0.0, 0.0]}
@@ -273,6 +279,24 @@ def batched_config(root, device, steps, n_rep=512):
             s.close()
     one = {k: v[0] / v[1] for k, v in t_one.items()}
     b.close()
+    # the plain FP64 form on two of the sampled replicas (one of each kind), same
+    # start, same steps, energies every 100 steps: its drift is the integrator's
+    plain_drift = []
+    for kind in ("lj", "rjl"):
+        r = next((k for k in sample if reps[k]["kind"] == kind), None)
+        if r is None:
+            continue
+        s = pf.Simulation(d, settings=reps[r]["settings"], form="plain", out_period=10 ** 9, device=device)
+        e = []
+        for k in range(h.shape[0]):
+            s.advance(1 if k == 0 else per)
+            en = s.energies()
+            e.append((en["pe"] + en["ke"]) / reps[r]["n"])
+        s.close()
+        pd = slopes(np.array(e), rows * dts[r])
+        plain_drift.append({"replica": r, "kind": kind, "atoms": reps[r]["n"],
+                            "temperature": reps[r]["temperature"], "plain_fp64": pd[0],
+                            "plain_fp64_second_half": pd[1], "batched": drift[r], "batched_second_half": drift2[r]})
     return {
         "workload": f"{R} replicas (LJ gas or Cu rjl slab, 500-20,000 atoms, 100-1,200 K, nve), {n_all} atoms, "
                     f"{steps} steps, one persistent cooperative kernel per 100 steps",
@@ -283,9 +307,70 @@ def batched_config(root, device, steps, n_rep=512):
         "force_rmse_rel_vs_plain": {"max": max(rel), "median": float(np.median(rel))},
         "nve_drift_eV_per_atom_per_ns": {"median_abs": float(np.median(np.abs(drift))),
                                          "max_abs": float(np.abs(drift).max()),
+                                         "second_half_median_abs": float(np.median(np.abs(drift2))),
                                          "fraction_below_1e-5": float((np.abs(drift) < 1e-5).mean()),
-                                         "window_fs": "steps x dt (0.5 fs LJ, 1 fs Cu), energies every 100 steps"},
+                                         "window_fs": "steps x dt (0.5 fs LJ, 1 fs Cu), energies every 100 steps",
+                                         "against_plain_fp64": plain_drift},
         "input_generation_s": t_gen}
+
+
+def learned_config(root, device, frames=200, run_steps=1000):
+    """The learned form: networks for the tb (C) and rjl (Cu) interactions trained
+    online on plain-form runs of a graphene/Cu(111) system at 300, 700 and 1,200 K
+    (per-atom energies and forces of the plain kernels), then run on a large
+    graphene/Cu system with the classical kernels checking the forces every 100
+    steps (fallback above 0.05 eV/A), beside the precision and plain forms of the
+    same system."""
+    import pfmds_gb300 as pf
+    from pfmds_gb300 import configs
+    model, train = None, []
+    t0 = time.perf_counter()
+    for T in (300.0, 700.0, 1200.0):
+        dT = os.path.join(root, f"learn_T{int(T)}")
+        configs.gr_on_cu(dT, n_gx=16, n_gy=10, n_cx=15, n_cy=8, layers=4, temperature=T, integrator="nve", dt=0.5,
+                         steps=10 ** 7, log_period=10, tb_list=(32, 4.5))
+        s = pf.Simulation(dT, form="plain", out_period=10 ** 9, device=device)
+        out = os.path.join(root, f"learned_{int(T)}.bin")
+        r, fr = s.learned_train(out, frames=frames, stride=5, iters=8, lr=2e-3 if model is None else 1e-3,
+                                model_in=model, force_weight=1.0)
+        train.append({"temperature": T, "atoms": s.natoms, "energy_rmse_eV": {"C_tb": r[0], "Cu_rjl": r[1]},
+                      "force_rmse_eV_per_A": fr})
+        model = out
+        s.close()
+    t_train = time.perf_counter() - t0
+    dbig = os.path.join(root, "learn_big")
+    configs.gr_on_cu(dbig, n_gx=128, n_gy=128, n_cx=123, n_cy=123, layers=6, temperature=600.0, integrator="nvt",
+                     dt=0.5, steps=10 ** 7, log_period=100, tb_list=(32, 4.5))
+    res = {}
+    for form in ("precision", "learned", "plain"):
+        s = pf.Simulation(dbig, form="plain" if form == "plain" else "precision", out_period=10 ** 9, device=device)
+        n = s.natoms
+        if form == "learned":  # the networks alone: no checks inside the timed steps
+            s.learned_use(model, check_period=0)
+        steps = {"precision": 100, "learned": 100, "plain": 10}[form]
+        s.advance(10)
+        t1 = time.perf_counter()
+        ms = s.advance_timed(steps)
+        wall = time.perf_counter() - t1
+        res[form] = {"value": n * steps / (ms / 1e3), "ms_per_md_step": ms / steps,
+                     "wall_atom_steps_per_s": n * steps / wall}
+        if form == "learned":
+            res[form]["force_rmse_vs_classical_eV_per_A"] = s.learned_check()
+        s.close()
+    # the checked run: classical kernels judge the networks every 100 steps
+    s = pf.Simulation(dbig, form="precision", out_period=10 ** 9, device=device)
+    s.learned_use(model, check_period=100, max_rmse=0.05)
+    s.advance(run_steps + 1)
+    res["learned"]["checked_run"] = dict(s.learned_status(), steps=run_steps, check_period=100, max_rmse=0.05)
+    s.close()
+    return {
+        "workload": f"graphene (tb) on Cu(111) (rjl, 6 layers), morsec coupling, {n} atoms, 600 K nvt, dt 0.5 fs; "
+                    f"networks trained on a {train[0]['atoms']}-atom system at 300/700/1,200 K, {frames} frames each",
+        "unit": "atom-steps/s", "training": train, "training_s": t_train,
+        "precision": res["precision"], "learned": res["learned"], "plain": res["plain"],
+        "learned_speedup_vs_plain": res["learned"]["value"] / res["plain"]["value"],
+        "learned_vs_precision": res["learned"]["value"] / res["precision"]["value"],
+        "check": "classical kernels recompute the forces every 100 steps; RMSE above 0.05 eV/A switches back"}
 
 
 def pinned_arrays(n, k):
@@ -459,6 +544,8 @@ def run_ours(args):
         extra = other_configs(d, device) if (rank == 0 and not args.no_extra) else None
         if extra is not None and args.batch_steps > 0:
             extra["batched_512"] = batched_config(d, device, args.batch_steps)
+        if extra is not None and args.learned_steps > 0:
+            extra["learned"] = learned_config(d, device, run_steps=args.learned_steps)
 
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
@@ -537,6 +624,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the LJ-gas, moire and batched configurations")
     ap.add_argument("--batch-steps", type=int, default=5000, help="MD steps of the batched configuration (0 skips)")
+    ap.add_argument("--learned-steps", type=int, default=1000, help="MD steps of the learned form's run (0 skips)")
     ap.add_argument("--drift-steps", type=int, default=10000,
                     help="MD steps of the NVE drift measurement (precision form; plain runs a fifth)")
     ap.add_argument("--quick", action="store_true",
