@@ -198,8 +198,11 @@ int pfmd_learned_train(pfmd_ctx* ctx, const char* model_in, const char* model_ou
 /* Switches the context's tb and rjl interactions to the networks in model_path.
  * Every check_period steps (0: never) the classical kernels recompute the forces
  * of the same configuration; if the RMSE between the two exceeds max_rmse (eV/A)
- * the run falls back to the classical kernels for good. */
-int pfmd_learned_use(pfmd_ctx* ctx, const char* model_path, long long check_period, double max_rmse);
+ * the run falls back to the classical kernels for good.  flags:
+ * PFMD_LEARNED_TENSOR_CORES runs the networks on the tensor cores (BF16 weights
+ * and activations, FP32 accumulation); otherwise FP32 on the CUDA cores. */
+#define PFMD_LEARNED_TENSOR_CORES 1
+int pfmd_learned_use(pfmd_ctx* ctx, const char* model_path, long long check_period, double max_rmse, int flags);
 /* RMSE (eV/A) between learned and classical forces at the current positions;
  * leaves the forces of the active form. */
 int pfmd_learned_check(pfmd_ctx* ctx, double* rmse);

@@ -106,7 +106,7 @@ def load(path=LIB_PATH):
     L.pfmd_batch_energy_history.argtypes = [vp, dp, llp, ip]
     L.pfmd_learned_train.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                      dp, dp]
-    L.pfmd_learned_use.argtypes = [vp, C.c_char_p, C.c_longlong, C.c_double]
+    L.pfmd_learned_use.argtypes = [vp, C.c_char_p, C.c_longlong, C.c_double, C.c_int]
     L.pfmd_learned_check.argtypes = [vp, dp]
     L.pfmd_learned_status.argtypes = [vp, ip, ip, dp, ip]
     # device buffers are passed as integer addresses (c_void_p)
@@ -275,8 +275,9 @@ class Simulation:
                                               force_weight, _dp(r), C.byref(fr)))
         return r[:self.n_interactions].copy(), fr.value
 
-    def learned_use(self, model_path, check_period=100, max_rmse=0.05):
-        self._check(load().pfmd_learned_use(self._h, model_path.encode(), check_period, max_rmse))
+    def learned_use(self, model_path, check_period=100, max_rmse=0.05, tensor_cores=False):
+        self._check(load().pfmd_learned_use(self._h, model_path.encode(), check_period, max_rmse,
+                                            1 if tensor_cores else 0))
 
     def learned_check(self):
         r = C.c_double()

@@ -243,6 +243,7 @@ class Engine {
   // learned form: a network per tb / rjl interaction (see learned.h)
   struct Lrn {
     bool on = false;
+    bool tc = false;  // network on the tensor cores (BF16)
     learned::Model model;
     DBuf<learned::DescPar> d;
     DBuf<learned::Net> net;
@@ -1072,7 +1073,10 @@ void Engine::enqueue_forces(bool energy, bool kick) {
     if (learned_active && k < static_cast<int>(lrn.size()) && lrn[static_cast<size_t>(k)].on) {
       Lrn& M = lrn[static_cast<size_t>(k)];
       learned::launch_desc(L1, M.d.p, A, box, M.G.p, ctl, st);
-      learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
+      if (M.tc)
+        learned::launch_mlp_tc(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
+      else
+        learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
       learned::launch_force(L1, M.d.p, M.g.p, M.e.p, energy, A, box, ctl, eslot, key, st, epi(first, last));
       continue;
     }
@@ -2254,7 +2258,7 @@ int pfmd_learned_train(pfmd_ctx* c, const char* model_in, const char* model_out,
   });
 }
 
-int pfmd_learned_use(pfmd_ctx* c, const char* model_path, long long check_period, double max_rmse) {
+int pfmd_learned_use(pfmd_ctx* c, const char* model_path, long long check_period, double max_rmse, int flags) {
   if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
   if (!model_path || check_period < 0) return PFMD_E_PARAM;
   return guard(c, [&] {
@@ -2266,6 +2270,7 @@ int pfmd_learned_use(pfmd_ctx* c, const char* model_path, long long check_period
       throw ::pfmd::Error(PFMD_E_IO, x.what());
     }
     e.learned_setup(ms);
+    for (auto& M : e.lrn) M.tc = (flags & PFMD_LEARNED_TENSOR_CORES) != 0;
     e.learned_active = true;
     e.check_period = check_period;
     e.max_rmse = max_rmse;

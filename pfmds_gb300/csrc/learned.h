@@ -51,6 +51,9 @@ void launch_desc(const ListDev& L, const DescPar* d, const Atoms& A, const Box& 
 // Per row: energy e[row] and g[row*NG..] = dE/dG (in un-normalised descriptor units).
 void launch_mlp(int rows, const float* G, const DescPar* d, const Net* net, float* e, float* g, Ctl* ctl,
                 cudaStream_t s);
+// The same on the tensor cores (tcgen05, BF16 operands, FP32 accumulation).
+void launch_mlp_tc(int rows, const float* G, const DescPar* d, const Net* net, float* e, float* g, Ctl* ctl,
+                   cudaStream_t s);
 // Forces of the learned energy (store/add and kick per Epi) and, at energy steps,
 // the interaction's energy into ctl->e_inter[ekey].  Needs L.row_of.
 void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, bool energy, const Atoms& A,

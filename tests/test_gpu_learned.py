@@ -137,3 +137,23 @@ def test_fallback_to_classical_kernels(tmp_path, built):
     assert np.abs(fs - fc).max() < 1e-6 * np.abs(fc).max()
     s.close()
     c.close()
+
+
+def test_tensor_core_network_matches_fp32(tmp_path, built):
+    """The tcgen05 BF16 network against the FP32 CUDA-core one on the same model
+    and configuration: energies and forces within BF16 rounding."""
+    d = _gr(tmp_path)
+    m = str(tmp_path / "m.bin")
+    _train(d, m, frames=20, stride=5, iters=4)
+    out = {}
+    for tc in (False, True):
+        s = pf.Simulation(d, form="precision", out_period=10 ** 9)
+        s.learned_use(m, check_period=0, tensor_cores=tc)
+        e = s.compute()
+        out[tc] = (e, s.state()[2])
+        s.close()
+    (e32, f32), (e16, f16) = out[False], out[True]
+    n = len(f32)
+    assert np.all(np.abs(e16[:2] - e32[:2]) < 2e-3 * n), (e16, e32)  # eV over the system
+    rel = np.sqrt(((f16 - f32) ** 2).mean()) / np.sqrt((f32 ** 2).mean())
+    assert rel < 3e-2, rel
