@@ -95,6 +95,9 @@ struct Box {
   double qinv[3];  // 2^32 / L
   float qs[3];     // L / 2^32
   double Ltol[3];  // L + 1e-7, the upper bound of the out-of-cell test (md_general.f90:346)
+  // 2^32 / L as qm * 2^(qe - 64) with qm in [2^63, 2^64): quantize_int's reciprocal
+  unsigned long long qm[3];
+  int qe[3];
 };
 
 // ---------------------------------------------------------------------------
@@ -119,6 +122,30 @@ __device__ __forceinline__ double mi_exact(const double4_32a& a, const double4_3
 __device__ __forceinline__ int quantize(double x, double qinv) {
   return (int)(unsigned int)(unsigned long long)__double2ll_rn(x * qinv);
 }
+// The same fixed-point coordinate from integer arithmetic on the double's bits,
+// for kernels bound by GB300's narrow FP64 pipe: with x = m 2^(e-1075) (m the
+// 53-bit significand) and 2^32/L = qm 2^(qe-64), x 2^32/L = (m qm / 2^64) 2^(e+qe-1075);
+// the high word of m*qm is one 64x64 integer multiply.  Rounds half up on the
+// truncated product, so it can differ from quantize() by one unit (L/2^32) at
+// near-ties; callers use one or the other consistently per run.
+__device__ __forceinline__ int quantize_int(double x, const Box& B, int k) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0) return 0;
+  const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const unsigned long long hi = __umul64hi(m, B.qm[k]);
+  const int sh = e + B.qe[k] - 1075;
+  unsigned long long r;
+  if (sh >= 0)
+    r = sh < 64 ? hi << sh : 0ull;
+  else if (sh > -64)
+    r = (hi + (1ull << (-sh - 1))) >> (-sh);
+  else
+    r = 0ull;
+  const unsigned int u = (unsigned int)r;
+  return (int)(b < 0 ? 0u - u : u);
+}
+
 // Minimum-image b - a from fixed-point coordinates, in FP32 (precision form and
 // the list-build prefilter).  Resolution L / 2^32; the relative error of dr is
 // that of one int->float conversion and one multiply.

@@ -429,6 +429,12 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     box.qinv[k] = 4294967296.0 / box.L[k];
     box.qs[k] = static_cast<float>(box.L[k] / 4294967296.0);
     box.Ltol[k] = box.L[k] + 0.0000001;
+    {  // 2^32 / L = qm * 2^(qe - 64), qm in [2^63, 2^64)
+      int ex = 0;
+      const double fr = std::frexp(box.qinv[k], &ex);  // qinv = fr * 2^ex, fr in [0.5, 1)
+      box.qm[k] = static_cast<unsigned long long>(std::ldexp(fr, 64));
+      box.qe[k] = ex;
+    }
   }
   // groups: create_particle_group (md_general.f90:57-80)
   if (S.group_types.size() > PFMD_MAX_GROUPS) throw Error(PFMD_E_PARAM, "error: too many groups");

@@ -219,7 +219,12 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
     p.z = drift1_fast(p.z, v.z, ts1, B.L[2]);
   }
   A.pos[i] = p;
-  if (write_posq) A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
+  if (write_posq) {
+    if (EXACT)
+      A.posq[i] = make_int4(quantize(p.x, B.qinv[0]), quantize(p.y, B.qinv[1]), quantize(p.z, B.qinv[2]), 0);
+    else
+      A.posq[i] = make_int4(quantize_int(p.x, B, 0), quantize_int(p.y, B, 1), quantize_int(p.z, B, 2), 0);
+  }
   if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 

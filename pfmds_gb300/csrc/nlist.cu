@@ -314,8 +314,7 @@ static constexpr int kCellCand = 1024;  // candidates staged per pass
 static constexpr int kCellRows = 64;    // rows per pass
 
 __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, CellGrid cg, Box B, float rcp2, Ctl* ctl) {
-  __shared__ int s_atom[kCellCand];
-  __shared__ int4 s_posq[kCellCand];
+  __shared__ float4 s_rel[kCellCand];  // candidate position relative to the cell corner, atom in w
   __shared__ int s_off[19];  // prefix offsets of up to 18 candidate runs
   __shared__ int s_beg[18];  // run starts in the cell-ordered arrays
   __shared__ int s_cnt[kCellRows];
@@ -366,6 +365,15 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
   __syncthreads();
   const int total = s_off[18];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // Positions relative to this cell's lower corner, as FP32: every candidate lies
+  // within one cell of the corner cell, so with at least 4 cells per dimension
+  // (cells at most L/4 wide) the fixed-point difference is the minimum image and a
+  // pair's separation is the plain difference of two relative positions.  Grids
+  // with fewer cells keep the per-pair minimum image.
+  const bool rel_ok = nx >= 4 && ny >= 4 && nz >= 4;
+  const unsigned int ref[3] = {(unsigned int)(((unsigned long long)cx << 32) / (unsigned long long)nx),
+                               (unsigned int)(((unsigned long long)cy << 32) / (unsigned long long)ny),
+                               (unsigned int)(((unsigned long long)cz << 32) / (unsigned long long)nz)};
   for (int rg = 0; rg < nr; rg += kCellRows) {
     const int nrg = min(kCellRows, nr - rg);
     for (int i = threadIdx.x; i < nrg; i += blockDim.x) s_cnt[i] = 0;
@@ -377,24 +385,45 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
         int r = 0;
         while (s_off[r + 1] <= g) ++r;  // g < total = s_off[18], so r < 18
         const int k = s_beg[r] + (g - s_off[r]);
-        s_atom[v] = cg.atom[k];
-        s_posq[v] = cg.posq[k];
+        const int4 q = cg.posq[k];
+        float4 rp;
+        if (rel_ok) {
+          rp.x = (float)(int)((unsigned int)q.x - ref[0]) * B.qs[0];
+          rp.y = (float)(int)((unsigned int)q.y - ref[1]) * B.qs[1];
+          rp.z = (float)(int)((unsigned int)q.z - ref[2]) * B.qs[2];
+        } else {  // the raw fixed-point coordinates, for the per-pair minimum image
+          rp.x = __int_as_float(q.x);
+          rp.y = __int_as_float(q.y);
+          rp.z = __int_as_float(q.z);
+        }
+        rp.w = __int_as_float(cg.atom[k]);
+        s_rel[v] = rp;
       }
       __syncthreads();
       for (int i = w; i < nrg; i += kCellWarps) {
         const int kr = r0 + rg + i;
         const int ai = cg.atom[kr], row = cg.jnd[kr];
         const int4 piq = cg.posq[kr];
+        const float ix = (float)(int)((unsigned int)piq.x - ref[0]) * B.qs[0];
+        const float iy = (float)(int)((unsigned int)piq.y - ref[1]) * B.qs[1];
+        const float iz = (float)(int)((unsigned int)piq.z - ref[2]) * B.qs[2];
         int cnt = s_cnt[i];
         for (int k0 = 0; k0 < nb; k0 += 32) {
           const int k = k0 + lane;
           bool hit = false;
           int aj = 0;
           if (k < nb) {
-            aj = s_atom[k];
+            const float4 c = s_rel[k];
+            aj = __float_as_int(c.w);
             if (aj != ai) {
-              float d[3];
-              hit = mi_q(piq, s_posq[k], B, d) < rcp2;
+              if (rel_ok) {
+                const float dx = c.x - ix, dy = c.y - iy, dz = c.z - iz;
+                hit = dx * dx + dy * dy + dz * dz < rcp2;
+              } else {
+                float d[3];
+                hit = mi_q(piq, make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z), 0), B, d) <
+                      rcp2;
+              }
             }
           }
           const unsigned m = __ballot_sync(0xffffffffu, hit);
