@@ -248,6 +248,7 @@ class Engine {
     DBuf<learned::DescPar> d;
     DBuf<learned::Net> net;
     DBuf<float> G, g, e, part, grad, m, v;
+    DBuf<float4> leg, cforce;
     DBuf<double> t, lpart, loss;
     int adam_step = 0;
   };
@@ -1083,7 +1084,8 @@ void Engine::enqueue_forces(bool energy, bool kick) {
         learned::launch_mlp_tc(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
       else
         learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
-      learned::launch_force(L1, M.d.p, M.g.p, M.e.p, energy, A, box, ctl, eslot, key, st, epi(first, last));
+      learned::launch_force(L1, M.d.p, M.g.p, M.e.p, M.leg.p, M.cforce.p, energy, A, box, ctl, eslot, key, st,
+                            epi(first, last));
       continue;
     }
     switch (I.spec.kind) {
@@ -1502,6 +1504,8 @@ void Engine::learned_setup(const std::vector<learned::Model>& ms) {
     M.g.alloc(rows * learned::NG);
     M.e.alloc(rows);
     M.t.alloc(rows);
+    M.leg.alloc(static_cast<size_t>(std::max(L.d.nmax, 1)) * static_cast<size_t>(std::max(L.d.stride, 1)));
+    M.cforce.alloc(rows);
     M.d.upload(&M.model.d, 1, st);
     M.net.upload(&M.model.n, 1, st);
     if (!L.row_of.p) {  // the force gather reads a partner's row

@@ -317,8 +317,69 @@ __device__ __forceinline__ void dT_du(const float* u, float ru, const float* v, 
   }
 }
 
+// Angular terms in two passes, each triplet evaluated once.  Centre pass, one
+// thread per row j: for every pair (p, k) of j's angular partners the weighted
+// sums and dT/du, dT/dv give j's own force term (dT/du + dT/dv) and the legs'
+// gradients, summed per partner slot into leg[p][j].  Gather pass, one thread per
+// row i: radial terms, i's centre term, and -leg[q][j] for every angular
+// neighbour j, q being i's slot in j's row.
+__global__ void __launch_bounds__(128) k_lcenter(ListDev L, const DescPar* __restrict__ Dp,
+                                                 const float* __restrict__ g, Atoms A, Box B, float4* leg,
+                                                 float4* cforce, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= L.rows) return;
+  const DescPar& d = *Dp;
+  const int n = L.nnum[row];
+  float ux[MAX_ANG], uy[MAX_ANG], uz[MAX_ANG], ur[MAX_ANG], uf[MAX_ANG], udf[MAX_ANG];
+  float lx[MAX_ANG], ly[MAX_ANG], lz[MAX_ANG];
+  int sl[MAX_ANG];
+  int na = 0;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  if (n > 0) {
+    const int4 pj = A.posq[L.pidx[row]];
+    for (int p = 0; p < n && na < MAX_ANG; ++p) {
+      float dr[3];
+      const float r = sqrtf(mi_q(pj, A.posq[ent(L, row, p)], B, dr));
+      if (r < d.rc_ang) {
+        fcut_d(r, d.rc_ang, uf[na], udf[na]);
+        ux[na] = dr[0];
+        uy[na] = dr[1];
+        uz[na] = dr[2];
+        ur[na] = r;
+        lx[na] = ly[na] = lz[na] = 0.f;
+        sl[na] = p;
+        ++na;
+      }
+    }
+    const float* gj = g + (size_t)row * NG + NR;
+    for (int a = 0; a < na; ++a)
+      for (int c = a + 1; c < na; ++c) {
+        const float u[3] = {ux[a], uy[a], uz[a]}, v[3] = {ux[c], uy[c], uz[c]};
+        const float cs = (u[0] * v[0] + u[1] * v[1] + u[2] * v[2]) / (ur[a] * ur[c]);
+        float SA, SdA, Se;
+        ang_sums(d, gj, cs, ur[a] * ur[a], ur[c] * ur[c], SA, SdA, Se);
+        float tu[3], tv[3];
+        dT_du(u, ur[a], v, ur[c], cs, SA, SdA, Se, uf[a], udf[a], uf[c], tu);
+        dT_du(v, ur[c], u, ur[a], cs, SA, SdA, Se, uf[c], udf[c], uf[a], tv);
+        fx += tu[0] + tv[0];
+        fy += tu[1] + tv[1];
+        fz += tu[2] + tv[2];
+        lx[a] += tu[0];
+        ly[a] += tu[1];
+        lz[a] += tu[2];
+        lx[c] += tv[0];
+        ly[c] += tv[1];
+        lz[c] += tv[2];
+      }
+    for (int a = 0; a < na; ++a) leg[(size_t)sl[a] * L.stride + row] = make_float4(lx[a], ly[a], lz[a], 0.f);
+  }
+  cforce[row] = make_float4(fx, fy, fz, 0.f);
+}
+
 __global__ void __launch_bounds__(128) k_lforce(ListDev L, const DescPar* __restrict__ Dp, const float* __restrict__ g,
-                                                const float* __restrict__ erow, int energy, Atoms A, Box B, Ctl* ctl,
+                                                const float* __restrict__ erow, const float4* __restrict__ leg,
+                                                const float4* __restrict__ cforce, int energy, Atoms A, Box B, Ctl* ctl,
                                                 int eslot, int ekey, Epi E) {
   if (ctl->stop) return;
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
@@ -332,13 +393,12 @@ __global__ void __launch_bounds__(128) k_lforce(ListDev L, const DescPar* __rest
     const int ai = L.pidx[row];
     const int4 pi = A.posq[ai];
     const float* gi = g + (size_t)row * NG;
-    float ux[MAX_ANG], uy[MAX_ANG], uz[MAX_ANG], ur[MAX_ANG], uf[MAX_ANG], udf[MAX_ANG];
-    int na = 0;
+    const float4 cf = cforce[row];
+    acc.add(cf.x, cf.y, cf.z);
     for (int p = 0; p < n; ++p) {
       const int aj = ent(L, row, p);
       float dr[3];
-      const float r2 = mi_q(pi, A.posq[aj], B, dr);
-      const float r = sqrtf(r2);
+      const float r = sqrtf(mi_q(pi, A.posq[aj], B, dr));
       if (r < d.rc_rad) {
         const float* gj = g + (size_t)L.row_of[aj] * NG;
         float fc, dfc;
@@ -353,66 +413,32 @@ __global__ void __launch_bounds__(128) k_lforce(ListDev L, const DescPar* __rest
         const float ir = 1.f / r;
         acc.add(c * dr[0] * ir, c * dr[1] * ir, c * dr[2] * ir);
       }
-      if (r < d.rc_ang) {
-        if (na < MAX_ANG) {
-          fcut_d(r, d.rc_ang, uf[na], udf[na]);
-          ux[na] = dr[0];
-          uy[na] = dr[1];
-          uz[na] = dr[2];
-          ur[na] = r;
-          ++na;
-        }
-        // leg terms: centre j = aj, pairs (i, k) of j's angular partners
+      if (r < d.rc_ang) {  // i is an angular partner of j: j's centre pass holds i's leg term
         const int rj = L.row_of[aj];
-        const float* gj = g + (size_t)rj * NG + NR;
         const int nj = L.nnum[rj];
-        const int4 pj = A.posq[aj];
-        const float u[3] = {-dr[0], -dr[1], -dr[2]};  // r_i - r_j
-        float fu, dfu;
-        fcut_d(r, d.rc_ang, fu, dfu);
-        for (int q = 0; q < nj; ++q) {
-          const int ak = ent(L, rj, q);
-          if (ak == ai) continue;
-          float v[3];
-          const float rv2 = mi_q(pj, A.posq[ak], B, v);
-          const float rv = sqrtf(rv2);
-          if (rv >= d.rc_ang) continue;
-          float fv, dfv;
-          fcut_d(rv, d.rc_ang, fv, dfv);
-          const float cs = (u[0] * v[0] + u[1] * v[1] + u[2] * v[2]) / (r * rv);
-          float SA, SdA, Se;
-          ang_sums(d, gj, cs, r2, rv2, SA, SdA, Se);
-          float t[3];
-          dT_du(u, r, v, rv, cs, SA, SdA, Se, fu, dfu, fv, t);
-          acc.add(-t[0], -t[1], -t[2]);
-        }
+        for (int q = 0; q < nj; ++q)
+          if (ent(L, rj, q) == ai) {
+            const float4 lg = leg[(size_t)q * L.stride + rj];
+            acc.add(-lg.x, -lg.y, -lg.z);
+            break;
+          }
       }
     }
-    // centre terms: pairs (j, k) of i's angular partners
-    for (int j = 0; j < na; ++j)
-      for (int k = j + 1; k < na; ++k) {
-        const float u[3] = {ux[j], uy[j], uz[j]}, v[3] = {ux[k], uy[k], uz[k]};
-        const float cs = (u[0] * v[0] + u[1] * v[1] + u[2] * v[2]) / (ur[j] * ur[k]);
-        float SA, SdA, Se;
-        ang_sums(d, gi + NR, cs, ur[j] * ur[j], ur[k] * ur[k], SA, SdA, Se);
-        float tu[3], tv[3];
-        dT_du(u, ur[j], v, ur[k], cs, SA, SdA, Se, uf[j], udf[j], uf[k], tu);
-        dT_du(v, ur[k], u, ur[j], cs, SA, SdA, Se, uf[k], udf[k], uf[j], tv);
-        acc.add(tu[0] + tv[0], tu[1] + tv[1], tu[2] + tv[2]);
-      }
     finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
   }
   if (energy) energy_reduce_f(ctl, eslot, ekey, ei);
 }
 
-void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, bool energy, const Atoms& A,
-                  const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s, const Epi& E) {
+void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, float4* leg, float4* cforce,
+                  bool energy, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s,
+                  const Epi& E) {
   if (L.rows == 0) {
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
   }
-  k_lforce<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, g, e, energy ? 1 : 0, A, B, ctl, eslot, ekey, E);
-  ++g_kernel_launches;
+  k_lcenter<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, g, A, B, leg, cforce, ctl);
+  k_lforce<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, g, e, leg, cforce, energy ? 1 : 0, A, B, ctl, eslot, ekey, E);
+  g_kernel_launches += 2;
 }
 
 // ---------------------------------------------------------------------------

@@ -56,8 +56,10 @@ void launch_mlp_tc(int rows, const float* G, const DescPar* d, const Net* net, f
                    cudaStream_t s);
 // Forces of the learned energy (store/add and kick per Epi) and, at energy steps,
 // the interaction's energy into ctl->e_inter[ekey].  Needs L.row_of.
-void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, bool energy, const Atoms& A,
-                  const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s, const Epi& E);
+// leg (nmax x stride, slot-major) and cforce (rows) are scratch of the two passes.
+void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, float4* leg, float4* cforce,
+                  bool energy, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s,
+                  const Epi& E);
 
 // Training on per-atom energy targets (mean squared error): gradients of one frame
 // into grad (sizeof(Net)/4 floats), reduced over rows in a fixed order; *loss_sum
