@@ -246,9 +246,20 @@ int pfmd_batch_set_tpa(pfmd_batch* batch, const int* tpa);
 int pfmd_batch_get_state(pfmd_batch* batch, int r, double* pos, double* vel, double* frc);
 /* Potential and kinetic energy of every replica at the last energy step. */
 int pfmd_batch_energies(pfmd_batch* batch, double* e_pot, double* e_kin);
-/* Energy history: rows x replicas x (potential, kinetic), one row per energy step
- * from step 0; *rows and *period (steps between rows) are returned; hist may be
- * NULL to query the size. */
+/* A settings-list run (run_md_simulation -ilist, run_md_simulation.f90:40-66) on
+ * the batched kernel: every entry advanced from step 0 to the end of its nve
+ * stage together, and for each entry the files its own run writes, with prefix =
+ * out_path + the entry's prefix -- the log (lines at the log period, then the
+ * closing record), snapshot_<step>.xyz, traj_<group>.xyz and final_<xyz> -- plus
+ * its closing record as one line to all_out_fd when that is >= 0 (list order).
+ * Every entry must run the same number of steps (PFMD_E_PARAM otherwise); the
+ * batch must be at step 0 (PFMD_E_STATE).  No per-step output block is written. */
+int pfmd_batch_run_list(pfmd_batch* b, const char* out_path, int all_out_fd, double* device_ms);
+
+/* Energy history: rows x replicas x 4 (the potential energies of the replica's
+ * interactions -- LJ gas: lj1g A-A, lj1g B-B, lj A-B; rjl slab: rjl, 0, 0 -- and
+ * the kinetic energy), one row per energy step from step 0; *rows and *period
+ * (steps between rows) are returned; hist may be NULL to query the size. */
 int pfmd_batch_energy_history(pfmd_batch* batch, double* hist, long long* rows, int* period);
 
 /* ---- rjl forces without device allocation ----------------------------------

@@ -32,7 +32,7 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_nlist_shape", "pfmd_get_nlist", "pfmd_nlist_load", "pfmd_get_gr_norm", "pfmd_set_group_n",
            "pfmd_get_stream", "pfmd_kernel_launches", "pfmd_advance_timed", "pfmd_time_kernel",
            "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
-           "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
+           "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
            "pfmd_learned_check", "pfmd_learned_status", "pfmd_rjl_forces_noalloc")
 
@@ -99,6 +99,7 @@ def load(path=LIB_PATH):
     L.pfmd_batch_info.argtypes = [vp, ip, llp, llp]
     L.pfmd_batch_replica.argtypes = [vp, C.c_int, ip, ip, ip]
     L.pfmd_batch_run.argtypes = [vp, C.c_longlong, dp]
+    L.pfmd_batch_run_list.argtypes = [vp, C.c_char_p, C.c_int, dp]
     L.pfmd_batch_tune.argtypes = [vp, C.c_int, ip]
     L.pfmd_batch_set_tpa.argtypes = [vp, ip]
     L.pfmd_batch_get_state.argtypes = [vp, C.c_int, dp, dp, dp]
@@ -375,6 +376,23 @@ class Batch:
         self._check(load().pfmd_batch_run(self._h, nsteps, C.byref(ms)))
         return ms.value
 
+    def run_list(self, out_path="", all_out=None):
+        """Run every entry to the end of its nve stage and write each entry's
+        files (log, snapshots, trajectory, final .xyz) under out_path + its
+        prefix; the closing records go to the file all_out when given.  Returns
+        the device time in ms."""
+        ms = C.c_double()
+        f = open(all_out, "w") if all_out else None
+        try:
+            if f:
+                f.flush()
+            self._check(load().pfmd_batch_run_list(self._h, out_path.encode(), f.fileno() if f else -1,
+                                                   C.byref(ms)))
+        finally:
+            if f:
+                f.close()
+        return ms.value
+
     def tune(self, steps=10):
         t = np.zeros(6, np.int32)
         self._check(load().pfmd_batch_tune(self._h, steps, _ip(t)))
@@ -398,10 +416,15 @@ class Batch:
 
     def history(self):
         """(rows, replicas, 2) array of (potential, kinetic) per energy step, and
-        the steps between rows."""
+        the steps between rows; history4() keeps the potential per interaction."""
+        h4, per = self.history4()
+        return np.stack([h4[..., :3].sum(-1), h4[..., 3]], axis=-1), per
+
+    def history4(self):
+        """(rows, replicas, 4): the three interaction energies and the kinetic energy."""
         rows, per = C.c_longlong(), C.c_int()
         self._check(load().pfmd_batch_energy_history(self._h, None, C.byref(rows), C.byref(per)))
-        h = np.zeros((max(rows.value, 0), self.n_replicas, 2))
+        h = np.zeros((max(rows.value, 0), self.n_replicas, 4))
         if rows.value:
             self._check(load().pfmd_batch_energy_history(self._h, _dp(h), C.byref(rows), C.byref(per)))
         return h, per.value

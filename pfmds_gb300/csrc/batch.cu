@@ -29,12 +29,14 @@
 // autotuner that times the persistent kernel with each candidate on a saved copy of
 // the state and restores it afterwards.
 #include <cuda_runtime.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <numeric>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -86,7 +88,7 @@ struct Dev {
   const LJSet* lj;
   const RJLc<float>* rjl;
   const Tile* tile;
-  double *tile_e, *tile_k, *e_pot, *e_kin, *hist;
+  double *tile_e, *tile_k, *e_pot, *e_kin, *hist;  // tile_e, e_pot: 3 interaction classes each
   unsigned int *bar_count, *bar_gen;
   int* status;  // [0] code, [1] replica, [2] row, [3] info
   long long* step;
@@ -390,8 +392,10 @@ __device__ void tile_density(const Dev& D, const Tile& t, bool energy, float& er
 
 // Forces of one tile, the fused second half-kick, and (energy steps) the tile's
 // potential and kinetic energy.
+// Energy classes: LJ replicas 0 = lj1g A-A, 1 = lj1g B-B, 2 = lj A-B; rjl replicas 0.
 template <int TPA>
-__device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, float& es, float& ec, double& ke) {
+__device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, float (&es)[3], float (&ec)[3],
+                           double& ke) {
   constexpr int RPW = 32 / TPA;
   const int lane = threadIdx.x & 31;
   const int row = lane % RPW, sub = lane / RPW;
@@ -404,7 +408,7 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
   const bool valid = row < t.nrows;
   const int n = valid ? D.nnum[a] : 0;
   Acc3<true> acc;
-  Acc1<true> e;
+  Acc1<true> e[3];
   if (n > 0) {
     const int4 pi = D.posq[a];
     if (R.kind == KIND_RJL) {
@@ -436,7 +440,7 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
             f_dfr_cut<float>(r, c.R1, c.R2, fcut, dfr);
             const float F = U * invr2 * ((c.c12t12 * U - c.c6t6) * fcut - (c.c12 * U - c.c6) * dfr);
             acc.add(-F * dr[0], -F * dr[1], -F * dr[2]);
-            if (energy && aj < a) e.add(U * (c.c12 * U - c.c6) * fcut);
+            if (energy && aj < a) e[si].add(U * (c.c12 * U - c.c6) * fcut);
           }
         } else {  // lj (LennardJones.f90:23-69), cosine switch
           const LJc<float>& c = P.ab;
@@ -446,15 +450,18 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
             fdfcut_cos_f(r, c.R1, c.R2, c.inv_w, fc, dfc);
             const float k = c.eps4 * (V * (12.f * V - 6.f) * (ir * ir) * fc - V * (V - 1.f) * dfc);
             acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
-            if (energy && si == 0) e.add(c.eps4 * V * (V - 1.f) * fc);
+            if (energy && si == 0) e[2].add(c.eps4 * V * (V - 1.f) * fc);
           }
         }
       }
     }
   }
   acc.template reduce<TPA>();
-  if (energy) e.template reduce<TPA>();
-  es = ec = 0.f;
+  if (energy)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) e[k].template reduce<TPA>();
+#pragma unroll
+  for (int k = 0; k < 3; ++k) es[k] = ec[k] = 0.f;
   ke = 0.0;
   if (valid && sub == 0) {
     const double4_32a f = make_double4_32a(acc.get(0), acc.get(1), acc.get(2), 0.0);
@@ -471,34 +478,40 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
       }
       if (energy && (mv & 2)) ke = D.mass[a] * (v.x * v.x + v.y * v.y + v.z * v.z) / 2 * kMassCoef;
     }
-    if (energy && R.kind == KIND_LJ) {
-      es = e.s;
-      ec = e.c;
-    }
+    if (energy && R.kind == KIND_LJ)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        es[k] = e[k].s;
+        ec[k] = e[k].c;
+      }
   }
 }
 
 template <int TPA>
 __device__ void run_tile(const Dev& D, int ti, int phase, bool kick, bool energy) {
   const Tile& t = D.tile[ti];
-  float s, c;
+  float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
   double ke = 0.0;
   if (phase == 0) {
-    tile_density<TPA>(D, t, energy, s, c);
+    tile_density<TPA>(D, t, energy, s[0], c[0]);
   } else {
     tile_force<TPA>(D, t, kick, energy, s, c, ke);
   }
   if (!energy) return;
-  // the tile's rows sit in one warp: a compensated FP32 merge of the row energies,
+  // the tile's rows sit in one warp: compensated FP32 merges of the row energies,
   // an FP64 sum of the kinetic energies
-  gmerge<32>(s, c);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gmerge<32>(s[k], c[k]);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
   if ((threadIdx.x & 31) == 0) {
-    if (phase == 0)
-      D.tile_e[ti] = (double)s - (double)c;  // rjl: the density pass holds the energy
-    else {
-      if (D.rep[t.rep].kind == KIND_LJ) D.tile_e[ti] = (double)s - (double)c;
+    double* te = D.tile_e + 3 * (size_t)ti;
+    if (phase == 0) {  // rjl: the density pass holds the energy
+      te[0] = (double)s[0] - (double)c[0];
+      te[1] = te[2] = 0.0;
+    } else {
+      if (D.rep[t.rep].kind == KIND_LJ)
+        for (int k = 0; k < 3; ++k) te[k] = (double)s[k] - (double)c[k];
       D.tile_k[ti] = ke;
     }
   }
@@ -564,20 +577,23 @@ __device__ void phase_energy(const Dev& D, long long s) {
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < D.R; r += nw) {
     const Rep& R = D.rep[r];
-    double ep = 0.0, ek = 0.0;
+    double ep[3] = {0.0, 0.0, 0.0}, ek = 0.0;
     for (int t = lane; t < R.ntile; t += 32) {
-      ep += D.tile_e[R.tile0 + t];
+      for (int k = 0; k < 3; ++k) ep[k] += D.tile_e[3 * (size_t)(R.tile0 + t) + k];
       ek += D.tile_k[R.tile0 + t];
     }
-    ep = warp_sum(ep);
+    for (int k = 0; k < 3; ++k) ep[k] = warp_sum(ep[k]);
     ek = warp_sum(ek);
     if (lane == 0) {
-      D.e_pot[r] = ep;
+      for (int k = 0; k < 3; ++k) D.e_pot[3 * r + k] = ep[k];
       D.e_kin[r] = ek;
       const long long h = s / D.energy_period;
-      if (h < D.hist_cap) {
-        D.hist[(h * D.R + r) * 2] = ep;
-        D.hist[(h * D.R + r) * 2 + 1] = ek;
+      if (s % D.energy_period == 0 && h < D.hist_cap) {
+        double* o = D.hist + (h * D.R + r) * 4;
+        o[0] = ep[0];
+        o[1] = ep[1];
+        o[2] = ep[2];
+        o[3] = ek;
       }
     }
   }
@@ -585,7 +601,8 @@ __device__ void phase_energy(const Dev& D, long long s) {
 
 // K MD steps of every replica.  Step s: (s > 0) first half-kick and drift; list
 // rebuild when s % period == 0; rjl density; forces and (s > 0) the second
-// half-kick; energies when s % energy_period == 0.
+// half-kick; energies when s % energy_period == 0 (history rows) and at the
+// launch's last step (e_pot / e_kin only).
 __global__ void __launch_bounds__(kThreads) k_batch(Dev D, int nsteps) {
   const long long s0 = *D.step;
   for (int it = 0; it < nsteps; ++it) {
@@ -623,7 +640,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(Dev D, int nsteps) {
       if (!phase_zero_momentum(D)) return;
       if (!barrier(D)) return;
     }
-    const bool energy = s % D.energy_period == 0;
+    const bool energy = s % D.energy_period == 0 || it == nsteps - 1;
     phase_tiles(D, 0, false, energy);
     if (!barrier(D)) return;
     phase_tiles(D, 1, s > 0, energy);
@@ -681,6 +698,13 @@ struct HostRep {
   int nmax_same = 0, nmax_cross = 0;
   LJPar aa{}, bb{}, ab{};
   RJLPar rjl{};
+  // what a settings-list run writes (md_simulation.f90:204-241, 262-300)
+  std::string integ_name, log_file, xyz_file;
+  long long snap_period = 1, traj_period = 1;
+  int traj_group = 0, n_ke = 0, n_nhc = 0;
+  std::vector<int> all_idx, traj_idx;  // group members in the reference's order (type, then atom)
+  std::vector<int> inter_class;        // energy class of each interaction, settings order
+  std::vector<std::string> types;
 };
 
 static int bucket_of(const HostRep& r) {
@@ -717,6 +741,7 @@ struct Batch {
   long long md_step = 0, hist_cap = 0;
   int rebuild_period = 10, energy_period = 10;
   long long zero_momentum_period = 1;
+  int out_period = 1;
   cudaStream_t st = nullptr;
   std::string err;
   std::vector<double> mass_h;
@@ -761,12 +786,38 @@ struct Batch {
     const auto& X = S.xyz;
     r.n = X.N;
     for (int k = 0; k < 3; ++k) r.L[k] = X.box[k];
-    if (S.integrators.empty() || S.integrators[0].name != "nve")
-      throw Error(PFMD_E_PARAM, r.settings + ": the batched form integrates nve only");
+    // the integrators that run (md_simulation.f90:121-136 skips those of length 0)
+    std::vector<const pfmd_io::IntegratorSpec*> runs;
+    for (const auto& is : S.integrators)
+      if (is.l > 0) runs.push_back(&is);
+    if (runs.size() != 1 || fortio::trim(runs[0]->name) != "nve")
+      throw Error(PFMD_E_PARAM, r.settings + ": the batched form integrates one nve stage only");
     if (S.new_velocities) throw Error(PFMD_E_PARAM, r.settings + ": the batched form takes velocities from the .xyz");
-    r.dt = S.integrators[0].dt;
-    r.log_period = S.integrators[0].period_log;
-    r.steps = S.integrators[0].l;
+    if (!S.changes.empty() || S.invert_z_vel)
+      throw Error(PFMD_E_PARAM, r.settings + ": the batched form has no group changes or z-velocity inversion");
+    const auto& I = *runs[0];
+    r.dt = I.dt;
+    r.log_period = std::max<long long>(1, I.period_log);
+    // steps 0..steps run (md_simulation.f90:113-134: the stage ends after l steps or at md_step_limit)
+    r.steps = std::min<long long>(I.l, S.md_step_limit);
+    r.integ_name = I.name;
+    r.snap_period = std::max<long long>(1, I.period_snapshot);
+    r.traj_period = std::max<long long>(1, S.period_traj);
+    r.traj_group = S.traj_group;
+    r.n_nhc = static_cast<int>(S.nhc.size());
+    r.log_file = S.logfilename;
+    r.xyz_file = S.init_xyz_filename;
+    r.types = X.types;
+    auto members = [&](int g) {
+      std::vector<int> idx;
+      if (g < 1 || g > static_cast<int>(S.group_types.size())) return idx;
+      for (const auto& nm : S.group_types[static_cast<size_t>(g - 1)])
+        for (int i = 0; i < X.N; ++i)
+          if (X.types[static_cast<size_t>(i)] == nm) idx.push_back(i);
+      return idx;
+    };
+    r.all_idx = members(S.all_atoms);
+    r.traj_idx = members(S.traj_group);
     std::vector<const pfmd_io::InteractionSpec*> lj1g, lj, rjl;
     for (const auto& in : S.interactions) {
       if (in.kind == pfmd_io::K_LJ1G) lj1g.push_back(&in);
@@ -815,6 +866,8 @@ struct Batch {
     } else {
       throw Error(PFMD_E_PARAM, r.settings + ": a replica is an LJ gas (lj1g, lj1g, lj) or an rjl slab");
     }
+    for (const auto& in : S.interactions)
+      r.inter_class.push_back(r.kind == KIND_RJL ? 0 : (&in == lj1g[0] ? 0 : (&in == lj1g[1] ? 1 : 2)));
     r.nmove = 0;
     r.zmp = S.zero_momentum_period;
     for (int i = 0; i < X.N; ++i) {
@@ -826,6 +879,7 @@ struct Batch {
       const bool mv = in_group(S, S.xyz_moving, t), ke = in_group(S, S.all_moving, t);
       mv_h.push_back(static_cast<unsigned char>((mv ? 1 : 0) | (ke ? 2 : 0)));
       r.nmove += mv ? 1 : 0;
+      r.n_ke += ke ? 1 : 0;
       sp_h.push_back(sp[static_cast<size_t>(i)]);
       mass_h.push_back(X.mass[static_cast<size_t>(i)]);
       for (int k = 0; k < 3; ++k) {
@@ -849,10 +903,10 @@ struct Batch {
       tile = Buf<Tile>();
       tile.alloc(t.size());
       tile_e = Buf<double>();
-      tile_e.alloc(t.size());
+      tile_e.alloc(3 * t.size());
       tile_k = Buf<double>();
       tile_k.alloc(t.size());
-      BCK(cudaMemsetAsync(tile_e.p, 0, tile_e.n * sizeof(double), st));
+      BCK(cudaMemsetAsync(tile_e.p, 0, tile_e.n * sizeof(double), st));  // 3 classes per tile
       BCK(cudaMemsetAsync(tile_k.p, 0, tile_k.n * sizeof(double), st));
     }
     ntile_used = static_cast<int>(t.size());
@@ -887,10 +941,15 @@ struct Batch {
         throw Error(PFMD_E_PARAM, "batch: every replica needs the same list period");
       if (r.zmp != zero_momentum_period)
         throw Error(PFMD_E_PARAM, "batch: every replica needs the same zero_momentum_period");
-      energy_period = std::min<int>(energy_period, static_cast<int>(r.log_period));
+      // every replica's log steps are history rows
+      energy_period = static_cast<int>(std::gcd<long long>(energy_period, r.log_period));
       nslot = std::max(nslot, r.nmax_same + r.nmax_cross);
     }
+    // energies also at the output period of md_simulation.f90:188 when it is not every step
+    // (every step is covered by the energies of a launch's last step)
+    if (o.out_period > 1) energy_period = std::gcd(energy_period, o.out_period);
     energy_period = std::max(1, energy_period);
+    out_period = std::max(1, o.out_period);
     stride = (N + 31) / 32 * 32;
     // replica table, cell grids
     std::vector<LJSet> ljs;
@@ -951,7 +1010,7 @@ struct Batch {
     rep.alloc(reps.size());
     lj.alloc(ljs.size());
     rjl.alloc(rjls.size());
-    e_pot.alloc(reps.size());
+    e_pot.alloc(3 * reps.size());
     e_kin.alloc(reps.size());
     vcm.alloc(3 * reps.size());
     status.alloc(4);
@@ -978,12 +1037,12 @@ struct Batch {
     BCK(cudaMemsetAsync(status.p, 0, 4 * sizeof(int), st));
     BCK(cudaMemsetAsync(bar.p, 0, 2 * sizeof(unsigned int), st));
     BCK(cudaMemsetAsync(step.p, 0, sizeof(long long), st));
-    BCK(cudaMemsetAsync(e_pot.p, 0, reps.size() * sizeof(double), st));
+    BCK(cudaMemsetAsync(e_pot.p, 0, 3 * reps.size() * sizeof(double), st));
     BCK(cudaMemsetAsync(e_kin.p, 0, reps.size() * sizeof(double), st));
     long long max_steps = 0;
     for (const auto& r : reps) max_steps = std::max(max_steps, r.steps);
     hist_cap = max_steps / energy_period + 2;
-    hist.alloc(static_cast<size_t>(hist_cap) * reps.size() * 2);
+    hist.alloc(static_cast<size_t>(hist_cap) * reps.size() * 4);
     BCK(cudaMemsetAsync(hist.p, 0, hist.n * sizeof(double), st));
     // threads per row: a heuristic start (the autotuner refines it)
     for (int b = 0; b < kBuckets; ++b) tpa[b] = (b / 3 == KIND_RJL) ? 2 : 2;
@@ -1148,6 +1207,152 @@ struct Batch {
   }
 };
 
+// A settings-list run on the batched kernel: every entry of the list advanced
+// together, and per entry the files of its own run (md_simulation.f90:204-241 and
+// 278-297) -- log lines at the log period, snapshots, trajectory frames, the
+// closing record (also to all_out_fd, as run_md_simulation.f90:52-62 collects
+// them) and final_<xyz>.  Entries must run the same number of steps.
+static void write_text(const std::string& fn, const std::string& text, const char* mode) {
+  FILE* f = std::fopen(fn.c_str(), mode);
+  if (!f) throw Error(PFMD_E_IO, "cannot open " + fn);
+  std::fputs(text.c_str(), f);
+  std::fclose(f);
+}
+
+static void run_list(Batch& B, const std::string& out_path, int all_out_fd, double* device_ms) {
+  const long long L = B.reps[0].steps;
+  for (const auto& r : B.reps)
+    if (r.steps != L)
+      throw Error(PFMD_E_PARAM, "batch: every list entry must run the same number of steps (" + r.settings +
+                                    ": " + std::to_string(r.steps) + ", first entry: " + std::to_string(L) + ")");
+  if (B.md_step != 0) throw Error(PFMD_E_STATE, "batch: a list run starts at step 0");
+  const size_t R = B.reps.size();
+  // steps after which some entry writes a trajectory frame or a snapshot
+  std::vector<long long> ev;
+  for (const auto& r : B.reps) {
+    for (long long s = 0; s <= L; s += r.traj_period) ev.push_back(s);
+    for (long long s = r.snap_period; s <= L; s += r.snap_period) ev.push_back(s);
+  }
+  std::sort(ev.begin(), ev.end());
+  ev.erase(std::unique(ev.begin(), ev.end()), ev.end());
+  double ms = 0.0;
+  std::vector<double4_32a> p4(static_cast<size_t>(B.N)), v4(static_cast<size_t>(B.N));
+  std::vector<double> hp, hv;
+  auto state_of = [&](const HostRep& r) {
+    hp.resize(3 * static_cast<size_t>(r.n));
+    hv.resize(3 * static_cast<size_t>(r.n));
+    for (int i = 0; i < r.n; ++i) {
+      const double4_32a& p = p4[static_cast<size_t>(r.atom0 + i)];
+      const double4_32a& v = v4[static_cast<size_t>(r.atom0 + i)];
+      hp[3 * i] = p.x, hp[3 * i + 1] = p.y, hp[3 * i + 2] = p.z;
+      hv[3 * i] = v.x, hv[3 * i + 1] = v.y, hv[3 * i + 2] = v.z;
+    }
+  };
+  auto fetch = [&] {
+    BCK(cudaMemcpyAsync(p4.data(), B.pos.p, p4.size() * sizeof(double4_32a), cudaMemcpyDeviceToHost, B.st));
+    BCK(cudaMemcpyAsync(v4.data(), B.vel.p, v4.size() * sizeof(double4_32a), cudaMemcpyDeviceToHost, B.st));
+    BCK(cudaStreamSynchronize(B.st));
+  };
+  for (const long long e : ev) {
+    if (e + 1 > B.md_step) ms += B.run(e + 1 - B.md_step);
+    fetch();
+    for (const auto& r : B.reps) {
+      const std::string prefix = out_path + r.prefix;
+      const bool snap = e != 0 && e % r.snap_period == 0, traj = e % r.traj_period == 0;
+      if (!snap && !traj) continue;
+      state_of(r);
+      const std::vector<double>& mass = B.mass_h;
+      const double* m = mass.data() + r.atom0;
+      if (snap)
+        write_text(prefix + "snapshot_" + fortio::fmt_i0pad(e, 6, 6) + ".xyz",
+                   pfmd_io::xyz_snapshot_text(r.L, static_cast<int>(r.all_idx.size()), r.all_idx.data(), hp.data(),
+                                              hv.data(), m, r.types),
+                   "w");
+      if (traj) {
+        const std::string t = pfmd_io::xyz_traj_frame_text(r.L, static_cast<int>(r.traj_idx.size()),
+                                                           r.traj_idx.data(), hp.data(), hv.data(), m, r.types, e);
+        if (!t.empty())
+          write_text(prefix + "traj_" + fortio::fmt_i0pad(r.traj_group, 2, 2) + ".xyz", t, "a");
+      }
+    }
+  }
+  if (L + 1 > B.md_step) ms += B.run(L + 1 - B.md_step);
+  fetch();
+  // energies: the history rows and the last step's totals
+  const long long rows = std::min<long long>(B.hist_cap, L / B.energy_period + 1);
+  std::vector<double> hist(static_cast<size_t>(rows) * R * 4), ep(3 * R), ek(R);
+  BCK(cudaMemcpyAsync(hist.data(), B.hist.p, hist.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
+  BCK(cudaMemcpyAsync(ep.data(), B.e_pot.p, ep.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
+  BCK(cudaMemcpyAsync(ek.data(), B.e_kin.p, ek.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
+  BCK(cudaStreamSynchronize(B.st));
+  const double kt_a_degree = 1.3806488 / 1.6021765654 * 1e-4;  // md_general.f90:304
+  for (size_t k = 0; k < R; ++k) {
+    const HostRep& r = B.reps[k];
+    const std::string prefix = out_path + r.prefix;
+    // (potential per interaction in settings order, potential, kinetic, temperature)
+    auto energies = [&](const double* cls, double ke, std::vector<double>& inter, double& pe, double& temp) {
+      inter.clear();
+      pe = 0.0;
+      for (int c : r.inter_class) {
+        inter.push_back(cls[c]);
+        pe += cls[c];
+      }
+      temp = 2 * ke / kt_a_degree / static_cast<double>(3 * std::max(r.n_ke, 1));
+    };
+    std::string log;
+    double sim_time = 0.0;  // accumulated one step at a time, as md_simulation.f90:243 does
+    std::vector<double> inter;
+    double pe = 0.0, temp = 0.0;
+    for (long long s = 0; s <= L; ++s) {
+      if (s != 0) sim_time = sim_time + r.dt;
+      if (s % r.log_period != 0) continue;
+      const double* h = hist.data() + (static_cast<size_t>(s / B.energy_period) * R + k) * 4;
+      energies(h, h[3], inter, pe, temp);
+      fortio::Rec q;
+      q.a(fortio::trim(r.integ_name), 6).i(s, 9);
+      q.f(sim_time, 24, 6).f(pe + h[3], 24, 6).f(0.0, 24, 6).f(pe + h[3], 24, 6).f(pe, 24, 6);
+      q.f(h[3], 24, 6).f(temp, 24, 6);
+      for (double v : inter) q.f(v, 20, 9);
+      for (int j = 0; j < r.n_nhc; ++j) q.f(0.0, 20, 9);  // chain energies stay 0 under nve
+      log += q.s + "\n";
+    }
+    // the closing record holds the energies of the last energy step (md_simulation.f90:188)
+    long long last = L;
+    if (B.out_period > 1) {
+      last = -1;
+      for (long long s = L; s >= 0 && last < 0; --s)
+        if (s % r.log_period == 0 || s % B.out_period == 0) last = s;
+    }
+    const double* cls;
+    double ke;
+    if (last == L) {
+      cls = ep.data() + 3 * k;
+      ke = ek[k];
+    } else {
+      const double* h = hist.data() + (static_cast<size_t>(last / B.energy_period) * R + k) * 4;
+      cls = h;
+      ke = h[3];
+    }
+    energies(cls, ke, inter, pe, temp);
+    fortio::Rec c;
+    c.a(fortio::trim(prefix), 32).i(L, 9).f(sim_time, 20, 9);
+    c.f(pe + ke, 20, 9).f(pe, 20, 9).f(ke, 20, 9).f(temp, 20, 9);
+    for (double v : inter) c.f(v, 20, 9);
+    if (all_out_fd >= 0) {
+      const std::string line = c.s + "\n";
+      ssize_t w = ::write(all_out_fd, line.data(), line.size());
+      (void)w;
+    }
+    write_text(prefix + fortio::trim(r.log_file), log + c.s + "\n", "w");
+    state_of(r);
+    write_text(prefix + "final_" + fortio::trim(r.xyz_file),
+               pfmd_io::xyz_snapshot_text(r.L, static_cast<int>(r.all_idx.size()), r.all_idx.data(), hp.data(),
+                                          hv.data(), B.mass_h.data() + r.atom0, r.types),
+               "w");
+  }
+  if (device_ms) *device_ms = ms;
+}
+
 }  // namespace batch
 }  // namespace pfmd
 
@@ -1224,6 +1429,11 @@ int pfmd_batch_run(pfmd_batch* c, long long nsteps, double* device_ms) {
   });
 }
 
+int pfmd_batch_run_list(pfmd_batch* c, const char* out_path, int all_out_fd, double* device_ms) {
+  if (!c || !c->b) return PFMD_E_STATE;
+  return bguard(c, [&] { pfmd::batch::run_list(*c->b, fortio::trim(out_path ? out_path : ""), all_out_fd, device_ms); });
+}
+
 int pfmd_batch_tune(pfmd_batch* c, int steps, int* tpa) {
   if (!c || !c->b) return PFMD_E_STATE;
   return bguard(c, [&] {
@@ -1274,9 +1484,13 @@ int pfmd_batch_energies(pfmd_batch* c, double* e_pot, double* e_kin) {
   if (!c || !c->b) return PFMD_E_STATE;
   return bguard(c, [&] {
     auto& B = *c->b;
-    if (e_pot) BCK(cudaMemcpyAsync(e_pot, B.e_pot.p, B.reps.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
-    if (e_kin) BCK(cudaMemcpyAsync(e_kin, B.e_kin.p, B.reps.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
+    const size_t R = B.reps.size();
+    std::vector<double> ep(3 * R);
+    BCK(cudaMemcpyAsync(ep.data(), B.e_pot.p, ep.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
+    if (e_kin) BCK(cudaMemcpyAsync(e_kin, B.e_kin.p, R * sizeof(double), cudaMemcpyDeviceToHost, B.st));
     BCK(cudaStreamSynchronize(B.st));
+    if (e_pot)
+      for (size_t r = 0; r < R; ++r) e_pot[r] = ep[3 * r] + ep[3 * r + 1] + ep[3 * r + 2];
   });
 }
 
@@ -1288,7 +1502,7 @@ int pfmd_batch_energy_history(pfmd_batch* c, double* hist, long long* rows, int*
     if (rows) *rows = avail;
     if (period) *period = B.energy_period;
     if (hist && avail > 0)
-      BCK(cudaMemcpyAsync(hist, B.hist.p, static_cast<size_t>(avail) * B.reps.size() * 2 * sizeof(double),
+      BCK(cudaMemcpyAsync(hist, B.hist.p, static_cast<size_t>(avail) * B.reps.size() * 4 * sizeof(double),
                           cudaMemcpyDeviceToHost, B.st));
     BCK(cudaStreamSynchronize(B.st));
   });

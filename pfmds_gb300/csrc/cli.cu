@@ -2,7 +2,9 @@
 // same options (-i -p -op -omp_n -ipath -ilist -opath -ofile), the same banner
 // lines and the same single-file and list modes.  Extra options of this
 // implementation: -form plain|precision (arithmetic form), -graphs 0|1,
-// -device n.
+// -device n, and -batch, which runs a whole list as one batch on the batched
+// kernel (pfmd_batch_run_list: the same files per entry; no per-step output
+// blocks).
 #include <unistd.h>
 
 #include <cstdio>
@@ -20,6 +22,7 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
   o.write_files = 1;
   std::string settings_files_list, settings_filename = "md_run_settings.txt", all_out_file = "all_out.txt",
                                    output_prefix, input_path, out_path;
+  bool batched = false;
   std::string banner;
   auto say = [&](const std::string& s) {
     std::fputs((s + "\n").c_str(), stdout);
@@ -61,6 +64,8 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
         o.use_graphs = static_cast<int>(fortio::to_int(next()));
       } else if (arg == "-device") {
         o.device = static_cast<int>(fortio::to_int(next()));
+      } else if (arg == "-batch") {
+        batched = true;
       }
     } catch (const std::exception& e) {
       std::fprintf(stderr, "%s\n", e.what());
@@ -69,7 +74,26 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
   }
   std::fflush(stdout);
   int rc = PFMD_OK;
-  if (!settings_files_list.empty()) {
+  if (batched && !settings_files_list.empty()) {
+    FILE* all_out = std::fopen((out_path + all_out_file).c_str(), "w");
+    if (!all_out) return PFMD_E_IO;
+    pfmd_batch* b = nullptr;
+    rc = pfmd_batch_create(input_path.c_str(), settings_files_list.c_str(), &o, &b);
+    double ms = 0.0;
+    if (rc == PFMD_OK) rc = pfmd_batch_run_list(b, out_path.c_str(), fileno(all_out), &ms);
+    if (rc == PFMD_OK) {
+      int reps = 0;
+      long long atoms = 0, steps = 0;
+      pfmd_batch_info(b, &reps, &atoms, &steps);
+      say(line);
+      say(Rec().a("BATCH: ").i(reps, 6).a(" entries").i(atoms, 12).a(" atoms").i(steps, 12).a(" steps").s);
+      say(Rec().a("DEVICE TIME: ", 24).f(ms / 1000.0, 10, 2).a(" S ").s);
+    } else {
+      std::fprintf(stderr, "%s\n", pfmd_batch_errmsg(b));
+    }
+    pfmd_batch_destroy(b);
+    std::fclose(all_out);
+  } else if (!settings_files_list.empty()) {
     fortio::ListReader lst;
     if (!lst.open(input_path + settings_files_list)) {
       std::fprintf(stderr, "cannot open %s\n", (input_path + settings_files_list).c_str());

@@ -40,8 +40,9 @@ def test_step0_forces_and_energies_match_single_system(tmp_path, built):
 def test_trajectory_follows_single_system_precision_form(tmp_path, built):
     ln, reps = _batch(tmp_path, n_rep=4, seed=5)
     b = pf.Batch(str(tmp_path), ln)
-    b.run(35)  # three list rebuilds, energies at 0, 10, 20, 30
+    b.run(31)  # three list rebuilds; the energies of step 30, the launch's last
     ep, ek = b.energies()
+    b.run(4)
     for r, rep in enumerate(reps):
         s = pf.Simulation(str(tmp_path), settings=rep["settings"], form="precision", out_period=10 ** 9)
         s.advance(31)  # steps 0..30: the energies of step 30
@@ -113,3 +114,74 @@ def test_unsupported_replica_is_rejected(tmp_path, built):
     with pytest.raises(pf.PfmdError) as ei:
         pf.Batch(str(tmp_path), ln)
     assert ei.value.code == pf.PFMD_E_PARAM and "nve" in str(ei.value)
+
+
+def _fields(line):
+    return [float(x) for x in line.split()[1:]]
+
+
+def _xyz_rows(path):
+    lines = open(path).read().splitlines()
+    n = int(lines[0])
+    rows = [ln.split() for ln in lines[2:2 + n]]
+    return np.array([[float(x) for x in r[:-1]] for r in rows]), [r[-1] for r in rows]
+
+
+@pytest.mark.parametrize("out_period", [1, 10 ** 6])
+def test_list_run_writes_what_single_runs_write(tmp_path, built, out_period):
+    """run_md_simulation -ilist ... -batch against the same list run entry by entry
+    (precision form): the same files, steps and times; energies and positions
+    within the FP32-pair tolerance after 65 steps."""
+    ln, reps = _batch(tmp_path, n_rep=4, steps=65, seed=4)
+    assert {r["kind"] for r in reps} == {"lj", "rjl"}
+    for r in reps:  # snapshots every 30 steps, trajectory frames every 20
+        sf = tmp_path / r["settings"]
+        txt = sf.read_text().replace("period_traj:\t\t\t\t100000000", "period_traj:\t\t\t\t20")
+        sf.write_text(txt.replace("100000000", "30"))
+    ob, os_ = tmp_path / "batch", tmp_path / "single"
+    ob.mkdir()
+    os_.mkdir()
+    common = ["-ipath", f"{tmp_path}/", "-ilist", ln, "-op", str(out_period)]
+    assert pf.run_md_simulation(common + ["-opath", f"{ob}/", "-batch"]) == 0
+    assert pf.run_md_simulation(common + ["-opath", f"{os_}/", "-form", "precision"]) == 0
+    names = sorted(p.name for p in os_.iterdir())
+    assert names == sorted(p.name for p in ob.iterdir())
+    for r in reps:
+        pre = r["name"] + "_"
+        assert {pre + "md_run.log", pre + "final_" + r["name"] + ".xyz", pre + "snapshot_000030.xyz",
+                pre + "snapshot_000060.xyz"} <= set(names)
+        lb = (ob / (pre + "md_run.log")).read_text().splitlines()
+        ls = (os_ / (pre + "md_run.log")).read_text().splitlines()
+        assert len(lb) == len(ls) == 8  # steps 0..60 by 10, then the closing record
+        for x, y in zip(lb, ls):
+            if x is not lb[-1]:
+                assert x.split()[0] == y.split()[0] == "nve"
+            fx, fy = _fields(x), _fields(y)
+            assert len(fx) == len(fy)
+            assert fx[:2] == fy[:2]  # step, time
+            assert np.allclose(fx[2:], fy[2:], rtol=2e-5, atol=1e-5 * r["n"]), (r, x, y)
+        for f in (pre + "final_" + r["name"] + ".xyz", pre + "snapshot_000060.xyz"):
+            pb, tb = _xyz_rows(ob / f)
+            ps, ts = _xyz_rows(os_ / f)
+            assert tb == ts
+            assert np.abs(pb - ps).max() < 1e-3, (r, f)  # printed to 4 decimals
+        for f in [n for n in names if n.startswith(pre + "traj_")]:
+            assert (ob / f).read_text().count("time_step") == (os_ / f).read_text().count("time_step") == 4
+    ab = (ob / "all_out.txt").read_text().split("\n")
+    as_ = (os_ / "all_out.txt").read_text().split("\n")
+    ab, as_ = [x for x in ab if x.strip()], [x for x in as_ if x.strip()]
+    assert len(ab) == len(as_) == len(reps)
+    for x, y, r in zip(ab, as_, reps):
+        fx, fy = _fields(x), _fields(y)
+        assert fx[:2] == fy[:2] and fx[0] == 65
+        assert np.allclose(fx[2:], fy[2:], rtol=2e-5, atol=1e-5 * r["n"]), (r, x, y)
+
+
+def test_list_run_needs_equal_lengths(tmp_path, built):
+    ln, reps = _batch(tmp_path, n_rep=2, steps=40, seed=4)
+    sf = tmp_path / reps[1]["settings"]
+    sf.write_text(sf.read_text().replace("md_step_limit:\t\t\t\t40", "md_step_limit:\t\t\t\t30"))
+    b = pf.Batch(str(tmp_path), ln)
+    with pytest.raises(pf.PfmdError) as ei:
+        b.run_list(str(tmp_path) + "/")
+    assert ei.value.code == pf.PFMD_E_PARAM and reps[1]["settings"] in str(ei.value)
