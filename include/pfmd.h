@@ -103,6 +103,21 @@ int pfmd_md(const char* input_path, const char* settings_filename, const pfmd_op
  * -i -p -op -omp_n -ipath -ilist -opath -ofile, plus -form plain|precision. */
 int pfmd_run_md_simulation(int argc, const char* const* argv);
 
+/* ---- analysis and fitting programs -------------------------------------------
+ * gr_on_cu_analysis (graphene_on_surface_analysis.f90:8-29): arr1 = mean, minimum
+ * and maximum z of the atoms of types C, C_a, C_b above height z; arr2 the same for
+ * CU, CU_fixed (position_analysis, md_general.f90:400-421).  Host-only. */
+int pfmd_gr_on_cu_analysis(const char* xyz_path, double z, double* arr1, double* arr2);
+/* The run_gr_analysis program (runners/run_gr_analysis.f90): -path -fl -o -z. */
+int pfmd_run_gr_analysis(int argc, const char* const* argv);
+/* The run_gr_moire_fitting program (runners/run_gr_moire_fitting.f90 with
+ * fit_gr_moire.f90): -fpfn -op -omp_n -delta_error_gold -delta_error_fit, plus
+ * -form plain|precision and -device n.  md() runs that do not depend on each
+ * other run concurrently on the GPU; files and fit_out.txt are the reference's,
+ * except that the original parameter file stays in place (the reference moves
+ * it to the first evaluation's numbered name, which is also written). */
+int pfmd_run_gr_moire_fitting(int argc, const char* const* argv);
+
 /* ---- state access -------------------------------------------------------- */
 
 int pfmd_natoms(const pfmd_ctx* ctx, int* n);

@@ -34,7 +34,8 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
            "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
-           "pfmd_learned_check", "pfmd_learned_status", "pfmd_rjl_forces_noalloc")
+           "pfmd_learned_check", "pfmd_learned_status", "pfmd_rjl_forces_noalloc",
+           "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting")
 
 _LIB = None
 
@@ -74,6 +75,9 @@ def load(path=LIB_PATH):
     L.pfmd_finish.argtypes = [vp]
     L.pfmd_md.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(Options)]
     L.pfmd_run_md_simulation.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    L.pfmd_run_gr_analysis.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    L.pfmd_run_gr_moire_fitting.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    L.pfmd_gr_on_cu_analysis.argtypes = [C.c_char_p, C.c_double, dp, dp]
     L.pfmd_natoms.argtypes = [vp, ip]
     L.pfmd_md_step.argtypes = [vp, llp, dp]
     L.pfmd_get_state.argtypes = [vp, dp, dp, dp]
@@ -430,8 +434,30 @@ class Batch:
         return h, per.value
 
 
+def _argv(name, args):
+    return len(args) + 1, (C.c_char_p * (len(args) + 1))(*([name.encode()] + [a.encode() for a in args]))
+
+
 def run_md_simulation(args):
     """The run_md_simulation command line, in-process."""
-    L = load()
-    argv = (C.c_char_p * (len(args) + 1))(*([b"run_md_simulation"] + [a.encode() for a in args]))
-    return L.pfmd_run_md_simulation(len(args) + 1, argv)
+    return load().pfmd_run_md_simulation(*_argv("run_md_simulation", args))
+
+
+def run_gr_moire_fitting(args):
+    """The run_gr_moire_fitting command line, in-process (md() runs on the GPU)."""
+    return load().pfmd_run_gr_moire_fitting(*_argv("run_gr_moire_fitting", args))
+
+
+def run_gr_analysis(args):
+    """The run_gr_analysis command line, in-process (host only)."""
+    return load().pfmd_run_gr_analysis(*_argv("run_gr_analysis", args))
+
+
+def gr_on_cu_analysis(path, z):
+    """(arr1, arr2): mean, minimum and maximum z above z of the carbon and of the
+    copper atoms of an .xyz file (host only)."""
+    a1, a2 = np.zeros(3), np.zeros(3)
+    rc = load().pfmd_gr_on_cu_analysis(str(path).encode(), float(z), _dp(a1), _dp(a2))
+    if rc:
+        raise PfmdError(rc, f"cannot analyse {path}")
+    return a1, a2

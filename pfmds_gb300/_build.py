@@ -15,8 +15,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 CU_SOURCES = ["nlist.cu", "forces_pair.cu", "forces_rjl.cu", "forces_tb.cu", "forces_cos.cu", "integrate.cu", "noalloc.cu", "batch.cu", "learned.cu", "learned_tc.cu",
-              "engine.cu", "cli.cu"]
+              "engine.cu", "cli.cu", "fit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+EXECUTABLES = [("run_md_simulation", "pfmd_run_md_simulation"), ("run_gr_analysis", "pfmd_run_gr_analysis"),
+               ("run_gr_moire_fitting", "pfmd_run_gr_moire_fitting")]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 
 
@@ -67,10 +69,18 @@ def build(verbose=False, jobs=None):
     lib = os.path.join(OUT, "libpfmd.so")
     if _stale(lib, objs):
         _run([nvcc(), *ARCH, "-shared", "-o", lib, *objs], verbose)
-    exe = os.path.join(OUT, "run_md_simulation")
-    main = os.path.join(CSRC, "run_md_simulation.cpp")
-    if _stale(exe, [lib, main]):
-        _run(["g++", "-O2", "-std=c++17", main, "-o", exe, "-L" + OUT, "-lpfmd", "-Wl,-rpath,$ORIGIN"], verbose)
+    # the drop-in executables: each main() calls its pfmd_run_* entry point
+    for name, entry in EXECUTABLES:
+        exe = os.path.join(OUT, name)
+        main = os.path.join(OUT, name + "_main.cpp")
+        text = ('#include "pfmd.h"\n'
+                f"int main(int argc, char** argv) {{ return {entry}(argc, argv); }}\n")
+        if not os.path.exists(main) or open(main).read() != text:
+            with open(main, "w") as f:
+                f.write(text)
+        if _stale(exe, [lib, main]):
+            _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, main, "-o", exe, "-L" + OUT, "-lpfmd",
+                  "-Wl,-rpath,$ORIGIN"], verbose)
     return lib
 
 

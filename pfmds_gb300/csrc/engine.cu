@@ -32,7 +32,7 @@
 
 namespace pfmd {
 
-long long g_kernel_launches = 0;
+thread_local long long g_kernel_launches = 0;
 
 struct Error : std::runtime_error {
   int code;
@@ -842,7 +842,8 @@ void Engine::tune_tpa() {
   for (auto& L : lists) {
     if (L.kind == L_NN_TB || L.d.rows == 0) continue;
     std::vector<int> n(static_cast<size_t>(L.d.rows));
-    CK(cudaMemcpy(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     double tot = 0;
     for (int v : n) tot += v;
     const int t = auto_tpa(L.d.rows, tot / static_cast<double>(n.size()), prec);

@@ -38,13 +38,24 @@ struct ReadError : std::runtime_error {
 // ---------------------------------------------------------------------------
 // List-directed reader over the records (lines) of one file.
 // ---------------------------------------------------------------------------
+// Per-thread input overlay: while a path is listed here, ListReader::open reads
+// the file it maps to instead.  Concurrent md() runs of the fitting runner use it
+// to read their own structure and parameter files under the names their settings
+// give.
+inline thread_local std::vector<std::pair<std::string, std::string>> t_overlay;
+inline const std::string& overlaid(const std::string& path) {
+  for (const auto& kv : t_overlay)
+    if (kv.first == path) return kv.second;
+  return path;
+}
+
 class ListReader {
  public:
   ListReader() = default;
   explicit ListReader(const std::string& path) { open(path); }
 
   bool open(const std::string& path) {
-    std::ifstream f(path);
+    std::ifstream f(overlaid(path));
     if (!f) return false;
     lines_.clear();
     std::string s;

@@ -28,7 +28,7 @@ namespace pfmd {
 
 // Kernels launched by this library (incremented by every launcher, also while a
 // stream is being captured into a graph).
-extern long long g_kernel_launches;
+extern thread_local long long g_kernel_launches;  // launches made by this host thread
 
 struct Atoms {
   int N;
