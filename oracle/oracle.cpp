@@ -139,6 +139,61 @@ static inline double df_cut_cos(double r, double R1, double R2) {
   if (r < R2) return -std::sin(PI_TRUNC * (r - R1) / (R2 - R1)) * PI_TRUNC / (R2 - R1) / r / 2;
   return 0.0;
 }
+// REBOsc_energy, REBOsolidcarbon.f90:27-92, over any list (the full one or a
+// truncated one); serial, rows in order.  P: A Q alpha B(3) beta(3) T g(6) R1 R2.
+static double rebosc_energy(const NL& nl, const std::vector<double>& P) {
+  const double A = P[0], Q = P[1], al = P[2], T = P[9], R1 = P[16], R2 = P[17];
+  const double* B = &P[3];
+  const double* be = &P[6];
+  const double* g = &P[10];
+  const size_t M = static_cast<size_t>(nl.nmax);
+  std::vector<double> bsp(M * nl.N, 0.0), bdh(M * nl.N, 0.0);
+  auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  for (int i = 0; i < nl.N; ++i) {
+    for (int p = 0; p < nl.nnum[i]; ++p) {
+      if (!(nl.R(p, i) < R2)) continue;
+      const int j = nl.L(p, i);
+      double s = 0.0, h = 0.0;
+      for (int q = 0; q < nl.nnum[i]; ++q) {
+        if (p == q || !(nl.R(q, i) < R2)) continue;
+        const double c = dot(nl.D(p, i), nl.D(q, i)) / (nl.R(p, i) * nl.R(q, i));
+        s = s + f_cut_cos(nl.R(q, i), R1, R2) *
+                    (g[0] + g[1] * c + g[2] * c * c + g[3] * c * c * c + g[4] * c * c * c * c + g[5] * c * c * c * c * c);
+        for (int l = 0; l < nl.nnum[j]; ++l) {
+          if (nl.L(l, j) == i || !(nl.R(l, j) < R2)) continue;
+          const double aa = nl.R(p, i) * nl.R(p, i);
+          const double ab = dot(nl.D(p, i), nl.D(q, i)), ac = dot(nl.D(p, i), nl.D(l, j));
+          const double bc = dot(nl.D(q, i), nl.D(l, j));
+          const double D = aa * bc - ab * ac;
+          h = h + f_cut_cos(nl.R(q, i), R1, R2) * f_cut_cos(nl.R(l, j), R1, R2) *
+                      (1.0 - D * D / (aa * nl.R(q, i) * nl.R(q, i) - ab * ab) /
+                                 (aa * nl.R(l, j) * nl.R(l, j) - ac * ac));
+        }
+      }
+      bsp[i * M + p] = std::pow(1.0 + s, -0.5);
+      bdh[i * M + p] = T * h;
+    }
+  }
+  double e = 0.0;
+  for (int i = 0; i < nl.N; ++i) {
+    for (int p = 0; p < nl.nnum[i]; ++p) {
+      const double r = nl.R(p, i);
+      if (!(r < R2)) continue;
+      const int j = nl.L(p, i);
+      if (j <= i) continue;
+      int q = 0;
+      for (; q < nl.nnum[j]; ++q)
+        if (nl.L(q, j) == i) break;
+      const double bq = q < nl.nmax ? bsp[j * M + q] : 0.0;
+      e = e + f_cut_cos(r, R1, R2) *
+                  ((1.0 + Q / r) * A * std::exp(-al * r) -
+                   ((bsp[i * M + p] + bq) / 2 + bdh[i * M + p]) *
+                       (B[0] * std::exp(-be[0] * r) + B[1] * std::exp(-be[1] * r) + B[2] * std::exp(-be[2] * r)));
+    }
+  }
+  return e;
+}
+
 // cut_off_poly.f90:6-17 (quintic switch used by the lj1g energy)
 static inline double ipow(double x, int n) {
   double r = 1.0;
@@ -607,7 +662,7 @@ class Sim {
       if (k == pfmd_io::K_LJC || k == pfmd_io::K_MORSEC) {
         size_t j = 0;
         for (; j < inters.size(); ++j)
-          if (inters[j].spec.kind == pfmd_io::K_TB) break;
+          if (inters[j].spec.kind == pfmd_io::K_TB || inters[j].spec.kind == pfmd_io::K_REBOSC) break;
         if (j < inters.size()) {
           update_nearest_neighbours_in_graphene(step, in.nl[2], inters[j].nl[0],
                                                 G(inters[j].group_nums[0]));
@@ -956,6 +1011,94 @@ class Sim {
       }
     }
   }
+  // calculate_truncated_nl, md_interactions.f90:333-375: row i and the rows within
+  // n-1 list steps of it in full, the rows at step n with one entry (back to the
+  // first row that lists them).  `has` stands for particle_index /= 0.
+  static void calculate_truncated_nl(NL& t, const NL& nl, int i, int n, std::vector<char>& has) {
+    std::fill(t.nnum.begin(), t.nnum.end(), 0);
+    std::fill(has.begin(), has.end(), 0);
+    auto copy_row = [&](int q) {
+      for (int p = 0; p < nl.nnum[q]; ++p) {
+        t.L(p, q) = nl.L(p, q);
+        for (int k = 0; k < 3; ++k) t.D(p, q)[k] = nl.D(p, q)[k];
+        t.R(p, q) = nl.R(p, q);
+      }
+      t.pidx[q] = nl.pidx[q];
+      has[q] = 1;
+    };
+    copy_row(i);
+    t.nnum[i] = nl.nnum[i];
+    for (int ni = 1; ni <= n; ++ni) {
+      if (ni < n) {
+        for (int j = 0; j < t.N; ++j)
+          for (int p = 0; p < t.nnum[j]; ++p) {
+            const int q = t.L(p, j);
+            if (t.nnum[q] == 0) copy_row(q);
+          }
+        for (int j = 0; j < t.N; ++j)
+          if (has[j]) t.nnum[j] = nl.nnum[j];
+      } else {
+        for (int j = 0; j < t.N; ++j)
+          for (int p = 0; p < t.nnum[j]; ++p) {
+            const int q = t.L(p, j);
+            if (t.nnum[q] == 0) {
+              t.nnum[q] = t.nnum[q] + 1;
+              const int s = t.nnum[q] - 1;
+              t.L(s, q) = j;
+              for (int k = 0; k < 3; ++k) t.D(s, q)[k] = -nl.D(p, j)[k];
+              t.R(s, q) = nl.R(p, j);
+              t.pidx[q] = nl.pidx[q];
+              has[q] = 1;
+            }
+          }
+      }
+    }
+  }
+  // shift_drs, md_interactions.f90:377-399 (nl_n == 1): atom row inl moved by -dx along k
+  static void shift_drs(NL& t, int inl, int k, double dx) {
+    for (int p = 0; p < t.nnum[inl]; ++p) {
+      double* d = t.D(p, inl);
+      d[k] = d[k] - dx;
+      t.R(p, inl) = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    }
+    for (int j = 0; j < t.N; ++j)
+      for (int p = 0; p < t.nnum[j]; ++p)
+        if (t.L(p, j) == inl) {
+          double* d = t.D(p, j);
+          d[k] = d[k] + dx;
+          t.R(p, j) = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        }
+  }
+  // calculate_forces_numerically, md_interactions.f90:273-310 (rebosc: neib_order 3)
+  void calculate_forces_numerically() {
+    const double dx = 1e-6;  // 10.**(-6)
+    for (auto& in : inters) {
+      if (in.spec.kind != pfmd_io::K_REBOSC) continue;
+      for (auto& nl : in.nl) {
+#pragma omp parallel
+        {
+          NL t;
+          t.N = nl.N;
+          t.nmax = nl.nmax;
+          create_neighbour_list(t);
+          std::vector<char> has(static_cast<size_t>(t.N), 0);
+#pragma omp for schedule(static)
+          for (int inl = 0; inl < nl.N; ++inl) {
+            calculate_truncated_nl(t, nl, inl, 3, has);
+            for (int k = 0; k < 3; ++k) {
+              shift_drs(t, inl, k, -dx);
+              const double e1 = rebosc_energy(t, in.spec.p);
+              shift_drs(t, inl, k, 2 * dx);
+              const double e2 = rebosc_energy(t, in.spec.p);
+              if (k != 2) shift_drs(t, inl, k, -dx);
+              double& f = atoms.frc[3 * static_cast<size_t>(nl.pidx[inl]) + k];
+              f = f + (e1 - e2) / 2 / dx;
+            }
+          }
+        }
+      }
+    }
+  }
   void calculate_forces() {  // md_interactions.f90:210-242
     for (auto& in : inters) {
       switch (in.spec.kind) {
@@ -979,6 +1122,8 @@ class Sim {
           break;
         case pfmd_io::K_RJL:
           RJL_forces(in.nl[0], in);
+          break;
+        case pfmd_io::K_REBOSC:  // numerical: calculate_forces_numerically
           break;
       }
     }
@@ -1063,6 +1208,8 @@ class Sim {
           }
           return P[0] * Er - P[1] * std::sqrt(Eb2);
         });
+      case pfmd_io::K_REBOSC:
+        return rebosc_energy(nl, P);
       case pfmd_io::K_TB: {  // TersoffBrenner.f90:26-72
         std::vector<double> B;
         tb_bond_order(nl, in, B);
@@ -1340,6 +1487,7 @@ class Sim {
     if (md_step % S.zero_momentum_period == 0) zero_momentum(G(S.all_atoms));
     zero_forces(G(S.all_atoms));
     calculate_forces();
+    calculate_forces_numerically();
     exe_time_forces += omp_get_wtime() - exe_t;
 
     exe_t = omp_get_wtime();
@@ -1606,6 +1754,7 @@ int orc_eval(orc_sim* h, int rebuild, double* e_inter) {
     s.update_interactions_neighbour_lists(step);
     s.zero_forces(s.G(s.S.all_atoms));
     s.calculate_forces();
+    s.calculate_forces_numerically();
     s.calculate_potential_energies();
     if (e_inter)
       for (size_t i = 0; i < s.inters.size(); ++i) e_inter[i] = s.inters[i].energy;

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-CU_SOURCES = ["nlist.cu", "forces_pair.cu", "forces_rjl.cu", "forces_tb.cu", "forces_cos.cu", "integrate.cu", "noalloc.cu", "batch.cu", "learned.cu", "learned_tc.cu",
+CU_SOURCES = ["nlist.cu", "forces_pair.cu", "forces_rjl.cu", "forces_tb.cu", "forces_rebo.cu", "forces_cos.cu", "integrate.cu", "noalloc.cu", "batch.cu", "learned.cu", "learned_tc.cu",
               "engine.cu", "cli.cu", "fit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EXECUTABLES = [("run_md_simulation", "pfmd_run_md_simulation"), ("run_gr_analysis", "pfmd_run_gr_analysis"),

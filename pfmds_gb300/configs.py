@@ -352,12 +352,61 @@ def rotated_graphene(m, n, reps_y=1, a=2.46):
 
 TB_CARBON = (6.325, 1.29, 1.5, 1.315, 0.80469, 0.011304, 19.0, 2.5)  # D S beta r0 delta a0 c0 d0
 
+# rebosc carbon (REBOsolidcarbon.f90:7-25 file layout: A Q alpha / B(3) / beta(3) / T /
+# g(6) / R1 R2).  Pair terms: the carbon set of Brenner et al., J. Phys.: Condens.
+# Matter 14 (2002) 783.  g: the quintic through that paper's six angular knots
+# G(-1, -2/3, -1/2, -1/3, 0, 1) = (-0.01, 0.028207, 0.052804, 0.097321, 0.3, 8.0).
+# T: a small dihedral weight chosen here.  Switch 1.7-2.0 A.
+REBO_CARBON = dict(
+    A=10953.544162170, Q=0.3134602960833, alpha=4.7465390606595,
+    B=(12388.79197798, 17.56740646509, 30.71493208065), beta=(4.7204523127, 1.4332132499, 1.3826912506),
+    T=-0.004048375,
+    g=(0.29999999999999905, 1.0055917166666617, 1.7516746249999886, 2.2404813333333253, 1.943325375000013,
+       0.7589269500000115),
+    R=(1.7, 2.0))
+
+
+def rebo_parameters_text(p=REBO_CARBON):
+    return (f"{p['A']!r}\t{p['Q']!r}\t{p['alpha']!r}\n" + "\t".join(map(repr, p["B"])) + "\n" +
+            "\t".join(map(repr, p["beta"])) + f"\n{p['T']!r}\n" + "\t".join(map(repr, p["g"])) +
+            f"\n{p['R'][0]!r}\t{p['R'][1]!r}\n")
+
+
+def graphene_rebo(d, nx=8, ny=5, seed=11, temperature=300.0, corrugation=0.15, dt=0.5, steps=100,
+                  log_period=10, integrator="nve", period=10, nmax=6, rc_list=2.3, vacuum=20.0,
+                  xyz_name="gr_rebo.xyz", settings_name="md_run_settings.txt"):
+    """A free graphene sheet under rebosc, atoms displaced by up to `corrugation` A
+    (so bond angles and dihedrals are not ideal)."""
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    gpos, (Lx, Ly) = graphene_sheet(nx, ny)
+    gpos[:, 2] = vacuum / 2
+    pos = gpos + rng.uniform(-corrugation, corrugation, size=gpos.shape)
+    pos[:, 0] %= Lx
+    pos[:, 1] %= Ly
+    n = len(pos)
+    types = ["C"] * n
+    mass = np.full(n, 12.011)
+    moving = np.ones(n, bool)
+    vel = maxwell_velocities(rng, mass, moving, temperature)
+    write_xyz(os.path.join(d, xyz_name), (Lx, Ly, vacuum), pos, vel, mass, types)
+    _write(d, "parameters_REBO_C.txt", rebo_parameters_text())
+    q1 = 3 * n * KB * temperature * 100.0 ** 2
+    text = _settings_text(
+        step_limit=steps, xyz_name=xyz_name, types=["C"], groups=[["C"], []], all_moving=1, xyz_moving=1,
+        z_moving=2, all_atoms=1, traj_group=1, period_traj=100000000,
+        integrators=[(integrator, dt, steps, 100000000, log_period)], ms_de=1e-8,
+        nhc=[(1, temperature, 3, q1)], t0=temperature,
+        interactions=[("rebosc", "parameters_REBO_C.txt", [(1, 1, nmax, rc_list, period)])])
+    _write(d, settings_name, text)
+    return settings_name
+
 
 def gr_on_cu(d, n_gx=10, n_gy=6, n_cx=9, n_cy=5, layers=4, fixed_layers=1, a_cu=3.615, height=3.0, vacuum=25.0,
              seed=7, temperature=300.0, disp=0.02, coupling="morsec", simplified=False, dt=0.5, steps=100,
              log_period=10, integrator="nvt", period=10, rotation=None, nhc_tau=100.0, xyz_name="gr_cu.xyz",
              morse=(0.1, 2.2, 1.7, 2.0), morse_r12=(7.0, 8.0), ljc=(0.0168, 2.2, 2.0), ljc_r12=(7.0, 8.0),
-             list_skin=0.5, tb_list=(4, 2.0), settings_name="md_run_settings.txt"):
+             list_skin=0.5, tb_list=(4, 2.0), settings_name="md_run_settings.txt", carbon="tb"):
     """Graphene sheet (tb) on a Cu(111) slab (rjl), coupled by morsec or ljc.
 
     Without `rotation` the sheet has n_gx x n_gy rectangular cells and the Cu
@@ -392,6 +441,7 @@ def gr_on_cu(d, n_gx=10, n_gy=6, n_cx=9, n_cy=5, layers=4, fixed_layers=1, a_cu=
     vel = maxwell_velocities(rng, mass, moving, temperature)
     write_xyz(os.path.join(d, xyz_name), box, pos, vel, mass, list(types))
     _write(d, "parameters_TB_C.txt", " ".join(f"{v}" for v in TB_CARBON) + "\n1.7\t2.0\n")
+    _write(d, "parameters_REBO_C.txt", rebo_parameters_text())
     _write(d, "parameters_RJL_Cu.txt", "0.0855\t1.224\t10.96\t2.278\t2.556\n4.5\t5.0\n")
     if coupling == "morsec":
         _write(d, "parameters_coupling.txt",
@@ -410,7 +460,8 @@ def gr_on_cu(d, n_gx=10, n_gy=6, n_cx=9, n_cy=5, layers=4, fixed_layers=1, a_cu=
         all_moving=4, xyz_moving=4, z_moving=6, all_atoms=5, traj_group=1, period_traj=100000000,
         integrators=[(integrator, dt, steps, 100000000, log_period)], ms_de=1e-8,
         nhc=[(4, temperature, 3, q1)], t0=temperature,
-        interactions=[("tb", "parameters_TB_C.txt", [(1, 1, tb_list[0], tb_list[1], period)]),
+        interactions=[(carbon, "parameters_TB_C.txt" if carbon == "tb" else "parameters_REBO_C.txt",
+                       [(1, 1, tb_list[0], tb_list[1], period)]),
                       ("rjl", "parameters_RJL_Cu.txt", [(2, 2, 64, 5.5, period)]),
                       (coupling, "parameters_coupling.txt", [(1, 2, 160, rc_c, period), (2, 1, 160, rc_c, period),
                                                              (1, 1, 3, 1.8, period)])])

@@ -211,6 +211,7 @@ struct InterH {
   CosPar cp{};
   RJLPar rjl{};
   TBPar tb{};
+  REBOPar rebo{};
   bool general = false;  // lj1g weights for a group not in ascending atom order
   DBuf<double> scratch;  // rjl 1/Eb, tb bond orders
   DBuf<double2> pair;    // rjl plain form: per-slot force coefficients
@@ -515,9 +516,11 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
 
   // interactions and their lists (create_interactions, md_interactions.f90:59-136)
   if (S.interactions.size() > PFMD_MAX_INTER) throw Error(PFMD_E_PARAM, "error: too many interactions");
+  // the first tb or rebosc interaction gives ljc / morsec their graphene
+  // neighbours (md_interactions.f90:158-164)
   int first_tb = -1;
   for (size_t k = 0; k < S.interactions.size(); ++k)
-    if (S.interactions[k].kind == pfmd_io::K_TB) {
+    if (S.interactions[k].kind == pfmd_io::K_TB || S.interactions[k].kind == pfmd_io::K_REBOSC) {
       first_tb = static_cast<int>(k);
       break;
     }
@@ -599,10 +602,15 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
         I.tb = TBPar{p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[6] * p[6], p[7] * p[7], {}, {}};
         derive(I.tb);
         break;
+      case pfmd_io::K_REBOSC:
+        I.rebo = REBOPar{p[0], p[1], p[2], {p[3], p[4], p[5]}, {p[6], p[7], p[8]}, p[9],
+                         {p[10], p[11], p[12], p[13], p[14], p[15]}, p[16], p[17]};
+        break;
     }
     if (sp.kind == pfmd_io::K_LJ || sp.kind == pfmd_io::K_LJ1G) derive(I.lj);
     if (sp.kind == pfmd_io::K_LJC || sp.kind == pfmd_io::K_MORSEC) derive(I.cp, sp.kind == pfmd_io::K_MORSEC);
-    if (sp.kind == pfmd_io::K_LJ1G || sp.kind == pfmd_io::K_RJL || sp.kind == pfmd_io::K_TB) {
+    if (sp.kind == pfmd_io::K_LJ1G || sp.kind == pfmd_io::K_RJL || sp.kind == pfmd_io::K_TB ||
+        sp.kind == pfmd_io::K_REBOSC) {
       // the reference indexes these lists' partners through the row arrays
       // (particle_index(nlist), Eb(nlist), nl%nlist(:,j)), which needs g1 == g2
       if (l1.g1 != l1.g2)
@@ -770,6 +778,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     }
     if (I.spec.kind == pfmd_io::K_TB)
       I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));  // B per list slot
+    if (I.spec.kind == pfmd_io::K_REBOSC)  // bsp, dbsp/dS and bdh per list slot
+      I.scratch.alloc(std::max<size_t>(3 * static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));
     if (I.lists[2] >= 0) {
       I.norm.alloc(static_cast<size_t>(std::max(N, 1)));  // normals per atom
       I.norm.zero(st);
@@ -779,7 +789,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     // lists whose kernels address a partner's row: tb (and the nn selection that
     // reads it), lj1g in a group that is not in ascending atom order
     std::vector<int> need;
-    if (I.spec.kind == pfmd_io::K_TB || (I.spec.kind == pfmd_io::K_LJ1G && I.general)) need.push_back(I.lists[0]);
+    if (I.spec.kind == pfmd_io::K_TB || I.spec.kind == pfmd_io::K_REBOSC || (I.spec.kind == pfmd_io::K_LJ1G && I.general))
+      need.push_back(I.lists[0]);
     for (int li : need) {
       ListH& L = lists[static_cast<size_t>(li)];
       if (L.row_of.p) continue;
@@ -1104,6 +1115,9 @@ void Engine::enqueue_forces(bool energy, bool kick) {
         break;
       case pfmd_io::K_TB:
         launch_tb(prec, energy, L1, I.tb, A, box, I.scratch.p, ctl, eslot, key, st, 3, epi(first, last));
+        break;
+      case pfmd_io::K_REBOSC:
+        launch_rebo(energy, L1, I.rebo, A, box, I.scratch.p, ctl, eslot, key, st, 3, epi(first, last));
         break;
       case pfmd_io::K_LJC:
       case pfmd_io::K_MORSEC:
@@ -1803,6 +1817,11 @@ double Engine::kernel_bytes(const std::string& name) {
       if (name == "rjl_force") return row_bytes(L1, IE + F, PC);
       if (name == "forces") b += row_bytes(L1, IE, PC) + row_bytes(L1, IE + F, PC);
     }
+    if (k == pfmd_io::K_REBOSC) {
+      if (name == "rebo_bond") return row_bytes(L1, 0, 24.0);
+      if (name == "rebo_force") return row_bytes(L1, F, 24.0);
+      if (name == "forces") b += row_bytes(L1, 0, 24.0) + row_bytes(L1, F, 24.0);
+    }
     if (k == pfmd_io::K_TB) {
       if (name == "tb_bond") return row_bytes(L1, 0, 8.0);
       if (name == "tb_force") return row_bytes(L1, F, 8.0);
@@ -1870,6 +1889,10 @@ double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
       if (kind == pfmd_io::K_RJL && (name == "rjl_density" || name == "rjl_force")) {
         launch_rjl(prec, false, L1, I.rjl, A, box, I.scratch.p, I.pair.p, ctl, eslot, 0, st,
                    name == "rjl_density" ? 1 : 2);
+        return true;
+      }
+      if (kind == pfmd_io::K_REBOSC && (name == "rebo_bond" || name == "rebo_force")) {
+        launch_rebo(false, L1, I.rebo, A, box, I.scratch.p, ctl, eslot, 0, st, name == "rebo_bond" ? 1 : 2);
         return true;
       }
       if (kind == pfmd_io::K_TB && (name == "tb_bond" || name == "tb_force")) {

@@ -119,6 +119,10 @@ struct TBPar {
   TBc<double> dd;
   TBc<float> f;
 };
+// rebosc, REBOsolidcarbon.f90:7-9: A Q alpha / B(3) / beta(3) / T / g(6) / R1 R2.
+struct REBOPar {
+  double A, Q, alpha, B[3], beta[3], T, g[6], R1, R2;
+};
 // Fill the derived constants of a parameter set.
 void derive(LJPar& P);
 void derive(CosPar& P, bool morse);
@@ -180,6 +184,10 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
 void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const Atoms& A, const Box& B,
                double* Bbuf, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts = 3,
                const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
+// rebosc (FP64 in both forms).  S3: 3 x nmax x stride doubles (per slot bsp,
+// dbsp/dS, bdh).  parts: 1 bond terms, 2 force
+void launch_rebo(bool energy, const ListDev& L, const REBOPar& P, const Atoms& A, const Box& B, double* S3, Ctl* ctl,
+                 int eslot, int ekey, cudaStream_t s, int parts = 3, const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
 // parts: 1 graphene side, 2 metal side
 void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
                 const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot,

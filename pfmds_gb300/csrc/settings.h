@@ -26,7 +26,7 @@ struct NLSpec {
   long long period = 1;
 };
 
-enum InterKind { K_LJ = 0, K_LJ1G = 1, K_LJC = 2, K_MORSEC = 3, K_RJL = 4, K_TB = 5 };
+enum InterKind { K_LJ = 0, K_LJ1G = 1, K_LJC = 2, K_MORSEC = 3, K_RJL = 4, K_TB = 5, K_REBOSC = 6 };
 
 struct InteractionSpec {
   std::string name;        // lj lj1g ljc morsec rjl tb
@@ -160,6 +160,14 @@ inline void read_params(InteractionSpec& in, const std::string& path) {
       break;
     case K_TB:  // TersoffBrenner.f90:13-24
       reals(8);
+      reals(2);
+      break;
+    case K_REBOSC:  // REBOsolidcarbon.f90:12-25: A Q alpha / B / beta / T / g / R1 R2
+      reals(3);
+      reals(3);
+      reals(3);
+      reals(1);
+      reals(6);
       reals(2);
       break;
   }
@@ -343,6 +351,9 @@ inline void read_settings(const std::string& input_path, const std::string& sett
       in.nl_n = 1;
     } else if (in.name == "rjl") {
       in.kind = K_RJL;
+      in.nl_n = 1;
+    } else if (in.name == "rebosc") {
+      in.kind = K_REBOSC;
       in.nl_n = 1;
     } else {
       // md_interactions.f90:119-120 prints this and carries on with an unset list

@@ -81,7 +81,7 @@ def test_fit_matches_the_oracle_restatement(tmp_path, built):
     for g, c in zip(gpu, cpu):
         fg, fc = _fields(g), _fields(c)
         assert fg[:5] == fc[:5], (g, c)  # evaluation number and parameters
-        assert np.allclose(fg[5:], fc[5:], rtol=0, atol=2.5e-6), (g, c)
+        assert np.allclose(fg[5:], fc[5:], rtol=1e-7, atol=5e-6), (g, c)  # printed to 6 decimals
     # every evaluation left its numbered parameter file and both final files
     for k in range(1, len(gpu) + 1):
         assert (tmp_path / "gpu" / "in" / f"{k:06d}parameters_coupling.txt").exists()
