@@ -54,10 +54,13 @@ typedef struct pfmd_options {
   int device;                /* CUDA device ordinal */
   int use_graphs;            /* capture repeated step segments in CUDA graphs */
   int threads_per_row;       /* force-kernel threads per list row: 1,2,4,...,32, 0 = automatic */
+  int async_io;              /* 1: snapshot and trajectory files are formatted and written by a
+                                background thread while the next steps run (complete when
+                                pfmd_finish / pfmd_md / pfmd_destroy returns); 0: at the event */
 } pfmd_options;
 
 /* Defaults of run_md_simulation.f90:10-24 (out_period 1, seed 1, no prefix),
- * plain form, device 0, graphs on. */
+ * plain form, device 0, graphs on, background file writing on. */
 void pfmd_default_options(pfmd_options* opt);
 
 /* ---- set-up and teardown ----------------------------------------------- */

@@ -13,8 +13,14 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <climits>
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -226,6 +232,86 @@ struct StepPlan {
   std::vector<char> rebuild;  // per list
 };
 
+// Snapshot and trajectory files (md_read_write.f90:65-107) are formatted and
+// written by one worker thread, in submission order, while the device runs the
+// next steps.  The state is copied to the host before a job is queued, so each
+// file holds its own step.  At most four jobs wait (the submitter blocks beyond
+// that); the first write error is kept for the engine to raise.
+class FileWriter {
+ public:
+  using Format = std::function<std::string()>;
+  FileWriter() : th_([this] { loop(); }) {}
+  ~FileWriter() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    if (th_.joinable()) th_.join();
+  }
+  void submit(std::string path, bool append, Format f) {
+    std::unique_lock<std::mutex> lk(mu_);
+    room_.wait(lk, [&] { return q_.size() < kMaxPending; });
+    q_.push_back(Job{std::move(path), append, std::move(f)});
+    cv_.notify_one();
+  }
+  // Waits for every queued job; returns the first error ("" if none).
+  std::string drain() {
+    std::unique_lock<std::mutex> lk(mu_);
+    room_.wait(lk, [&] { return q_.empty() && !busy_; });
+    return err_;
+  }
+  std::string error() {
+    std::lock_guard<std::mutex> lk(mu_);
+    return err_;
+  }
+  // Formats and writes one file on the calling thread (what the worker does).
+  static std::string write(const std::string& path, bool append, const Format& f) {
+    const std::string text = f();
+    if (text.empty()) return "";
+    FILE* fp = std::fopen(path.c_str(), append ? "a" : "w");
+    if (!fp) return "cannot open " + path;
+    std::fputs(text.c_str(), fp);
+    std::fclose(fp);
+    return "";
+  }
+
+ private:
+  struct Job {
+    std::string path;
+    bool append = false;
+    Format f;
+  };
+  void loop() {
+    for (;;) {
+      Job j;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || !q_.empty(); });
+        if (q_.empty()) return;
+        j = std::move(q_.front());
+        q_.pop_front();
+        busy_ = true;
+      }
+      room_.notify_all();
+      const std::string e = write(j.path, j.append, j.f);
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        busy_ = false;
+        if (!e.empty() && err_.empty()) err_ = e;
+      }
+      room_.notify_all();
+    }
+  }
+  static constexpr size_t kMaxPending = 4;
+  std::mutex mu_;
+  std::condition_variable cv_, room_;
+  std::deque<Job> q_;
+  bool stop_ = false, busy_ = false;
+  std::string err_;
+  std::thread th_;  // declared last: starts once the members above exist
+};
+
 class Engine {
  public:
   pfmd_options opt{};
@@ -353,10 +439,14 @@ class Engine {
   void run_plans(const std::vector<StepPlan>& plans);
   void host_events(const StepPlan& p);
   void get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f);
+  std::unique_ptr<FileWriter> writer;  // snapshot / trajectory files (opt.async_io)
+  void emit_file(const std::string& path, bool append, FileWriter::Format f);
+  void check_writer(bool wait);
   std::string nlists_load_text();
 };
 
 Engine::~Engine() {
+  writer.reset();  // its queued jobs read this engine's groups and types
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   for (auto& kv : graphs)
@@ -832,6 +922,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     std::string ln = prefix + fortio::trim(S.logfilename);
     log = std::fopen(ln.c_str(), "w");
     if (!log) throw Error(PFMD_E_IO, "cannot open log file " + ln);
+    if (opt.async_io) writer.reset(new FileWriter());
   }
   outln(fortio::Rec().a("PREPARATIONS TIME: ", 24).f(now_s() - t_start, 10, 2).a(" S ").s);
   outln(fortio::Rec().a("RUNNING ON ", 24).i(opt.num_threads, 6).a(" OPENMP THREADS").s);
@@ -1350,34 +1441,48 @@ void Engine::host_events(const StepPlan& p) {
   }
   const bool snap = opt.write_files && s % I.period_snapshot == 0 && s != 0;
   const bool traj = opt.write_files && s % S.period_traj == 0;
+  check_writer(false);
   if (snap || traj) {
-    std::vector<double> hp, hv;
-    get_state_host(hp, hv, nullptr);
+    // the step's state, shared by the jobs that format it
+    auto st8 = std::make_shared<std::pair<std::vector<double>, std::vector<double>>>();
+    get_state_host(st8->first, st8->second, nullptr);
+    const std::array<double, 3> L3 = {box.L[0], box.L[1], box.L[2]};
+    const double* mass = S.xyz.mass.data();
+    const std::vector<std::string>* types = &S.xyz.types;
     if (snap) {
-      std::string fn = prefix + "snapshot_" + fortio::fmt_i0pad(s, 6, 6) + ".xyz";
       const auto& g = groups[static_cast<size_t>(S.all_atoms - 1)];
       const int gn = hctl->group_n[S.all_atoms - 1];
-      std::string text = pfmd_io::xyz_snapshot_text(box.L, gn, g.idx.data(), hp.data(), hv.data(),
-                                                    S.xyz.mass.data(), S.xyz.types);
-      FILE* f = std::fopen(fn.c_str(), "w");
-      if (!f) throw Error(PFMD_E_IO, "cannot open " + fn);
-      std::fputs(text.c_str(), f);
-      std::fclose(f);
+      const int* idx = g.idx.data();
+      emit_file(prefix + "snapshot_" + fortio::fmt_i0pad(s, 6, 6) + ".xyz", false, [=] {
+        return pfmd_io::xyz_snapshot_text(L3.data(), gn, idx, st8->first.data(), st8->second.data(), mass, *types);
+      });
     }
     if (traj) {
-      std::string fn = prefix + "traj_" + fortio::fmt_i0pad(S.traj_group, 2, 2) + ".xyz";
       const auto& g = groups[static_cast<size_t>(S.traj_group - 1)];
       const int gn = hctl->group_n[S.traj_group - 1];
-      std::string text = pfmd_io::xyz_traj_frame_text(box.L, gn, g.idx.data(), hp.data(), hv.data(),
-                                                      S.xyz.mass.data(), S.xyz.types, s);
-      if (!text.empty()) {
-        FILE* f = std::fopen(fn.c_str(), "a");
-        if (!f) throw Error(PFMD_E_IO, "cannot open " + fn);
-        std::fputs(text.c_str(), f);
-        std::fclose(f);
-      }
+      const int* idx = g.idx.data();
+      emit_file(prefix + "traj_" + fortio::fmt_i0pad(S.traj_group, 2, 2) + ".xyz", true, [=] {
+        return pfmd_io::xyz_traj_frame_text(L3.data(), gn, idx, st8->first.data(), st8->second.data(), mass, *types,
+                                            s);
+      });
     }
   }
+}
+
+void Engine::emit_file(const std::string& path, bool append, FileWriter::Format f) {
+  if (writer) {
+    writer->submit(path, append, std::move(f));
+    return;
+  }
+  const std::string e = FileWriter::write(path, append, f);
+  if (!e.empty()) throw Error(PFMD_E_IO, e);
+}
+
+// Raises the background writer's first error; wait: after the queued files are written.
+void Engine::check_writer(bool wait) {
+  if (!writer) return;
+  const std::string e = wait ? writer->drain() : writer->error();
+  if (!e.empty()) throw Error(PFMD_E_IO, e);
 }
 
 void Engine::advance(long long max_steps, int* fin) {
@@ -1466,6 +1571,7 @@ void Engine::finish() {
   for (size_t k = 0; k < inters.size(); ++k) r.f(c.e_inter[k], 20, 9);
   write_all_out(r.s);
   if (log) std::fputs((r.s + "\n").c_str(), log);
+  check_writer(true);  // every snapshot and trajectory frame is on disk
   if (md_step != 0 && opt.write_files) {
     std::vector<double> hp, hv;
     get_state_host(hp, hv, nullptr);
@@ -1967,6 +2073,7 @@ void pfmd_default_options(pfmd_options* o) {
   o->device = 0;
   o->use_graphs = 1;
   o->threads_per_row = 0;
+  o->async_io = 1;
 }
 
 int pfmd_create_from_files(const char* input_path, const char* settings_filename, const pfmd_options* opt,

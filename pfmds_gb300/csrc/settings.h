@@ -11,8 +11,10 @@
 // checked, only their order matters (as in the reference).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fortio.h"
@@ -377,6 +379,62 @@ inline void read_settings(const std::string& input_path, const std::string& sett
   }
 }
 
+// Fw.d appended to out (fortio::fmt_f without temporaries).
+inline void put_f(std::string& out, double x, int w, int d) {
+  if (!std::isfinite(x)) {
+    out += fortio::fmt_f(x, w, d);
+    return;
+  }
+  char buf[512];
+  int n = std::snprintf(buf, sizeof buf, "%.*f", d, x);
+  const char* s = buf;
+  if (n > w) {  // drop the optional leading zero of "0.xxx" / "-0.xxx"
+    if (buf[0] == '0' && buf[1] == '.') {
+      ++s;
+      --n;
+    } else if (buf[0] == '-' && buf[1] == '0' && buf[2] == '.') {
+      buf[1] = '-';
+      ++s;
+      --n;
+    }
+  }
+  if (n > w) {
+    out.append(static_cast<size_t>(w), '*');
+    return;
+  }
+  out.append(static_cast<size_t>(w - n), ' ');
+  out.append(s, static_cast<size_t>(n));
+}
+
+// The per-atom lines of a file, line(k, out) for k = 0..n-1, formatted by up to
+// 16 threads in contiguous chunks when n is large; the text is that of one pass.
+template <class F>
+inline std::string atom_lines(int n, F line) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = n < 8192 ? 1 : static_cast<int>(std::min(16u, hw));
+  std::vector<std::string> part(static_cast<size_t>(nt));
+  auto run = [&](int t) {
+    const int k0 = static_cast<int>(static_cast<long long>(n) * t / nt);
+    const int k1 = static_cast<int>(static_cast<long long>(n) * (t + 1) / nt);
+    part[static_cast<size_t>(t)].reserve(static_cast<size_t>(k1 - k0) * 240);
+    for (int k = k0; k < k1; ++k) line(k, part[static_cast<size_t>(t)]);
+  };
+  if (nt == 1) {
+    run(0);
+    return std::move(part[0]);
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(run, t);
+  run(0);
+  for (auto& x : th) x.join();
+  size_t tot = 0;
+  for (const auto& p : part) tot += p.size();
+  std::string out;
+  out.reserve(tot);
+  for (const auto& p : part) out += p;
+  return out;
+}
+
 // write_particle_group (md_read_write.f90:65-83): a new .xyz file with a group's atoms.
 inline std::string xyz_snapshot_text(const double box[3], int n, const int* idx, const double* pos,
                                      const double* vel, const double* mass,
@@ -390,14 +448,15 @@ inline std::string xyz_snapshot_text(const double box[3], int n, const int* idx,
   h.f(0.0, 16, 6).f(0.0, 16, 6).f(0.0, 16, 6).f(box[2], 16, 6);
   h.a(" \" Properties=pos:R:3:vel:R:3:mass:R:1:species:S:1");
   out += h.s + "\n";
-  for (int k = 0; k < n; ++k) {
-    int i = idx[k];
-    Rec a;
-    for (int c = 0; c < 3; ++c) a.f(pos[3 * i + c], 27, 16);
-    for (int c = 0; c < 3; ++c) a.f(vel[3 * i + c], 27, 16);
-    a.f(mass[i], 27, 16).a("    ").a(types[static_cast<size_t>(i)], -1, 32);
-    out += a.s + "\n";
-  }
+  out += atom_lines(n, [&](int k, std::string& o) {
+    const int i = idx[k];
+    for (int c = 0; c < 3; ++c) put_f(o, pos[3 * i + c], 27, 16);
+    for (int c = 0; c < 3; ++c) put_f(o, vel[3 * i + c], 27, 16);
+    put_f(o, mass[i], 27, 16);
+    o += "    ";
+    o += fmt_a(types[static_cast<size_t>(i)], -1, 32);
+    o += "\n";
+  });
   return out;
 }
 
@@ -415,14 +474,15 @@ inline std::string xyz_traj_frame_text(const double box[3], int n, const int* id
   h.f(0.0, 10, 4).f(0.0, 10, 4).f(0.0, 10, 4).f(box[2], 10, 4);
   h.a(" \" Properties=pos:R:3:vel:R:3:mass:R:1:species:S:1");
   out += h.s + "\n";
-  for (int k = 0; k < n; ++k) {
-    int i = idx[k];
-    Rec a;
-    for (int c = 0; c < 3; ++c) a.f(pos[3 * i + c], 10, 4);
-    for (int c = 0; c < 3; ++c) a.f(vel[3 * i + c], 10, 4);
-    a.f(mass[i], 10, 4).a("    ").a(trim(types[static_cast<size_t>(i)]));
-    out += a.s + "\n";
-  }
+  out += atom_lines(n, [&](int k, std::string& o) {
+    const int i = idx[k];
+    for (int c = 0; c < 3; ++c) put_f(o, pos[3 * i + c], 10, 4);
+    for (int c = 0; c < 3; ++c) put_f(o, vel[3 * i + c], 10, 4);
+    put_f(o, mass[i], 10, 4);
+    o += "    ";
+    o += trim(types[static_cast<size_t>(i)]);
+    o += "\n";
+  });
   return out;
 }
 

@@ -104,3 +104,17 @@ def test_list_directed_input(shim):
                                  ("1.5-3", 1.5e-3), ("2.278", 2.278), ("-0.25e1", -2.5)])
 def test_real_input(shim, s, v):
     assert shim.sh_to_real(s.encode()) == v
+
+
+@pytest.mark.parametrize("x,w,d", [(0.5, 27, 16), (-0.5, 27, 16), (0.25, 3, 2), (-0.25, 4, 2), (-0.25, 3, 2),
+                                   (123.456, 10, 4), (-1e9, 10, 4), (0.0, 10, 4), (-0.0, 27, 16),
+                                   (1.0 / 3.0, 27, 16), (99999.99999, 10, 4), (float("nan"), 10, 4),
+                                   (float("-inf"), 27, 16)])
+def test_xyz_writer_f_matches_fmt_f(shim, x, w, d):
+    assert call(shim, "sh_put_f", x, w, d) == call(shim, "sh_fmt_f", x, w, d)
+
+
+@pytest.mark.parametrize("n", [5, 20000])
+def test_threaded_snapshot_text_matches_line_by_line(shim, n):
+    shim.sh_snapshot_matches.argtypes = [C.c_int, C.c_double]
+    assert shim.sh_snapshot_matches(n, 0.731) == 1
