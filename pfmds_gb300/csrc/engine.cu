@@ -1944,6 +1944,8 @@ double Engine::kernel_bytes(const std::string& name) {
     b += 32.0 * static_cast<double>(groups[static_cast<size_t>(S.all_atoms - 1)].idx.size());  // zero_forces
     return b;
   }
+  if (name == "kick_drift")  // force, velocity, position, kc read; velocity, position, posq written
+    return 160.0 * static_cast<double>(groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size());
   if (name == "lists") {
     for (auto& L : lists) {
       if (L.kind == L_NN_TB) continue;
@@ -1967,6 +1969,11 @@ double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
     if (name == "forces") {
       launch_zero_forces(gref(S.all_atoms), A, ctl, st);
       enqueue_forces(false);
+      return true;
+    }
+    if (name == "kick_drift") {
+      // zero time steps: the same loads, FP64 work and stores, the state unchanged
+      launch_kick_drift(gref(S.xyz_moving), 0.0, 0.0, true, 0, !prec, A, box, ctl, st, false);
       return true;
     }
     if (name == "lists") {

@@ -38,17 +38,22 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
       if constexpr (PREC) {
         // r and 1/r from one reciprocal square root
         const float ir = rsqrtf(r2), r = r2 * ir;
-        float2 ab = make_float2(0.f, 0.f);
-        if (r <= c.R2) {
-          float fc, rdfc;
-          fdfrcut_cos_f(r, c.R1, c.R2, c.inv_w, fc, rdfc);
-          const float x = r * c.inv_r0 - 1.f;
-          const float eq = __expf(c.m2q * x), ep = __expf(c.mp * x);
-          eb2.add(eq * fc);
-          if (ENERGY) er.add(ep * fc);
-          ab.x = c.a2 * (c.pr0 * fc - rdfc) * ep * ir;
-          ab.y = c.xi * (c.qr0 * fc - 0.5f * rdfc) * eq * ir;
-        }
+        // the cosine switch without branches: t is 0 below R1 and 1 from R2 on; entries
+        // beyond R2 (about a fifth of the 5.5 A list) are masked, not skipped, so the
+        // warp stays converged
+        const float t = __saturatef((r - c.R1) * c.inv_w);
+        float sn, cs;
+        __sincosf(3.14159265358979f * t, &sn, &cs);
+        const float in = r <= c.R2 ? 1.f : 0.f;
+        const float fc = (0.5f + 0.5f * cs) * in;
+        const float rdfc = -sn * (3.14159265358979f * 0.5f) * c.inv_w * in;
+        const float x = r * c.inv_r0 - 1.f;
+        const float eq = __expf(c.m2q * x), ep = __expf(c.mp * x);
+        eb2.add(eq * fc);
+        if (ENERGY) er.add(ep * fc);
+        float2 ab;
+        ab.x = c.a2 * (c.pr0 * fc - rdfc) * ep * ir;
+        ab.y = c.xi * (c.qr0 * fc - 0.5f * rdfc) * eq * ir;
         reinterpret_cast<float2*>(pair)[(size_t)p * L.stride + g.row] = ab;
       } else {
         const R r = sqrt(r2);
@@ -115,7 +120,9 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
       ieb_i = __int_as_float(pi.w);
     else
       ieb_i = ieb[ai];
-#pragma unroll 4
+    // unroll 2: measured faster than 4 or 8 on the 65,536-atom slab (fewer live
+    // registers, more resident warps for the gather latency)
+#pragma unroll 2
     for (int p = g.sub; p < n; p += TPA) {
       const int aj = ent(L, g.row, p);
       R dr[3];

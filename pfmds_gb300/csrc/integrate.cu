@@ -170,9 +170,23 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
 // begin: also do k_step_begin's work for an nve step without group changes: every
 // thread checks the previous drift's out-of-cell verdict, one thread advances the
 // step counter and the previous-step potential energy.
+// The atom's force, velocity, position and mass are loaded before the control
+// block is read (any index below the group's capacity names a valid atom), so
+// those loads overlap instead of forming a chain of dependent round trips.
 template <bool EXACT>
 __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, int begin, Atoms A,
                              Box B, Ctl* ctl) {
+  const int ind = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool have = ind < g.cap;
+  const int i = have ? g.idx[ind] : 0;
+  double4_32a f = make_double4_32a(0.0, 0.0, 0.0, 0.0), v = f, p = f;
+  double km = 0.0;  // kc (fast kick) or the mass (exact kick)
+  if (have) {
+    f = A.frc[i];
+    v = A.vel[i];
+    p = A.pos[i];
+    km = EXACT ? A.mass[i] : A.kc[i];
+  }
   if (ctl->stop) return;
   if (begin) {
     if (ctl->pending_oob) {
@@ -185,11 +199,7 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
       ctl->pe_prev = ctl->pe_last;
     }
   }
-  const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   if (ind >= ctl->group_n[g.g]) return;
-  const int i = g.idx[ind];
-  const double4_32a f = A.frc[i];
-  double4_32a v = A.vel[i];
   if (nhc_scale) {
     const double s = ctl->nhc[nhc_scale - 1].s;
     v.x *= s;
@@ -197,18 +207,16 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
     v.z *= s;
   }
   if (EXACT) {
-    const double m = A.mass[i];
-    v.x = kick1(v.x, f.x, m, ts2);
-    v.y = kick1(v.y, f.y, m, ts2);
-    v.z = kick1(v.z, f.z, m, ts2);
+    v.x = kick1(v.x, f.x, km, ts2);
+    v.y = kick1(v.y, f.y, km, ts2);
+    v.z = kick1(v.z, f.z, km, ts2);
   } else {
-    const double kt = A.kc[i] * ts2;
+    const double kt = km * ts2;
     v.x = kick1_fast(v.x, f.x, kt);
     v.y = kick1_fast(v.y, f.y, kt);
     v.z = kick1_fast(v.z, f.z, kt);
   }
   A.vel[i] = v;
-  double4_32a p = A.pos[i];
   if (EXACT) {
     p.x = drift1(p.x, v.x, ts1, B.L[0]);
     p.y = drift1(p.y, v.y, ts1, B.L[1]);

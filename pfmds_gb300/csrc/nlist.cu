@@ -46,29 +46,48 @@ __global__ void k_bin_count(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
   atomicAdd(&cg.count[c], 1);
 }
 
-__global__ void k_bin_scan(CellGrid cg, Ctl* ctl) {
+// Exclusive scan of the cell counts by one block of 1024 threads: 1024 cells per
+// pass (coalesced), shuffles within each warp, a second shuffle level over the 32
+// warp totals, and a carry from pass to pass.
+__global__ void __launch_bounds__(1024) k_bin_scan(CellGrid cg, Ctl* ctl) {
   if (ctl->stop) return;
-  __shared__ int sh[1024];
-  const int n = cg.ncell, t = threadIdx.x, nt = blockDim.x;
-  const int chunk = (n + nt - 1) / nt;
-  const int b = t * chunk, e = min(n, b + chunk);
-  int s = 0;
-  for (int c = b; c < e; ++c) s += cg.count[c];
-  sh[t] = s;
+  __shared__ int wsum[32];
+  __shared__ int carry_s;
+  const int n = cg.ncell, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) carry_s = 0;
   __syncthreads();
-  for (int o = 1; o < nt; o <<= 1) {  // inclusive Hillis-Steele scan
-    int v = t >= o ? sh[t - o] : 0;
+  for (int base = 0; base < n; base += 1024) {
+    const int c = base + t;
+    const int v = c < n ? cg.count[c] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    sh[t] += v;
+    if (w == 0) {
+      int s = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      wsum[lane] = s;
+    }
+    __syncthreads();
+    const int carry = carry_s;
+    const int excl = carry + (w ? wsum[w - 1] : 0) + x - v;
+    if (c < n) {
+      cg.start[c] = excl;
+      cg.cursor[c] = excl;
+    }
+    __syncthreads();  // every thread has read carry_s and wsum
+    if (t == 1023) carry_s = carry + wsum[31];
     __syncthreads();
   }
-  int run = sh[t] - s;
-  for (int c = b; c < e; ++c) {
-    cg.start[c] = run;
-    cg.cursor[c] = run;
-    run += cg.count[c];
-  }
-  if (t == nt - 1) cg.start[n] = sh[t];
+  if (t == 0) cg.start[n] = carry_s;
 }
 
 __global__ void k_bin_scatter(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
