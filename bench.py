@@ -332,7 +332,7 @@ def learned_config(root, device, frames=200, run_steps=1000):
         s = pf.Simulation(dT, form="plain", out_period=10 ** 9, device=device)
         out = os.path.join(root, f"learned_{int(T)}.bin")
         r, fr = s.learned_train(out, frames=frames, stride=5, iters=8, lr=2e-3 if model is None else 1e-3,
-                                model_in=model, force_weight=1.0)
+                                model_in=model, force_weight=1.0, tensor_cores=True)
         train.append({"temperature": T, "atoms": s.natoms, "energy_rmse_eV": {"C_tb": r[0], "Cu_rjl": r[1]},
                       "force_rmse_eV_per_A": fr})
         model = out
@@ -355,6 +355,16 @@ def learned_config(root, device, frames=200, run_steps=1000):
         if form.startswith("learned"):
             res[form]["force_rmse_vs_classical_eV_per_A"] = s.learned_check()
         s.close()
+    # one training gradient (energies and force matching) of both networks on the
+    # large system: the FP32 CUDA-core kernel against the tcgen05 kernel
+    s = pf.Simulation(dbig, form="plain", out_period=10 ** 9, device=device)
+    grad_ms = {}
+    for tc in (False, True):
+        s.learned_gradient(model, tensor_cores=tc, n_networks=2)  # warm-up
+        grad_ms["tensor_cores" if tc else "fp32"] = min(
+            s.learned_gradient(model, tensor_cores=tc, n_networks=2, timed=True)[2] for _ in range(3))
+    s.close()
+    res["training_gradient_ms"] = grad_ms
     # the checked run: classical kernels judge the networks every 100 steps
     s = pf.Simulation(dbig, form="precision", out_period=10 ** 9, device=device)
     s.learned_use(model, check_period=100, max_rmse=0.05, tensor_cores=True)
@@ -372,6 +382,8 @@ def learned_config(root, device, frames=200, run_steps=1000):
         "precision": res["precision"], "learned": res["learned"],
         "learned_tensor_cores": res["learned_tensor_cores"], "plain": res["plain"],
         "checked_run": res["checked_run"],
+        "training_gradient_ms": res["training_gradient_ms"],
+        "training_kernels": "tcgen05 (BF16 operands, FP32 accumulation); fp32 beside it",
         "learned_speedup_vs_plain": res["learned_tensor_cores"]["value"] / res["plain"]["value"],
         "learned_vs_precision": res["learned_tensor_cores"]["value"] / res["precision"]["value"],
         "check": "classical kernels recompute the forces every 100 steps; RMSE above 0.05 eV/A switches back"}

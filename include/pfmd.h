@@ -212,14 +212,26 @@ int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
  * (eV) on the last frame; force_rmse (may be NULL): learned against plain force
  * RMSE (eV/A) over all atoms on the last frame. */
 int pfmd_learned_train(pfmd_ctx* ctx, const char* model_in, const char* model_out, int frames, int stride,
-                       int iters, double lr, double force_weight, double* rmse, double* force_rmse);
+                       int iters, double lr, double force_weight, int flags, double* rmse, double* force_rmse);
+/* flags of pfmd_learned_train / pfmd_learned_gradient / pfmd_learned_use:
+ * PFMD_LEARNED_TENSOR_CORES runs the networks (training: forward, tangent, backward
+ * and the weight-gradient sums) on the tensor cores, BF16 operands with FP32
+ * accumulation; otherwise FP32 on the CUDA cores. */
+#define PFMD_LEARNED_TENSOR_CORES 1
+/* Floats per network in a gradient (and in a model file's weight block). */
+#define PFMD_LEARNED_NET_FLOATS 7361
+/* The training-loss gradient of the networks in model_in (NULL: new networks,
+ * normalised on this configuration) at the current configuration, with the
+ * loss of pfmd_learned_train, and no update: grad receives PFMD_LEARNED_NET_FLOATS
+ * floats per network (in interaction order: W1, b1, W2, b2, w3, b3), loss (may be
+ * NULL) the sum of squared per-atom energy errors of each network, device_ms (may
+ * be NULL) the device time of the gradient kernels. */
+int pfmd_learned_gradient(pfmd_ctx* ctx, const char* model_in, double force_weight, int flags, float* grad,
+                          double* loss, double* device_ms);
 /* Switches the context's tb and rjl interactions to the networks in model_path.
  * Every check_period steps (0: never) the classical kernels recompute the forces
  * of the same configuration; if the RMSE between the two exceeds max_rmse (eV/A)
- * the run falls back to the classical kernels for good.  flags:
- * PFMD_LEARNED_TENSOR_CORES runs the networks on the tensor cores (BF16 weights
- * and activations, FP32 accumulation); otherwise FP32 on the CUDA cores. */
-#define PFMD_LEARNED_TENSOR_CORES 1
+ * the run falls back to the classical kernels for good.  flags as above. */
 int pfmd_learned_use(pfmd_ctx* ctx, const char* model_path, long long check_period, double max_rmse, int flags);
 /* RMSE (eV/A) between learned and classical forces at the current positions;
  * leaves the forces of the active form. */

@@ -24,6 +24,7 @@ PFMD_E_TIMEOUT = 6
 PFMD_E_IO = 7
 PFMD_E_STATE = 8
 FORMS = {"plain": 0, "precision": 1}
+NET_FLOATS = 7361  # floats per network of the learned form (PFMD_LEARNED_NET_FLOATS)
 
 # every entry point include/pfmd.h declares
 EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pfmd_errmsg", "pfmd_strerror",
@@ -34,7 +35,7 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
            "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
-           "pfmd_learned_check", "pfmd_learned_status", "pfmd_rjl_forces_noalloc",
+           "pfmd_learned_check", "pfmd_learned_status", "pfmd_learned_gradient", "pfmd_rjl_forces_noalloc",
            "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting")
 
 _LIB = None
@@ -110,7 +111,8 @@ def load(path=LIB_PATH):
     L.pfmd_batch_energies.argtypes = [vp, dp, dp]
     L.pfmd_batch_energy_history.argtypes = [vp, dp, llp, ip]
     L.pfmd_learned_train.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
-                                     dp, dp]
+                                     C.c_int, dp, dp]
+    L.pfmd_learned_gradient.argtypes = [vp, C.c_char_p, C.c_double, C.c_int, C.POINTER(C.c_float), dp, dp]
     L.pfmd_learned_use.argtypes = [vp, C.c_char_p, C.c_longlong, C.c_double, C.c_int]
     L.pfmd_learned_check.argtypes = [vp, dp]
     L.pfmd_learned_status.argtypes = [vp, ip, ip, dp, ip]
@@ -269,16 +271,30 @@ class Simulation:
     def set_group_n(self, group, n):
         self._check(load().pfmd_set_group_n(self._h, group, n))
 
-    def learned_train(self, model_out, frames, stride=10, iters=4, lr=1e-3, model_in=None, force_weight=1.0):
-        """Online training from this plain-form run; returns the per-interaction
-        per-atom energy RMSE (eV) of the last frame (NaN where no network) and the
-        learned-against-plain force RMSE (eV/A) on it."""
+    def learned_train(self, model_out, frames, stride=10, iters=4, lr=1e-3, model_in=None, force_weight=1.0,
+                      tensor_cores=False):
+        """Online training from this plain-form run (tensor_cores: the training
+        kernels on tcgen05); returns the per-interaction per-atom energy RMSE (eV)
+        of the last frame (NaN where no network) and the learned-against-plain force
+        RMSE (eV/A) on it."""
         r = np.zeros(max(1, self.n_interactions))
         fr = C.c_double()
         self._check(load().pfmd_learned_train(self._h, model_in.encode() if model_in else None,
                                               model_out.encode() if model_out else None, frames, stride, iters, lr,
-                                              force_weight, _dp(r), C.byref(fr)))
+                                              force_weight, 1 if tensor_cores else 0, _dp(r), C.byref(fr)))
         return r[:self.n_interactions].copy(), fr.value
+
+    def learned_gradient(self, model_in=None, force_weight=1.0, tensor_cores=False, n_networks=1, timed=False):
+        """(gradient, loss[, device ms]): the training-loss gradient of each network
+        at this configuration (rows of NET_FLOATS floats), its summed squared energy
+        error and, with timed, the device time of the gradient kernels."""
+        g = np.zeros((n_networks, NET_FLOATS), np.float32)
+        loss = np.zeros(n_networks)
+        ms = C.c_double()
+        self._check(load().pfmd_learned_gradient(self._h, model_in.encode() if model_in else None, force_weight,
+                                                 1 if tensor_cores else 0,
+                                                 g.ctypes.data_as(C.POINTER(C.c_float)), _dp(loss), C.byref(ms)))
+        return (g, loss, ms.value) if timed else (g, loss)
 
     def learned_use(self, model_path, check_period=100, max_rmse=0.05, tensor_cores=False):
         self._check(load().pfmd_learned_use(self._h, model_path.encode(), check_period, max_rmse,

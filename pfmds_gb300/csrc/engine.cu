@@ -351,7 +351,8 @@ class Engine {
   void learned_setup(const std::vector<learned::Model>& ms);
   void learned_upload_desc(Lrn& L);
   double learned_check(bool switch_on_fail);
-  void learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride, int iters,
+  void learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride, int iters, int flags,
+                     float* grad_out, double* loss_out, double* grad_ms,
                      double lr, double force_weight, double* rmse_out, double* force_rmse);
   DBuf<double4_32a> fref;
   DBuf<float4> fres;
@@ -1699,8 +1700,18 @@ double Engine::learned_check(bool switch_on_fail) {
 // rjl kernels give per-atom energies of the current configuration; each network
 // takes `iters` Adam steps on its atoms' descriptors.  rmse_out[k] (per
 // interaction, NaN where no network) = per-atom energy RMSE of the last frame.
+// grad_out: the gradient mode -- one frame, the loss gradient of each network into
+// grad_out (NET_FLOATS each) and its summed squared energy error into loss_out,
+// no update and nothing saved.
 void Engine::learned_train(const std::string& model_in, const std::string& model_out, int frames, int stride,
-                           int iters, double lr, double force_weight, double* rmse_out, double* force_rmse) {
+                           int iters, int flags, float* grad_out, double* loss_out, double* grad_ms, double lr,
+                           double force_weight, double* rmse_out, double* force_rmse) {
+  const bool tc = (flags & PFMD_LEARNED_TENSOR_CORES) != 0;
+  if (grad_out) {
+    frames = 1;
+    stride = 0;
+    iters = 1;
+  }
   if (prec) throw Error(PFMD_E_STATE, "learned training runs on the plain form (FP64 targets)");
   std::vector<learned::Model> ms;
   const bool fresh = model_in.empty();
@@ -1719,7 +1730,7 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
   for (auto& M : lrn) {
     if (!M.on) continue;
     const int rows = static_cast<int>(M.e.n);
-    const int blocks = learned::train_blocks(rows);
+    const int blocks = std::max(learned::train_blocks(rows), learned::train_tc_grid(rows));
     M.part.alloc(static_cast<size_t>(blocks) * learned::NET_FLOATS);
     M.lpart.alloc(static_cast<size_t>(blocks));
     M.grad.alloc(learned::NET_FLOATS);
@@ -1821,8 +1832,34 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
         T.m = M.m.p;
         T.v = M.v.p;
         T.loss = M.loss.p;
-        learned::launch_train_grad(rows, M.G.p, fm ? U[k].p : nullptr, M.t.p, 1.0f,
-                                   static_cast<float>(force_weight), M.net.p, T, st);
+        if (grad_out && grad_ms) {
+          if (!ev0) {
+            CK(cudaEventCreate(&ev0));
+            CK(cudaEventCreate(&ev1));
+          }
+          CK(cudaEventRecord(ev0, st));
+        }
+        if (tc)
+          learned::launch_train_grad_tc(rows, M.G.p, fm ? U[k].p : nullptr, M.t.p, 1.0f,
+                                        static_cast<float>(force_weight), M.net.p, T, ctl, st);
+        else
+          learned::launch_train_grad(rows, M.G.p, fm ? U[k].p : nullptr, M.t.p, 1.0f,
+                                     static_cast<float>(force_weight), M.net.p, T, st);
+        if (grad_out && grad_ms) {
+          CK(cudaEventRecord(ev1, st));
+          CK(cudaEventSynchronize(ev1));
+          float ms = 0.f;
+          CK(cudaEventElapsedTime(&ms, ev0, ev1));
+          *grad_ms += ms;
+        }
+        if (grad_out) {
+          int slot = 0;
+          for (size_t q = 0; q < k; ++q) slot += lrn[q].on ? 1 : 0;
+          CK(cudaMemcpyAsync(grad_out + static_cast<size_t>(slot) * learned::NET_FLOATS, M.grad.p,
+                             sizeof(float) * learned::NET_FLOATS, cudaMemcpyDeviceToHost, st));
+          if (loss_out) CK(cudaMemcpyAsync(loss_out + slot, M.loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+          continue;
+        }
         ++M.adam_step;
         learned::launch_adam(M.net.p, T, M.adam_step, static_cast<float>(lr), st);
       }
@@ -1832,6 +1869,13 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
       CK(cudaMemcpyAsync(frc.p, fref.p, sizeof(double4_32a) * static_cast<size_t>(N), cudaMemcpyDeviceToDevice, st));
     read_ctl();
     if (hctl->error) raise_device_error();
+  }
+  if (grad_out) {
+    CK(cudaStreamSynchronize(st));
+    read_ctl();
+    if (hctl->error) raise_device_error();
+    clear_graphs();
+    return;
   }
   // the error of the final networks on the last frame
   for (size_t k = 0; k < inters.size(); ++k) {
@@ -2397,12 +2441,23 @@ int pfmd_flush_l2(pfmd_ctx* c, long long bytes) {
 }
 
 int pfmd_learned_train(pfmd_ctx* c, const char* model_in, const char* model_out, int frames, int stride, int iters,
-                       double lr, double force_weight, double* rmse, double* force_rmse) {
+                       double lr, double force_weight, int flags, double* rmse, double* force_rmse) {
   if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
   if (frames < 1 || stride < 0 || !(lr > 0.0) || force_weight < 0.0) return PFMD_E_PARAM;
   return guard(c, [&] {
-    c->e->learned_train(model_in ? model_in : "", model_out ? model_out : "", frames, stride, iters, lr,
-                        force_weight, rmse, force_rmse);
+    c->e->learned_train(model_in ? model_in : "", model_out ? model_out : "", frames, stride, iters, flags, nullptr,
+                        nullptr, nullptr, lr, force_weight, rmse, force_rmse);
+  });
+}
+
+int pfmd_learned_gradient(pfmd_ctx* c, const char* model_in, double force_weight, int flags, float* grad,
+                          double* loss, double* device_ms) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  if (!grad || force_weight < 0.0) return PFMD_E_PARAM;
+  if (device_ms) *device_ms = 0.0;
+  return guard(c, [&] {
+    c->e->learned_train(model_in ? model_in : "", "", 1, 0, 1, flags, grad, loss, device_ms, 1e-3, force_weight,
+                        nullptr, nullptr);
   });
 }
 

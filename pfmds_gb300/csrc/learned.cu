@@ -746,6 +746,10 @@ void launch_train_grad(int rows, const float* G, const float* U, const double* t
   k_train<<<blocks, 256, sizeof(TrainSmem), s>>>(rows, G, U, target_by_row, wE, U ? wF : 0.f, net, T.part,
                                                  T.lpart);
   ++g_kernel_launches;
+  launch_train_reduce(blocks, rows, T, s);
+}
+
+void launch_train_reduce(int blocks, int rows, TrainBuf& T, cudaStream_t s) {
   k_train_reduce<<<nblk(NET_FLOATS, 256), 256, 0, s>>>(blocks, rows, T.part, T.lpart, T.grad, T.loss);
   ++g_kernel_launches;
 }

@@ -81,6 +81,13 @@ void launch_train_grad(int rows, const float* G, const float* U, const double* t
 void launch_residual(int n, const double4_32a* fpred, const double4_32a* fref, float4* res, cudaStream_t s);
 void launch_desc_vjp(const ListDev& L, const DescPar* d, const Atoms& A, const Box& B, const float4* res, float* U,
                      Ctl* ctl, cudaStream_t s);
+// The same gradient on the tensor cores (tcgen05, BF16 operands, FP32 accumulation):
+// one persistent CTA per SM, partials per CTA (T.part needs train_tc_grid(rows) rows).
+void launch_train_grad_tc(int rows, const float* G, const float* U, const double* target_by_row, float wE, float wF,
+                          const Net* net, TrainBuf& T, Ctl* ctl, cudaStream_t s);
+int train_tc_grid(int rows);
+// Sums `blocks` per-block partials in a fixed order into T.grad and T.loss.
+void launch_train_reduce(int blocks, int rows, TrainBuf& T, cudaStream_t s);
 void launch_adam(Net* net, TrainBuf& T, int step, float lr, cudaStream_t s);
 constexpr int NET_FLOATS = static_cast<int>(sizeof(Net) / sizeof(float));
 int train_blocks(int rows);

@@ -157,3 +157,38 @@ def test_tensor_core_network_matches_fp32(tmp_path, built):
     assert np.all(np.abs(e16[:2] - e32[:2]) < 2e-3 * n), (e16, e32)  # eV over the system
     rel = np.sqrt(((f16 - f32) ** 2).mean()) / np.sqrt((f32 ** 2).mean())
     assert rel < 3e-2, rel
+
+
+def test_tensor_core_training_gradient_matches_fp32(tmp_path, built):
+    """The tcgen05 training kernel (BF16 operands, FP32 accumulation) gives the
+    gradient of the FP32 kernel, block by block (W1, b1, W2, b2, w3, b3), to BF16
+    accuracy, and repeats bit for bit."""
+    d = _gr(tmp_path)
+    m = str(tmp_path / "m.bin")
+    _train(d, m, frames=6, stride=5, iters=4)
+    s = pf.Simulation(d, form="plain", out_period=10 ** 9)
+    s.advance(3)
+    g32, l32 = s.learned_gradient(m, force_weight=1.0, tensor_cores=False, n_networks=2)
+    gtc, ltc = s.learned_gradient(m, force_weight=1.0, tensor_cores=True, n_networks=2)
+    gtc2, _ = s.learned_gradient(m, force_weight=1.0, tensor_cores=True, n_networks=2)
+    assert np.array_equal(gtc, gtc2)
+    np.testing.assert_allclose(ltc, l32, rtol=3e-2)
+    NH, NG = 64, 48
+    cuts = np.cumsum([0, NH * NG, NH, NH * NH, NH, NH, 1])
+    for k in range(2):
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            x, y = gtc[k, a:b].astype(np.float64), g32[k, a:b].astype(np.float64)
+            rel = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-30)
+            assert rel < 5e-2, (k, a, b, rel)
+
+
+def test_tensor_core_training_lowers_energy_and_force_errors(tmp_path, built):
+    d = _gr(tmp_path)
+    m0, m1 = str(tmp_path / "m0.bin"), str(tmp_path / "m1.bin")
+    r0, f0 = _train(d, m0, frames=1, stride=0, iters=1)
+    s = pf.Simulation(d, form="plain", out_period=10 ** 9)
+    r1, f1 = s.learned_train(m1, frames=60, stride=5, iters=8, lr=2e-3, model_in=m0, tensor_cores=True)
+    s.close()
+    assert (r1[:2] < r0[:2]).all(), (r0, r1)
+    assert (r1[:2] < 0.05).all(), r1
+    assert f1 < f0, (f0, f1)
