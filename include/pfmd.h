@@ -57,10 +57,15 @@ typedef struct pfmd_options {
   int async_io;              /* 1: snapshot and trajectory files are formatted and written by a
                                 background thread while the next steps run (complete when
                                 pfmd_finish / pfmd_md / pfmd_destroy returns); 0: at the event */
+  int skin_lists;            /* precision form, 1: at its update step a list is rebuilt only when
+                                an atom of its groups moved, since the build plus over the last
+                                period, more than half of (r_cut - the interaction's cut-off);
+                                0: at every update step, as the reference (the plain form always) */
 } pfmd_options;
 
 /* Defaults of run_md_simulation.f90:10-24 (out_period 1, seed 1, no prefix),
- * plain form, device 0, graphs on, background file writing on. */
+ * plain form, device 0, graphs on, background file writing on, skin-triggered
+ * list rebuilds on (precision form). */
 void pfmd_default_options(pfmd_options* opt);
 
 /* ---- set-up and teardown ----------------------------------------------- */
@@ -158,6 +163,10 @@ int pfmd_get_nlist(pfmd_ctx* ctx, int inter, int list, int* nnum, int* lessnnum,
 /* Largest neighbour count of every list, in nlists_load order
  * (md_interactions.f90:427-444); maxnnum holds one int per list. */
 int pfmd_nlist_load(pfmd_ctx* ctx, int* maxnnum, int* count);
+/* Rebuilds so far of every list, in nlists_load order: for a skin-triggered list
+ * (pfmd_options.skin_lists) the rebuilds done, -1 for a list rebuilt at every
+ * update step.  builds holds one long long per list. */
+int pfmd_nlist_builds(pfmd_ctx* ctx, long long* builds, int* count);
 /* gr_norm of an ljc / morsec interaction (graphenenorm.f90:38-56), 3 per row. */
 int pfmd_get_gr_norm(pfmd_ctx* ctx, int inter, double* norm);
 

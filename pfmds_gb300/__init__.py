@@ -35,7 +35,7 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
            "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
-           "pfmd_learned_check", "pfmd_learned_status", "pfmd_learned_gradient", "pfmd_rjl_forces_noalloc",
+           "pfmd_learned_check", "pfmd_learned_status", "pfmd_learned_gradient", "pfmd_nlist_builds", "pfmd_rjl_forces_noalloc",
            "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting")
 
 _LIB = None
@@ -51,7 +51,7 @@ class Options(C.Structure):
     _fields_ = [("form", C.c_int), ("rand_seed", C.c_int), ("out_period", C.c_int), ("out_fd", C.c_int),
                 ("all_out_fd", C.c_int), ("write_files", C.c_int), ("output_prefix", C.c_char_p),
                 ("num_threads", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int),
-                ("threads_per_row", C.c_int), ("async_io", C.c_int)]
+                ("threads_per_row", C.c_int), ("async_io", C.c_int), ("skin_lists", C.c_int)]
 
 
 def load(path=LIB_PATH):
@@ -105,6 +105,7 @@ def load(path=LIB_PATH):
     L.pfmd_batch_replica.argtypes = [vp, C.c_int, ip, ip, ip]
     L.pfmd_batch_run.argtypes = [vp, C.c_longlong, dp]
     L.pfmd_batch_run_list.argtypes = [vp, C.c_char_p, C.c_int, dp]
+    L.pfmd_nlist_builds.argtypes = [vp, llp, ip]
     L.pfmd_batch_tune.argtypes = [vp, C.c_int, ip]
     L.pfmd_batch_set_tpa.argtypes = [vp, ip]
     L.pfmd_batch_get_state.argtypes = [vp, C.c_int, dp, dp, dp]
@@ -155,13 +156,14 @@ class Simulation:
 
     def __init__(self, input_path, settings="md_run_settings.txt", form="plain", out_period=1, write_files=False,
                  prefix="", use_graphs=True, out_fd=-1, all_out_fd=-1, seed=1, num_threads=1, device=0,
-                 threads_per_row=0, async_io=True):
+                 threads_per_row=0, async_io=True, skin_lists=True):
         L = load()
         self._prefix = prefix.encode()
         self.opts = default_options(form=form, out_period=out_period, write_files=1 if write_files else 0,
                                     output_prefix=self._prefix, use_graphs=1 if use_graphs else 0, out_fd=out_fd,
                                     all_out_fd=all_out_fd, rand_seed=seed, num_threads=num_threads, device=device,
-                                    threads_per_row=threads_per_row, async_io=1 if async_io else 0)
+                                    threads_per_row=threads_per_row, async_io=1 if async_io else 0,
+                                    skin_lists=1 if skin_lists else 0)
         self._h = C.c_void_p()
         ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
         rc = L.pfmd_create_from_files(ip.encode(), settings.encode(), C.byref(self.opts), C.byref(self._h))
@@ -266,6 +268,13 @@ class Simulation:
         buf = np.zeros(64, np.int32)
         cnt = C.c_int()
         self._check(load().pfmd_nlist_load(self._h, _ip(buf), C.byref(cnt)))
+        return buf[:cnt.value].copy()
+
+    def nlist_builds(self):
+        """Rebuilds of every list so far (-1: a list rebuilt at every update step)."""
+        buf = np.zeros(64, np.int64)
+        cnt = C.c_int()
+        self._check(load().pfmd_nlist_builds(self._h, buf.ctypes.data_as(C.POINTER(C.c_longlong)), C.byref(cnt)))
         return buf[:cnt.value].copy()
 
     def set_group_n(self, group, n):

@@ -82,9 +82,20 @@ struct Ctl {
   // small reduction results
   double red[PFMD_RED_SLOTS];
   int maxnnum[PFMD_MAX_LISTS];
+  // skin-triggered rebuilds (precision form): list_need[id] is 1 when list id must
+  // be rebuilt at its next update step; skin_done counts the blocks of the kernel
+  // that records a rebuild
+  int list_need[PFMD_MAX_LISTS];
+  unsigned int skin_done[PFMD_MAX_LISTS];
+  unsigned int skin_max[PFMD_MAX_LISTS][2];  // squared displacements (float bits): since the build, last period
+  long long list_builds[PFMD_MAX_LISTS];     // rebuilds of each skin-managed list
   unsigned int counter[PFMD_RED_SLOTS];
   double partial[PFMD_PARTIALS];  // per-block partial sums of the grid reductions
 };
+
+// A skin-managed list whose atoms all stayed within half the skin since its last
+// build keeps its rows: its build kernels return at once.
+__device__ __forceinline__ bool skin_keep(const Ctl* ctl, int skin) { return skin >= 0 && ctl->list_need[skin] == 0; }
 
 // Box lengths, halves, and the fixed-point scales of the force-side positions:
 // a coordinate is stored as round(x * 2^32 / L) modulo 2^32 (posq), so the

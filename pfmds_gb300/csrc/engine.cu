@@ -208,6 +208,8 @@ struct ListH {
   long long period = 1;
   int src = -1;  // converse: source list; nn: the tb list
   bool has_grid = false;
+  double half_skin = 0.0;  // skin-triggered rebuilds: half of r_cut minus the interaction's cut-off
+  DBuf<int4> xref, xprev;  // fixed-point positions at the last build / the last update step (skin >= 0)
 };
 
 struct InterH {
@@ -632,6 +634,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
                                        : pass1_tpa(L.d.tpa, std::max(nmax, 2) / 2.0, opt.form == PFMD_FORM_PRECISION);
     L.d.row_group = row_g - 1;
     L.d.col_group = col_g - 1;
+    L.d.skin = -1;
     L.d.row_cap = static_cast<int>(groups[static_cast<size_t>(row_g - 1)].idx.size());
     L.d.col_cap = static_cast<int>(groups[static_cast<size_t>(col_g - 1)].idx.size());
     if (nmax < 0) throw Error(PFMD_E_PARAM, "error: negative neighb_num_max");
@@ -893,6 +896,32 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
       L.d.row_of = L.row_of.p;
     }
   }
+  // skin-triggered rebuilds (precision form): at an update step a list keeps its
+  // rows when no atom of its groups moved more than half of (r_cut - the
+  // interaction's cut-off) since it was built; its converse list follows it
+  if (prec && opt.skin_lists && changes.empty()) {
+    for (auto& I : inters) {
+      double rint = -1.0;
+      switch (I.spec.kind) {
+        case pfmd_io::K_LJ:
+        case pfmd_io::K_LJ1G: rint = I.lj.R2; break;
+        case pfmd_io::K_LJC:
+        case pfmd_io::K_MORSEC: rint = I.cp.R2; break;
+        case pfmd_io::K_RJL: rint = I.rjl.R2; break;
+        case pfmd_io::K_TB: rint = I.tb.R2; break;
+        case pfmd_io::K_REBOSC: rint = I.rebo.R2; break;
+      }
+      ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
+      if (!(rint > 0.0) || !(L1.rc > rint)) continue;
+      L1.d.skin = L1.d.id;
+      L1.half_skin = 0.5 * (L1.rc - rint);
+      L1.xref.alloc(static_cast<size_t>(std::max(N, 1)));
+      L1.xprev.alloc(static_cast<size_t>(std::max(N, 1)));
+      L1.xref.zero(st);
+      L1.xprev.zero(st);
+      if (I.lists[1] >= 0) lists[static_cast<size_t>(I.lists[1])].d.skin = L1.d.id;
+    }
+  }
   plan_fusion();
   // control block
   CK(cudaMalloc(&ctl, sizeof(Ctl)));
@@ -903,6 +932,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   hctl->md_step = -1;
   hctl->oob_atom = INT_MAX;
   for (size_t g = 0; g < groups.size(); ++g) hctl->group_n[g] = static_cast<int>(groups[g].idx.size());
+  for (int l = 0; l < PFMD_MAX_LISTS; ++l) hctl->list_need[l] = 1;  // every list is built first
   for (size_t c = 0; c < S.nhc.size(); ++c) {
     const auto& h = S.nhc[c];
     NHCDev& d = hctl->nhc[c];
@@ -1079,6 +1109,8 @@ bool Engine::is_event(const StepPlan& p) const {
 void Engine::enqueue_lists(const StepPlan& p) {
   for (auto& I : inters) {
     ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
+    const bool skin = L1.d.skin >= 0 && p.rebuild[static_cast<size_t>(I.lists[0])];
+    if (skin) launch_skin_check(L1.d, A, box, L1.xref.p, L1.xprev.p, L1.half_skin, ctl, st);
     if (p.rebuild[static_cast<size_t>(I.lists[0])]) {
       launch_bin(L1.d, L1.cg, A, ctl, st);
       launch_build_list(prec, L1.d, L1.cg, A, box, L1.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
@@ -1090,6 +1122,7 @@ void Engine::enqueue_lists(const StepPlan& p) {
       launch_build_list(prec, L2.d, L2.cg, A, box, L2.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
                         1, L1.d.rows, ctl, st);
     }
+    if (skin) launch_skin_commit(L1.d, A, L1.xref.p, ctl, st);
     if (I.lists[2] >= 0 && p.rebuild[static_cast<size_t>(I.lists[2])]) {
       ListH& L3 = lists[static_cast<size_t>(I.lists[2])];
       if (L3.kind == L_NN_TB) {
@@ -1616,6 +1649,12 @@ void Engine::learned_setup(const std::vector<learned::Model>& ms) {
     M.on = true;
     M.model = *m;
     ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
+    // the descriptors reach past the interaction's own cut-off: its list is rebuilt
+    // at every update step again
+    if (L.d.skin >= 0) {
+      L.d.skin = -1;
+      clear_graphs();
+    }
     if (L.rc < std::max(m->d.rc_rad, m->d.rc_ang))
       throw Error(PFMD_E_PARAM, "learned form: the " + inters[k].spec.name + " list needs r_cut >= " +
                                     std::to_string(std::max(m->d.rc_rad, m->d.rc_ang)) + " A for its descriptors");
@@ -2021,6 +2060,8 @@ double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
       return true;
     }
     if (name == "lists") {
+      // every list rebuilt, skin-triggered or not
+      CK(cudaMemsetAsync(ctl->list_need, 1, sizeof(ctl->list_need), st));
       StepPlan p;
       p.step = 0;
       p.first = true;
@@ -2125,6 +2166,7 @@ void pfmd_default_options(pfmd_options* o) {
   o->use_graphs = 1;
   o->threads_per_row = 0;
   o->async_io = 1;
+  o->skin_lists = 1;
 }
 
 int pfmd_create_from_files(const char* input_path, const char* settings_filename, const pfmd_options* opt,
@@ -2348,6 +2390,23 @@ int pfmd_nlist_load(pfmd_ctx* c, int* maxnnum, int* count) {
       for (int j = 0; j < I.spec.nl_n; ++j) {
         const auto& L = e.lists[static_cast<size_t>(I.lists[j])];
         if (maxnnum) maxnnum[k] = e.hctl->maxnnum[L.d.id];
+        ++k;
+      }
+    if (count) *count = k;
+  });
+}
+
+int pfmd_nlist_builds(pfmd_ctx* c, long long* builds, int* count) {
+  if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
+  return guard(c, [&] {
+    auto& e = *c->e;
+    e.read_ctl();
+    int k = 0;
+    for (auto& I : e.inters)
+      for (int j = 0; j < I.spec.nl_n; ++j) {
+        const auto& L = e.lists[static_cast<size_t>(I.lists[j])];
+        // a converse list follows its source's rebuilds
+        if (builds) builds[k] = (L.d.skin >= 0) ? e.hctl->list_builds[L.d.skin] : -1;
         ++k;
       }
     if (count) *count = k;

@@ -58,6 +58,7 @@ struct ListDev {
   const int* row_of;   // atom -> row (g1 == g2 lists that need it), else null
   int row_group, col_group;  // 0-based group numbers (sizes in Ctl::group_n)
   int row_cap, col_cap;
+  int skin;  // index into Ctl::list_need when its rebuilds are skin-triggered, else -1
 };
 
 struct CellGrid {
@@ -153,6 +154,11 @@ struct Epi {
 // ---------------- neighbour lists (nlist.cu) ----------------
 void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s);
+// Skin-triggered rebuilds (L.skin >= 0): the displacement test before a list's
+// update step and the reference update after it.
+void launch_skin_check(const ListDev& L, const Atoms& A, const Box& B, const int4* xref, int4* xprev,
+                       double half_skin, Ctl* ctl, cudaStream_t s);
+void launch_skin_commit(const ListDev& L, const Atoms& A, int4* xref, Ctl* ctl, cudaStream_t s);
 // Regular list (converse=0), or the converse of a list with src_rows rows
 // (converse=1, built at the source list's rebuild steps).  The plain form tests
 // candidates with an FP32 prefilter at r_cut + prefilter_margin, then exactly.

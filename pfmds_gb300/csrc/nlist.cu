@@ -36,7 +36,7 @@ __global__ void k_pack_posq(Atoms A, Box B) {
 }
 
 __global__ void k_bin_count(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
-  if (ctl->stop) return;
+  if (ctl->stop || skin_keep(ctl, L.skin)) return;
   int n2 = ctl->group_n[L.col_group];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n2) return;
@@ -49,8 +49,8 @@ __global__ void k_bin_count(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
 // Exclusive scan of the cell counts by one block of 1024 threads: 1024 cells per
 // pass (coalesced), shuffles within each warp, a second shuffle level over the 32
 // warp totals, and a carry from pass to pass.
-__global__ void __launch_bounds__(1024) k_bin_scan(CellGrid cg, Ctl* ctl) {
-  if (ctl->stop) return;
+__global__ void __launch_bounds__(1024) k_bin_scan(CellGrid cg, int skin, Ctl* ctl) {
+  if (ctl->stop || skin_keep(ctl, skin)) return;
   __shared__ int wsum[32];
   __shared__ int carry_s;
   const int n = cg.ncell, t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(1024) k_bin_scan(CellGrid cg, Ctl* ctl) {
 }
 
 __global__ void k_bin_scatter(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
-  if (ctl->stop) return;
+  if (ctl->stop || skin_keep(ctl, L.skin)) return;
   int n2 = ctl->group_n[L.col_group];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n2) return;
@@ -106,8 +106,8 @@ __global__ void k_bin_scatter(ListDev L, CellGrid cg, Atoms A, Ctl* ctl) {
 // cell order (no per-row sort) are the same on every run.  One warp per cell;
 // cells of more than 32 atoms (rare: large or sparse cells) use an insertion
 // sort by one lane.
-__global__ void k_cell_sort(CellGrid cg, Ctl* ctl) {
-  if (ctl->stop) return;
+__global__ void k_cell_sort(CellGrid cg, int skin, Ctl* ctl) {
+  if (ctl->stop || skin_keep(ctl, skin)) return;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= cg.ncell) return;
@@ -167,7 +167,7 @@ template <bool PREC, int CAP, bool SORT>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid cg, Atoms A, Box B, double rc2,
                                                              float rcp2, int converse, int src_rows, Ctl* ctl) {
   __shared__ int sbuf[kBuildWarps][CAP];
-  if (ctl->stop) return;
+  if (ctl->stop || skin_keep(ctl, L.skin)) return;
   const int n1 = ctl->group_n[L.row_group];
   const int n2 = ctl->group_n[L.col_group];
   if (!converse) {
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
   __shared__ int s_off[19];  // prefix offsets of up to 18 candidate runs
   __shared__ int s_beg[18];  // run starts in the cell-ordered arrays
   __shared__ int s_cnt[kCellRows];
-  if (ctl->stop) return;
+  if (ctl->stop || skin_keep(ctl, L.skin)) return;
   const int n1 = ctl->group_n[L.row_group];
   // update_neighbour_list only acts when the group and the list are non-empty
   if (n1 == 0 || L.rows == 0) return;
@@ -574,10 +574,90 @@ void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
   if (A.N > 0) { k_pack_posq<<<blocks_for(A.N, 256), 256, 0, s>>>(A, B); ++g_kernel_launches; }
 }
 
+// Skin-triggered rebuilds (precision form).  At a list's update step every atom of
+// its groups records its displacement since the list was built (xref) and over
+// the last period (xprev, then updated), as maxima of the squares; k_skin_decide
+// asks for a rebuild when the two maxima add up to more than half the skin, so
+// the list stays complete through the next period if no atom moves faster than
+// in the last one.  Maxima by atomicMax on the bits of non-negative floats: the
+// same result in any order.
+__global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* xprev, int both, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nr = ctl->group_n[L.row_group], nc = ctl->group_n[L.col_group];
+  int a = -1;
+  if (i < L.row_cap) {
+    if (i < nr) a = L.row_idx[i];
+  } else if (both && i - L.row_cap < nc) {
+    a = L.col_idx[i - L.row_cap];
+  }
+  unsigned int ub = 0u, up = 0u;
+  if (a >= 0) {
+    const int4 q = A.posq[a];
+    float d[3];
+    ub = __float_as_uint(mi_q(xref[a], q, B, d));
+    up = __float_as_uint(mi_q(xprev[a], q, B, d));
+    xprev[a] = q;
+  }
+  // one atomic per warp
+  ub = __reduce_max_sync(0xffffffffu, ub);
+  up = __reduce_max_sync(0xffffffffu, up);
+  if ((threadIdx.x & 31) == 0) {
+    if (ub) atomicMax(&ctl->skin_max[L.skin][0], ub);
+    if (up) atomicMax(&ctl->skin_max[L.skin][1], up);
+  }
+}
+__global__ void k_skin_decide(int id, float half_skin, Ctl* ctl) {
+  if (ctl->stop) return;
+  const float b = sqrtf(__uint_as_float(ctl->skin_max[id][0])), p = sqrtf(__uint_as_float(ctl->skin_max[id][1]));
+  if (!(b + p <= half_skin)) ctl->list_need[id] = 1;
+  ctl->skin_max[id][0] = 0u;
+  ctl->skin_max[id][1] = 0u;
+}
+// After the update step: a rebuilt list's atoms give the new reference positions;
+// the last block to finish clears the flag (every block has read it by then).
+__global__ void k_skin_commit(ListDev L, Atoms A, int4* xref, Ctl* ctl) {
+  if (ctl->stop) return;
+  __shared__ int need;
+  if (threadIdx.x == 0) need = ctl->list_need[L.skin];
+  __syncthreads();
+  if (need)
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.N; a += gridDim.x * blockDim.x) xref[a] = A.posq[a];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int done = atomicAdd(&ctl->skin_done[L.skin], 1u);
+    if (done == gridDim.x - 1) {
+      if (need) ctl->list_builds[L.skin] += 1;
+      ctl->list_need[L.skin] = 0;
+      ctl->skin_done[L.skin] = 0;
+    }
+  }
+}
+
+void launch_skin_check(const ListDev& L, const Atoms& A, const Box& B, const int4* xref, int4* xprev,
+                       double half_skin, Ctl* ctl, cudaStream_t s) {
+  if (L.skin < 0) return;
+  const int both = L.row_group != L.col_group ? 1 : 0;  // a self list checks its rows once
+  const int n = L.row_cap + (both ? L.col_cap : 0);
+  if (n > 0) {
+    k_skin_check<<<blocks_for(n, 256), 256, 0, s>>>(L, A, B, xref, xprev, both, ctl);
+    ++g_kernel_launches;
+  }
+  k_skin_decide<<<1, 1, 0, s>>>(L.skin, static_cast<float>(half_skin), ctl);
+  ++g_kernel_launches;
+}
+void launch_skin_commit(const ListDev& L, const Atoms& A, int4* xref, Ctl* ctl, cudaStream_t s) {
+  if (L.skin < 0) return;
+  const int grid = std::max(1, std::min(blocks_for(A.N, 256), 152));
+  k_skin_commit<<<grid, 256, 0, s>>>(L, A, xref, ctl);
+  ++g_kernel_launches;
+}
+
 void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s) {
   cudaMemsetAsync(cg.count, 0, sizeof(int) * (size_t)cg.ncell, s);
   if (L.col_cap > 0) { k_bin_count<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, A, ctl); ++g_kernel_launches; }
-  { k_bin_scan<<<1, 1024, 0, s>>>(cg, ctl); ++g_kernel_launches; }
+  { k_bin_scan<<<1, 1024, 0, s>>>(cg, L.skin, ctl); ++g_kernel_launches; }
   if (L.col_cap > 0) { k_bin_scatter<<<blocks_for(L.col_cap, 256), 256, 0, s>>>(L, cg, A, ctl); ++g_kernel_launches; }
 }
 
@@ -604,7 +684,7 @@ void launch_build_list(bool prec, const ListDev& L, const CellGrid& cg, const At
                        double prefilter_margin, int converse, int src_rows, Ctl* ctl, cudaStream_t s) {
   const double rc2 = rc * rc;
   if (!L.sorted) {
-    { k_cell_sort<<<blocks_for((long long)cg.ncell * 32, 256), 256, 0, s>>>(cg, ctl); ++g_kernel_launches; }
+    { k_cell_sort<<<blocks_for((long long)cg.ncell * 32, 256), 256, 0, s>>>(cg, L.skin, ctl); ++g_kernel_launches; }
   }
   if (prec) {
     if (L.sorted)
