@@ -61,6 +61,9 @@ typedef struct pfmd_options {
                                 an atom of its groups moved, since the build plus over the last
                                 period, more than half of (r_cut - the interaction's cut-off);
                                 0: at every update step, as the reference (the plain form always) */
+  int fuse_steps;            /* precision form, nve with one rjl interaction over all atoms, 1: a
+                                step's force kernel also runs the next step's first half-kick and
+                                drift (the same arithmetic, one launch less per step); 0: separate */
 } pfmd_options;
 
 /* Defaults of run_md_simulation.f90:10-24 (out_period 1, seed 1, no prefix),

@@ -51,7 +51,8 @@ class Options(C.Structure):
     _fields_ = [("form", C.c_int), ("rand_seed", C.c_int), ("out_period", C.c_int), ("out_fd", C.c_int),
                 ("all_out_fd", C.c_int), ("write_files", C.c_int), ("output_prefix", C.c_char_p),
                 ("num_threads", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int),
-                ("threads_per_row", C.c_int), ("async_io", C.c_int), ("skin_lists", C.c_int)]
+                ("threads_per_row", C.c_int), ("async_io", C.c_int), ("skin_lists", C.c_int),
+                ("fuse_steps", C.c_int)]
 
 
 def load(path=LIB_PATH):
@@ -156,14 +157,14 @@ class Simulation:
 
     def __init__(self, input_path, settings="md_run_settings.txt", form="plain", out_period=1, write_files=False,
                  prefix="", use_graphs=True, out_fd=-1, all_out_fd=-1, seed=1, num_threads=1, device=0,
-                 threads_per_row=0, async_io=True, skin_lists=True):
+                 threads_per_row=0, async_io=True, skin_lists=True, fuse_steps=True):
         L = load()
         self._prefix = prefix.encode()
         self.opts = default_options(form=form, out_period=out_period, write_files=1 if write_files else 0,
                                     output_prefix=self._prefix, use_graphs=1 if use_graphs else 0, out_fd=out_fd,
                                     all_out_fd=all_out_fd, rand_seed=seed, num_threads=num_threads, device=device,
                                     threads_per_row=threads_per_row, async_io=1 if async_io else 0,
-                                    skin_lists=1 if skin_lists else 0)
+                                    skin_lists=1 if skin_lists else 0, fuse_steps=1 if fuse_steps else 0)
         self._h = C.c_void_p()
         ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
         rc = L.pfmd_create_from_files(ip.encode(), settings.encode(), C.byref(self.opts), C.byref(self._h))

@@ -69,6 +69,9 @@ struct Ctl {
   int pending_oob;  // an atom left the cell in the last drift; checked at step start
   int oob_atom;     // smallest offending atom (0-based) of the pending check
   int converged;    // nvms exit
+  // the same flag for a drift fused into the previous step's force kernel, by the
+  // parity of the step it begins (the kernel that sets one slot tests the other)
+  int pending_fused[2];
   int pad0;
   long long md_step;  // the step being executed
   // energies
@@ -92,6 +95,39 @@ struct Ctl {
   unsigned int counter[PFMD_RED_SLOTS];
   double partial[PFMD_PARTIALS];  // per-block partial sums of the grid reductions
 };
+
+// An out-of-cell verdict of the last drift waits to be raised.
+__device__ __forceinline__ bool oob_pending(const Ctl* ctl) {
+  return ctl->pending_oob || ctl->pending_fused[0] || ctl->pending_fused[1];
+}
+
+// Velocity Verlet pieces shared by the integration kernels and the fused force
+// epilogue.  kt = dt/2/(m*mass_coef) formed once per atom: one FMA per component.
+__device__ __forceinline__ double kick1_fast(double v, double f, double kt) { return fma(f, kt, v); }
+// One shift back into [0, L] (md_integrators.f90:19-24): x > L and x < 0.0 decided
+// on the bit patterns (L > 0; the patterns of x >= +0 order like the values,
+// x < 0.0 is a set sign bit other than -0.0).  NaN stays NaN either way.
+__device__ __forceinline__ double wrap1(double x, double L) {
+  const long long b = __double_as_longlong(x);
+  if (b > __double_as_longlong(L))
+    x = x - L;
+  else if (b < 0 && b != (long long)0x8000000000000000ULL)
+    x = x + L;
+  return x;
+}
+// the precision form's drift: one FMA, then the shift
+__device__ __forceinline__ double drift1_fast(double x, double v, double ts1, double L) {
+  return wrap1(fma(v, ts1, x), L);
+}
+// !(x > -tol .and. x < L + tol) with tol = 1e-7 (md_general.f90:346), evaluated
+// on the bit patterns with integer compares (GB300's FP64 pipe is narrow).  For
+// x >= +0 the patterns order like the values; a negative x (sign bit set, -0.0
+// included) is inside iff its magnitude is below tol.  NaN is outside either way.
+__device__ __forceinline__ bool out_of_cell(double x, double Ltol) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b >= __double_as_longlong(Ltol)
+                : (unsigned long long)b >= (unsigned long long)__double_as_longlong(-0.0000001);
+}
 
 // A skin-managed list whose atoms all stayed within half the skin since its last
 // build keeps its rows: its build kernels return at once.

@@ -232,6 +232,9 @@ struct StepPlan {
   long long step;
   bool first, energy, out, zero_mom, check_all;
   std::vector<char> rebuild;  // per list
+  // the next step's kick and drift fused into this step's force kernel / this
+  // step's kick and drift done by the previous step's
+  bool drift_next = false, drifted = false;
 };
 
 // Snapshot and trajectory files (md_read_write.f90:65-107) are formatted and
@@ -324,7 +327,13 @@ class Engine {
   Atoms A{};
   DBuf<double4_32a> pos, vel, frc;
   DBuf<double> mass, kc;
-  DBuf<int4> posq;
+  DBuf<int4> posq, posq2;  // fixed-point positions; two buffers when kick-drift fuses into the forces
+  int posq_cur = 0;         // which buffer A.posq is (0: posq, 1: posq2)
+  bool fuse_drift = false;  // the precision rjl force kernel may run the next step's kick and drift
+  void flip_posq() {
+    posq_cur ^= 1;
+    A.posq = posq_cur ? posq2.p : posq.p;
+  }
   std::vector<GroupH> groups;
   std::vector<ListH> lists;
   std::vector<InterH> inters;
@@ -437,7 +446,7 @@ class Engine {
   bool is_event(const StepPlan& p) const;
   void enqueue_step(const StepPlan& p);
   void enqueue_lists(const StepPlan& p);
-  void enqueue_forces(bool energy, bool kick = false);
+  void enqueue_forces(bool energy, bool kick = false, bool drift_next = false);
   void plan_fusion();
   void run_plans(const std::vector<StepPlan>& plans);
   void host_events(const StepPlan& p);
@@ -923,6 +932,17 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     }
   }
   plan_fusion();
+  // the next step's kick and drift in the force kernel: precision form, one rjl
+  // interaction whose rows are every atom and which kicks last, an xyz-moving group
+  // and no z-moving one, no group changes or z-velocity inversion
+  if (prec && opt.fuse_steps && fuse_kick_drift && inters.size() == 1 && inters[0].spec.kind == pfmd_io::K_RJL &&
+      kick_last &&
+      changes.empty() && !S.invert_z_vel && groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size() > 0 &&
+      groups[static_cast<size_t>(S.z_moving - 1)].idx.empty() &&
+      lists[static_cast<size_t>(inters[0].lists[0])].d.rows == N) {
+    fuse_drift = true;
+    posq2.alloc(static_cast<size_t>(std::max(N, 1)));
+  }
   // control block
   CK(cudaMalloc(&ctl, sizeof(Ctl)));
   CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
@@ -1199,13 +1219,18 @@ void Engine::plan_fusion() {
   }
 }
 
-void Engine::enqueue_forces(bool energy, bool kick) {
+void Engine::enqueue_forces(bool energy, bool kick, bool drift_next) {
   // which launch is the first / last force writer
   const int nint = static_cast<int>(inters.size());
   auto epi = [&](bool first, bool last) {
     Epi e{0, 0, prec ? 0 : 1, ts[1], mflag.p, eatom_out};
     e.store = (first && store_first) ? 1 : 0;
     e.kick = (last && kick && kick_last) ? 1 : 0;
+    if (last && e.kick && drift_next) {
+      e.drift = 1;
+      e.ts1 = ts[0];
+      e.posq_next = posq_cur ? posq.p : posq2.p;
+    }
     return e;
   };
   for (int k = 0; k < nint; ++k) {
@@ -1260,7 +1285,9 @@ void Engine::enqueue_step(const StepPlan& p) {
   // an nve step without group changes lets the kick-drift kernel open the step
   const bool fused_begin = !p.first && integ == I_NVE && changes.empty() && !S.invert_z_vel && fuse_kick_drift &&
                            groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size() > 0;
-  if (fused_begin) {
+  if (p.drifted) {
+    launch_step_begin_fused(ctl, st);  // kick and drift ran in the previous step's force kernel
+  } else if (fused_begin) {
     // (nothing: k_kick_drift below)
   } else if (S.invert_z_vel) {
     launch_step_begin(0, static_cast<int>(changes.size()), changes.data(), 0, S.ms_de, ctl, st);
@@ -1281,7 +1308,9 @@ void Engine::enqueue_step(const StepPlan& p) {
         else
           launch_scale(static_cast<int>(c), gc, A, ctl, st);
       }
-    if (fuse_kick_drift) {
+    if (p.drifted) {
+      // (done)
+    } else if (fuse_kick_drift) {
       launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st, fused_begin);
       if (gz.cap > 0) {
         launch_kick(gz, false, ts[1], !prec, A, ctl, st);
@@ -1298,7 +1327,8 @@ void Engine::enqueue_step(const StepPlan& p) {
   const GroupRef gall = gref(S.all_atoms);
   if (p.zero_mom) launch_zero_momentum(gall, A, ctl, st);
   if (!store_first) launch_zero_forces(gall, A, ctl, st);
-  enqueue_forces(p.energy, !p.first);
+  enqueue_forces(p.energy, !p.first, p.drift_next);
+  if (p.drift_next) flip_posq();  // the next step reads the positions written by this one
   if (!p.first) {
     if (!kick_last) {
       launch_kick(gx, true, ts[1], !prec, A, ctl, st);
@@ -1330,6 +1360,7 @@ static std::string plan_key(const StepPlan& p) {
   k.reserve(8 + p.rebuild.size());
   k.push_back(static_cast<char>('A' + (p.first ? 1 : 0) + 2 * (p.energy ? 1 : 0) + 4 * (p.out ? 1 : 0) +
                                 8 * (p.zero_mom ? 1 : 0) + 16 * (p.check_all ? 1 : 0)));
+  k.push_back(static_cast<char>('a' + (p.drift_next ? 1 : 0) + 2 * (p.drifted ? 1 : 0)));
   for (char r : p.rebuild) k.push_back(r ? '1' : '0');
   k.push_back('|');
   return k;
@@ -1346,8 +1377,14 @@ void Engine::run_plans(const std::vector<StepPlan>& plans) {
       if (e->timing) cudaEventRecord(e->ev1, e->st);
     }
   } record_end{this};
-  std::string key = std::to_string(integrator_index) + ":";
-  for (const auto& p : plans) key += plan_key(p);
+  // the key carries the positions buffer the segment starts from: a graph replays
+  // the buffer pointers it captured
+  std::string key = std::to_string(integrator_index) + ":" + std::to_string(posq_cur) + ":";
+  int flips = 0;
+  for (const auto& p : plans) {
+    key += plan_key(p);
+    flips += p.drift_next ? 1 : 0;
+  }
   GraphEntry* ge = nullptr;
   if (opt.use_graphs && plans.size() >= 2) {
     ge = &graphs[key];
@@ -1356,6 +1393,7 @@ void Engine::run_plans(const std::vector<StepPlan>& plans) {
   if (ge && ge->exec) {
     CK(cudaGraphLaunch(ge->exec, st));
     launches += ge->kernels;
+    if (flips & 1) flip_posq();  // as enqueue_step did while the graph was captured
   } else if (ge && ge->seen >= 2) {
     if (graphs.size() > 64) {  // keep the cache bounded
       for (auto it = graphs.begin(); it != graphs.end();) {
@@ -1544,6 +1582,15 @@ void Engine::advance(long long max_steps, int* fin) {
         break;
     }
     need_check_all = plans.front().check_all;
+    // each force kernel also runs the next step's kick and drift when both steps
+    // are nve steps of this segment and the first computes no energies or output
+    if (fuse_drift && integ == I_NVE && !learned_active)
+      for (size_t i = 0; i + 1 < plans.size(); ++i) {
+        StepPlan& a = plans[i];
+        StepPlan& b = plans[i + 1];
+        if (a.first || a.energy || a.out || b.first || b.check_all) continue;
+        a.drift_next = b.drifted = true;
+      }
     run_plans(plans);
     read_ctl();
     if (hctl->error) raise_device_error();
@@ -2167,6 +2214,7 @@ void pfmd_default_options(pfmd_options* o) {
   o->threads_per_row = 0;
   o->async_io = 1;
   o->skin_lists = 1;
+  o->fuse_steps = 1;
 }
 
 int pfmd_create_from_files(const char* input_path, const char* settings_filename, const pfmd_options* opt,

@@ -235,6 +235,44 @@ __device__ __forceinline__ void finish_force(const Atoms& A, const Epi& E, int a
   }
 }
 
+// finish_force, then (E.drift) the next step's first half-kick and drift of the
+// atom, fused into this kernel: the same FMAs as k_kick_drift, so a run is the
+// same bit for bit either way.  The previous drift's out-of-cell verdict is read
+// first (set before this kernel started): a pending one stops the run at the
+// next step's begin, with this step complete.  The new verdict goes to the other
+// parity slot, which no thread of this kernel reads.
+__device__ __forceinline__ void finish_force_drift(const Atoms& A, const Epi& E, const Box& B, Ctl* ctl, int ai,
+                                                   double fx, double fy, double fz) {
+  finish_force(A, E, ai, fx, fy, fz);
+  if (!E.drift) return;
+  const long long s = ctl->md_step;
+  if (ctl->pending_oob || ctl->pending_fused[s & 1]) {
+    set_error_at(ctl, ST_OUT_OF_CELL, EK_OOB, ctl->oob_atom + 1, 0, 0, s + 1);
+    return;
+  }
+  const int4 q = A.posq[ai];
+  if (!(E.mflag[ai] & 1)) {  // not moving: the same position in the next buffer
+    E.posq_next[ai] = make_int4(q.x, q.y, q.z, 0);
+    return;
+  }
+  const double4_32a f = A.frc[ai];
+  double4_32a v = A.vel[ai], p = A.pos[ai];
+  const double kt = A.kc[ai] * E.ts2;
+  v.x = kick1_fast(v.x, f.x, kt);
+  v.y = kick1_fast(v.y, f.y, kt);
+  v.z = kick1_fast(v.z, f.z, kt);
+  A.vel[ai] = v;
+  p.x = drift1_fast(p.x, v.x, E.ts1, B.L[0]);
+  p.y = drift1_fast(p.y, v.y, E.ts1, B.L[1]);
+  p.z = drift1_fast(p.z, v.z, E.ts1, B.L[2]);
+  A.pos[ai] = p;
+  E.posq_next[ai] = make_int4(quantize_int(p.x, B, 0), quantize_int(p.y, B, 1), quantize_int(p.z, B, 2), 0);
+  if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) {
+    atomicMin(&ctl->oob_atom, ai);
+    ctl->pending_fused[(s + 1) & 1] = 1;
+  }
+}
+
 // Energy of one row into the interaction's total (every thread of the grid calls it).
 __device__ __forceinline__ void energy_reduce(Ctl* ctl, int eslot, int ekey, double erow) {
   double v[1] = {erow}, out[1];

@@ -141,7 +141,12 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
     }
   }
   acc.template reduce<TPA>();
-  if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
+  if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) {
+    if constexpr (PREC)
+      finish_force_drift(A, E, B, ctl, ai, acc.get(0), acc.get(1), acc.get(2));
+    else
+      finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
+  }
 }
 
 void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const Atoms& A, const Box& B, void* Eb,

@@ -46,7 +46,7 @@ __global__ void k_step_begin(int phase, Changes ch, int nvms, double ms_de, Ctl*
       if (n > c.to_cap) n = c.to_cap;
       ctl->group_n[c.to] = n;
     }
-    if (ctl->pending_oob) {
+    if (oob_pending(ctl)) {
       set_error(ctl, ST_OUT_OF_CELL, EK_OOB, ctl->oob_atom + 1, 0, 0);
       return;
     }
@@ -62,15 +62,6 @@ __global__ void k_step_begin(int phase, Changes ch, int nvms, double ms_de, Ctl*
   }
 }
 
-// !(x > -tol .and. x < L + tol) with tol = 1e-7 (md_general.f90:346), evaluated
-// on the bit patterns with integer compares (GB300's FP64 pipe is narrow).  For
-// x >= +0 the patterns order like the values; a negative x (sign bit set, -0.0
-// included) is inside iff its magnitude is below tol.  NaN is outside either way.
-__device__ __forceinline__ bool out_of_cell(double x, double Ltol) {
-  const long long b = __double_as_longlong(x);
-  return b >= 0 ? b >= __double_as_longlong(Ltol)
-                : (unsigned long long)b >= (unsigned long long)__double_as_longlong(-0.0000001);
-}
 __device__ __forceinline__ void flag_oob(Ctl* ctl, int i) {
   atomicMin(&ctl->oob_atom, i);
   ctl->pending_oob = 1;
@@ -101,26 +92,9 @@ __global__ void k_invert_z(Atoms A, Box B, Ctl* ctl) {
 __device__ __forceinline__ double kick1(double v, double f, double m, double ts2) {
   return __dadd_rn(v, __dmul_rn(__ddiv_rn(__ddiv_rn(f, m), c_mass_coef), ts2));
 }
-// the same with kt = dt/2/(m*mass_coef) formed once per atom: one FMA
-__device__ __forceinline__ double kick1_fast(double v, double f, double kt) { return fma(f, kt, v); }
-// One shift back into [0, L] (md_integrators.f90:19-24): x > L and x < 0.0 decided
-// on the bit patterns (L > 0; the patterns of x >= +0 order like the values,
-// x < 0.0 is a set sign bit other than -0.0).  NaN stays NaN either way.
-__device__ __forceinline__ double wrap1(double x, double L) {
-  const long long b = __double_as_longlong(x);
-  if (b > __double_as_longlong(L))
-    x = x - L;
-  else if (b < 0 && b != (long long)0x8000000000000000ULL)
-    x = x + L;
-  return x;
-}
 // x = x + v*ts(1) then the shift, rounded as written
 __device__ __forceinline__ double drift1(double x, double v, double ts1, double L) {
   return wrap1(__dadd_rn(x, __dmul_rn(v, ts1)), L);
-}
-// the precision form: one FMA
-__device__ __forceinline__ double drift1_fast(double x, double v, double ts1, double L) {
-  return wrap1(fma(v, ts1, x), L);
 }
 
 template <bool EXACT>
@@ -189,7 +163,7 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   }
   if (ctl->stop) return;
   if (begin) {
-    if (ctl->pending_oob) {
+    if (oob_pending(ctl)) {
       // the step counter has not advanced yet: the error belongs to the step begun here
       set_error_at(ctl, ST_OUT_OF_CELL, EK_OOB, ctl->oob_atom + 1, 0, 0, ctl->md_step + 1);
       return;
@@ -234,6 +208,16 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
       A.posq[i] = make_int4(quantize_int(p.x, B, 0), quantize_int(p.y, B, 1), quantize_int(p.z, B, 2), 0);
   }
   if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
+}
+
+__global__ void k_step_begin_fused(Ctl* ctl) {
+  if (ctl->stop) return;
+  ctl->md_step = ctl->md_step + 1;
+  ctl->pe_prev = ctl->pe_last;
+}
+void launch_step_begin_fused(Ctl* ctl, cudaStream_t s) {
+  k_step_begin_fused<<<1, 1, 0, s>>>(ctl);
+  ++g_kernel_launches;
 }
 
 __device__ __forceinline__ double ke_of(const Atoms& A, int i) {

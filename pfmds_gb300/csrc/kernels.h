@@ -149,6 +149,12 @@ struct Epi {
   const unsigned char* mflag;
   double* eatom;  // energy steps: per-atom energy of the interaction (rjl: the row energy;
                   // tb: half of every bond), or null
+  // drift (precision rjl force kernel, nve): after the second half-kick also the
+  // next step's first half-kick and drift of the row's atom, its fixed-point
+  // position into posq_next (the buffer the next step reads)
+  int drift = 0;
+  double ts1 = 0.0;
+  int4* posq_next = nullptr;
 };
 
 // ---------------- neighbour lists (nlist.cu) ----------------
@@ -210,6 +216,9 @@ void launch_invert_z(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_kick(const GroupRef& g, bool xyz, double ts2, bool exact, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, const Atoms& A, const Box& B,
                   Ctl* ctl, cudaStream_t s);
+// The step-begin bookkeeping of a step whose kick and drift ran in the previous
+// step's force kernel: the step counter and the previous potential energy.
+void launch_step_begin_fused(Ctl* ctl, cudaStream_t s);
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,

@@ -42,3 +42,22 @@ def test_skin_lists_skip_rebuilds_and_stay_complete(tmp_path, built):
     assert np.minimum(dd, box - dd).max() < 1e-4
     assert np.sqrt(((fs - fr) ** 2).mean()) / np.sqrt((fr ** 2).mean()) < 1e-3
     assert s.energies()["conserved"] == pytest.approx(r.energies()["conserved"], rel=1e-6)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_fused_kick_drift_is_bitwise_the_separate_one(tmp_path, built, graphs):
+    """The force kernel that also runs the next step's kick and drift gives the
+    same trajectory, bit for bit, as the separate kick-drift kernel, across list
+    rebuilds, energy steps and segment ends."""
+    configs.cu_slab(str(tmp_path), nx=8, ny=8, nz=6, steps=400, log_period=10, temperature=300.0)
+    d = str(tmp_path)
+    runs = []
+    for fuse in (True, False):
+        s = pf.Simulation(d, form="precision", out_period=10 ** 6, fuse_steps=fuse, use_graphs=graphs)
+        for n in (7, 30, 1, 45):
+            s.advance(n)
+        runs.append(s.state() + (s.energies()["conserved"],))
+        s.close()
+    for a, b in zip(runs[0][:3], runs[1][:3]):
+        assert np.array_equal(a, b)
+    assert runs[0][3] == runs[1][3]
