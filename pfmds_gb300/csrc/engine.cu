@@ -2132,8 +2132,20 @@ double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
         return true;
       }
       if (kind == pfmd_io::K_RJL && (name == "rjl_density" || name == "rjl_force")) {
+        // the force pass as the step runs it: with the kick and, when steps fuse, the
+        // next step's kick and drift -- here with zero time steps, so the state keeps
+        // its values
+        Epi e{0, 0, prec ? 0 : 1, 0.0, mflag.p, nullptr};
+        if (name == "rjl_force" && kick_last && mflag.p) {
+          e.kick = 1;
+          if (fuse_drift) {
+            e.drift = 1;
+            e.ts1 = 0.0;
+            e.posq_next = posq_cur ? posq.p : posq2.p;
+          }
+        }
         launch_rjl(prec, false, L1, I.rjl, A, box, I.scratch.p, I.pair.p, ctl, eslot, 0, st,
-                   name == "rjl_density" ? 1 : 2);
+                   name == "rjl_density" ? 1 : 2, e);
         return true;
       }
       if (kind == pfmd_io::K_REBOSC && (name == "rebo_bond" || name == "rebo_force")) {
