@@ -564,7 +564,7 @@ def run_ours(args):
         if extra is not None and args.batch_steps > 0:
             extra["batched_512"] = batched_config(d, device, args.batch_steps)
         if extra is not None and args.learned_steps > 0:
-            extra["learned"] = learned_config(d, device, run_steps=args.learned_steps)
+            extra["learned"] = learned_config(d, device, frames=args.learned_frames, run_steps=args.learned_steps)
 
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
@@ -653,6 +653,9 @@ def main():
                     help="MD steps of the NVE drift measurement (precision form; plain runs a fifth)")
     ap.add_argument("--quick", action="store_true",
                     help="headline timing loop only (no plain form, e2e, roofline or CPU legs), for profiling")
+    ap.add_argument("--learned-only", action="store_true",
+                    help="the learned form's leg alone (prints its JSON), for profiling its kernels")
+    ap.add_argument("--learned-frames", type=int, default=200, help="training frames per temperature")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -660,6 +663,10 @@ def main():
     __graft_entry__.build()
     if args.impl == "reference":
         run_reference(args)
+    elif args.learned_only:
+        with tempfile.TemporaryDirectory() as d:
+            print(json.dumps(learned_config(d, 0, frames=args.learned_frames, run_steps=args.learned_steps)),
+                  flush=True)
     else:
         run_ours(args)
 
