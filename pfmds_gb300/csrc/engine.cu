@@ -326,6 +326,7 @@ class Engine {
   Box box{};
   Atoms A{};
   DBuf<double4_32a> pos, vel, frc;
+  DBuf<double> stage;  // 9 N doubles: xyz-interleaved positions, velocities, forces in transfer
   DBuf<double> mass, kc;
   DBuf<int4> posq, posq2;  // fixed-point positions; two buffers when kick-drift fuses into the forces
   int posq_cur = 0;         // which buffer A.posq is (0: posq, 1: posq2)
@@ -451,6 +452,7 @@ class Engine {
   void run_plans(const std::vector<StepPlan>& plans);
   void host_events(const StepPlan& p);
   void get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f);
+  void get_state_to(double* p, double* v, double* f);
   std::unique_ptr<FileWriter> writer;  // snapshot / trajectory files (opt.async_io)
   void emit_file(const std::string& path, bool append, FileWriter::Format f);
   void check_writer(bool wait);
@@ -1111,7 +1113,8 @@ StepPlan Engine::plan(long long s) const {
     const ListH& L = lists[k];
     long long per = L.period;
     if (L.kind == L_CONVERSE) per = lists[static_cast<size_t>(L.src)].period;
-    p.rebuild[k] = (s % per == 0) ? 1 : 0;
+    // after set_state the first step also updates the lists
+    p.rebuild[k] = (s % per == 0 || need_check_all) ? 1 : 0;
   }
   return p;
 }
@@ -1430,33 +1433,27 @@ void Engine::run_plans(const std::vector<StepPlan>& plans) {
   need_check_all = false;
 }
 
-void Engine::get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f) {
-  std::vector<double4_32a> tp(static_cast<size_t>(N)), tv(static_cast<size_t>(N)), tf;
-  if (N) {
-    CK(cudaMemcpyAsync(tp.data(), pos.p, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(tv.data(), vel.p, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, st));
-    if (f) {
-      tf.resize(static_cast<size_t>(N));
-      CK(cudaMemcpyAsync(tf.data(), frc.p, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, st));
-    }
+// The state as xyz-interleaved doubles, converted on the device and copied
+// straight into the destinations (any of them may be null).
+void Engine::get_state_to(double* p, double* v, double* f) {
+  if (N <= 0) return;
+  const size_t n3 = 3 * static_cast<size_t>(N);
+  if (!stage.p) stage.alloc(3 * n3);
+  double* dst[3] = {p, v, f};
+  const double4_32a* src[3] = {pos.p, vel.p, frc.p};
+  for (int k = 0; k < 3; ++k) {
+    if (!dst[k]) continue;
+    launch_d4_to_xyz(N, src[k], stage.p + k * n3, st);
+    CK(cudaMemcpyAsync(dst[k], stage.p + k * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, st));
   }
   CK(cudaStreamSynchronize(st));
+}
+
+void Engine::get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f) {
   p.resize(3 * static_cast<size_t>(N));
   v.resize(3 * static_cast<size_t>(N));
   if (f) f->resize(3 * static_cast<size_t>(N));
-  for (int i = 0; i < N; ++i) {
-    p[3 * i] = tp[i].x;
-    p[3 * i + 1] = tp[i].y;
-    p[3 * i + 2] = tp[i].z;
-    v[3 * i] = tv[i].x;
-    v[3 * i + 1] = tv[i].y;
-    v[3 * i + 2] = tv[i].z;
-    if (f) {
-      (*f)[3 * i] = tf[i].x;
-      (*f)[3 * i + 1] = tf[i].y;
-      (*f)[3 * i + 2] = tf[i].z;
-    }
-  }
+  get_state_to(p.data(), v.data(), f ? f->data() : nullptr);
 }
 
 std::string Engine::nlists_load_text() {  // md_interactions.f90:427-444
@@ -2304,14 +2301,7 @@ int pfmd_md_step(const pfmd_ctx* c, long long* s, double* t) {
 
 int pfmd_get_state(pfmd_ctx* c, double* pos, double* vel, double* frc) {
   if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
-  return guard(c, [&] {
-    std::vector<double> p, v, f;
-    c->e->get_state_host(p, v, &f);
-    size_t n = 3 * static_cast<size_t>(c->e->N);
-    if (pos) std::memcpy(pos, p.data(), n * sizeof(double));
-    if (vel) std::memcpy(vel, v.data(), n * sizeof(double));
-    if (frc) std::memcpy(frc, f.data(), n * sizeof(double));
-  });
+  return guard(c, [&] { c->e->get_state_to(pos, vel, frc); });
 }
 
 int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
@@ -2319,17 +2309,18 @@ int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
   return guard(c, [&] {
     pfmd::Engine& e = *c->e;
     const int N = e.N;
-    std::vector<double4_32a> t(static_cast<size_t>(N));
+    const size_t n3 = 3 * static_cast<size_t>(N);
+    if (N && (pos || vel) && !e.stage.p) e.stage.alloc(3 * n3);
+    // copied as given, converted on the device
     if (pos && N) {
-      for (int i = 0; i < N; ++i) t[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
-      e.pos.upload(t.data(), t.size(), e.st);
-      CK(cudaStreamSynchronize(e.st));
+      CK(cudaMemcpyAsync(e.stage.p, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, e.st));
+      pfmd::launch_xyz_to_d4(N, e.stage.p, e.pos.p, e.st);
       pfmd::launch_pack_posq(e.A, e.box, e.ctl, e.st);
-      e.need_check_all = true;
+      e.need_check_all = true;  // also rebuilds the lists (skin-triggered ones if needed) at the next step
     }
     if (vel && N) {
-      for (int i = 0; i < N; ++i) t[i] = make_double4_32a(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
-      e.vel.upload(t.data(), t.size(), e.st);
+      CK(cudaMemcpyAsync(e.stage.p + n3, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, e.st));
+      pfmd::launch_xyz_to_d4(N, e.stage.p + n3, e.vel.p, e.st);
     }
     CK(cudaStreamSynchronize(e.st));
   });

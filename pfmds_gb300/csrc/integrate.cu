@@ -210,6 +210,30 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 
+__global__ void k_xyz_to_d4(int n, const double* __restrict__ xyz, double4_32a* d4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d4[i] = make_double4_32a(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0);
+}
+__global__ void k_d4_to_xyz(int n, const double4_32a* __restrict__ d4, double* xyz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double4_32a v = d4[i];
+    xyz[3 * i] = v.x;
+    xyz[3 * i + 1] = v.y;
+    xyz[3 * i + 2] = v.z;
+  }
+}
+void launch_xyz_to_d4(int n, const double* xyz, double4_32a* d4, cudaStream_t s) {
+  if (n <= 0) return;
+  k_xyz_to_d4<<<(n + 255) / 256, 256, 0, s>>>(n, xyz, d4);
+  ++g_kernel_launches;
+}
+void launch_d4_to_xyz(int n, const double4_32a* d4, double* xyz, cudaStream_t s) {
+  if (n <= 0) return;
+  k_d4_to_xyz<<<(n + 255) / 256, 256, 0, s>>>(n, d4, xyz);
+  ++g_kernel_launches;
+}
+
 __global__ void k_step_begin_fused(Ctl* ctl) {
   if (ctl->stop) return;
   ctl->md_step = ctl->md_step + 1;

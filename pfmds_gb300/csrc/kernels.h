@@ -205,6 +205,12 @@ void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const Li
                 const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot,
                 int ekey, cudaStream_t s, int parts = 3);
 
+// ---------------- state transfer (integrate.cu) ----------------
+// xyz-interleaved doubles (the reference's (3,N) arrays, as the host passes them)
+// to / from the device's 32-byte atom records, on the device.
+void launch_xyz_to_d4(int n, const double* xyz, double4_32a* d4, cudaStream_t s);
+void launch_d4_to_xyz(int n, const double4_32a* d4, double* xyz, cudaStream_t s);
+
 // ---------------- integration and reductions (integrate.cu) ----------------
 // phase: 0 = group changes + out-of-cell check, 1 = nvms exit test, 2 = both
 void launch_step_begin(int phase, int n_changes, const ChangeSpec* changes, int nvms, double ms_de,
