@@ -278,6 +278,7 @@ def batched_config(root, device, steps, n_rep=512):
             t_one[form][1] += s.advance_timed(20) / 1e3
             s.close()
     one = {k: v[0] / v[1] for k, v in t_one.items()}
+    graphs = b.graphs()
     b.close()
     # the plain FP64 form on two of the sampled replicas (one of each kind), same
     # start, same steps, energies every 100 steps: its drift is the integrator's
@@ -299,7 +300,8 @@ def batched_config(root, device, steps, n_rep=512):
                             "plain_fp64_second_half": pd[1], "batched": drift[r], "batched_second_half": drift2[r]})
     return {
         "workload": f"{R} replicas (LJ gas or Cu rjl slab, 500-20,000 atoms, 100-1,200 K, nve), {n_all} atoms, "
-                    f"{steps} steps, one persistent cooperative kernel per 100 steps",
+                    f"{steps} steps, one persistent cooperative kernel per 100 steps"
+                    + (", the run replayed as a captured CUDA graph" if graphs > 0 else ", launched directly"),
         "value": rate, "unit": "atom-steps/s", "ms_per_md_step": ms / (steps - 10),
         "tpa_per_bucket": dict(zip(["lj<2k", "lj<8k", "lj>=8k", "rjl<2k", "rjl<8k", "rjl>=8k"], tpa)),
         "one_at_a_time_sample": {"replicas": len(sample), "plain": one["plain"], "precision": one["precision"]},

@@ -277,6 +277,10 @@ int pfmd_batch_replica(const pfmd_batch* batch, int r, int* atom0, int* n, int* 
  * drift, lists at the list period, forces, kick; energies at the log period);
  * *device_ms (may be NULL) is the device time of the launches. */
 int pfmd_batch_run(pfmd_batch* batch, long long nsteps, double* device_ms);
+/* Runs are captured as CUDA graphs (one per run length) and replayed: *n is the
+ * number held now, -1 if the driver could not capture the cooperative launch
+ * (runs then launch directly). */
+int pfmd_batch_graphs(const pfmd_batch* batch, int* n);
 /* Autotuner: times `steps` MD steps with threads per list row 1, 2, 4 and 8 for
  * each size bucket (kind x {<2,000, <8,000, larger} atoms) on a saved copy of the
  * state, keeps the fastest and restores the state; only at a list-period boundary.

@@ -33,7 +33,7 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_nlist_shape", "pfmd_get_nlist", "pfmd_nlist_load", "pfmd_get_gr_norm", "pfmd_set_group_n",
            "pfmd_get_stream", "pfmd_kernel_launches", "pfmd_advance_timed", "pfmd_time_kernel",
            "pfmd_flush_l2", "pfmd_batch_create", "pfmd_batch_destroy", "pfmd_batch_errmsg", "pfmd_batch_info",
-           "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
+           "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_graphs", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
            "pfmd_learned_check", "pfmd_learned_status", "pfmd_learned_gradient", "pfmd_nlist_builds", "pfmd_rjl_forces_noalloc",
            "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting")
@@ -106,6 +106,7 @@ def load(path=LIB_PATH):
     L.pfmd_batch_replica.argtypes = [vp, C.c_int, ip, ip, ip]
     L.pfmd_batch_run.argtypes = [vp, C.c_longlong, dp]
     L.pfmd_batch_run_list.argtypes = [vp, C.c_char_p, C.c_int, dp]
+    L.pfmd_batch_graphs.argtypes = [vp, ip]
     L.pfmd_nlist_builds.argtypes = [vp, llp, ip]
     L.pfmd_batch_tune.argtypes = [vp, C.c_int, ip]
     L.pfmd_batch_set_tpa.argtypes = [vp, ip]
@@ -405,6 +406,12 @@ class Batch:
         ms = C.c_double()
         self._check(load().pfmd_batch_run(self._h, nsteps, C.byref(ms)))
         return ms.value
+
+    def graphs(self):
+        """CUDA graphs held for runs (-1: runs launch directly)."""
+        n = C.c_int()
+        self._check(load().pfmd_batch_graphs(self._h, C.byref(n)))
+        return n.value
 
     def run_list(self, out_path="", all_out=None):
         """Run every entry to the end of its nve stage and write each entry's

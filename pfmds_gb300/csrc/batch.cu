@@ -35,6 +35,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <numeric>
 #include <stdexcept>
@@ -762,7 +763,18 @@ struct Batch {
   int ntile = 0;
 
   ~Batch() {
+    clear_graphs();
     if (st) cudaStreamDestroy(st);
+  }
+
+  // The launches of a run of n steps in chunks, captured once as a CUDA graph and
+  // replayed: the kernel reads its step counter from device memory, so a replay
+  // continues where the last one stopped.  A change of tiles drops the graphs.
+  std::map<std::pair<long long, int>, cudaGraphExec_t> graphs;
+  bool graphs_ok = true;  // false if the driver cannot capture the cooperative launch
+  void clear_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
   }
 
   void load(const std::string& input_path, const std::string& list_file) {
@@ -890,6 +902,7 @@ struct Batch {
   }
 
   void build_tiles() {
+    clear_graphs();
     std::vector<Tile> t;
     for (size_t r = 0; r < reps.size(); ++r) {
       const int T = tpa[bucket_of(reps[r])], rpw = 32 / T;
@@ -1138,11 +1151,47 @@ struct Batch {
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
+    auto launches = [&] {
+      for (long long done = 0; done < nsteps;) {
+        const int k = static_cast<int>(std::min<long long>(chunk, nsteps - done));
+        launch(k);
+        done += k;
+      }
+    };
+    const auto key = std::make_pair(nsteps, chunk);
+    auto it = graphs.find(key);
+    if (it == graphs.end() && graphs_ok) {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        const long long before = g_kernel_launches;
+        for (long long done = 0; done < nsteps && ok;) {
+          int k = static_cast<int>(std::min<long long>(chunk, nsteps - done));
+          Dev D = dev_view();
+          void* args[] = {&D, &k};
+          ok = cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_batch), dim3(grid), dim3(kThreads), args, 0,
+                                           st) == cudaSuccess;
+          done += k;
+        }
+        g_kernel_launches = before;  // counted when the graph runs
+        ok = (cudaStreamEndCapture(st, &g) == cudaSuccess) && ok && g != nullptr;
+        if (ok) ok = cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+      }
+      if (ok) {
+        it = graphs.emplace(key, ge).first;
+      } else {
+        cudaGetLastError();  // not capturable here: launch directly from now on
+        graphs_ok = false;
+      }
+    }
     BCK(cudaEventRecord(e0, st));
-    for (long long done = 0; done < nsteps;) {
-      const int k = static_cast<int>(std::min<long long>(chunk, nsteps - done));
-      launch(k);
-      done += k;
+    if (it != graphs.end()) {
+      BCK(cudaGraphLaunch(it->second, st));
+      g_kernel_launches += (nsteps + chunk - 1) / chunk;
+    } else {
+      launches();
     }
     BCK(cudaEventRecord(e1, st));
     BCK(cudaEventSynchronize(e1));
@@ -1432,6 +1481,12 @@ int pfmd_batch_run(pfmd_batch* c, long long nsteps, double* device_ms) {
 int pfmd_batch_run_list(pfmd_batch* c, const char* out_path, int all_out_fd, double* device_ms) {
   if (!c || !c->b) return PFMD_E_STATE;
   return bguard(c, [&] { pfmd::batch::run_list(*c->b, fortio::trim(out_path ? out_path : ""), all_out_fd, device_ms); });
+}
+
+int pfmd_batch_graphs(const pfmd_batch* c, int* n) {
+  if (!c || !c->b || !n) return PFMD_E_STATE;
+  *n = c->b->graphs_ok ? static_cast<int>(c->b->graphs.size()) : -1;
+  return PFMD_OK;
 }
 
 int pfmd_batch_tune(pfmd_batch* c, int steps, int* tpa) {
