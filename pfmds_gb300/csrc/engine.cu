@@ -2497,6 +2497,8 @@ int pfmd_set_group_n(pfmd_ctx* c, int group, int n) {
     const int cap = static_cast<int>(e.groups[static_cast<size_t>(group - 1)].idx.size());
     e.hctl->group_n[group - 1] = std::max(0, std::min(n, cap));
     e.upload_ctl_groups();
+    // rows change with the group: skin-triggered lists rebuild at their next update step
+    CK(cudaMemsetAsync(e.ctl->list_need, 1, sizeof(e.ctl->list_need), e.st));
     CK(cudaStreamSynchronize(e.st));
   });
 }
