@@ -2047,7 +2047,11 @@ double Engine::kernel_bytes(const std::string& name) {
       // precision) and the force pass reads them back
       const double PC = prec ? 8.0 : 16.0;
       if (name == "rjl_density") return row_bytes(L1, IE, PC);
-      if (name == "rjl_force") return row_bytes(L1, IE + F, PC);
+      // with the next step's kick and drift fused in: k_kick_drift's 160 B per moving atom
+      if (name == "rjl_force")
+        return row_bytes(L1, IE + F, PC) +
+               (fuse_drift ? 160.0 * static_cast<double>(groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size())
+                           : 0.0);
       if (name == "forces") b += row_bytes(L1, IE, PC) + row_bytes(L1, IE + F, PC);
     }
     if (k == pfmd_io::K_REBOSC) {
