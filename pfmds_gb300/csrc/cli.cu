@@ -64,6 +64,12 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
         o.use_graphs = static_cast<int>(fortio::to_int(next()));
       } else if (arg == "-device") {
         o.device = static_cast<int>(fortio::to_int(next()));
+      } else if (arg == "-skin") {
+        o.skin_lists = static_cast<int>(fortio::to_int(next()));
+      } else if (arg == "-fuse") {
+        o.fuse_steps = static_cast<int>(fortio::to_int(next()));
+      } else if (arg == "-async_io") {
+        o.async_io = static_cast<int>(fortio::to_int(next()));
       } else if (arg == "-batch") {
         batched = true;
       }
