@@ -447,7 +447,7 @@ class Engine {
   bool is_event(const StepPlan& p) const;
   void enqueue_step(const StepPlan& p);
   void enqueue_lists(const StepPlan& p);
-  void enqueue_forces(bool energy, bool kick = false, bool drift_next = false);
+  void enqueue_forces(bool energy, bool kick = false, bool drift_next = false, bool begin = false);
   void plan_fusion();
   void run_plans(const std::vector<StepPlan>& plans);
   void host_events(const StepPlan& p);
@@ -1222,7 +1222,7 @@ void Engine::plan_fusion() {
   }
 }
 
-void Engine::enqueue_forces(bool energy, bool kick, bool drift_next) {
+void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin) {
   // which launch is the first / last force writer
   const int nint = static_cast<int>(inters.size());
   auto epi = [&](bool first, bool last) {
@@ -1234,6 +1234,7 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next) {
       e.ts1 = ts[0];
       e.posq_next = posq_cur ? posq.p : posq2.p;
     }
+    e.begin = (first && begin) ? 1 : 0;
     return e;
   };
   for (int k = 0; k < nint; ++k) {
@@ -1288,8 +1289,16 @@ void Engine::enqueue_step(const StepPlan& p) {
   // an nve step without group changes lets the kick-drift kernel open the step
   const bool fused_begin = !p.first && integ == I_NVE && changes.empty() && !S.invert_z_vel && fuse_kick_drift &&
                            groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size() > 0;
+  // a drifted step (its kick and drift ran in the previous step's force kernel)
+  // that launches nothing before a single rjl interaction opens in that
+  // interaction's density pass
+  bool begin_in_forces = false;
   if (p.drifted) {
-    launch_step_begin_fused(ctl, st);  // kick and drift ran in the previous step's force kernel
+    bool rebuilds = false;
+    for (char r : p.rebuild) rebuilds = rebuilds || r;
+    begin_in_forces = !rebuilds && !p.zero_mom && store_first && inters.size() == 1 &&
+                      inters[0].spec.kind == pfmd_io::K_RJL && inters[0].lists[2] < 0 && !learned_active;
+    if (!begin_in_forces) launch_step_begin_fused(ctl, st);
   } else if (fused_begin) {
     // (nothing: k_kick_drift below)
   } else if (S.invert_z_vel) {
@@ -1330,7 +1339,7 @@ void Engine::enqueue_step(const StepPlan& p) {
   const GroupRef gall = gref(S.all_atoms);
   if (p.zero_mom) launch_zero_momentum(gall, A, ctl, st);
   if (!store_first) launch_zero_forces(gall, A, ctl, st);
-  enqueue_forces(p.energy, !p.first, p.drift_next);
+  enqueue_forces(p.energy, !p.first, p.drift_next, begin_in_forces);
   if (p.drift_next) flip_posq();  // the next step reads the positions written by this one
   if (!p.first) {
     if (!kick_last) {

@@ -16,13 +16,41 @@
 
 namespace pfmd {
 
+// Launches with programmatic stream serialisation: the grid is set up while the
+// previous kernel on the stream drains, and waits in griddepcontrol.wait (first
+// statement of both rjl kernels) until that kernel has completed and its writes
+// are visible.  Neither kernel triggers its dependents early: an early trigger
+// let the next grid's blocks take SM slots from the running one (38.3 us per
+// MD step against 32.1 on the 65,536-atom slab).
+template <class K, class... Args>
+static void launch_dependent(K kern, int grid, int block, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // inv_eb holds 1/Eb per atom: double for the plain form, float for the precision form.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb,
-                                                     double2* pair, Ctl* ctl, int eslot, int ekey, double* eatom) {
+                                                     double2* pair, Ctl* ctl, int eslot, int ekey, double* eatom,
+                                                     int begin) {
   using T = RT<PREC>;
   using R = typename T::R;
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
   if (ctl->stop) return;
+  if (begin && blockIdx.x == 0 && threadIdx.x == 0) {
+    // nothing else in this launch reads these two
+    ctl->md_step = ctl->md_step + 1;
+    ctl->pe_prev = ctl->pe_last;
+  }
   const Grp<TPA> g;
   const bool valid = g.row < L.rows;
   const int n = valid ? L.nnum[g.row] : 0;
@@ -31,12 +59,18 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   Acc1<PREC> eb2, er;
   if (n > 0) {
     const auto pi = T::load(A, ai);
-    // precision: no unrolling measured fastest on the 65,536-atom slab (14.4 us
+    // the next slot's partner index is loaded one iteration ahead, so its load
+    // overlaps this slot's gather instead of preceding the next one (14.6 -> 14.4 us
+    // on the 65,536-atom slab); precision: no unrolling measured fastest (14.4 us
     // against 15.6 with 4)
+    int aj = g.sub < n ? ent(L, g.row, g.sub) : ai;
 #pragma unroll(PREC ? 1 : 4)
     for (int p = g.sub; p < n; p += TPA) {
       R dr[3];
-      const R r2 = T::d2(pi, T::load(A, ent(L, g.row, p)), B, dr);
+      const int pn = p + TPA;
+      const int aj_next = pn < n ? ent(L, g.row, pn) : ai;
+      const R r2 = T::d2(pi, T::load(A, aj), B, dr);
+      aj = aj_next;
       if constexpr (PREC) {
         // r and 1/r from one reciprocal square root
         const float ir = rsqrtf(r2), r = r2 * ir;
@@ -104,6 +138,7 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
 template <bool PREC, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A, Box B, const void* inv_eb,
                                                    const double2* pair, Ctl* ctl, Epi E) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
   using T = RT<PREC>;
   using R = typename T::R;
   using IE = typename std::conditional<PREC, float, double>::type;
@@ -123,10 +158,13 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
     else
       ieb_i = ieb[ai];
     // unroll 2: measured faster than 4 or 8 on the 65,536-atom slab (fewer live
-    // registers, more resident warps for the gather latency)
+    // registers, more resident warps for the gather latency); the partner index is
+    // loaded one iteration ahead, as in the density pass
+    int aj = g.sub < n ? ent(L, g.row, g.sub) : ai;
 #pragma unroll 2
     for (int p = g.sub; p < n; p += TPA) {
-      const int aj = ent(L, g.row, p);
+      const int pn = p + TPA;
+      const int aj_next = pn < n ? ent(L, g.row, pn) : ai;
       R dr[3];
       if constexpr (PREC) {
         const int4 pj = A.posq[aj];
@@ -140,6 +178,7 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
         const R k = ab.x - ab.y * (ieb_i + ieb[aj]);
         acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
       }
+      aj = aj_next;
     }
   }
   acc.template reduce<TPA>();
@@ -155,6 +194,7 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
                 double2* pair, Ctl* ctl, int eslot, int ekey, cudaStream_t s, int parts, const Epi& E) {
   if (L.rows == 0) {
     if (energy && (parts & 1)) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
+    if (E.begin && (parts & 1)) launch_step_begin_fused(ctl, s);
     return;
   }
   with_bool(prec, [&](auto pr) {
@@ -165,9 +205,11 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
       with_tpa(tpa1, [&](auto t) {
         constexpr int TP = decltype(t)::value;
         if (energy)
-          k_rjl_density<PR, true, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey, E.eatom);
+          launch_dependent(k_rjl_density<PR, true, TP>, grid, 256, s, L, P, A, B, Eb, pair, ctl, eslot, ekey,
+                           E.eatom, E.begin);
         else
-          k_rjl_density<PR, false, TP><<<grid, 256, 0, s>>>(L, P, A, B, Eb, pair, ctl, eslot, ekey, nullptr);
+          launch_dependent(k_rjl_density<PR, false, TP>, grid, 256, s, L, P, A, B, Eb, pair, ctl, eslot, ekey,
+                           (double*)nullptr, E.begin);
         ++g_kernel_launches;
       });
     }
@@ -176,7 +218,8 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
       const int grid = nblk((long long)L.rows * L.tpa, 128);
       with_tpa(L.tpa, [&](auto t) {
         constexpr int TP = decltype(t)::value;
-        k_rjl_force<PR, TP><<<grid, 128, 0, s>>>(L, P, A, B, Eb, pair, ctl, E);
+        launch_dependent(k_rjl_force<PR, TP>, grid, 128, s, L, P, A, B, (const void*)Eb, (const double2*)pair, ctl,
+                         E);
         ++g_kernel_launches;
       });
     }

@@ -155,6 +155,11 @@ struct Epi {
   int drift = 0;
   double ts1 = 0.0;
   int4* posq_next = nullptr;
+  // begin (rjl density pass): its first thread also opens the step (the step
+  // counter and the previous potential energy, as k_step_begin_fused), for a step
+  // whose kick and drift ran in the previous force kernel and that launches
+  // nothing before the density pass
+  int begin = 0;
 };
 
 // ---------------- neighbour lists (nlist.cu) ----------------
