@@ -321,22 +321,24 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_build(ListDev L, CellGrid 
   }
 }
 
-// Self lists (row group == column group) without sorting: one block per cell.
-// The rows are the cell's own atoms.  The block stages the candidates of the
-// surrounding cells (the same x-runs, in the same order, as k_build) in shared
-// memory once, and its warps scan them for each of the cell's rows, so a
-// candidate is read from global memory once per cell instead of once per row.
-// Rows and entries come out exactly as k_build<PREC, CAP, false> writes them;
-// lessnnum is not kept (no kernel reads it for unsorted rows).
+// Self lists (row group == column group) without sorting: one warp per cell,
+// four cells per block.  The warp stages the candidates of the surrounding cells
+// (the same x-runs, in the same order, as k_build) in its share of shared memory,
+// then each lane takes one of the cell's rows and scans the staged candidates in
+// order; every lane reads the same candidate at once (a shared-memory broadcast),
+// so a (row, candidate) test costs about a dozen instructions for up to 32 rows.
+// A lane appends its hits in candidate order: rows and entries come out exactly as
+// k_build<PREC, CAP, false> writes them.  lessnnum is not kept (no kernel reads
+// it for unsorted rows).  On the 65,536-atom slab (6,615 cells) a rebuild takes as
+// long as with one 4-warp block per cell and a warp per row, and a list kept by
+// the skin test launches a quarter of the blocks.
 static constexpr int kCellWarps = 4;
-static constexpr int kCellCand = 1024;  // candidates staged per pass
-static constexpr int kCellRows = 64;    // rows per pass
+static constexpr int kWarpCand = 256;  // candidates staged per pass, per warp
 
 __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, CellGrid cg, Box B, float rcp2, Ctl* ctl) {
-  __shared__ float4 s_rel[kCellCand];  // candidate position relative to the cell corner, atom in w
-  __shared__ int s_off[19];  // prefix offsets of up to 18 candidate runs
-  __shared__ int s_beg[18];  // run starts in the cell-ordered arrays
-  __shared__ int s_cnt[kCellRows];
+  __shared__ float4 s_rel_all[kCellWarps][kWarpCand];  // candidate relative to the cell corner, atom in w
+  __shared__ int s_off_all[kCellWarps][19];             // prefix offsets of up to 18 candidate runs
+  __shared__ int s_beg_all[kCellWarps][18];             // run starts in the cell-ordered arrays
   if (ctl->stop || skin_keep(ctl, L.skin)) return;
   const int n1 = ctl->group_n[L.row_group];
   // update_neighbour_list only acts when the group and the list are non-empty
@@ -345,15 +347,21 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
     if (blockIdx.x == 0 && threadIdx.x == 0) set_error(ctl, ST_PARAM, EK_NONE, L.id, n1, L.rows);
     return;
   }
-  const int c = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c = blockIdx.x * kCellWarps + w;
+  if (c >= cg.ncell) return;
   const int r0 = cg.start[c], nr = cg.start[c + 1] - r0;
   if (nr == 0) return;
+  float4* s_rel = s_rel_all[w];
+  int* s_off = s_off_all[w];
+  int* s_beg = s_beg_all[w];
   const int nx = cg.nc[0], ny = cg.nc[1], nz = cg.nc[2];
   const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
-  if (threadIdx.x < 18) {
-    // run t: (y, z) row t/2 of the 3x3 (fewer when a dimension has < 3 cells),
-    // z outer, y inner; x-run t&1
-    const int t = threadIdx.x, which = t & 1, yz = t >> 1;
+  // run t: (y, z) row t/2 of the 3x3 (fewer when a dimension has < 3 cells), z
+  // outer, y inner; x-run t&1
+  int len = 0;
+  if (lane < 18) {
+    const int t = lane, which = t & 1, yz = t >> 1;
     const int my = ny < 3 ? ny : 3, mz = nz < 3 ? nz : 3;
     int b = 0, e = 0;
     if (yz < my * mz) {
@@ -374,16 +382,19 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
       }
     }
     s_beg[t] = b;
-    s_off[t + 1] = e - b;
+    len = e - b;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_off[0] = 0;
-    for (int t = 0; t < 18; ++t) s_off[t + 1] += s_off[t];
+  // exclusive prefix of the run lengths over lanes 0..17
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
   }
-  __syncthreads();
+  if (lane < 18) s_off[lane + 1] = incl;
+  if (lane == 0) s_off[0] = 0;
+  __syncwarp();
   const int total = s_off[18];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // Positions relative to this cell's lower corner, as FP32: every candidate lies
   // within one cell of the corner cell, so with at least 4 cells per dimension
   // (cells at most L/4 wide) the fixed-point difference is the minimum image and a
@@ -393,82 +404,77 @@ __global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(ListDev L, Cell
   const unsigned int ref[3] = {(unsigned int)(((unsigned long long)cx << 32) / (unsigned long long)nx),
                                (unsigned int)(((unsigned long long)cy << 32) / (unsigned long long)ny),
                                (unsigned int)(((unsigned long long)cz << 32) / (unsigned long long)nz)};
-  for (int rg = 0; rg < nr; rg += kCellRows) {
-    const int nrg = min(kCellRows, nr - rg);
-    for (int i = threadIdx.x; i < nrg; i += blockDim.x) s_cnt[i] = 0;
-    for (int b0 = 0; b0 < total; b0 += kCellCand) {
-      const int nb = min(kCellCand, total - b0);
-      __syncthreads();  // the previous pass is done with the staged candidates
-      for (int v = threadIdx.x; v < nb; v += blockDim.x) {
+  for (int rg = 0; rg < nr; rg += 32) {
+    const bool has_row = rg + lane < nr;
+    const int kr = r0 + rg + (has_row ? lane : 0);
+    const int ai = cg.atom[kr], row = cg.jnd[kr];
+    const int4 piq = cg.posq[kr];
+    const float ix = (float)(int)((unsigned int)piq.x - ref[0]) * B.qs[0];
+    const float iy = (float)(int)((unsigned int)piq.y - ref[1]) * B.qs[1];
+    const float iz = (float)(int)((unsigned int)piq.z - ref[2]) * B.qs[2];
+    int cnt = 0;
+    for (int b0 = 0; b0 < total; b0 += kWarpCand) {
+      const int nb = min(kWarpCand, total - b0);
+      __syncwarp();  // the previous pass is done with the staged candidates
+      int r = 0;
+#pragma unroll 4
+      for (int v = lane; v < nb; v += 32) {
         const int g = b0 + v;
-        int r = 0;
         while (s_off[r + 1] <= g) ++r;  // g < total = s_off[18], so r < 18
-        const int k = s_beg[r] + (g - s_off[r]);
-        const int4 q = cg.posq[k];
-        float4 rp;
-        if (rel_ok) {
-          rp.x = (float)(int)((unsigned int)q.x - ref[0]) * B.qs[0];
-          rp.y = (float)(int)((unsigned int)q.y - ref[1]) * B.qs[1];
-          rp.z = (float)(int)((unsigned int)q.z - ref[2]) * B.qs[2];
-        } else {  // the raw fixed-point coordinates, for the per-pair minimum image
-          rp.x = __int_as_float(q.x);
-          rp.y = __int_as_float(q.y);
-          rp.z = __int_as_float(q.z);
+        {
+          const int k = s_beg[r] + (g - s_off[r]);
+          const int4 q = cg.posq[k];
+          float4 rp;
+          if (rel_ok) {
+            rp.x = (float)(int)((unsigned int)q.x - ref[0]) * B.qs[0];
+            rp.y = (float)(int)((unsigned int)q.y - ref[1]) * B.qs[1];
+            rp.z = (float)(int)((unsigned int)q.z - ref[2]) * B.qs[2];
+          } else {  // the raw fixed-point coordinates, for the per-pair minimum image
+            rp.x = __int_as_float(q.x);
+            rp.y = __int_as_float(q.y);
+            rp.z = __int_as_float(q.z);
+          }
+          rp.w = __int_as_float(cg.atom[k]);
+          s_rel[v] = rp;
         }
-        rp.w = __int_as_float(cg.atom[k]);
-        s_rel[v] = rp;
       }
-      __syncthreads();
-      for (int i = w; i < nrg; i += kCellWarps) {
-        const int kr = r0 + rg + i;
-        const int ai = cg.atom[kr], row = cg.jnd[kr];
-        const int4 piq = cg.posq[kr];
-        const float ix = (float)(int)((unsigned int)piq.x - ref[0]) * B.qs[0];
-        const float iy = (float)(int)((unsigned int)piq.y - ref[1]) * B.qs[1];
-        const float iz = (float)(int)((unsigned int)piq.z - ref[2]) * B.qs[2];
-        int cnt = s_cnt[i];
-        for (int k0 = 0; k0 < nb; k0 += 32) {
-          const int k = k0 + lane;
-          bool hit = false;
-          int aj = 0;
-          if (k < nb) {
-            const float4 c = s_rel[k];
-            aj = __float_as_int(c.w);
-            if (aj != ai) {
-              if (rel_ok) {
-                const float dx = c.x - ix, dy = c.y - iy, dz = c.z - iz;
-                hit = dx * dx + dy * dy + dz * dz < rcp2;
-              } else {
-                float d[3];
-                hit = mi_q(piq, make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z), 0), B, d) <
-                      rcp2;
-              }
+      __syncwarp();
+      if (has_row) {
+        if (rel_ok) {
+#pragma unroll 4
+          for (int k = 0; k < nb; ++k) {
+            const float4 q = s_rel[k];
+            const int aj = __float_as_int(q.w);
+            const float dx = q.x - ix, dy = q.y - iy, dz = q.z - iz;
+            if (aj != ai && dx * dx + dy * dy + dz * dz < rcp2) {
+              if (cnt < L.nmax) L.nlist[(size_t)cnt * L.stride + row] = aj;
+              ++cnt;
             }
           }
-          const unsigned m = __ballot_sync(0xffffffffu, hit);
-          if (hit) {
-            const int p = cnt + __popc(m & ((1u << lane) - 1u));
-            if (p < L.nmax) L.nlist[(size_t)p * L.stride + row] = aj;
+        } else {
+          for (int k = 0; k < nb; ++k) {
+            const float4 q = s_rel[k];
+            const int aj = __float_as_int(q.w);
+            float d[3];
+            if (aj != ai &&
+                mi_q(piq, make_int4(__float_as_int(q.x), __float_as_int(q.y), __float_as_int(q.z), 0), B, d) < rcp2) {
+              if (cnt < L.nmax) L.nlist[(size_t)cnt * L.stride + row] = aj;
+              ++cnt;
+            }
           }
-          cnt += __popc(m);
         }
-        if (lane == 0) s_cnt[i] = cnt;
       }
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nrg; i += blockDim.x) {
-      const int kr = r0 + rg + i;
-      const int row = cg.jnd[kr], cnt = s_cnt[i];
+    if (has_row) {
       if (cnt > L.nmax) {
         // 'error: too many neighbours', ind, nnumind  (md_neighbours.f90:80)
         set_error(ctl, ST_NLIST_OVERFLOW, EK_OVERFLOW, L.id, row + 1, L.nmax + 1);
       } else {
         L.nnum[row] = cnt;
-        L.pidx[row] = cg.atom[kr];
+        L.pidx[row] = ai;
         L.bnd[row] = INT_MAX;  // lessnnum of an unsorted row is formed when it is read back
       }
     }
-    __syncthreads();  // s_cnt is reset for the next group of rows
   }
 }
 
@@ -690,7 +696,7 @@ void launch_build_list(bool prec, const ListDev& L, const CellGrid& cg, const At
     if (L.sorted)
       build_dispatch<true, true>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
     else if (!converse && L.row_group == L.col_group && cg.ncell > 0)
-      { k_build_cells<<<cg.ncell, kCellWarps * 32, 0, s>>>(L, cg, B, (float)rc2, ctl); ++g_kernel_launches; }
+      { k_build_cells<<<(cg.ncell + kCellWarps - 1) / kCellWarps, kCellWarps * 32, 0, s>>>(L, cg, B, (float)rc2, ctl); ++g_kernel_launches; }
     else
       build_dispatch<true, false>(L, cg, A, B, rc2, (float)rc2, converse, src_rows, ctl, s);
   } else {
