@@ -54,9 +54,12 @@ def test_fused_kick_drift_is_bitwise_the_separate_one(tmp_path, built, graphs):
     runs = []
     for fuse in (True, False):
         s = pf.Simulation(d, form="precision", out_period=10 ** 6, fuse_steps=fuse, use_graphs=graphs)
+        energies = []
         for n in (7, 30, 1, 45):
             s.advance(n)
-        runs.append(s.state() + (s.energies()["conserved"],))
+            e = s.energies()
+            energies.append((e["ke"], e["pe"], e["conserved"]))
+        runs.append(s.state() + (energies,))
         s.close()
     for a, b in zip(runs[0][:3], runs[1][:3]):
         assert np.array_equal(a, b)
