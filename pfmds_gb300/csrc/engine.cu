@@ -373,6 +373,9 @@ class Engine {
   Ctl* ctl = nullptr;
   Ctl* hctl = nullptr;  // pinned host copy (header part)
   size_t ctl_head = 0;
+  // hctl equals the device's header: set by read_ctl, cleared when an API call
+  // that may launch work starts (energies reads the copy while it holds)
+  bool ctl_fresh = false;
   cudaStream_t st = nullptr;
   bool prec = false;
   bool fuse_kick_drift = true;
@@ -1019,6 +1022,7 @@ void Engine::tune_tpa() {
 void Engine::read_ctl() {
   CK(cudaMemcpyAsync(hctl, ctl, ctl_head, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  ctl_fresh = true;
 }
 
 void Engine::upload_ctl_groups() {
@@ -1442,19 +1446,50 @@ void Engine::run_plans(const std::vector<StepPlan>& plans) {
   need_check_all = false;
 }
 
-// The state as xyz-interleaved doubles, converted on the device and copied
-// straight into the destinations (any of them may be null).
+// A device view of a host array of n doubles, or null.  Page-locked host memory
+// (cudaHostAlloc, cudaHostRegister, or a pinned tensor) is reached by the GPU
+// over NVLink-C2C / PCIe, so the conversion kernels read and write it in place
+// instead of going through a staging copy.  Both ends of the array must lie in
+// page-locked memory with a device address; anything else (pageable memory)
+// takes the staging copy.
+static const double* host_view(const void* h, size_t n) {
+  if (!h || n == 0) return nullptr;
+  cudaPointerAttributes a0, a1;
+  const double* last = static_cast<const double*>(h) + (n - 1);
+  if (cudaPointerGetAttributes(&a0, h) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  const double* d = static_cast<const double*>(a0.devicePointer);
+  if (static_cast<const double*>(a1.devicePointer) != d + (n - 1)) return nullptr;
+  return d;
+}
+
+// The state as xyz-interleaved doubles, converted on the device and written
+// straight into the destinations (any of them may be null): in place when the
+// destination is page-locked, else through a staging copy.
 void Engine::get_state_to(double* p, double* v, double* f) {
   if (N <= 0) return;
   const size_t n3 = 3 * static_cast<size_t>(N);
-  if (!stage.p) stage.alloc(3 * n3);
   double* dst[3] = {p, v, f};
   const double4_32a* src[3] = {pos.p, vel.p, frc.p};
+  double* out[3] = {nullptr, nullptr, nullptr};
+  bool staged[3] = {false, false, false};
   for (int k = 0; k < 3; ++k) {
     if (!dst[k]) continue;
-    launch_d4_to_xyz(N, src[k], stage.p + k * n3, st);
-    CK(cudaMemcpyAsync(dst[k], stage.p + k * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, st));
+    out[k] = const_cast<double*>(host_view(dst[k], n3));
+    if (!out[k]) {
+      if (!stage.p) stage.alloc(3 * n3);
+      out[k] = stage.p + k * n3;
+      staged[k] = true;
+    }
   }
+  launch_d4_to_xyz(N, src, out, st);
+  for (int k = 0; k < 3; ++k)
+    if (staged[k])
+      CK(cudaMemcpyAsync(dst[k], stage.p + k * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
 }
 
@@ -1757,6 +1792,7 @@ void Engine::ensure_lists() {
 }
 
 double Engine::learned_check(bool switch_on_fail) {
+  ctl_fresh = false;  // launches the classical kernels
   const bool was = learned_active;
   ensure_lists();
   const GroupRef gall = gref(S.all_atoms);
@@ -2203,7 +2239,17 @@ struct pfmd_ctx {
 };
 
 template <class F>
+static int guard_keep(pfmd_ctx* c, F f);
+
+template <class F>
 static int guard(pfmd_ctx* c, F f) {
+  if (c && c->e) c->e->ctl_fresh = false;  // the call may launch work
+  return guard_keep(c, f);
+}
+
+// For calls that launch nothing that writes the control block.
+template <class F>
+static int guard_keep(pfmd_ctx* c, F f) {
   try {
     f();
     return PFMD_OK;
@@ -2314,7 +2360,7 @@ int pfmd_md_step(const pfmd_ctx* c, long long* s, double* t) {
 
 int pfmd_get_state(pfmd_ctx* c, double* pos, double* vel, double* frc) {
   if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
-  return guard(c, [&] { c->e->get_state_to(pos, vel, frc); });
+  return guard_keep(c, [&] { c->e->get_state_to(pos, vel, frc); });
 }
 
 int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
@@ -2323,17 +2369,23 @@ int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
     pfmd::Engine& e = *c->e;
     const int N = e.N;
     const size_t n3 = 3 * static_cast<size_t>(N);
-    if (N && (pos || vel) && !e.stage.p) e.stage.alloc(3 * n3);
-    // copied as given, converted on the device
+    // read in place when page-locked, else copied as given; converted on the device
+    const double* in[3] = {nullptr, nullptr, nullptr};
+    double4_32a* to[3] = {e.pos.p, e.vel.p, nullptr};
+    const double* h[2] = {pos, vel};
+    for (int k = 0; k < 2 && N; ++k) {
+      if (!h[k]) continue;
+      in[k] = pfmd::host_view(h[k], n3);
+      if (!in[k]) {
+        if (!e.stage.p) e.stage.alloc(3 * n3);
+        CK(cudaMemcpyAsync(e.stage.p + k * n3, h[k], sizeof(double) * n3, cudaMemcpyHostToDevice, e.st));
+        in[k] = e.stage.p + k * n3;
+      }
+    }
+    pfmd::launch_xyz_to_d4(N, in, to, e.st);
     if (pos && N) {
-      CK(cudaMemcpyAsync(e.stage.p, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, e.st));
-      pfmd::launch_xyz_to_d4(N, e.stage.p, e.pos.p, e.st);
       pfmd::launch_pack_posq(e.A, e.box, e.ctl, e.st);
       e.need_check_all = true;  // also rebuilds the lists (skin-triggered ones if needed) at the next step
-    }
-    if (vel && N) {
-      CK(cudaMemcpyAsync(e.stage.p + n3, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, e.st));
-      pfmd::launch_xyz_to_d4(N, e.stage.p + n3, e.vel.p, e.st);
     }
     CK(cudaStreamSynchronize(e.st));
   });
@@ -2342,9 +2394,9 @@ int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
 int pfmd_energies(pfmd_ctx* c, double* e_inter, double* pe, double* ke, double* temp, double* e_nhc,
                   double* e_cons) {
   if (!c || !c->e || !c->e->ctl) return PFMD_E_STATE;
-  return guard(c, [&] {
+  return guard_keep(c, [&] {
     pfmd::Engine& e = *c->e;
-    e.read_ctl();
+    if (!e.ctl_fresh) e.read_ctl();
     if (e_inter)
       for (size_t k = 0; k < e.inters.size(); ++k) e_inter[k] = e.hctl->e_inter[k];
     if (pe) *pe = e.hctl->pe_last;

@@ -210,29 +210,64 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 
-__global__ void k_xyz_to_d4(int n, const double* __restrict__ xyz, double4_32a* d4) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) d4[i] = make_double4_32a(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0);
+// xyz-interleaved arrays <-> double4 records, up to three arrays per launch
+// (blockIdx.y picks one; null ones are skipped).  One thread per double of the
+// interleaved array, so a warp reads or writes 256 contiguous bytes of it: the
+// interleaved side may be page-locked host memory reached over NVLink-C2C, where
+// whole-line accesses matter; the double4 side is device memory.
+struct XyzArrays {
+  const double* xyz[3];
+  double4_32a* d4[3];
+};
+struct D4Arrays {
+  const double4_32a* d4[3];
+  double* xyz[3];
+};
+__global__ void k_xyz_to_d4(long long n3, XyzArrays a) {
+  const int k = blockIdx.y;
+  const double* __restrict__ xyz = a.xyz[k];
+  if (!xyz) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  const long long i = t / 3;
+  const int c = (int)(t - 3 * i);
+  double* r = reinterpret_cast<double*>(a.d4[k] + i);
+  r[c] = xyz[t];
+  if (c == 0) r[3] = 0.0;
 }
-__global__ void k_d4_to_xyz(int n, const double4_32a* __restrict__ d4, double* xyz) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    const double4_32a v = d4[i];
-    xyz[3 * i] = v.x;
-    xyz[3 * i + 1] = v.y;
-    xyz[3 * i + 2] = v.z;
+__global__ void k_d4_to_xyz(long long n3, D4Arrays a) {
+  const int k = blockIdx.y;
+  double* xyz = a.xyz[k];
+  if (!xyz) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  const long long i = t / 3;
+  const int c = (int)(t - 3 * i);
+  xyz[t] = reinterpret_cast<const double*>(a.d4[k] + i)[c];
+}
+void launch_xyz_to_d4(int n, const double* const xyz[3], double4_32a* const d4[3], cudaStream_t s) {
+  if (n <= 0) return;
+  XyzArrays a;
+  for (int k = 0; k < 3; ++k) {
+    a.xyz[k] = xyz[k];
+    a.d4[k] = d4[k];
   }
-}
-void launch_xyz_to_d4(int n, const double* xyz, double4_32a* d4, cudaStream_t s) {
-  if (n <= 0) return;
-  k_xyz_to_d4<<<(n + 255) / 256, 256, 0, s>>>(n, xyz, d4);
+  const long long n3 = 3LL * n;
+  k_xyz_to_d4<<<dim3((unsigned)((n3 + 255) / 256), 3), 256, 0, s>>>(n3, a);
   ++g_kernel_launches;
 }
-void launch_d4_to_xyz(int n, const double4_32a* d4, double* xyz, cudaStream_t s) {
+void launch_d4_to_xyz(int n, const double4_32a* const d4[3], double* const xyz[3], cudaStream_t s) {
   if (n <= 0) return;
-  k_d4_to_xyz<<<(n + 255) / 256, 256, 0, s>>>(n, d4, xyz);
+  D4Arrays a;
+  for (int k = 0; k < 3; ++k) {
+    a.d4[k] = d4[k];
+    a.xyz[k] = xyz[k];
+  }
+  const long long n3 = 3LL * n;
+  k_d4_to_xyz<<<dim3((unsigned)((n3 + 255) / 256), 3), 256, 0, s>>>(n3, a);
   ++g_kernel_launches;
 }
+
 
 __global__ void k_step_begin_fused(Ctl* ctl) {
   if (ctl->stop) return;

@@ -213,8 +213,10 @@ void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const Li
 // ---------------- state transfer (integrate.cu) ----------------
 // xyz-interleaved doubles (the reference's (3,N) arrays, as the host passes them)
 // to / from the device's 32-byte atom records, on the device.
-void launch_xyz_to_d4(int n, const double* xyz, double4_32a* d4, cudaStream_t s);
-void launch_d4_to_xyz(int n, const double4_32a* d4, double* xyz, cudaStream_t s);
+// xyz-interleaved <-> double4 records, up to three arrays in one launch (null
+// entries skipped)
+void launch_xyz_to_d4(int n, const double* const xyz[3], double4_32a* const d4[3], cudaStream_t s);
+void launch_d4_to_xyz(int n, const double4_32a* const d4[3], double* const xyz[3], cudaStream_t s);
 
 // ---------------- integration and reductions (integrate.cu) ----------------
 // phase: 0 = group changes + out-of-cell check, 1 = nvms exit test, 2 = both
