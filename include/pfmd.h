@@ -136,10 +136,15 @@ int pfmd_natoms(const pfmd_ctx* ctx, int* n);
 int pfmd_md_step(const pfmd_ctx* ctx, long long* md_step, double* simulation_time);
 
 /* particles%positions / velocities / forces (md_general.f90:11-16); any pointer
- * may be NULL. */
+ * may be NULL.  Arrays are 3*N doubles, xyz per atom.  Page-locked arrays
+ * (cudaHostAlloc, cudaHostRegister) are written in place by the device; others
+ * through a staging copy.  Returns when the arrays are filled. */
 int pfmd_get_state(pfmd_ctx* ctx, double* pos, double* vel, double* frc);
 /* Overwrites positions and/or velocities (NULL leaves them); the next step checks
- * the positions as check_positions does. */
+ * the positions as check_positions does and puts every list through its update
+ * (a skin-triggered list is rebuilt if the new positions moved too far).
+ * Page-locked arrays are read in place by the device.  Returns when the arrays
+ * may be reused. */
 int pfmd_set_state(pfmd_ctx* ctx, const double* pos, const double* vel);
 
 /* Energies of the last energy step: interactions%energy (one per interaction),
