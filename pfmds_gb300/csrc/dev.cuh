@@ -89,8 +89,13 @@ struct Ctl {
   // be rebuilt at its next update step; skin_done counts the blocks of the kernel
   // that records a rebuild
   int list_need[PFMD_MAX_LISTS];
+  // two-level lists: outer_need[id] is 1 when list id's outer list (a wider list
+  // its rows are filtered from) must be rebuilt too
+  int outer_need[PFMD_MAX_LISTS];
   unsigned int skin_done[PFMD_MAX_LISTS];
-  unsigned int skin_max[PFMD_MAX_LISTS][2];  // squared displacements (float bits): since the build, last period
+  // squared displacements (float bits): since the build, over the last period,
+  // since the outer list's build
+  unsigned int skin_max[PFMD_MAX_LISTS][3];
   long long list_builds[PFMD_MAX_LISTS];     // rebuilds of each skin-managed list
   unsigned int counter[PFMD_RED_SLOTS];
   double partial[PFMD_PARTIALS];  // per-block partial sums of the grid reductions
@@ -131,7 +136,12 @@ __device__ __forceinline__ bool out_of_cell(double x, double Ltol) {
 
 // A skin-managed list whose atoms all stayed within half the skin since its last
 // build keeps its rows: its build kernels return at once.
-__device__ __forceinline__ bool skin_keep(const Ctl* ctl, int skin) { return skin >= 0 && ctl->list_need[skin] == 0; }
+// A list's rebuild kernels return at once when the skin test keeps it: skin is
+// the list's id, or PFMD_MAX_LISTS + id for the outer list of list id.
+__device__ __forceinline__ bool skin_keep(const Ctl* ctl, int skin) {
+  if (skin < 0) return false;
+  return skin >= PFMD_MAX_LISTS ? ctl->outer_need[skin - PFMD_MAX_LISTS] == 0 : ctl->list_need[skin] == 0;
+}
 
 // Box lengths, halves, and the fixed-point scales of the force-side positions:
 // a coordinate is stored as round(x * 2^32 / L) modulo 2^32 (posq), so the

@@ -89,6 +89,12 @@ static const double MOMENTA_COEF = 1.3806488 / 1.6605389217 * 1e-6;
 // Threads per list row: enough threads to fill the GPU (~152 SMs x 32 resident
 // warps) when rows are few, but at least ~2 entries per thread, and one thread
 // per row for large lists so that a warp reads 32 consecutive rows' slots.
+// Two-level lists: the outer list is this much (A) wider than the list, and it
+// is rebuilt when an atom moved more than half of it, less a tolerance for the
+// FP32 displacement test, since its build.
+static constexpr double kOuterMargin = 1.0;
+static constexpr double kOuterTol = 1e-3;
+
 static int auto_tpa(int rows, double mean_entries, bool prec) {
   const double want = 152.0 * 32 * 32 / std::max(rows, 1);
   int t = 1;
@@ -210,6 +216,10 @@ struct ListH {
   bool has_grid = false;
   double half_skin = 0.0;  // skin-triggered rebuilds: half of r_cut minus the interaction's cut-off
   DBuf<int4> xref, xprev;  // fixed-point positions at the last build / the last update step (skin >= 0)
+  // two-level list: the wider list this list's rows are filtered from, and the
+  // positions at its last build
+  std::unique_ptr<ListH> outer;
+  DBuf<int4> xout;
 };
 
 struct InterH {
@@ -450,6 +460,7 @@ class Engine {
   bool is_event(const StepPlan& p) const;
   void enqueue_step(const StepPlan& p);
   void enqueue_lists(const StepPlan& p);
+  void alloc_list(ListH& L);
   void enqueue_forces(bool energy, bool kick = false, bool drift_next = false, bool begin = false);
   void plan_fusion();
   void run_plans(const std::vector<StepPlan>& plans);
@@ -815,67 +826,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     g.d.alloc(std::max<size_t>(g.idx.size(), 1));
     g.d.upload(g.idx.data(), g.idx.size(), st);
   }
-  const double maxL = std::max(box.L[0], std::max(box.L[1], box.L[2]));
-  for (auto& L : lists) {
-    const size_t rows = static_cast<size_t>(std::max(L.d.rows, 1));
-    L.nnum.alloc(rows);
-    L.nnum.zero(st);
-    L.nlist.alloc(std::max<size_t>(static_cast<size_t>(L.d.nmax), 1) * static_cast<size_t>(L.d.stride));
-    L.nlist.zero(st);
-    L.pidx.alloc(rows);
-    L.pidx.zero(st);
-    L.less.alloc(rows);
-    L.less.zero(st);
-    L.bnd.alloc(rows);
-    L.bnd.zero(st);
-    L.d.nnum = L.nnum.p;
-    L.d.nlist = L.nlist.p;
-    L.d.pidx = L.pidx.p;
-    L.d.lessnnum = L.less.p;
-    L.d.bnd = L.bnd.p;
-    L.d.row_idx = groups[static_cast<size_t>(L.d.row_group)].d.p;
-    L.d.col_idx = groups[static_cast<size_t>(L.d.col_group)].d.p;
-    L.d.row_of = nullptr;
-    {
-      const auto& cg = groups[static_cast<size_t>(L.d.col_group)].idx;
-      L.col_inv.assign(static_cast<size_t>(N), -1);
-      for (size_t k = 0; k < cg.size(); ++k) L.col_inv[static_cast<size_t>(cg[k])] = static_cast<int>(k);
-    }
-    if (L.kind != L_NN_TB) {
-      // cells at least r_cut (+ a margin for FP32 binning) wide
-      const double margin = 1e-3 * L.rc + 2e-3 + 4e-6 * maxL;
-      long long ncell = 1;
-      for (int k = 0; k < 3; ++k) {
-        int nc = static_cast<int>(std::floor(box.L[k] / (L.rc + margin)));
-        L.cg.nc[k] = std::max(1, nc);
-      }
-      const long long cap = 8LL * std::max(L.d.col_cap, 1) + 64;
-      for (;;) {
-        ncell = 1LL * L.cg.nc[0] * L.cg.nc[1] * L.cg.nc[2];
-        if (ncell <= cap) break;
-        int k = 0;
-        for (int a = 1; a < 3; ++a)
-          if (L.cg.nc[a] > L.cg.nc[k]) k = a;
-        L.cg.nc[k] = std::max(1, L.cg.nc[k] / 2);
-      }
-      L.cg.ncell = static_cast<int>(ncell);
-      L.cstart.alloc(static_cast<size_t>(ncell) + 1);
-      L.ccount.alloc(static_cast<size_t>(ncell));
-      L.ccursor.alloc(static_cast<size_t>(ncell));
-      L.cjnd.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
-      L.catom.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
-      L.cposq.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
-      L.ccell.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
-      L.cg.start = L.cstart.p;
-      L.cg.count = L.ccount.p;
-      L.cg.cursor = L.ccursor.p;
-      L.cg.jnd = L.cjnd.p;
-      L.cg.atom = L.catom.p;
-      L.cg.posq = L.cposq.p;
-      L.cg.cell_of = L.ccell.p;
-      L.has_grid = true;
-    }
-  }
+  for (auto& L : lists) alloc_list(L);
   for (auto& I : inters) {
     const ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
     if (I.spec.kind == pfmd_io::K_RJL) {
@@ -934,6 +885,23 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
       L1.xref.zero(st);
       L1.xprev.zero(st);
       if (I.lists[1] >= 0) lists[static_cast<size_t>(I.lists[1])].d.skin = L1.d.id;
+      // two-level: a self list built by cells gets an outer list kOuterMargin
+      // wider (its own cell grid, four times the slots), and a rebuild filters
+      // the outer rows while no atom moved more than half the margin since the
+      // outer build
+      if (L1.kind == L_REGULAR && !L1.d.sorted && L1.d.row_group == L1.d.col_group && L1.has_grid && N > 0) {
+        auto O = std::make_unique<ListH>();
+        O->kind = L_REGULAR;
+        O->rc = L1.rc + kOuterMargin;
+        O->period = L1.period;
+        O->d = L1.d;
+        O->d.nmax = std::min(1024, 4 * std::max(L1.d.nmax, 1));
+        O->d.skin = PFMD_MAX_LISTS + L1.d.id;
+        alloc_list(*O);
+        L1.outer = std::move(O);
+        L1.xout.alloc(static_cast<size_t>(N));
+        L1.xout.zero(st);
+      }
     }
   }
   plan_fusion();
@@ -957,7 +925,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   hctl->md_step = -1;
   hctl->oob_atom = INT_MAX;
   for (size_t g = 0; g < groups.size(); ++g) hctl->group_n[g] = static_cast<int>(groups[g].idx.size());
-  for (int l = 0; l < PFMD_MAX_LISTS; ++l) hctl->list_need[l] = 1;  // every list is built first
+  for (int l = 0; l < PFMD_MAX_LISTS; ++l) hctl->list_need[l] = hctl->outer_need[l] = 1;  // every list is built first
   for (size_t c = 0; c < S.nhc.size(); ++c) {
     const auto& h = S.nhc[c];
     NHCDev& d = hctl->nhc[c];
@@ -1016,6 +984,68 @@ void Engine::tune_tpa() {
     for (auto& kv : graphs)
       if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     graphs.clear();
+  }
+}
+
+void Engine::alloc_list(ListH& L) {
+  const double maxL = std::max(box.L[0], std::max(box.L[1], box.L[2]));
+  const size_t rows = static_cast<size_t>(std::max(L.d.rows, 1));
+  L.nnum.alloc(rows);
+  L.nnum.zero(st);
+  L.nlist.alloc(std::max<size_t>(static_cast<size_t>(L.d.nmax), 1) * static_cast<size_t>(L.d.stride));
+  L.nlist.zero(st);
+  L.pidx.alloc(rows);
+  L.pidx.zero(st);
+  L.less.alloc(rows);
+  L.less.zero(st);
+  L.bnd.alloc(rows);
+  L.bnd.zero(st);
+  L.d.nnum = L.nnum.p;
+  L.d.nlist = L.nlist.p;
+  L.d.pidx = L.pidx.p;
+  L.d.lessnnum = L.less.p;
+  L.d.bnd = L.bnd.p;
+  L.d.row_idx = groups[static_cast<size_t>(L.d.row_group)].d.p;
+  L.d.col_idx = groups[static_cast<size_t>(L.d.col_group)].d.p;
+  L.d.row_of = nullptr;
+  {
+    const auto& cg = groups[static_cast<size_t>(L.d.col_group)].idx;
+    L.col_inv.assign(static_cast<size_t>(N), -1);
+    for (size_t k = 0; k < cg.size(); ++k) L.col_inv[static_cast<size_t>(cg[k])] = static_cast<int>(k);
+  }
+  if (L.kind != L_NN_TB) {
+    // cells at least r_cut (+ a margin for FP32 binning) wide
+    const double margin = 1e-3 * L.rc + 2e-3 + 4e-6 * maxL;
+    long long ncell = 1;
+    for (int k = 0; k < 3; ++k) {
+      int nc = static_cast<int>(std::floor(box.L[k] / (L.rc + margin)));
+      L.cg.nc[k] = std::max(1, nc);
+    }
+    const long long cap = 8LL * std::max(L.d.col_cap, 1) + 64;
+    for (;;) {
+      ncell = 1LL * L.cg.nc[0] * L.cg.nc[1] * L.cg.nc[2];
+      if (ncell <= cap) break;
+      int k = 0;
+      for (int a = 1; a < 3; ++a)
+        if (L.cg.nc[a] > L.cg.nc[k]) k = a;
+      L.cg.nc[k] = std::max(1, L.cg.nc[k] / 2);
+    }
+    L.cg.ncell = static_cast<int>(ncell);
+    L.cstart.alloc(static_cast<size_t>(ncell) + 1);
+    L.ccount.alloc(static_cast<size_t>(ncell));
+    L.ccursor.alloc(static_cast<size_t>(ncell));
+    L.cjnd.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+    L.catom.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+    L.cposq.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+    L.ccell.alloc(std::max<size_t>(static_cast<size_t>(L.d.col_cap), 1));
+    L.cg.start = L.cstart.p;
+    L.cg.count = L.ccount.p;
+    L.cg.cursor = L.ccursor.p;
+    L.cg.jnd = L.cjnd.p;
+    L.cg.atom = L.catom.p;
+    L.cg.posq = L.cposq.p;
+    L.cg.cell_of = L.ccell.p;
+    L.has_grid = true;
   }
 }
 
@@ -1137,11 +1167,21 @@ void Engine::enqueue_lists(const StepPlan& p) {
   for (auto& I : inters) {
     ListH& L1 = lists[static_cast<size_t>(I.lists[0])];
     const bool skin = L1.d.skin >= 0 && p.rebuild[static_cast<size_t>(I.lists[0])];
-    if (skin) launch_skin_check(L1.d, A, box, L1.xref.p, L1.xprev.p, L1.half_skin, ctl, st);
+    ListH* O = (skin && L1.outer) ? L1.outer.get() : nullptr;
+    if (skin)
+      launch_skin_check(L1.d, A, box, L1.xref.p, L1.xprev.p, O ? L1.xout.p : nullptr, L1.half_skin,
+                        0.5 * kOuterMargin - kOuterTol, ctl, st);
     if (p.rebuild[static_cast<size_t>(I.lists[0])]) {
-      launch_bin(L1.d, L1.cg, A, ctl, st);
-      launch_build_list(prec, L1.d, L1.cg, A, box, L1.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
-                        0, 0, ctl, st);
+      const double pm = 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2]));
+      if (O) {
+        // the outer list's kernels return at once unless it must be rebuilt too
+        launch_bin(O->d, O->cg, A, ctl, st);
+        launch_build_list(prec, O->d, O->cg, A, box, O->rc, pm, 0, 0, ctl, st);
+        launch_filter_outer(L1.d, O->d, A, box, L1.rc, ctl, st);
+      } else {
+        launch_bin(L1.d, L1.cg, A, ctl, st);
+        launch_build_list(prec, L1.d, L1.cg, A, box, L1.rc, pm, 0, 0, ctl, st);
+      }
     }
     if (I.lists[1] >= 0 && p.rebuild[static_cast<size_t>(I.lists[1])]) {
       ListH& L2 = lists[static_cast<size_t>(I.lists[1])];
@@ -1149,7 +1189,7 @@ void Engine::enqueue_lists(const StepPlan& p) {
       launch_build_list(prec, L2.d, L2.cg, A, box, L2.rc, 1e-3 + 4e-6 * std::max(box.L[0], std::max(box.L[1], box.L[2])),
                         1, L1.d.rows, ctl, st);
     }
-    if (skin) launch_skin_commit(L1.d, A, L1.xref.p, ctl, st);
+    if (skin) launch_skin_commit(L1.d, A, L1.xref.p, O ? L1.xout.p : nullptr, ctl, st);
     if (I.lists[2] >= 0 && p.rebuild[static_cast<size_t>(I.lists[2])]) {
       ListH& L3 = lists[static_cast<size_t>(I.lists[2])];
       if (L3.kind == L_NN_TB) {
@@ -2562,8 +2602,10 @@ int pfmd_set_group_n(pfmd_ctx* c, int group, int n) {
     const int cap = static_cast<int>(e.groups[static_cast<size_t>(group - 1)].idx.size());
     e.hctl->group_n[group - 1] = std::max(0, std::min(n, cap));
     e.upload_ctl_groups();
-    // rows change with the group: skin-triggered lists rebuild at their next update step
+    // rows change with the group: skin-triggered lists (and outer lists) rebuild at
+    // their next update step
     CK(cudaMemsetAsync(e.ctl->list_need, 1, sizeof(e.ctl->list_need), e.st));
+    CK(cudaMemsetAsync(e.ctl->outer_need, 1, sizeof(e.ctl->outer_need), e.st));
     CK(cudaStreamSynchronize(e.st));
   });
 }

@@ -167,9 +167,13 @@ void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s);
 void launch_bin(const ListDev& L, const CellGrid& cg, const Atoms& A, Ctl* ctl, cudaStream_t s);
 // Skin-triggered rebuilds (L.skin >= 0): the displacement test before a list's
 // update step and the reference update after it.
+// xout (or null): the positions at the outer list's build, for a two-level list.
 void launch_skin_check(const ListDev& L, const Atoms& A, const Box& B, const int4* xref, int4* xprev,
-                       double half_skin, Ctl* ctl, cudaStream_t s);
-void launch_skin_commit(const ListDev& L, const Atoms& A, int4* xref, Ctl* ctl, cudaStream_t s);
+                       const int4* xout, double half_skin, double half_margin, Ctl* ctl, cudaStream_t s);
+void launch_skin_commit(const ListDev& L, const Atoms& A, int4* xref, int4* xout, Ctl* ctl, cudaStream_t s);
+// A two-level list's rows from its outer list O: the entries within rc.
+void launch_filter_outer(const ListDev& L, const ListDev& O, const Atoms& A, const Box& B, double rc, Ctl* ctl,
+                         cudaStream_t s);
 // Regular list (converse=0), or the converse of a list with src_rows rows
 // (converse=1, built at the source list's rebuild steps).  The plain form tests
 // candidates with an FP32 prefilter at r_cut + prefilter_margin, then exactly.

@@ -587,7 +587,15 @@ void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
 // the list stays complete through the next period if no atom moves faster than
 // in the last one.  Maxima by atomicMax on the bits of non-negative floats: the
 // same result in any order.
-__global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* xprev, int both, Ctl* ctl) {
+//
+// Two-level lists (xout non-null): the list's rows are filtered from an outer
+// list built with a radius `margin` wider.  Every pair now within the list's
+// radius was within it plus twice the largest displacement at the outer build,
+// so the outer list is rebuilt (binning and the cell kernels) only when a
+// rebuild is due and some atom moved more than half the margin since the outer
+// build; otherwise a rebuild is the filter pass alone.
+__global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* xprev, const int4* xout, int both,
+                             Ctl* ctl) {
   if (ctl->stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nr = ctl->group_n[L.row_group], nc = ctl->group_n[L.col_group];
@@ -597,38 +605,55 @@ __global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* 
   } else if (both && i - L.row_cap < nc) {
     a = L.col_idx[i - L.row_cap];
   }
-  unsigned int ub = 0u, up = 0u;
+  unsigned int ub = 0u, up = 0u, uo = 0u;
   if (a >= 0) {
     const int4 q = A.posq[a];
     float d[3];
     ub = __float_as_uint(mi_q(xref[a], q, B, d));
     up = __float_as_uint(mi_q(xprev[a], q, B, d));
+    if (xout) uo = __float_as_uint(mi_q(xout[a], q, B, d));
     xprev[a] = q;
   }
   // one atomic per warp
   ub = __reduce_max_sync(0xffffffffu, ub);
   up = __reduce_max_sync(0xffffffffu, up);
+  uo = __reduce_max_sync(0xffffffffu, uo);
   if ((threadIdx.x & 31) == 0) {
     if (ub) atomicMax(&ctl->skin_max[L.skin][0], ub);
     if (up) atomicMax(&ctl->skin_max[L.skin][1], up);
+    if (uo) atomicMax(&ctl->skin_max[L.skin][2], uo);
   }
 }
-__global__ void k_skin_decide(int id, float half_skin, Ctl* ctl) {
+__global__ void k_skin_decide(int id, float half_skin, float half_margin, int outer, Ctl* ctl) {
   if (ctl->stop) return;
   const float b = sqrtf(__uint_as_float(ctl->skin_max[id][0])), p = sqrtf(__uint_as_float(ctl->skin_max[id][1]));
-  if (!(b + p <= half_skin)) ctl->list_need[id] = 1;
+  const bool need = ctl->list_need[id] != 0 || !(b + p <= half_skin);
+  if (need) ctl->list_need[id] = 1;
+  if (outer) {
+    const float o = sqrtf(__uint_as_float(ctl->skin_max[id][2]));
+    if (ctl->outer_need[id] != 0 || (need && !(o <= half_margin))) ctl->outer_need[id] = 1;
+  }
   ctl->skin_max[id][0] = 0u;
   ctl->skin_max[id][1] = 0u;
+  ctl->skin_max[id][2] = 0u;
 }
-// After the update step: a rebuilt list's atoms give the new reference positions;
-// the last block to finish clears the flag (every block has read it by then).
-__global__ void k_skin_commit(ListDev L, Atoms A, int4* xref, Ctl* ctl) {
+// After the update step: a rebuilt list's atoms give the new reference positions
+// (and a rebuilt outer list's, the outer reference); the last block to finish
+// clears the flags (every block has read them by then).
+__global__ void k_skin_commit(ListDev L, Atoms A, int4* xref, int4* xout, Ctl* ctl) {
   if (ctl->stop) return;
-  __shared__ int need;
-  if (threadIdx.x == 0) need = ctl->list_need[L.skin];
+  __shared__ int need, oneed;
+  if (threadIdx.x == 0) {
+    need = ctl->list_need[L.skin];
+    oneed = xout ? ctl->outer_need[L.skin] : 0;
+  }
   __syncthreads();
   if (need)
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.N; a += gridDim.x * blockDim.x) xref[a] = A.posq[a];
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.N; a += gridDim.x * blockDim.x) {
+      const int4 q = A.posq[a];
+      xref[a] = q;
+      if (oneed) xout[a] = q;
+    }
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -636,27 +661,93 @@ __global__ void k_skin_commit(ListDev L, Atoms A, int4* xref, Ctl* ctl) {
     if (done == gridDim.x - 1) {
       if (need) ctl->list_builds[L.skin] += 1;
       ctl->list_need[L.skin] = 0;
+      ctl->outer_need[L.skin] = 0;
       ctl->skin_done[L.skin] = 0;
     }
   }
 }
 
 void launch_skin_check(const ListDev& L, const Atoms& A, const Box& B, const int4* xref, int4* xprev,
-                       double half_skin, Ctl* ctl, cudaStream_t s) {
+                       const int4* xout, double half_skin, double half_margin, Ctl* ctl, cudaStream_t s) {
   if (L.skin < 0) return;
   const int both = L.row_group != L.col_group ? 1 : 0;  // a self list checks its rows once
   const int n = L.row_cap + (both ? L.col_cap : 0);
   if (n > 0) {
-    k_skin_check<<<blocks_for(n, 256), 256, 0, s>>>(L, A, B, xref, xprev, both, ctl);
+    k_skin_check<<<blocks_for(n, 256), 256, 0, s>>>(L, A, B, xref, xprev, xout, both, ctl);
     ++g_kernel_launches;
   }
-  k_skin_decide<<<1, 1, 0, s>>>(L.skin, static_cast<float>(half_skin), ctl);
+  k_skin_decide<<<1, 1, 0, s>>>(L.skin, static_cast<float>(half_skin), static_cast<float>(half_margin),
+                                xout ? 1 : 0, ctl);
   ++g_kernel_launches;
 }
-void launch_skin_commit(const ListDev& L, const Atoms& A, int4* xref, Ctl* ctl, cudaStream_t s) {
+void launch_skin_commit(const ListDev& L, const Atoms& A, int4* xref, int4* xout, Ctl* ctl, cudaStream_t s) {
   if (L.skin < 0) return;
   const int grid = std::max(1, std::min(blocks_for(A.N, 256), 152));
-  k_skin_commit<<<grid, 256, 0, s>>>(L, A, xref, ctl);
+  k_skin_commit<<<grid, 256, 0, s>>>(L, A, xref, xout, ctl);
+  ++g_kernel_launches;
+}
+
+// The rows of a two-level list from its outer list O (same rows): the entries of
+// each outer row within rc, in the outer row's order.  kFilterTpa threads per
+// row, lanes laid out as in the force kernels (row = lane % rows-per-warp), so a
+// warp reads 8 rows' slots coalesced; each round the hits of a row's lanes are
+// ranked by one ballot and appended in slot order.
+static constexpr int kFilterTpa = 4;
+__global__ void __launch_bounds__(256) k_filter_outer(ListDev L, ListDev O, const int4* __restrict__ posq, Box B,
+                                                      float rcp2, Ctl* ctl) {
+  if (ctl->stop || skin_keep(ctl, L.skin)) return;
+  const int n1 = ctl->group_n[L.row_group];
+  if (n1 == 0 || L.rows == 0) return;
+  constexpr int RPW = 32 / kFilterTpa;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int row = (gt >> 5) * RPW + (lane % RPW);
+  const int sub = lane / RPW;
+  const bool valid = row < n1 && row < L.rows;
+  const int n = valid ? O.nnum[row] : 0;
+  const int ai = valid ? O.pidx[row] : 0;
+  const int4 pi = posq[ai];
+  int nw = n;  // every lane of the warp runs the same number of rounds
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nw = max(nw, __shfl_xor_sync(0xffffffffu, nw, o));
+  unsigned rowmask = 0u;
+#pragma unroll
+  for (int k = 0; k < kFilterTpa; ++k) rowmask |= 1u << (lane % RPW + k * RPW);
+  const unsigned below = rowmask & ((1u << lane) - 1u);
+  int cnt = 0;
+  for (int base = 0; base < nw; base += kFilterTpa) {
+    const int p = base + sub;
+    bool hit = false;
+    int aj = 0;
+    if (p < n) {
+      aj = O.nlist[(size_t)p * O.stride + row];
+      float d[3];
+      hit = mi_q(pi, posq[aj], B, d) < rcp2;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (hit) {
+      const int q = cnt + __popc(m & below);
+      if (q < L.nmax) L.nlist[(size_t)q * L.stride + row] = aj;
+    }
+    cnt += __popc(m & rowmask);
+  }
+  if (valid && sub == 0) {
+    if (cnt > L.nmax) {
+      // 'error: too many neighbours', ind, nnumind  (md_neighbours.f90:80)
+      set_error(ctl, ST_NLIST_OVERFLOW, EK_OVERFLOW, L.id, row + 1, L.nmax + 1);
+    } else {
+      L.nnum[row] = cnt;
+      L.pidx[row] = ai;
+      L.bnd[row] = INT_MAX;  // lessnnum of an unsorted row is formed when it is read back
+    }
+  }
+}
+
+void launch_filter_outer(const ListDev& L, const ListDev& O, const Atoms& A, const Box& B, double rc, Ctl* ctl,
+                         cudaStream_t s) {
+  if (L.rows == 0) return;
+  const long long threads = (long long)L.rows * kFilterTpa;
+  k_filter_outer<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(L, O, A.posq, B, (float)(rc * rc), ctl);
   ++g_kernel_launches;
 }
 

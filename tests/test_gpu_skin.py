@@ -44,6 +44,24 @@ def test_skin_lists_skip_rebuilds_and_stay_complete(tmp_path, built):
     assert s.energies()["conserved"] == pytest.approx(r.energies()["conserved"], rel=1e-6)
 
 
+def test_two_level_rebuild_holds_every_pair_within_the_list_radius(tmp_path, built):
+    """A rebuild filters the rows of the wider outer list, built steps earlier at
+    other positions: the result holds exactly the pairs within the list radius
+    now (up to FP32 rounding at the radius)."""
+    configs.cu_slab(str(tmp_path), nx=8, ny=8, nz=6, steps=400, log_period=10, temperature=600.0)
+    d = str(tmp_path)
+    box = np.array([float(x) for x in (tmp_path / "cu_slab.xyz").read_text().splitlines()[1].split('"')[1].split()])[[0, 4, 8]]
+    s = pf.Simulation(d, form="precision", out_period=10 ** 6)
+    s.advance(150)
+    s.time_kernel("lists", reps=1)  # every list rebuilt at the current positions
+    p = s.state()[0]
+    lst = s.nlist(0, 0)
+    have = {(int(lst["pidx"][i]), int(j)) for i in range(len(lst["nnum"]))
+            for j in lst["pidx"][lst["nlist"][i, :lst["nnum"][i]]]}
+    assert _pairs_within(p, box, 5.5 - 1e-3) <= have <= _pairs_within(p, box, 5.5 + 1e-3)
+    s.close()
+
+
 @pytest.mark.parametrize("graphs", [True, False])
 def test_fused_kick_drift_is_bitwise_the_separate_one(tmp_path, built, graphs):
     """The force kernel that also runs the next step's kick and drift gives the
