@@ -161,6 +161,13 @@ static void fill_rjl(RJLc<R>& c, const RJLPar& P) {
   c.a2 = (R)(2.0 * P.A0);
   c.pr0 = (R)(P.p / P.r0);
   c.qr0 = (R)(P.q / P.r0);
+  const double log2e = 1.4426950408889634;
+  c.eqa = (R)(-2.0 * P.q * log2e / P.r0);
+  c.eqb = (R)(2.0 * P.q * log2e);
+  c.epa = (R)(-P.p * log2e / P.r0);
+  c.epb = (R)(P.p * log2e);
+  c.tb = (R)(-P.R1 / (P.R2 - P.R1));
+  c.dsw = (R)(-0.5 * 3.14159265358979323846 / (P.R2 - P.R1));
 }
 void derive(RJLPar& P) {
   fill_rjl(P.d, P);

@@ -37,6 +37,13 @@ static void launch_dependent(K kern, int grid, int block, cudaStream_t s, Args..
   cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
+// 2^x by the ex2.approx instruction (relative error about 2^-22).
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // inv_eb holds 1/Eb per atom: double for the plain form, float for the precision form.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb,
@@ -77,14 +84,14 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
         // the cosine switch without branches: t is 0 below R1 and 1 from R2 on; entries
         // beyond R2 (about a fifth of the 5.5 A list) are masked, not skipped, so the
         // warp stays converged
-        const float t = __saturatef((r - c.R1) * c.inv_w);
+        const float t = __saturatef(fmaf(r, c.inv_w, c.tb));
         float sn, cs;
         __sincosf(3.14159265358979f * t, &sn, &cs);
         const float in = r <= c.R2 ? 1.f : 0.f;
         const float fc = (0.5f + 0.5f * cs) * in;
-        const float rdfc = -sn * (3.14159265358979f * 0.5f) * c.inv_w * in;
-        const float x = r * c.inv_r0 - 1.f;
-        const float eq = __expf(c.m2q * x), ep = __expf(c.mp * x);
+        const float rdfc = sn * c.dsw * in;
+        // each exponential is one FMA into the hardware's base-2 exponential
+        const float eq = ex2_approx(fmaf(c.eqa, r, c.eqb)), ep = ex2_approx(fmaf(c.epa, r, c.epb));
         eb2.add(eq * fc);
         if (ENERGY) er.add(ep * fc);
         float2 ab;

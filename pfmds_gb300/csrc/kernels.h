@@ -105,6 +105,11 @@ struct CosPar {  // ljc: eps sig delt; morsec: D r0 a delt
 template <class R>
 struct RJLc {
   R A0, xi, R1, R2, inv_w, inv_r0, m2q, mp, a2, pr0, qr0;
+  // the two exponents in base 2 as linear functions of r: -2q (r/r0 - 1) log2(e)
+  // = eqa r + eqb, and -p (r/r0 - 1) log2(e) = epa r + epb
+  R eqa, eqb, epa, epb;
+  // the switch argument t = (r - R1)/(R2 - R1) = r inv_w + tb; dsw = -pi/2 inv_w
+  R tb, dsw;
 };
 struct RJLPar {
   double A0, xi, p, q, r0, R1, R2;
