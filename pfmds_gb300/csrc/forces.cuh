@@ -330,6 +330,13 @@ static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 // Entry `p` of list row `row` (slot-major storage).
 __device__ __forceinline__ int ent(const ListDev& L, int row, int p) { return L.nlist[(size_t)p * L.stride + row]; }
 
+// 2^x by the ex2.approx instruction (relative error about 2^-22).
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Calls F with an integral_constant for the list's threads-per-row.
 template <class F>
 static inline void with_tpa(int tpa, F f) {

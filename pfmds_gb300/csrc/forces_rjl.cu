@@ -37,13 +37,6 @@ static void launch_dependent(K kern, int grid, int block, cudaStream_t s, Args..
   cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
-// 2^x by the ex2.approx instruction (relative error about 2^-22).
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
 // inv_eb holds 1/Eb per atom: double for the plain form, float for the precision form.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb,
