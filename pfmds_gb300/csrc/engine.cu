@@ -896,13 +896,16 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
       // wider (its own cell grid, four times the slots), and a rebuild filters
       // the outer rows while no atom moved more than half the margin since the
       // outer build
-      if (L1.kind == L_REGULAR && !L1.d.sorted && L1.d.row_group == L1.d.col_group && L1.has_grid && N > 0) {
+      // (only where four times the slots fit the kernels' 1,024, so the outer
+      // list cannot overflow where the list itself would not)
+      if (L1.kind == L_REGULAR && !L1.d.sorted && L1.d.row_group == L1.d.col_group && L1.has_grid && N > 0 &&
+          4 * L1.d.nmax <= 1024) {
         auto O = std::make_unique<ListH>();
         O->kind = L_REGULAR;
         O->rc = L1.rc + kOuterMargin;
         O->period = L1.period;
         O->d = L1.d;
-        O->d.nmax = std::min(1024, 4 * std::max(L1.d.nmax, 1));
+        O->d.nmax = 4 * std::max(L1.d.nmax, 1);
         O->d.skin = PFMD_MAX_LISTS + L1.d.id;
         alloc_list(*O);
         L1.outer = std::move(O);
