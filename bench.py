@@ -592,7 +592,9 @@ def run_ours(args):
                    "list_rebuilds": {"timed": builds, "update_steps": K * S // 10,
                                      "rule": "skin-triggered at the reference's update steps: rebuild when the "
                                              "displacement since the build plus over the last period exceeds "
-                                             "half of 5.5 - 5.0 A"},
+                                             "half of 5.5 - 5.0 A; a rebuild filters a 6.5 A outer list, itself "
+                                             "rebuilt by the cell kernels only when an atom moved 0.5 A since its "
+                                             "build"},
                    "kick_drift": "fused into the previous step's force kernel except after energy steps"},
         "force_rmse": {"value": rmse, "rel": rmse / frms, "unit": "eV/A", "against": "plain FP64 form"},
         "nve_drift": {"value": d_pre, "unit": "eV/atom/ns", "window_fs": args.drift_steps * DT_FS,
