@@ -676,12 +676,11 @@ __global__ void k_skin_commit(ListDev L, Atoms A, int4* xref, int4* xout, Ctl* c
   }
   __syncthreads();
   if (!need && !oneed) return;  // nothing rebuilt: the flags are already clear
-  if (need)
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.N; a += gridDim.x * blockDim.x) {
-      const int4 q = A.posq[a];
-      xref[a] = q;
-      if (oneed) xout[a] = q;
-    }
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.N; a += gridDim.x * blockDim.x) {
+    const int4 q = A.posq[a];
+    if (need) xref[a] = q;
+    if (oneed) xout[a] = q;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
