@@ -595,6 +595,23 @@ void launch_pack_posq(const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s) {
 // so the outer list is rebuilt (binning and the cell kernels) only when a
 // rebuild is due and some atom moved more than half the margin since the outer
 // build; otherwise a rebuild is the filter pass alone.
+// The decision from the recorded maxima (read atomically: the blocks that
+// recorded them may still be in flight on other SMs until their fences), then the
+// maxima cleared for the next update step.
+__device__ __forceinline__ void skin_decide(Ctl* ctl, int id, float half_skin, float half_margin, bool outer) {
+  const float b = sqrtf(__uint_as_float(atomicMax(&ctl->skin_max[id][0], 0u)));
+  const float p = sqrtf(__uint_as_float(atomicMax(&ctl->skin_max[id][1], 0u)));
+  const bool need = ctl->list_need[id] != 0 || !(b + p <= half_skin);
+  if (need) ctl->list_need[id] = 1;
+  if (outer) {
+    const float o = sqrtf(__uint_as_float(atomicMax(&ctl->skin_max[id][2], 0u)));
+    if (ctl->outer_need[id] != 0 || (need && !(o <= half_margin))) ctl->outer_need[id] = 1;
+  }
+  ctl->skin_max[id][0] = 0u;
+  ctl->skin_max[id][1] = 0u;
+  ctl->skin_max[id][2] = 0u;
+}
+
 __global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* xprev, const int4* xout, int both,
                              float half_skin, float half_margin, Ctl* ctl) {
   if (ctl->stop) return;
@@ -637,32 +654,12 @@ __global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* 
   __syncthreads();
   if (!last || threadIdx.x != 0) return;
   __threadfence();
-  const int id = L.skin;
-  const float b = sqrtf(__uint_as_float(atomicMax(&ctl->skin_max[id][0], 0u)));
-  const float p = sqrtf(__uint_as_float(atomicMax(&ctl->skin_max[id][1], 0u)));
-  const bool need = ctl->list_need[id] != 0 || !(b + p <= half_skin);
-  if (need) ctl->list_need[id] = 1;
-  if (xout) {
-    const float o = sqrtf(__uint_as_float(atomicMax(&ctl->skin_max[id][2], 0u)));
-    if (ctl->outer_need[id] != 0 || (need && !(o <= half_margin))) ctl->outer_need[id] = 1;
-  }
-  ctl->skin_max[id][0] = 0u;
-  ctl->skin_max[id][1] = 0u;
-  ctl->skin_max[id][2] = 0u;
-  ctl->skin_done[id] = 0u;
+  skin_decide(ctl, L.skin, half_skin, half_margin, xout != nullptr);
+  ctl->skin_done[L.skin] = 0u;
 }
 __global__ void k_skin_decide(int id, float half_skin, float half_margin, int outer, Ctl* ctl) {
   if (ctl->stop) return;
-  const float b = sqrtf(__uint_as_float(ctl->skin_max[id][0])), p = sqrtf(__uint_as_float(ctl->skin_max[id][1]));
-  const bool need = ctl->list_need[id] != 0 || !(b + p <= half_skin);
-  if (need) ctl->list_need[id] = 1;
-  if (outer) {
-    const float o = sqrtf(__uint_as_float(ctl->skin_max[id][2]));
-    if (ctl->outer_need[id] != 0 || (need && !(o <= half_margin))) ctl->outer_need[id] = 1;
-  }
-  ctl->skin_max[id][0] = 0u;
-  ctl->skin_max[id][1] = 0u;
-  ctl->skin_max[id][2] = 0u;
+  skin_decide(ctl, id, half_skin, half_margin, outer != 0);
 }
 // After the update step: a rebuilt list's atoms give the new reference positions
 // (and a rebuilt outer list's, the outer reference); the last block to finish
