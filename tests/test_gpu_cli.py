@@ -88,3 +88,35 @@ def test_list_mode_with_all_out(tmp_path, built):
     for f in files:
         _same_text(open(a / f).read(), open(b / f).read(), f, atol=2e-6 if f.endswith((".log", ".txt")) else 1e-8,
                    rtol=0)
+
+
+def test_precision_switches(tmp_path, built):
+    """-fuse 0 and -async_io 0 change how the precision form runs, not what it
+    writes: the same files, bit for bit (timings aside).  -skin 0 rebuilds every
+    list at every update step: the same files within FP32 summation-order noise."""
+    base = tmp_path / "base"
+    configs.cu_slab(str(base), nx=4, ny=4, nz=4, steps=60, log_period=10, temperature=300.0)
+    runs = {}
+    for name, extra in (("default", []), ("plain_sched", ["-fuse", "0", "-async_io", "0"]),
+                        ("noskin", ["-skin", "0"])):
+        d = tmp_path / name
+        shutil.copytree(base, d)
+        out = _run(pf.EXE_PATH, d, ["-i", "md_run_settings.txt", "-op", "20", "-form", "precision"] + extra)
+        runs[name] = (d, out)
+    d0, out0 = runs["default"]
+    files = _outputs(d0)
+    assert "md_run.log" in files
+    # the list-load lines report the largest row of lists of different ages
+    # when one run keeps lists the other rebuilds
+    load = re.compile(r"^\s*\w+\s+\d+\s+\d+\s*/\s*\d+\s*$")
+    for name, exact in (("plain_sched", True), ("noskin", False)):
+        d, out = runs[name]
+        assert _outputs(d) == files
+        tol = dict(atol=0.0, rtol=0.0) if exact else dict(atol=1e-6, rtol=1e-6)
+        if exact:
+            _same_text(out, out0, name + " stdout", **tol)
+        else:
+            keep = lambda t: "\n".join(x for x in t.splitlines() if not load.match(x))
+            _same_text(keep(out), keep(out0), name + " stdout", **tol)
+        for f in files:
+            _same_text(open(d / f).read(), open(d0 / f).read(), name + " " + f, **tol)
