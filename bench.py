@@ -367,7 +367,7 @@ def learned_config(root, device, frames=200, run_steps=1000):
             s.learned_gradient(model, tensor_cores=tc, n_networks=2, timed=True)[2] for _ in range(3))
     s.close()
     res["training_gradient_ms"] = grad_ms
-    # the checked run: classical kernels judge the networks every 100 steps
+    # the checked run: classical kernels check the networks every 100 steps
     s = pf.Simulation(dbig, form="precision", out_period=10 ** 9, device=device)
     s.learned_use(model, check_period=100, max_rmse=0.05, tensor_cores=True)
     try:

@@ -1,5 +1,5 @@
 // Learned form: a per-atom neural-network potential standing in for the tb and rjl
-// interactions (the classical kernels stay as its fallback and as the judge of its
+// interactions (the classical kernels stay as its fallback and as the check on its
 // error).  Each atom's environment within the interaction's own neighbour list is
 // described by Behler-Parrinello symmetry functions -- 32 radial
 //   G_k = sum_j exp(-eta_k (r_ij - rs_k)^2) fc(r_ij)

@@ -1,7 +1,7 @@
 """Learned form: networks trained on the plain kernels' per-atom energies stand in
 for tb and rjl; the analytic forces are checked against finite differences of the
 library's own energy and of the FP64 CPU reference (oracle/learned_ref.py), and the
-classical kernels judge and replace the networks when they drift."""
+classical kernels check and replace the networks when they drift."""
 import numpy as np
 import pytest
 
