@@ -495,7 +495,7 @@ namespace pfmd_io {
 // x <- 16807 x mod (2^31 - 1), returning x / (2^31 - 1).  PFMDS draws from the
 // compiler's RAND intrinsic from every OpenMP thread (md_general.f90:120-136), so
 // its velocities depend on the thread count; this generator is one serial stream
-// in atom order and is shared by the driver and the oracle.
+// in atom order and is shared by the engine and the oracle.
 struct MinStd {
   long long x;
   explicit MinStd(long long seed) {
