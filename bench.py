@@ -38,6 +38,12 @@ MD_PER_STEP = 10
 DT_FS = 1.0
 
 
+def bench_config():
+    """The workload as both arms name it (the same dict in both JSON lines)."""
+    return {"workload": WORKLOAD, "atoms": 65536, "md_steps_per_step": MD_PER_STEP,
+            "l2": "flushed (256 MiB write) between timed GPU steps"}
+
+
 def make_workload(d, seed=2024):
     from pfmds_gb300 import configs
     return configs.cu_slab(d, nx=32, ny=32, nz=16, seed=seed, temperature=300.0, dt=DT_FS, steps=10 ** 8,
@@ -462,6 +468,24 @@ def traffic_from_profiles(kernel, form):
     return None if e is None else float(e)
 
 
+def mean_entries(sim, inter, lst):
+    """Mean entries per row of one neighbour list (k of the byte model)."""
+    nl = sim.nlist(inter, lst)
+    return float(nl["nnum"].mean())
+
+
+def fp64_pipe_from_profiles(kernel):
+    """FP64-pipe utilisation (% of peak) of a plain-form kernel from the committed
+    ncu summary figures, or None."""
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        j = json.load(f)
+    e = j.get(f"plain:{kernel}:fp64_pipe_pct")
+    return None if e is None else {"pct_of_peak": float(e), "source": "ncu (profiles/)"}
+
+
 def run_ours(args):
     import pfmds_gb300 as pf
     rank, world, dist = dist_init()
@@ -502,18 +526,38 @@ def run_ours(args):
         drift = (e1 - e0) / n / (K * S * DT_FS * 1e-6)  # eV/atom/ns over the timed window
 
         # roofline of the dominant kernel: time shares per MD step
+        # roofline of the dominant kernel by time per MD step, on the algorithmic
+        # bytes per atom of the hot-path model: a list pass reads 4 B per entry, the
+        # force pass also the own position (16 B fixed point) and writes the force
+        # (12 B FP32), and velocity Verlet streams 128 B per atom (x, v, f, 1/m read;
+        # x, v written); the rjl density pass is an extra list pass of 4k + 16 B
+        k_mean = mean_entries(sim, 0, 0)
+        model = {"rjl_force": 4 * k_mean + 16 + 12 + 128, "rjl_density": 4 * k_mean + 16}
         cands = {}
         per_list = builds / (K * S) if builds >= 0 else 1.0 / 10  # rebuilds per MD step in the timed region
         for name, per_md in (("rjl_force", 1.0), ("rjl_density", 1.0), ("lists", per_list)):
             ms, b = sim.time_kernel(name, reps=50)
             cands[name] = (ms, b, ms * per_md)
-        dom = max(cands, key=lambda k: cands[k][2])
-        ms, b, _ = cands[dom]
-        achieved = b / (ms * 1e-3) / 1e9
+        dom = max(("rjl_force", "rjl_density"), key=lambda k: cands[k][2])
+        ms, b_impl, _ = cands[dom]
+        b_alg = model[dom] * n
+        achieved = b_alg / (ms * 1e-3) / 1e9
         traffic = traffic_from_profiles(dom, "precision")
+        step_bytes = (model["rjl_force"] + model["rjl_density"]) * n  # 8k + 172 per atom-step
+        step_ms = total_ms / (K * S)
         roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                    "traffic": traffic, "alg_bytes_per_launch": int(b), "ms_per_launch": ms,
+                    "traffic": traffic, "alg_bytes_per_launch": int(b_alg),
+                    "alg_bytes_per_atom": round(model[dom], 1), "entries_per_row": round(k_mean, 2),
+                    "ms_per_launch": ms,
+                    "impl_bytes_per_launch": int(b_impl),
+                    "impl_overhead": "the 8 B per list entry pair-term cache that the density pass writes and "
+                                     "the force pass reads, the FP64 force record (32 B) and 1/Eb (4 B per row "
+                                     "and per entry) are implementation traffic, not algorithmic bytes",
+                    "step": {"alg_bytes_per_atom_step": round(model["rjl_force"] + model["rjl_density"], 1),
+                             "ms_per_md_step": step_ms,
+                             "achieved": round(step_bytes / (step_ms * 1e-3) / 1e9, 1),
+                             "frac": round(step_bytes / (step_ms * 1e-3) / 1e9 / hbm_peak, 4)},
                     "kernel_ms_per_md_step": {k: round(v[2], 5) for k, v in cands.items()}}
 
         # end to end through the C ABI with host buffers (pinned when torch can pin)
@@ -545,6 +589,16 @@ def run_ours(args):
             pms += plain.advance_timed(S)
         pms = dist_max(dist, pms)
         plain_rate = atoms_all * S * Kp / (pms / 1e3)
+        pk = {}
+        for name in ("rjl_force", "rjl_density"):
+            pk[name] = plain.time_kernel(name, reps=5)[0]
+        pdom = max(pk, key=pk.get)
+        # plain FP64 model: position 24 B, force 24 B instead of 16 and 12
+        p_model = {"rjl_force": 4 * k_mean + 24 + 24 + 128, "rjl_density": 4 * k_mean + 24}
+        p_ach = p_model[pdom] * n / (pk[pdom] * 1e-3) / 1e9
+        plain_roof = {"bound": "fp64", "kernel": pdom, "ms_per_launch": pk[pdom],
+                      "hbm_achieved": round(p_ach, 1), "hbm_frac": round(p_ach / hbm_peak, 4),
+                      "fp64_pipe": fp64_pipe_from_profiles(pdom)}
         ref_p = pf.Simulation(d, form="plain", out_period=10 ** 9, device=device)
         pre_p = pf.Simulation(d, form="precision", out_period=10 ** 9, device=device)
         ref_p.advance(1)
@@ -554,13 +608,24 @@ def run_ours(args):
         import numpy as np
         rmse = float(np.sqrt(((fq - fp) ** 2).mean()))
         frms = float(np.sqrt((fp ** 2).mean()))
-        # NVE drift: least-squares slope of the conserved energy over a long run of
-        # each form from the same start (the workload's 10,000 steps for the
-        # precision form, 2,000 for the slower plain form)
-        d_pre, rms_pre = nve_drift(pre_p, args.drift_steps)
-        d_pla, rms_pla = nve_drift(ref_p, max(100, args.drift_steps // 5))
-        plain_line = {"value": plain_rate, "ms_per_step": pms / Kp, "dtype": "f64",
-                      "speedup_of_precision_form": value / plain_rate}
+        # NVE drift of both forms over the same window from the same equilibrated
+        # state: the precision form runs args.equil_steps first, then each form
+        # runs args.drift_steps from that state, with the conserved energy
+        # (md_simulation.f90:205's column) sampled every 100 fs
+        pre_p.advance(args.equil_steps)
+        pe_, ve_, _ = pre_p.state()
+        pre_p.close()
+        drift_forms = {}
+        for form in ("precision", "plain"):
+            s_ = pf.Simulation(d, form=form, out_period=10 ** 9, device=device)
+            s_.set_state(pe_, ve_)
+            s_.advance(1)  # step 0: lists, forces and energies of the equilibrated state
+            drift_forms[form] = nve_drift(s_, args.drift_steps)
+            s_.close()
+        d_pre, rms_pre = drift_forms["precision"]
+        d_pla, rms_pla = drift_forms["plain"]
+        plain_line = {"value": plain_rate, "ms_per_step": pms / Kp, "ms_per_md_step": pms / Kp / S, "dtype": "f64",
+                      "roofline": plain_roof, "speedup_of_precision_form": value / plain_rate}
 
         extra = other_configs(d, device) if (rank == 0 and not args.no_extra) else None
         if extra is not None and args.batch_steps > 0:
@@ -576,7 +641,7 @@ def run_ours(args):
                    "sample": f"{args.cpu_md_steps} MD steps of the same 65,536-atom workload "
                              f"({t:.1f} s, O(N^2) list search at step 0 as the reference), FP64 oracle, OpenMP"}
         clocks = clk.summary()
-        for s in (sim, plain, ref_p, pre_p):
+        for s in (sim, plain, ref_p):
             s.close()
     if rank != 0:
         return
@@ -586,21 +651,22 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "dtype_detail": "precision form: FP32 pair forces with Kahan sums; FP64 positions, velocities, energies",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "precision", "md_steps_per_step": S,
-                   "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}",
-                   "atoms_per_replica": n,
-                   "list_rebuilds": {"timed": builds, "update_steps": K * S // 10,
-                                     "rule": "skin-triggered at the reference's update steps: rebuild when the "
-                                             "displacement since the build plus over the last period exceeds "
-                                             "half of 5.5 - 5.0 A; a rebuild filters a 6.5 A outer list, itself "
-                                             "rebuilt by the cell kernels only when an atom moved 0.5 A since its "
-                                             "build"},
-                   "kick_drift": "fused into the previous step's force kernel except after energy steps"},
+        "config": bench_config(),
+        "form": "precision", "parallelism": f"replicas x{world}", "atoms_per_replica": n,
+        "list_rebuilds": {"timed": builds, "update_steps": K * S // 10,
+                          "rule": "skin-triggered at the reference's update steps: rebuild when the "
+                                  "displacement since the build plus over the last period exceeds "
+                                  "half of 5.5 - 5.0 A; a rebuild filters a 6.5 A outer list, itself "
+                                  "rebuilt by the cell kernels only when an atom moved 0.5 A since its "
+                                  "build"},
+        "kick_drift": "fused into the previous step's force kernel except after energy steps",
         "force_rmse": {"value": rmse, "rel": rmse / frms, "unit": "eV/A", "against": "plain FP64 form"},
         "nve_drift": {"value": d_pre, "unit": "eV/atom/ns", "window_fs": args.drift_steps * DT_FS,
-                      "fit": "least-squares slope of the conserved energy, one sample per 100 fs",
+                      "equilibration_fs": args.equil_steps * DT_FS,
+                      "fit": "least-squares slope of the conserved energy, one sample per 100 fs, both forms "
+                             "from the same state after the equilibration",
                       "rms_about_fit_eV_per_atom": rms_pre, "timed_window_value": drift,
-                      "plain_fp64": {"value": d_pla, "window_fs": max(100, args.drift_steps // 5) * DT_FS,
+                      "plain_fp64": {"value": d_pla, "window_fs": args.drift_steps * DT_FS,
                                      "rms_about_fit_eV_per_atom": rms_pla}},
         "plain": plain_line,
         "roofline": roofline,
@@ -634,8 +700,7 @@ def run_reference(args):
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "atom-steps/s", "n_gpus": 0,
             "steps": K, "warmup": W, "ms_per_step": t / K * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": "reference FP64 algorithm (CPU oracle)",
-                       "md_steps_per_step": S},
+            "config": bench_config(), "form": "reference FP64 algorithm (CPU oracle)",
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{K} timed steps of {S} MD steps after {W} warm-up steps"},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -654,7 +719,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=5000, help="MD steps of the batched configuration (0 skips)")
     ap.add_argument("--learned-steps", type=int, default=1000, help="MD steps of the learned form's run (0 skips)")
     ap.add_argument("--drift-steps", type=int, default=10000,
-                    help="MD steps of the NVE drift measurement (precision form; plain runs a fifth)")
+                    help="MD steps of the NVE drift measurement (both forms, after the equilibration)")
+    ap.add_argument("--equil-steps", type=int, default=2000,
+                    help="MD steps of precision-form equilibration before the drift window")
     ap.add_argument("--quick", action="store_true",
                     help="headline timing loop only (no plain form, e2e, roofline or CPU legs), for profiling")
     ap.add_argument("--learned-only", action="store_true",
@@ -663,11 +730,16 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.impl == "reference":
+        # the reference arm builds and loads only the CPU oracle: nothing of the
+        # CUDA library is loaded into this process
+        from oracle import build_oracle
+        build_oracle.build()
+        run_reference(args)
+        return
     import __graft_entry__
     __graft_entry__.build()
-    if args.impl == "reference":
-        run_reference(args)
-    elif args.learned_only:
+    if args.learned_only:
         with tempfile.TemporaryDirectory() as d:
             print(json.dumps(learned_config(d, 0, frames=args.learned_frames, run_steps=args.learned_steps)),
                   flush=True)

@@ -4,10 +4,10 @@
  * PFMDS (Fortran 90 + OpenMP) has no plugin or FFI layer: its hot path is the
  * body of md() in code_source/MOLECULAR_DYNAMICS/md_simulation.f90, reached from
  * the run_md_simulation command line.  Each entry point below names the reference
- * subroutine or program it replaces; a Fortran md() calls them through the
- * ISO_C_BINDING interface module shown in INTEGRATION.md, a C or C++ host calls
- * them directly, and run_md_simulation (built from this library) is the drop-in
- * executable.
+ * subroutine or program it replaces; a Fortran md() calls them through an
+ * ISO_C_BINDING interface module (one bind(C) interface per entry point, with
+ * the same argument order), a C or C++ host calls them directly, and
+ * run_md_simulation (built from this library) is the drop-in executable.
  *
  * Conventions: plain C types only.  Per-atom arrays are xyz-interleaved doubles
  * (3*N), i.e. the Fortran (3,N) column-major layout of particles%positions.
