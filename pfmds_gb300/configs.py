@@ -178,7 +178,7 @@ def _uniform_min_sep_batched(rng, n, box, dmin):
 def lj_gas(d, n_a=2000, n_b=2000, box=60.0, seed=12345, temperature=100.0, r1=6.5, r2=7.5,
            rc_list=8.5, period=10, nmax=64, integrators=None, step_limit=None, log_period=100,
            nhc_tau=100.0, min_sep=2.5, ms_de=1e-8, interleave=True, xyz_name="AB.xyz",
-           settings_name="md_run_settings.txt", fast_sampler=False):
+           settings_name="md_run_settings.txt", fast_sampler=False, period_traj=100000000):
     """Binary LJ gas (A-B Lorentz-Berthelot) in a periodic cube; writes AB.xyz, the three
     parameter files and md_run_settings.txt into directory d.  Returns the settings name."""
     os.makedirs(d, exist_ok=True)
@@ -207,7 +207,7 @@ def lj_gas(d, n_a=2000, n_b=2000, box=60.0, seed=12345, temperature=100.0, r1=6.
     text = _settings_text(
         step_limit=step_limit, xyz_name=xyz_name, types=["A", "B"],
         groups=[["A", "B"], ["A"], ["B"], []], all_moving=1, xyz_moving=1, z_moving=4,
-        all_atoms=1, traj_group=3, period_traj=100000000, integrators=integrators, ms_de=ms_de,
+        all_atoms=1, traj_group=3, period_traj=period_traj, integrators=integrators, ms_de=ms_de,
         nhc=[(1, temperature, 3, q1)], t0=temperature,
         interactions=[("lj", "parameters_LJ_A-B.txt", [(2, 3, nmax, rc_list, period),
                                                        (3, 2, nmax, rc_list, period)]),
@@ -258,6 +258,63 @@ def cu_slab(d, nx=32, ny=32, nz=16, a=3.615, fixed_layers=2, seed=2024, temperat
         all_atoms=1, traj_group=2, period_traj=100000000,
         integrators=[(integrator, dt, steps, 100000000, log_period)], ms_de=1e-8,
         nhc=[(2, temperature, 3, q1)], t0=temperature,
+        interactions=[("rjl", "parameters_RJL_Cu.txt", [(1, 1, nmax, rc_list, period)])])
+    _write(d, settings_name, text)
+    return settings_name
+
+
+def cu_deposit(d, nx=6, ny=6, nz=4, a=3.615, fixed_layers=1, z_layers=1, n_dep=4, seed=31,
+               temperature=300.0, disp=0.05, dt=1.0, integrators=None, log_period=5, rc_list=5.5, period=10,
+               nmax=64, vacuum=25.0, change=(3, 30, 5), invert_z_vel=True, dep_speed=0.02,
+               xyz_name="cu_dep.xyz", settings_name="md_run_settings.txt"):
+    """Cu fcc (001) slab under rjl with the reference's less common step-loop
+    paths switched on:
+      * the top `z_layers` (001) layers are CU_z, moved only along z
+        (integrate_verlet_z_*, molecular_static_1D_velocities);
+      * `n_dep` CU_dep atoms (a small cluster, 2.6 A apart) sit in the band
+        0.8-0.9 Lz where invert_z_velocities reflects z velocities; they join the
+        xyz-moving group one at a time through change_particle_group_N
+        (change = (ts1, ts2, frec)): group 4 [CU, CU_dep] starts with the size
+        of group 2 [CU];
+      * the bottom `fixed_layers` layers are CU_fixed.
+    Groups: 1 all, 2 CU, 3 CU_z, 4 CU + CU_dep (xyz-moving), 5 all moving
+    (temperature), 6 CU_dep (trajectory)."""
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    pos, box = fcc_slab(nx, ny, nz, a, vacuum=vacuum)
+    layer = np.rint((pos[:, 2] - pos[:, 2].min()) / (a / 2)).astype(int)
+    top = layer.max()
+    types = np.where(layer < fixed_layers, "CU_fixed", np.where(layer > top - z_layers, "CU_z", "CU"))
+    pos = pos + rng.uniform(-disp, disp, size=pos.shape)
+    mass = np.full(len(pos), 63.546)
+    vel = maxwell_velocities(rng, mass, types != "CU_fixed", temperature)
+    vel[types == "CU_z", :2] = 0.0
+    # the deposited cluster: a square of side 2.6 A in the band, half of it in the
+    # lower half of the band moving up (inverted at once), half moving down
+    zb = 0.85 * box[2]
+    dep = np.array([[box[0] / 2 + 2.6 * (k % 2), box[1] / 2 + 2.6 * ((k // 2) % 2), zb + (1.0 if k % 2 else -1.0)]
+                    for k in range(n_dep)])
+    dvel = np.zeros((n_dep, 3))
+    dvel[:, 2] = dep_speed * np.where(np.arange(n_dep) % 2 == 0, 1.0, -1.0)
+    pos = np.concatenate([pos, dep]) % np.asarray(box)
+    vel = np.concatenate([vel, dvel])
+    mass = np.concatenate([mass, np.full(n_dep, 63.546)])
+    types = list(types) + ["CU_dep"] * n_dep
+    write_xyz(os.path.join(d, xyz_name), box, pos, vel, mass, types)
+    _write(d, "parameters_RJL_Cu.txt", "0.0855\t1.224\t10.96\t2.278\t2.556\n4.5\t5.0\n")
+    if integrators is None:
+        integrators = [("nvt", dt, 20, 100000000, log_period), ("nve", dt, 20, 100000000, log_period),
+                       ("nvms", dt, 20, 100000000, log_period)]
+    nmov = sum(1 for t in types if t == "CU")
+    q1 = 3 * nmov * KB * temperature * 100.0 ** 2
+    ts1, ts2, frec = change
+    text = _settings_text(
+        step_limit=sum(i[2] for i in integrators), xyz_name=xyz_name, types=["CU", "CU_fixed", "CU_z", "CU_dep"],
+        groups=[["CU", "CU_fixed", "CU_z", "CU_dep"], ["CU"], ["CU_z"], ["CU", "CU_dep"], ["CU", "CU_z", "CU_dep"],
+                ["CU_dep"]],
+        all_moving=5, xyz_moving=4, z_moving=3, all_atoms=1, traj_group=6, period_traj=10,
+        integrators=integrators, ms_de=1e-12, nhc=[(2, temperature, 3, q1)], t0=temperature,
+        changes=[(2, 4, ts1, ts2, frec)] if change else [], invert_z_vel=invert_z_vel,
         interactions=[("rjl", "parameters_RJL_Cu.txt", [(1, 1, nmax, rc_list, period)])])
     _write(d, settings_name, text)
     return settings_name
