@@ -182,6 +182,18 @@ int pfmd_get_gr_norm(pfmd_ctx* ctx, int inter, double* norm);
  * of group `group` (1-based) to n, clamped to the group's capacity. */
 int pfmd_set_group_n(pfmd_ctx* ctx, int group, int n);
 
+/* Test hook for the bounded device waits; it has no counterpart in the
+ * reference, which stops on errors and never waits on the device.  The waits
+ * are the batched kernel's grid barrier and the tensor-core network kernels'
+ * mbarrier waits; each gives up after a poll limit and the call then returns
+ * PFMD_E_TIMEOUT.  spin_limit != 0 replaces the built-in limits (0 restores
+ * them); stall = 1 makes every wait launched from then on impossible (the
+ * barrier expects one arrival more than the grid has; the network kernels wait
+ * for an mbarrier phase that no MMA completes), so the timeout path runs.
+ * Process-wide, read at each launch; batched runs launch directly (no CUDA
+ * graph) while it is set.  For tests of the timeout path only. */
+int pfmd_debug_waits(unsigned int spin_limit, int stall);
+
 /* The CUDA stream every kernel of ctx is launched on (a cudaStream_t). */
 int pfmd_get_stream(pfmd_ctx* ctx, void** stream);
 /* Number of kernels the library has launched on ctx so far (graph nodes count
@@ -322,13 +334,18 @@ int pfmd_batch_energy_history(pfmd_batch* batch, double* hist, long long* rows, 
  *
  * Computes the plain (FP64) rjl forces and total energy of n_atoms atoms that
  * all belong to one rjl interaction (rows = atoms 0..n_atoms-1, a full list):
- *   pos     device, n_atoms x 3 doubles (x, y, z of atom i at pos[3i..3i+2])
+ *   pos     device, n_atoms x 3 doubles (x, y, z of atom i at pos[3i..3i+2]),
+ *           each coordinate wrapped into [0, box): the minimum image is the
+ *           reference's single shift (md_general.f90:423-441), exact only for
+ *           separations within one box length
  *   box     host, the three periodic box lengths
  *   params  host, the parameter file's seven values: A0 xi p q r0 R1 R2
  *   nnum    device, n_atoms ints: entries of each row
  *   nbr     device, n_atoms x max_nbr ints, row i at nbr[i*max_nbr]: 0-based
- *           partner atoms (counts above max_nbr are cut, entries outside
- *           0..n_atoms-1 skipped)
+ *           partner atoms; entries outside 0..n_atoms-1 are skipped, and a row
+ *           whose count exceeds max_nbr (the reference stops with 'too many
+ *           neighbours') gets NaN forces and a NaN energy, which its partners'
+ *           forces then carry too
  *   frc     device, n_atoms x 3 doubles, written (not added to)
  *   energy  device, one double, or NULL to skip the energy
  *   stream  cudaStream_t to launch on (NULL: the default stream); the call
@@ -339,9 +356,11 @@ int pfmd_batch_energy_history(pfmd_batch* batch, double* hist, long long* rows, 
  *
  * Its scratch (1/Eb per atom, per-block energy partials; about 8 MiB) is a
  * fixed array inside the library, held by every device that loads it until the
- * process exits.  The first call on each device looks up that array's device
- * address with that device current; make that first call before any stream
- * capture.  All calls share the one array, so calls whose kernels overlap on
+ * process exits.  The first call on each device (and again after a device reset
+ * or in another CUDA context) looks up that array's device address with that
+ * device current; make that first call before any stream capture.  A CUDA error
+ * pending from the caller's earlier work is reported (PFMD_E_CUDA) and left
+ * pending.  All calls share the one array, so calls whose kernels overlap on
  * the GPU (other streams, other host threads) race: order them on one stream
  * or with events. */
 int pfmd_rjl_forces_noalloc(int n_atoms, const double* pos, const double box[3], const double params[7],

@@ -36,7 +36,7 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_graphs", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
            "pfmd_learned_check", "pfmd_learned_status", "pfmd_learned_gradient", "pfmd_nlist_builds", "pfmd_rjl_forces_noalloc",
-           "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting")
+           "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting", "pfmd_debug_waits")
 
 _LIB = None
 
@@ -120,9 +120,16 @@ def load(path=LIB_PATH):
     L.pfmd_learned_check.argtypes = [vp, dp]
     L.pfmd_learned_status.argtypes = [vp, ip, ip, dp, ip]
     # device buffers are passed as integer addresses (c_void_p)
+    L.pfmd_debug_waits.argtypes = [C.c_uint, C.c_int]
     L.pfmd_rjl_forces_noalloc.argtypes = [C.c_int, vp, dp, dp, vp, vp, C.c_int, vp, vp, vp, C.c_char_p, C.c_int]
     _LIB = L
     return L
+
+
+def debug_waits(spin_limit=0, stall=False):
+    """Test hook of the bounded device waits (pfmd_debug_waits): a poll limit
+    (0: built-in) and whether the next waits are made impossible."""
+    load().pfmd_debug_waits(int(spin_limit), 1 if stall else 0)
 
 
 def strerror(code):

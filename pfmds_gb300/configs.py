@@ -307,14 +307,13 @@ def cu_deposit(d, nx=6, ny=6, nz=4, a=3.615, fixed_layers=1, z_layers=1, n_dep=4
                        ("nvms", dt, 20, 100000000, log_period)]
     nmov = sum(1 for t in types if t == "CU")
     q1 = 3 * nmov * KB * temperature * 100.0 ** 2
-    ts1, ts2, frec = change
     text = _settings_text(
         step_limit=sum(i[2] for i in integrators), xyz_name=xyz_name, types=["CU", "CU_fixed", "CU_z", "CU_dep"],
         groups=[["CU", "CU_fixed", "CU_z", "CU_dep"], ["CU"], ["CU_z"], ["CU", "CU_dep"], ["CU", "CU_z", "CU_dep"],
                 ["CU_dep"]],
         all_moving=5, xyz_moving=4, z_moving=3, all_atoms=1, traj_group=6, period_traj=10,
         integrators=integrators, ms_de=1e-12, nhc=[(2, temperature, 3, q1)], t0=temperature,
-        changes=[(2, 4, ts1, ts2, frec)] if change else [], invert_z_vel=invert_z_vel,
+        changes=[(2, 4) + tuple(change)] if change else [], invert_z_vel=invert_z_vel,
         interactions=[("rjl", "parameters_RJL_Cu.txt", [(1, 1, nmax, rc_list, period)])])
     _write(d, settings_name, text)
     return settings_name

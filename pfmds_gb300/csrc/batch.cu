@@ -90,7 +90,9 @@ struct Dev {
   const RJLc<float>* rjl;
   const Tile* tile;
   double *tile_e, *tile_k, *e_pot, *e_kin, *hist;  // tile_e, e_pot: 3 interaction classes each
-  unsigned int *bar_count, *bar_gen;
+  unsigned int *bar_count, *bar_gen, *bar_flag;  // bar_flag: status when the last block arrived
+  unsigned int spin_limit;                        // polls before a barrier gives up
+  unsigned int bar_extra;                         // arrivals expected beyond the grid (0; 1 stalls)
   int* status;  // [0] code, [1] replica, [2] row, [3] info
   long long* step;
 };
@@ -106,33 +108,45 @@ __device__ __forceinline__ void fail(const Dev& D, int code, int rep, int row, i
   }
 }
 
-// Grid barrier for a cooperative launch (all blocks co-resident).  The spin is
-// bounded: after ~2^22 polls the block records PFMD_E_TIMEOUT and goes on, so every
-// block leaves the kernel at its next status check.
+// Grid barrier for a cooperative launch (all blocks co-resident).  The block
+// that arrives last copies the status word into bar_flag before it releases the
+// others, and every block returns that copy, so all blocks leave or pass the
+// same barrier together: an error raised after the release by a fast block is
+// seen by everyone at the next barrier.  The spin is bounded: after
+// D.spin_limit polls a block records PFMD_E_TIMEOUT and returns false.
 __device__ __forceinline__ bool barrier(const Dev& D) {
+  __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* gen = D.bar_gen;
     const unsigned int g = *gen;
     __threadfence();
-    if (atomicAdd(D.bar_count, 1u) == gridDim.x - 1) {
+    int ok;
+    if (atomicAdd(D.bar_count, 1u) == gridDim.x - 1 + D.bar_extra) {
+      const int st = *(volatile int*)D.status;
+      *(volatile unsigned int*)D.bar_flag = static_cast<unsigned int>(st);
       *D.bar_count = 0u;
       __threadfence();
       atomicAdd(D.bar_gen, 1u);
+      ok = st == 0;
     } else {
       unsigned int spins = 0;
+      bool released = true;
       while (*gen == g) {
-        if (++spins > (1u << 22)) {
+        if (++spins > D.spin_limit) {
           fail(D, PFMD_E_TIMEOUT, -1, -1, 0);
+          released = false;
           break;
         }
         __nanosleep(64);
       }
+      __threadfence();
+      ok = released && *(volatile unsigned int*)D.bar_flag == 0u;
     }
-    __threadfence();
+    s_ok = ok;
   }
   __syncthreads();
-  return *(volatile int*)D.status == 0;
+  return s_ok != 0;
 }
 
 __device__ __forceinline__ bool oob(double x, double Ltol) {
@@ -1044,7 +1058,7 @@ struct Batch {
     e_kin.alloc(reps.size());
     vcm.alloc(3 * reps.size());
     status.alloc(4);
-    bar.alloc(2);
+    bar.alloc(3);
     step.alloc(1);
     std::vector<double4_32a> p4(n), v4(n);
     std::vector<double> kc_h(n);
@@ -1065,7 +1079,7 @@ struct Batch {
     BCK(cudaMemsetAsync(frc.p, 0, n * sizeof(double4_32a), st));
     BCK(cudaMemsetAsync(nnum.p, 0, n * sizeof(int), st));
     BCK(cudaMemsetAsync(status.p, 0, 4 * sizeof(int), st));
-    BCK(cudaMemsetAsync(bar.p, 0, 2 * sizeof(unsigned int), st));
+    BCK(cudaMemsetAsync(bar.p, 0, 3 * sizeof(unsigned int), st));
     BCK(cudaMemsetAsync(step.p, 0, sizeof(long long), st));
     BCK(cudaMemsetAsync(e_pot.p, 0, 3 * reps.size() * sizeof(double), st));
     BCK(cudaMemsetAsync(e_kin.p, 0, reps.size() * sizeof(double), st));
@@ -1133,6 +1147,9 @@ struct Batch {
     D.hist = hist.p;
     D.bar_count = bar.p;
     D.bar_gen = bar.p + 1;
+    D.bar_flag = bar.p + 2;
+    D.spin_limit = g_wait_hook.spin_limit ? g_wait_hook.spin_limit : (1u << 22);
+    D.bar_extra = g_wait_hook.stall ? 1u : 0u;
     D.status = status.p;
     D.step = step.p;
     return D;
@@ -1176,8 +1193,11 @@ struct Batch {
       }
     };
     const auto key = std::make_pair(nsteps, chunk);
-    auto it = graphs.find(key);
-    if (it == graphs.end() && graphs_ok) {
+    // while the wait test hook is set, launch directly: a graph would keep the
+    // launch arguments of its capture
+    const bool hooked = g_wait_hook.spin_limit != 0 || g_wait_hook.stall != 0;
+    auto it = hooked ? graphs.end() : graphs.find(key);
+    if (it == graphs.end() && graphs_ok && !hooked) {
       cudaGraph_t g = nullptr;
       cudaGraphExec_t ge = nullptr;
       bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;

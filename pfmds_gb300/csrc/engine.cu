@@ -39,6 +39,7 @@
 namespace pfmd {
 
 thread_local long long g_kernel_launches = 0;
+WaitHook g_wait_hook;
 
 struct Error : std::runtime_error {
   int code;
@@ -470,6 +471,7 @@ class Engine {
   void alloc_list(ListH& L);
   void enqueue_forces(bool energy, bool kick = false, bool drift_next = false, bool begin = false);
   void plan_fusion();
+  void refresh_mflag();
   void run_plans(const std::vector<StepPlan>& plans);
   void host_events(const StepPlan& p);
   void get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f);
@@ -1104,6 +1106,8 @@ void Engine::raise_device_error() {
     default:
       if (c.error == PFMD_E_PARAM)
         msg = "error: group1%N>nl%N" + fortio::list_int(c.err_info[1]) + fortio::list_int(c.err_info[2]);
+      else if (c.error == PFMD_E_TIMEOUT)
+        msg = "error: a bounded device wait gave up (block" + fortio::list_int(c.err_info[0]) + ")";
       else
         msg = "device error";
   }
@@ -1274,6 +1278,23 @@ void Engine::plan_fusion() {
       mflag.upload(fl.data(), fl.size(), st);
     }
   }
+}
+
+// The per-atom moving flags that the force kernels' fused kick reads, from the
+// current sizes of the xyz- and z-moving groups (pfmd_set_group_n changes them
+// between steps, as change_particle_group_N does inside md()).
+void Engine::refresh_mflag() {
+  if (!kick_last || !mflag.p) return;
+  std::vector<unsigned char> fl(static_cast<size_t>(N), 0);
+  auto mark = [&](int g1based, unsigned char bit) {
+    const auto& idx = groups[static_cast<size_t>(g1based - 1)].idx;
+    const int cap = static_cast<int>(idx.size());
+    const int n = hctl ? std::min<int>(hctl->group_n[g1based - 1], cap) : cap;
+    for (int k = 0; k < n; ++k) fl[static_cast<size_t>(idx[static_cast<size_t>(k)])] |= bit;
+  };
+  mark(S.xyz_moving, 1);
+  mark(S.z_moving, 2);
+  mflag.upload(fl.data(), fl.size(), st);
 }
 
 void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin) {
@@ -2612,6 +2633,7 @@ int pfmd_set_group_n(pfmd_ctx* c, int group, int n) {
     const int cap = static_cast<int>(e.groups[static_cast<size_t>(group - 1)].idx.size());
     e.hctl->group_n[group - 1] = std::max(0, std::min(n, cap));
     e.upload_ctl_groups();
+    e.refresh_mflag();
     // rows change with the group: skin-triggered lists (and outer lists) rebuild at
     // their next update step
     CK(cudaMemsetAsync(e.ctl->list_need, 1, sizeof(e.ctl->list_need), e.st));
@@ -2734,6 +2756,12 @@ int pfmd_learned_status(const pfmd_ctx* c, int* active, int* checks, double* las
 int pfmd_kernel_launches(const pfmd_ctx* c, long long* n) {
   if (!c || !c->e || !n) return PFMD_E_STATE;
   *n = c->e->launches;
+  return PFMD_OK;
+}
+
+int pfmd_debug_waits(unsigned int spin_limit, int stall) {
+  pfmd::g_wait_hook.spin_limit = spin_limit;
+  pfmd::g_wait_hook.stall = stall ? 1 : 0;
   return PFMD_OK;
 }
 

@@ -30,6 +30,18 @@ namespace pfmd {
 // stream is being captured into a graph).
 extern thread_local long long g_kernel_launches;  // launches made by this host thread
 
+// Bounded device waits (the batched kernel's grid barrier, the tensor-core
+// kernels' mbarrier waits) read these at launch time.  spin_limit != 0 replaces
+// their built-in poll limits; stall != 0 makes the waits impossible (the grid
+// barrier expects one arrival more than the grid has, the tensor-core kernels
+// wait for an mbarrier phase that no MMA completes), so that tests can make
+// them run out.  Set by pfmd_debug_waits.
+struct WaitHook {
+  unsigned int spin_limit = 0;
+  int stall = 0;
+};
+extern WaitHook g_wait_hook;
+
 struct Atoms {
   int N;
   double4_32a* pos;

@@ -85,10 +85,11 @@ __device__ __forceinline__ void mma_commit(unsigned long long* mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
                : "memory");
 }
-// Bounded wait for the mbarrier phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned int parity) {
+// Bounded wait for the mbarrier phase with the given parity: at most `limit`
+// polls; false on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned int parity, unsigned int limit) {
   const unsigned int a = smem_u32(mbar);
-  for (unsigned int it = 0; it < (1u << 24); ++it) {
+  for (unsigned int it = 0; it < limit; ++it) {
     unsigned int done;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
@@ -132,7 +133,8 @@ __device__ __forceinline__ float dsilu_f(float z) {
 
 __global__ void __launch_bounds__(128, 1) k_mlp_tc(int rows, const float* __restrict__ G,
                                                    const DescPar* __restrict__ Dp, const Net* __restrict__ net,
-                                                   float* e_out, float* g_out, Ctl* ctl) {
+                                                   float* e_out, float* g_out, Ctl* ctl, unsigned int wait_limit,
+                                                   int stall) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // the operand tiles want 1024-byte alignment; the launch adds 1024 bytes of slack
   unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -181,11 +183,11 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(int rows, const float* __rest
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (t == 0) {
+    if (t == 0 && !stall) {  // stall (test hook): nothing arrives on the mbarrier
       mma_k64(tmem, aA, b_addr);
       mma_commit(&S.mbar);
     }
-    const bool ok = mbar_wait(&S.mbar, phase);
+    const bool ok = mbar_wait(&S.mbar, phase, wait_limit);
     phase ^= 1u;
     if (!ok) S.timeout = 1;
     tc_after_sync();
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(int rows, const float* __rest
     // a product that did not complete in time: give it one more bounded wait before
     // the accumulator is released
     if (t == 0) {
-      mbar_wait(&S.mbar, phase);
+      mbar_wait(&S.mbar, phase, wait_limit);
       set_error(ctl, PFMD_E_TIMEOUT, EK_NONE, blockIdx.x, 0, 0);
     }
   }
@@ -237,6 +239,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(int rows, const float* __rest
   tc_after_sync();
   if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
 }
+
+// Polls of an mbarrier wait before it gives up (the test hook may lower it).
+static unsigned int wait_limit() { return g_wait_hook.spin_limit ? g_wait_hook.spin_limit : (1u << 24); }
 
 void launch_mlp_tc(int rows, const float* G, const DescPar* d, const Net* net, float* e, float* g, Ctl* ctl,
                    cudaStream_t s) {
@@ -249,7 +254,8 @@ void launch_mlp_tc(int rows, const float* G, const DescPar* d, const Net* net, f
   }
   const int ntiles = (rows + TC_ROWS - 1) / TC_ROWS;
   const int grid = ntiles < 148 * 2 ? ntiles : 148 * 2;
-  k_mlp_tc<<<grid, TC_ROWS, sizeof(TcSmem) + 1024, s>>>(rows, G, d, net, e, g, ctl);
+  k_mlp_tc<<<grid, TC_ROWS, sizeof(TcSmem) + 1024, s>>>(rows, G, d, net, e, g, ctl, wait_limit(),
+                                                        g_wait_hook.stall);
   ++g_kernel_launches;
 }
 
@@ -351,7 +357,7 @@ __device__ __forceinline__ void zero16(unsigned char* p) { *reinterpret_cast<uin
 __global__ void __launch_bounds__(128, 1) k_train_tc(int rows, const float* __restrict__ G,
                                                      const float* __restrict__ U, const double* __restrict__ tgt,
                                                      float wE, float wF, const Net* __restrict__ net, float* part,
-                                                     double* lpart, Ctl* ctl) {
+                                                     double* lpart, Ctl* ctl, unsigned int wait_limit, int stall) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   TrSmem& S = *reinterpret_cast<TrSmem*>(base);
@@ -400,11 +406,11 @@ __global__ void __launch_bounds__(128, 1) k_train_tc(int rows, const float* __re
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (t == 0) {
+    if (t == 0 && !stall) {  // stall (test hook): nothing arrives on the mbarrier
       issue();
       mma_commit(&S.mbar);
     }
-    const bool ok = mbar_wait(&S.mbar, phase);
+    const bool ok = mbar_wait(&S.mbar, phase, wait_limit);
     phase ^= 1u;
     if (!ok) S.timeout = 1;
     tc_after_sync();
@@ -542,7 +548,7 @@ __global__ void __launch_bounds__(128, 1) k_train_tc(int rows, const float* __re
   }
   if (S.timeout) {
     if (t == 0) {
-      mbar_wait(&S.mbar, phase);
+      mbar_wait(&S.mbar, phase, wait_limit);
       set_error(ctl, PFMD_E_TIMEOUT, EK_NONE, blockIdx.x, 0, 0);
     }
   }
@@ -570,7 +576,7 @@ void launch_train_grad_tc(int rows, const float* G, const float* U, const double
   }
   const int grid = train_tc_grid(rows);
   k_train_tc<<<grid, TC_ROWS, sizeof(TrSmem) + 1024, s>>>(rows, G, U, target_by_row, wE, U ? wF : 0.f, net, T.part,
-                                                          T.lpart, ctl);
+                                                          T.lpart, ctl, wait_limit(), g_wait_hook.stall);
   ++g_kernel_launches;
   launch_train_reduce(grid, rows, T, s);
 }

@@ -17,6 +17,8 @@
 // gathers F_i -= (a - b (1/Eb_i + 1/Eb_j)) dr with the pair terms recomputed
 // (no per-entry cache), pass 3 sums the block partials of the energy in a fixed
 // order.
+#include <math_constants.h>
+
 #include <cstdarg>
 #include <cstdio>
 #include <mutex>
@@ -38,7 +40,11 @@ static constexpr int kNoAllocMaxBlocks = kNoAllocMaxAtoms / kNoAllocBlock;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxAtoms + kNoAllocMaxBlocks];
 
 static constexpr int kNoAllocMaxDevices = 64;
+// The address is cached per device together with the id of the CUDA context it
+// was looked up in: a device reset, or a caller's own driver-API context, makes
+// the next call look it up again in the context that is current then.
 static double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+static unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};
 static std::mutex g_noalloc_mu;
 
 __device__ __forceinline__ double4_32a na_pos(const double* __restrict__ pos, int i) {
@@ -46,7 +52,9 @@ __device__ __forceinline__ double4_32a na_pos(const double* __restrict__ pos, in
 }
 
 // One thread per atom.  Counts above max_nbr are cut to max_nbr and entries
-// outside [0, n) are skipped, so a malformed list cannot read out of bounds.
+// outside [0, n) are skipped, so a malformed list cannot read out of bounds; a
+// cut row gets NaN for its 1/Eb and its energy, so the error shows in the
+// energy and in the forces of the row and of its partners.
 __global__ void __launch_bounds__(kNoAllocBlock)
     k_na_rjl_density(int n, const double* __restrict__ pos, Box B, RJLc<double> c, const int* __restrict__ nnum,
                      const int* __restrict__ nbr, int max_nbr, double* __restrict__ scratch, int energy) {
@@ -71,8 +79,9 @@ __global__ void __launch_bounds__(kNoAllocBlock)
       }
     }
     const double eb = sqrt(eb2);
-    scratch[i] = 1.0 / eb;
-    erow[0] = c.A0 * er - c.xi * eb;
+    const bool cut = nnum[i] > max_nbr;
+    scratch[i] = cut ? CUDART_NAN : 1.0 / eb;
+    erow[0] = cut ? CUDART_NAN : c.A0 * er - c.xi * eb;
   }
   if (energy) {
     block_sum<1>(erow);
@@ -109,6 +118,7 @@ __global__ void __launch_bounds__(kNoAllocBlock)
       f[2] -= k * dr[2];
     }
   }
+  if (nnum[i] > max_nbr) f[0] = f[1] = f[2] = CUDART_NAN;  // a cut row
   frc[3 * (size_t)i] = f[0];
   frc[3 * (size_t)i + 1] = f[1];
   frc[3 * (size_t)i + 2] = f[2];
@@ -123,18 +133,47 @@ __global__ void __launch_bounds__(kNoAllocBlock)
   if (threadIdx.x == 0) *energy = v[0];
 }
 
-// Device address of the scratch array on the current device, looked up once per
-// device.  Host code cannot use g_noalloc_scratch's name as a device pointer.
+// Id of the CUDA context current on this thread (0 when none is), through the
+// driver entry point the runtime hands out; no driver library is linked.
+static unsigned long long current_ctx_id() {
+  using GetCur = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCur get_cur = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<GetCur>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_cur && get_id && get_cur(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
+
+// Device address of the scratch array in the current device's current context,
+// looked up once per device and context.  Host code cannot use
+// g_noalloc_scratch's name as a device pointer.
 static cudaError_t noalloc_scratch(double** out, int* dev) {
   cudaError_t err = cudaGetDevice(dev);
   if (err != cudaSuccess) return err;
   if (*dev < 0 || *dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[*dev]) {
+  unsigned long long ctx = current_ctx_id();
+  if (!g_noalloc_ptr[*dev] || ctx == 0 || ctx != g_noalloc_ctx[*dev]) {
     void* p = nullptr;
     err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (err != cudaSuccess) return err;
     g_noalloc_ptr[*dev] = static_cast<double*>(p);
+    g_noalloc_ctx[*dev] = ctx ? ctx : current_ctx_id();  // the lookup made the primary context current
   }
   *out = g_noalloc_ptr[*dev];
   return cudaSuccess;
@@ -171,9 +210,15 @@ extern "C" int pfmd_rjl_forces_noalloc(int n_atoms, const double* pos, const dou
   if (!(params[4] > 0.0) || !(params[6] > params[5]))
     return na_fail(err, err_len, PFMD_E_PARAM, "pfmd_rjl_forces_noalloc: need r0 > 0 and R2 > R1");
 
+  // an error left by the caller's earlier work is reported as such (and not
+  // cleared), not as a failure of this call's launches
+  cudaError_t ce = cudaPeekAtLastError();
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, PFMD_E_CUDA, "pfmd_rjl_forces_noalloc: a CUDA error was pending before the call: %s",
+                   cudaGetErrorString(ce));
   double* scratch = nullptr;
   int dev = -1;
-  cudaError_t ce = noalloc_scratch(&scratch, &dev);
+  ce = noalloc_scratch(&scratch, &dev);
   if (ce != cudaSuccess)
     return na_fail(err, err_len, PFMD_E_CUDA, "pfmd_rjl_forces_noalloc: scratch address on device %d: %s", dev,
                    cudaGetErrorString(ce));

@@ -89,3 +89,35 @@ def test_matches_context_forces_on_two_calls(tmp_path, built):
         assert np.abs(f - f_ref).max() <= 1e-9 * scale, f"call {call + 1}"
         assert abs(e - e_ref) <= 1e-9 * abs(e_ref), f"call {call + 1}: {e} vs {e_ref}"
     sim.close()
+
+
+@pytest.mark.gpu
+def test_rows_longer_than_max_nbr_give_nan(tmp_path, built):
+    """A row whose count exceeds max_nbr is cut; its force and the energy come
+    back NaN instead of plausible wrong values."""
+    torch = pytest.importorskip("torch")
+    configs.cu_slab(str(tmp_path), nx=NX, ny=NY, nz=NZ, steps=100, log_period=10)
+    box = np.asarray(configs.fcc_slab(NX, NY, NZ, A, vacuum=25.0)[1], dtype=np.float64)
+    params = np.array([float(x) for x in open(tmp_path / "parameters_RJL_Cu.txt").read().split()])
+    sim = pf.Simulation(str(tmp_path), form="plain")
+    n = sim.natoms
+    sim.compute(rebuild=True)
+    pos = sim.state()[0]
+    cnt, nbr = _atom_list(sim, n)
+    sim.close()
+    width = int(cnt.max()) - 1
+    cut = cnt > width
+    assert cut.any() and not cut.all()
+    dev = torch.device("cuda:0")
+    pos_d = torch.from_numpy(np.ascontiguousarray(pos)).to(dev)
+    nnum_d = torch.from_numpy(cnt).to(dev)
+    nbr_d = torch.from_numpy(np.ascontiguousarray(nbr[:, :width])).to(dev)
+    frc_d = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+    e_d = torch.zeros(1, dtype=torch.float64, device=dev)
+    rc, msg = _call(n, pos_d.data_ptr(), box, params, nnum_d.data_ptr(), nbr_d.data_ptr(), width,
+                    frc_d.data_ptr(), e_d.data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+    assert rc == pf.PFMD_OK, msg
+    torch.cuda.synchronize(dev)
+    f = frc_d.cpu().numpy()
+    assert np.isnan(f[cut]).all()
+    assert np.isnan(float(e_d.cpu()[0]))
