@@ -115,3 +115,153 @@ def forces_fd(pos, box, idx, model, atoms, h=1e-4):
             pm[a, c] -= h
             f[n, c] = -(energy(pp, box, idx, model) - energy(pm, box, idx, model)) / (2 * h)
     return f
+
+
+# ---- descriptor Jacobian, network gradient and the training loss ----------
+# The training loss of the library's learned form (learned.h: launch_train_grad)
+#   L(W) = wE * mean_rows (E_row - t_row)^2 + wF * sum_atoms |F - F_ref|^2 / (3 N)
+# with F = -dE/dx of the summed network energies, restated here in FP64 so that
+# tests can check the library's gradient of L with respect to the network's
+# weights (FP32 CUDA-core and BF16 tensor-core kernels) by central differences
+# of this L.
+
+def _fc_d(r, rc):
+    """fc and dfc/dr of the cosine cut-off, zero beyond rc."""
+    inside = r < rc
+    k = np.pi / rc
+    return (0.5 * (np.cos(k * r) + 1.0) * inside, -0.5 * k * np.sin(k * r) * inside)
+
+
+def descriptors_jacobian(pos, box, idx, desc):
+    """G (n x 48, un-normalised) of the atoms idx among themselves and
+    J = dG/dx (n x 48 x N x 3) over all N atoms of pos."""
+    box = np.asarray(box, float)
+    N = len(pos)
+    n = len(idx)
+    G = np.zeros((n, NG))
+    J = np.zeros((n, NG, N, 3))
+    p = pos[idx]
+    rs, er = desc["rs"], desc["eta_r"]
+    for a in range(n):
+        d = p - p[a]
+        d -= box * np.round(d / box)
+        r = np.sqrt((d * d).sum(1))
+        r[a] = np.inf
+        ia = idx[a]
+        # radial
+        m = np.nonzero(r < desc["rc_rad"])[0]
+        rr, dd = r[m], d[m]
+        fc, dfc = _fc_d(rr, desc["rc_rad"])
+        ex = np.exp(-er[None, :] * (rr[:, None] - rs[None, :]) ** 2)  # (m, NR)
+        G[a, :NR] = (ex * fc[:, None]).sum(0)
+        dg = ex * (-2.0 * er[None, :] * (rr[:, None] - rs[None, :]) * fc[:, None] + dfc[:, None])  # dg/dr
+        unit = dd / rr[:, None]
+        for q, j in enumerate(m):
+            contrib = dg[q][:, None] * unit[q][None, :]  # (NR, 3)
+            J[a, :NR, idx[j]] += contrib
+            J[a, :NR, ia] -= contrib
+        # angular
+        m = np.nonzero(r < desc["rc_ang"])[0]
+        if len(m) < 2:
+            continue
+        u, ru = d[m], r[m]
+        fa, dfa = _fc_d(ru, desc["rc_ang"])
+        jj, kk = np.triu_indices(len(m), 1)
+        U, V, RU, RV = u[jj], u[kk], ru[jj], ru[kk]
+        cs = (U * V).sum(1) / (RU * RV)
+        dcs_du = V / (RU * RV)[:, None] - cs[:, None] * U / (RU ** 2)[:, None]
+        dcs_dv = U / (RU * RV)[:, None] - cs[:, None] * V / (RV ** 2)[:, None]
+        for il in range(2):
+            lam = desc["lam"][il]
+            t = 1.0 + lam * cs
+            pos_t = t > 0
+            t = np.where(pos_t, t, 0.0)
+            for iz in range(4):
+                z = desc["zeta"][iz]
+                c0 = 2.0 ** (1 - z)
+                tz = t ** z
+                dtz = np.where(pos_t, z * t ** (z - 1) * lam, 0.0)  # d t^z / d cs
+                for ie in range(2):
+                    eta = desc["eta_a"][ie]
+                    E = np.exp(-eta * (RU ** 2 + RV ** 2))
+                    Bq = E * fa[jj] * fa[kk]
+                    col = NR + (il * 4 + iz) * 2 + ie
+                    G[a, col] += (c0 * tz * Bq).sum()
+                    dB_du = Bq[:, None] * (-2.0 * eta * U) + (E * dfa[jj] * fa[kk])[:, None] * U / RU[:, None]
+                    dB_dv = Bq[:, None] * (-2.0 * eta * V) + (E * fa[jj] * dfa[kk])[:, None] * V / RV[:, None]
+                    gu = c0 * (dtz[:, None] * dcs_du * Bq[:, None] + tz[:, None] * dB_du)
+                    gv = c0 * (dtz[:, None] * dcs_dv * Bq[:, None] + tz[:, None] * dB_dv)
+                    for q in range(len(jj)):
+                        J[a, col, idx[m[jj[q]]]] += gu[q]
+                        J[a, col, idx[m[kk[q]]]] += gv[q]
+                        J[a, col, ia] -= gu[q] + gv[q]
+    return G, J
+
+
+def net_vector(model):
+    """The network's weights as one vector in the library's Net layout
+    (W1, b1, W2, b2, w3, b3)."""
+    w = model["net"]
+    return np.concatenate([w["W1"].ravel(), w["b1"], w["W2"].ravel(), w["b2"], w["w3"], [w["b3"]]])
+
+
+def with_net_vector(model, v):
+    k = 0
+
+    def take(m):
+        nonlocal k
+        out = v[k:k + m]
+        k += m
+        return out
+    net = dict(W1=take(NH * NG).reshape(NH, NG), b1=take(NH), W2=take(NH * NH).reshape(NH, NH), b2=take(NH),
+               w3=take(NH), b3=take(1)[0])
+    return dict(kind=model["kind"], desc=model["desc"], net=net)
+
+
+def energies_and_dEdG(G, model):
+    """Row energies and dE_row/dG (un-normalised descriptor units)."""
+    d, w = model["desc"], model["net"]
+    x = (G - d["mean"]) * d["inv_std"]
+    z1 = x @ w["W1"].T + w["b1"]
+    a1 = _silu(z1)
+    z2 = a1 @ w["W2"].T + w["b2"]
+    a2 = _silu(z2)
+    E = a2 @ w["w3"] + w["b3"]
+
+    def dsilu(z):
+        s = 1.0 / (1.0 + np.exp(-z))
+        return s * (1.0 + z * (1.0 - s))
+    gz2 = w["w3"][None, :] * dsilu(z2)
+    gz1 = (gz2 @ w["W2"]) * dsilu(z1)
+    return E, (gz1 @ w["W1"]) * d["inv_std"]
+
+
+def training_loss(model, G, J, targets, f_ref, w_energy=1.0, w_force=1.0):
+    """L(W) at a configuration: G, J from descriptors_jacobian, per-row energy
+    targets and reference forces (N x 3)."""
+    E, g = energies_and_dEdG(G, model)
+    loss = w_energy * np.mean((E - targets) ** 2)
+    if w_force:
+        F = -np.einsum("rf,rfac->ac", g, J)
+        loss += w_force * ((F - f_ref) ** 2).sum() / (3 * len(f_ref))
+    return loss
+
+
+def rjl_atom_energies(pos, box, idx, par):
+    """Per-atom rjl energies A0 sum exp(-p(r/r0-1)) fc - xi sqrt(sum exp(-2q(r/r0-1)) fc)
+    with the cosine switch fc between R1 and R2 (r <= R2), over the atoms idx
+    (RosatoGuillopeLegrand.f90:23-49; cut_off_function.f90:6-16 with its pi)."""
+    A0, xi, p, q, r0, R1, R2 = par
+    box = np.asarray(box, float)
+    P = pos[idx]
+    out = np.zeros(len(idx))
+    for a in range(len(idx)):
+        d = P - P[a]
+        d -= box * np.round(d / box)
+        r = np.sqrt((d * d).sum(1))
+        r[a] = np.inf
+        r = r[r <= R2]
+        fc = np.where(r < R1, 1.0, 0.5 * (1.0 + np.cos(3.14159265358979 * (r - R1) / (R2 - R1))))
+        x = r / r0 - 1.0
+        out[a] = A0 * (np.exp(-p * x) * fc).sum() - xi * np.sqrt((np.exp(-2 * q * x) * fc).sum())
+    return out

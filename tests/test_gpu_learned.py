@@ -192,3 +192,57 @@ def test_tensor_core_training_lowers_energy_and_force_errors(tmp_path, built):
     assert (r1[:2] < r0[:2]).all(), (r0, r1)
     assert (r1[:2] < 0.05).all(), r1
     assert f1 < f0, (f0, f1)
+
+
+def test_training_gradient_matches_fp64_loss(tmp_path, built):
+    """The library's training-loss gradient -- FP32 CUDA-core kernel and BF16
+    tensor-core kernel -- against central differences of the FP64 loss of
+    oracle/learned_ref.py (energies against per-atom rjl energies, forces
+    against the oracle's FP64 forces), along random directions within each block
+    of the network's weights and across all of them."""
+    from oracle.pyoracle import Oracle
+    d = str(tmp_path)
+    configs.cu_slab(d, nx=3, ny=3, nz=3, steps=10 ** 6, log_period=10, temperature=800.0)
+    m = str(tmp_path / "m.bin")
+    s = pf.Simulation(d, form="plain", out_period=10 ** 9)
+    s.learned_train(m, frames=20, stride=5, iters=4, lr=2e-3)
+    s.close()
+    s = pf.Simulation(d, form="plain", out_period=10 ** 9)  # the input configuration
+    g32, loss32 = s.learned_gradient(m, force_weight=1.0)
+    gtc, losstc = s.learned_gradient(m, force_weight=1.0, tensor_cores=True)
+    s.close()
+    o = Oracle(d, out_period=1, threads=1)
+    o.step()
+    pos, _, f_ref = o.state()
+    lines = open(tmp_path / "cu_slab.xyz").read().splitlines()
+    box = np.array([float(x) for x in lines[1].split('"')[1].split()])[[0, 4, 8]]
+    par = [float(x) for x in open(tmp_path / "parameters_RJL_Cu.txt").read().split()]
+    idx = np.arange(len(pos))
+    model = learned_ref.load_models(m)[0]
+    G, J = learned_ref.descriptors_jacobian(pos, box, idx, model["desc"])
+    t = learned_ref.rjl_atom_energies(pos, box, idx, par)
+    v0 = learned_ref.net_vector(model)
+
+    def loss(v):
+        return learned_ref.training_loss(learned_ref.with_net_vector(model, v), G, J, t, f_ref)
+
+    E, _ = learned_ref.energies_and_dEdG(G, model)
+    assert loss32[0] == pytest.approx(((E - t) ** 2).sum(), rel=2e-3)
+    blocks = {"W1": (0, 3072), "b1": (3072, 3136), "W2": (3136, 7232), "b2": (7232, 7296), "w3": (7296, 7360),
+              "b3": (7360, 7361), "all": (0, learned_ref.NET_FLOATS)}
+    rng = np.random.default_rng(7)
+    h = 1e-5
+    report = {}
+    for name, (a, b) in blocks.items():
+        for _ in range(3 if b - a > 1 else 1):
+            dvec = np.zeros(learned_ref.NET_FLOATS)
+            dvec[a:b] = rng.standard_normal(b - a)
+            dvec /= np.linalg.norm(dvec)
+            fd = (loss(v0 + h * dvec) - loss(v0 - h * dvec)) / (2 * h)
+            gn = np.abs(np.concatenate([g32[0][a:b], [fd]])).max()
+            e32 = abs(float(g32[0] @ dvec) - fd)
+            etc = abs(float(gtc[0] @ dvec) - fd)
+            report.setdefault(name, []).append((fd, e32, etc))
+            assert e32 <= 2e-3 * (abs(fd) + 1e-2 * gn), (name, fd, float(g32[0] @ dvec))
+            assert etc <= 6e-2 * (abs(fd) + 1e-2 * gn), (name, fd, float(gtc[0] @ dvec))
+    print("loss gradient along directions (fd, |fp32 - fd|, |tc - fd|):", report)
