@@ -253,6 +253,9 @@ struct StepPlan {
   // the next step's kick and drift fused into this step's force kernel / this
   // step's kick and drift done by the previous step's
   bool drift_next = false, drifted = false;
+  // nvt with the pair kernel's fused chain: the chain's second-half scaling is
+  // left to the next step's k_nhc (same segment, no energy or output step)
+  bool nhc_defer = false;
 };
 
 // Snapshot and trajectory files (md_read_write.f90:65-107) are formatted and
@@ -401,7 +404,17 @@ class Engine {
   // force-phase fusion (Epi): the first force kernel stores instead of adding,
   // the last one applies the second half-kick
   bool store_first = false, kick_last = false;
-  DBuf<unsigned char> mflag;  // per atom: bit 0 in the xyz group, bit 1 in the z group
+  DBuf<unsigned char> mflag;  // per atom: bit 0 in the xyz group, bit 1 in the z group, bit 2 in chain 0's
+  // all lj / lj1g lists in one atom-major launch (k_pair_atoms)
+  bool pair_fused = false;
+  int pair_tpa = 1;
+  DBuf<int> pair_off;
+  DBuf<int2> pair_task;
+  DBuf<PairSlot> pair_slots;
+  bool nhc_fused = false;    // the pair kernel reduces chain 0's kinetic energy and updates it
+  bool nhc_pending = false;  // chain 0's last scaling still to be applied (by the next k_nhc)
+  void plan_pair_fusion();
+  PairSet pair_set() const;
   bool need_check_all = true;
 
   // md() loop state
@@ -917,6 +930,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     }
   }
   plan_fusion();
+  plan_pair_fusion();
   // the next step's kick and drift in the force kernel: precision form, one rjl
   // interaction whose rows are every atom and which kicks last, an xyz-moving group
   // and no z-moving one, no group changes or z-velocity inversion
@@ -989,6 +1003,24 @@ void Engine::tune_tpa() {
     if (t != L.d.tpa || t1 != L.d.tpa1) {
       L.d.tpa = t;
       L.d.tpa1 = t1;
+      changed = true;
+    }
+  }
+  if (pair_fused) {
+    // the all-pairs kernel: threads per atom from the entries an atom heads in all
+    double tot = 0;
+    for (const auto& I : inters)
+      for (int j = 0; j < (I.spec.kind == pfmd_io::K_LJ ? 2 : 1); ++j) {
+        const ListH& L = lists[static_cast<size_t>(I.lists[j])];
+        std::vector<int> n(static_cast<size_t>(std::max(L.d.rows, 0)));
+        if (n.empty()) continue;
+        CK(cudaMemcpyAsync(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int v : n) tot += v;
+      }
+    const int t = auto_tpa(N, tot / std::max(N, 1), prec);
+    if (t != pair_tpa) {
+      pair_tpa = t;
       changed = true;
     }
   }
@@ -1294,10 +1326,105 @@ void Engine::refresh_mflag() {
   };
   mark(S.xyz_moving, 1);
   mark(S.z_moving, 2);
+  if (nhc_fused) mark(S.nhc[0].group, 4);
   mflag.upload(fl.data(), fl.size(), st);
 }
 
+// All-pairs fusion: every interaction is lj or lj1g (at most kMaxPairSlots lists
+// and kMaxPairKeys interactions), the all-atoms group holds every atom, the
+// moving groups are disjoint and no group changes size.  One atom-major kernel
+// then forms, stores and kicks every atom's force.  Chain 0 fuses in as well
+// when it is the only chain and no z-velocity inversion runs between the steps.
+void Engine::plan_pair_fusion() {
+  if (!opt.fuse_steps || inters.empty() || !changes.empty() || N == 0 || !fuse_kick_drift) return;
+  int nslot = 0;
+  for (const auto& I : inters) {
+    if (I.spec.kind == pfmd_io::K_LJ)
+      nslot += 2;
+    else if (I.spec.kind == pfmd_io::K_LJ1G)
+      nslot += 1;
+    else
+      return;
+  }
+  if (nslot > kMaxPairSlots || static_cast<int>(inters.size()) > kMaxPairKeys) return;
+  if (static_cast<int>(groups[static_cast<size_t>(S.all_atoms - 1)].idx.size()) != N) return;
+  // an atom's tasks: the rows it heads, in slot order (lj rows before lj1g rows
+  // in the usual settings, so the kinds agree across a warp); and the slot table:
+  // the fields of each list the row loops read (list buffers keep their
+  // addresses for the life of the engine) and the parameters
+  std::vector<std::vector<int2>> t(static_cast<size_t>(N));
+  std::vector<PairSlot> slots;
+  double cap = 0.0;
+  int key = 0;
+  for (const auto& I : inters) {
+    const int nl = I.spec.kind == pfmd_io::K_LJ ? 2 : 1;
+    for (int j = 0; j < nl; ++j) {
+      const ListH& L = lists[static_cast<size_t>(I.lists[j])];
+      const auto& g = groups[static_cast<size_t>(L.d.row_group)].idx;
+      const int slot = static_cast<int>(slots.size());
+      for (int r = 0; r < L.d.rows && r < static_cast<int>(g.size()); ++r) {
+        t[static_cast<size_t>(g[static_cast<size_t>(r)])].push_back(make_int2(slot, r));
+        cap += 0.5 * std::max(L.d.nmax, 2);
+      }
+      PairSlot sl{};
+      sl.L = RowList{L.d.nnum, L.d.nlist, L.d.lessnnum, L.d.bnd, L.d.row_of, L.d.stride, L.d.sorted};
+      sl.P = I.lj;
+      sl.kind = I.spec.kind == pfmd_io::K_LJ ? 0 : 1;
+      sl.general = I.general ? 1 : 0;
+      sl.ekey = j == 0 ? key : -1;  // lj's energy is that of its first list (LennardJones.f90:23-46)
+      slots.push_back(sl);
+    }
+    ++key;
+  }
+  std::vector<int> off(static_cast<size_t>(N) + 1, 0);
+  std::vector<int2> flat;
+  for (int a = 0; a < N; ++a) {
+    off[static_cast<size_t>(a) + 1] = off[static_cast<size_t>(a)] + static_cast<int>(t[static_cast<size_t>(a)].size());
+    for (const int2& x : t[static_cast<size_t>(a)]) flat.push_back(x);
+  }
+  pair_off.alloc(off.size());
+  pair_off.upload(off.data(), off.size(), st);
+  pair_task.alloc(std::max<size_t>(flat.size(), 1));
+  if (!flat.empty()) pair_task.upload(flat.data(), flat.size(), st);
+  pair_slots.alloc(slots.size());
+  pair_slots.upload(slots.data(), slots.size(), st);
+  pair_fused = true;
+  store_first = true;
+  kick_last = true;
+  nhc_fused = S.nhc.size() == 1 && !S.invert_z_vel;
+  mflag.alloc(static_cast<size_t>(std::max(N, 1)));
+  refresh_mflag();
+  // until tune_tpa measures the rows: half of each headed row's capacity
+  pair_tpa = auto_tpa(N, cap / N, prec);
+  CK(cudaStreamSynchronize(st));
+}
+
+PairSet Engine::pair_set() const {
+  PairSet P{};
+  P.natoms = N;
+  P.tpa = pair_tpa;
+  P.task_off = pair_off.p;
+  P.task = pair_task.p;
+  P.slots = pair_slots.p;
+  int slot = 0;
+  for (size_t k = 0; k < inters.size(); ++k) {
+    slot += inters[k].spec.kind == pfmd_io::K_LJ ? 2 : 1;
+    P.keys[k] = static_cast<int>(k);
+  }
+  P.nslot = slot;
+  P.nkey = static_cast<int>(inters.size());
+  return P;
+}
+
 void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin) {
+  if (pair_fused && !learned_active) {
+    // every lj / lj1g list in one launch: stores every force, kicks (second half)
+    // and, under nvt, reduces and updates chain 0
+    Epi e{1, kick ? 1 : 0, prec ? 0 : 1, ts[1], mflag.p, eatom_out};
+    const int chain = (kick && nhc_fused && integ == I_NVT) ? 0 : -1;
+    launch_pair_atoms(prec, energy, pair_set(), A, box, ctl, st, e, chain, ts[1], ts[2], ts[3]);
+    return;
+  }
   // which launch is the first / last force writer
   const int nint = static_cast<int>(inters.size());
   auto epi = [&](bool first, bool last) {
@@ -1389,7 +1516,9 @@ void Engine::enqueue_step(const StepPlan& p) {
     if (nvt)
       for (size_t c = 0; c < S.nhc.size(); ++c) {
         const GroupRef gc = gref(S.nhc[c].group);
-        launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st);
+        // a pending scaling of chain 0 (the previous step's second half) comes first
+        launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st, (c == 0 && nhc_pending) ? 1 : 0);
+        if (c == 0) nhc_pending = false;
         if (static_cast<int>(c) == fused_nhc_chain)
           scale_chain = static_cast<int>(c) + 1;
         else
@@ -1424,6 +1553,14 @@ void Engine::enqueue_step(const StepPlan& p) {
     if (nvt)
       for (size_t c = 0; c < S.nhc.size(); ++c) {
         const GroupRef gc = gref(S.nhc[c].group);
+        if (c == 0 && nhc_fused && pair_fused && !learned_active) {
+          // the pair kernel reduced the kinetic energy and updated the chain
+          if (p.nhc_defer)
+            nhc_pending = true;
+          else
+            launch_scale(0, gc, A, ctl, st);
+          continue;
+        }
         launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st);
         launch_scale(static_cast<int>(c), gc, A, ctl, st);
       }
@@ -1447,7 +1584,7 @@ static std::string plan_key(const StepPlan& p) {
   k.reserve(8 + p.rebuild.size());
   k.push_back(static_cast<char>('A' + (p.first ? 1 : 0) + 2 * (p.energy ? 1 : 0) + 4 * (p.out ? 1 : 0) +
                                 8 * (p.zero_mom ? 1 : 0) + 16 * (p.check_all ? 1 : 0)));
-  k.push_back(static_cast<char>('a' + (p.drift_next ? 1 : 0) + 2 * (p.drifted ? 1 : 0)));
+  k.push_back(static_cast<char>('a' + (p.drift_next ? 1 : 0) + 2 * (p.drifted ? 1 : 0) + 4 * (p.nhc_defer ? 1 : 0)));
   for (char r : p.rebuild) k.push_back(r ? '1' : '0');
   k.push_back('|');
   return k;
@@ -1702,6 +1839,13 @@ void Engine::advance(long long max_steps, int* fin) {
         StepPlan& b = plans[i + 1];
         if (a.first || a.energy || a.out || b.first || b.check_all) continue;
         a.drift_next = b.drifted = true;
+      }
+    // chain 0's second-half scaling waits for the next step's k_nhc when both
+    // steps are in this segment and the first computes no energies or output
+    if (nhc_fused && pair_fused && integ == I_NVT && !learned_active)
+      for (size_t i = 0; i + 1 < plans.size(); ++i) {
+        StepPlan& a = plans[i];
+        if (!a.first && !a.energy && !a.out) a.nhc_defer = true;
       }
     run_plans(plans);
     read_ctl();

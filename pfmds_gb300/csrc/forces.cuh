@@ -212,7 +212,7 @@ __device__ __forceinline__ void finish_force(const Atoms& A, const Epi& E, int a
   }
   A.frc[ai] = f;
   if (E.kick) {
-    const unsigned char m = E.mflag[ai];
+    const unsigned char m = E.mflag[ai] & 3;  // bit 1: xyz-moving, bit 2: z-moving
     if (m) {
       double4_32a v = A.vel[ai];
       if (E.exact) {
@@ -273,6 +273,53 @@ __device__ __forceinline__ void finish_force_drift(const Atoms& A, const Epi& E,
   }
 }
 
+// Reduction slot (Ctl::counter) of the all-pairs kernel k_pair_atoms.
+constexpr int kPairSlot = 20;
+constexpr double kMassCoef = 1.6605389217 / 1.6021765654 * 100.0;  // amu A^2/fs^2 -> eV (md_integrators.f90:62)
+constexpr double kKtPerKelvin = 1.3806488 / 1.6021765654 * 1e-4;   // k_B in eV/K (md_general.f90:304)
+
+// Kinetic energy of atom i (calculate_kinetic_energy's term, md_general.f90:161-180).
+__device__ __forceinline__ double ke_of(const Atoms& A, int i) {
+  const double4_32a v = A.vel[i];
+  return A.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z) / 2 * kMassCoef;
+}
+
+// The chain part of integrate_nose_hoover_chain (md_integrators.f90:200-245)
+// for the group's kinetic energy ke: both half-updates of the chain and the
+// scale factor s (k_scale / k_kick_drift apply it).  One thread.
+__device__ __forceinline__ void nhc_chain_update(NHCDev& hd, double ke, double ts2, double ts3, double ts4) {
+  NHCDev h = hd;  // one set of independent loads, not a chain of dependent ones
+  const double kt = kKtPerKelvin * h.T;
+  const int M = h.M;
+  double kedif = 2.0 * ke - 3.0 * h.L * kt;
+  double b = 0.0;
+  if (M == 1) {
+    h.v[0] = h.v[0] + kedif / h.q[0] * ts3;
+  } else {
+    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) / h.q[M - 1] * ts3;
+    for (int i = M - 2; i >= 1; --i) {
+      b = exp(-h.v[i + 1] * ts4);
+      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) / h.q[i] * ts3 * b;
+    }
+    b = exp(-h.v[1] * ts4);
+    h.v[0] = h.v[0] * (b * b) + kedif / h.q[0] * ts3 * b;
+  }
+  h.s = exp(-h.v[0] * ts2);
+  kedif = 2.0 * ke * (h.s * h.s) - 3.0 * h.L * kt;
+  for (int i = 0; i < M; ++i) h.x[i] = h.x[i] + h.v[i] * ts2;
+  if (M == 1) {
+    h.v[0] = h.v[0] + kedif / h.q[0] * ts3;
+  } else {
+    h.v[0] = h.v[0] * (b * b) + kedif / h.q[0] * ts3 * b;
+    for (int i = 1; i <= M - 2; ++i) {
+      b = exp(-h.v[i + 1] * ts4);
+      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) / h.q[i] * ts3 * b;
+    }
+    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) / h.q[M - 1] * ts3;
+  }
+  hd = h;
+}
+
 // Energy of one row into the interaction's total (every thread of the grid calls it).
 __device__ __forceinline__ void energy_reduce(Ctl* ctl, int eslot, int ekey, double erow) {
   double v[1] = {erow}, out[1];
@@ -329,6 +376,7 @@ static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 // Entry `p` of list row `row` (slot-major storage).
 __device__ __forceinline__ int ent(const ListDev& L, int row, int p) { return L.nlist[(size_t)p * L.stride + row]; }
+__device__ __forceinline__ int ent(const RowList& L, int row, int p) { return L.nlist[(size_t)p * L.stride + row]; }
 
 // 2^x by the ex2.approx instruction (relative error about 2^-22).
 __device__ __forceinline__ float ex2_approx(float x) {

@@ -3,6 +3,69 @@
 
 namespace pfmd {
 
+// One list row of lj: thread `sub` of the row's TPA threads adds its share of
+// the row's force to acc and (ENERGY) of its energy to e.
+template <bool PREC, bool ENERGY, int TPA, class LT>
+__device__ __forceinline__ void lj_row(const LT& L, const LJc<typename RT<PREC>::R>& c, const Atoms& A,
+                                       const Box& B, int row, int sub, int n, const typename RT<PREC>::P4& pi,
+                                       Acc3<PREC>& acc, Acc1<PREC>& e) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+#pragma unroll 4
+  for (int p = sub; p < n; p += TPA) {
+    R dr[3];
+    const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, row, p)), B, dr));
+    if (r < c.R2) {
+      const R ir = xrcp<PREC>(r);
+      const R x = c.sig * ir, x2 = x * x, V = x2 * x2 * x2;
+      R fc, dfc;
+      fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
+      const R k = c.eps4 * (V * (R(12) * V - R(6)) * (ir * ir) * fc - V * (V - R(1)) * dfc);
+      acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
+      if (ENERGY) e.add(c.eps4 * V * (V - R(1)) * fc);
+    }
+  }
+}
+
+// One list row of lj1g (row atom ai), as lj_row.
+template <bool PREC, bool ENERGY, bool GENERAL, int TPA, class LT>
+__device__ __forceinline__ void lj1g_row(const LT& L, const LJc<typename RT<PREC>::R>& c, const Atoms& A,
+                                         const Box& B, int row, int sub, int n, int ai,
+                                         const typename RT<PREC>::P4& pi, Acc3<PREC>& acc, Acc1<PREC>& e) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+  const int less = L.lessnnum[row];
+#pragma unroll 4
+  for (int p = sub; p < n; p += TPA) {
+    const int aj = ent(L, row, p);
+    R dr[3];
+    const R r2 = T::d2(pi, T::load(A, aj), B, dr);
+    const R r = xsqrt<PREC>(r2);
+    if (r < c.R2) {  // beyond R2 the clamped switch makes force and energy exactly zero
+      R w = R(1);
+      if (GENERAL) w = R((p < less ? 1 : 0) + (row < L.bnd[L.row_of[aj]] ? 1 : 0));
+      const R invr2 = xrcp<PREC>(r2);
+      const R U = invr2 * invr2 * invr2;
+      R fcut, dfr;
+      f_dfr_cut<R>(r, c.R1, c.R2, fcut, dfr);
+      const R F = w * (U * invr2 * ((c.c12t12 * U - c.c6t6) * fcut - (c.c12 * U - c.c6) * dfr));
+      acc.add(-F * dr[0], -F * dr[1], -F * dr[2]);
+      // the half list p <= lessnnum(i); in a row kept in cell order (groups in
+      // atom order only) that is the partners with a smaller atom index
+      if (ENERGY && (L.sorted ? p < less : aj < ai)) {
+        R fp;
+        if constexpr (PREC) {
+          const R x = (r - c.R1) * c.inv_w;
+          fp = r <= c.R1 ? R(1) : R(1) + x * x * x * (R(-10) + R(15) * x - R(6) * x * x);
+        } else {
+          fp = fcut_poly(r, c.R1, c.R2);
+        }
+        e.add(U * (c.c12 * U - c.c6) * fp);
+      }
+    }
+  }
+}
+
 // lj: LennardJones.f90:23-69 (cosine switch, full list, force on the row atom)
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_lj(ListDev L, LJPar P, Atoms A, Box B, Ctl* ctl, int eslot, int ekey,
@@ -17,23 +80,7 @@ __global__ void __launch_bounds__(256) k_lj(ListDev L, LJPar P, Atoms A, Box B, 
   const auto& c = cst<PREC>(P);
   Acc3<PREC> acc;
   Acc1<PREC> e;
-  if (n > 0) {
-    const auto pi = T::load(A, ai);
-#pragma unroll 4
-    for (int p = g.sub; p < n; p += TPA) {
-      R dr[3];
-      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, g.row, p)), B, dr));
-      if (r < c.R2) {
-        const R ir = xrcp<PREC>(r);
-        const R x = c.sig * ir, x2 = x * x, V = x2 * x2 * x2;
-        R fc, dfc;
-        fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
-        const R k = c.eps4 * (V * (R(12) * V - R(6)) * (ir * ir) * fc - V * (V - R(1)) * dfc);
-        acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
-        if (ENERGY) e.add(c.eps4 * V * (V - R(1)) * fc);
-      }
-    }
-  }
+  if (n > 0) lj_row<PREC, ENERGY, TPA>(L, c, A, B, g.row, g.sub, n, T::load(A, ai), acc, e);
   acc.template reduce<TPA>();
   if (ENERGY) e.template reduce<TPA>();
   if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
@@ -60,39 +107,7 @@ __global__ void __launch_bounds__(256) k_lj1g(ListDev L, LJPar P, Atoms A, Box B
   const auto& c = cst<PREC>(P);
   Acc3<PREC> acc;
   Acc1<PREC> e;
-  if (n > 0) {
-    const int less = L.lessnnum[g.row];
-    const auto pi = T::load(A, ai);
-#pragma unroll 4
-    for (int p = g.sub; p < n; p += TPA) {
-      const int aj = ent(L, g.row, p);
-      R dr[3];
-      const R r2 = T::d2(pi, T::load(A, aj), B, dr);
-      const R r = xsqrt<PREC>(r2);
-      if (r < c.R2) {  // beyond R2 the clamped switch makes force and energy exactly zero
-        R w = R(1);
-        if (GENERAL) w = R((p < less ? 1 : 0) + (g.row < L.bnd[L.row_of[aj]] ? 1 : 0));
-        const R invr2 = xrcp<PREC>(r2);
-        const R U = invr2 * invr2 * invr2;
-        R fcut, dfr;
-        f_dfr_cut<R>(r, c.R1, c.R2, fcut, dfr);
-        const R F = w * (U * invr2 * ((c.c12t12 * U - c.c6t6) * fcut - (c.c12 * U - c.c6) * dfr));
-        acc.add(-F * dr[0], -F * dr[1], -F * dr[2]);
-        // the half list p <= lessnnum(i); in a row kept in cell order (groups in
-        // atom order only) that is the partners with a smaller atom index
-        if (ENERGY && (L.sorted ? p < less : aj < ai)) {
-          R fp;
-          if constexpr (PREC) {
-            const R x = (r - c.R1) * c.inv_w;
-            fp = r <= c.R1 ? R(1) : R(1) + x * x * x * (R(-10) + R(15) * x - R(6) * x * x);
-          } else {
-            fp = fcut_poly(r, c.R1, c.R2);
-          }
-          e.add(U * (c.c12 * U - c.c6) * fp);
-        }
-      }
-    }
-  }
+  if (n > 0) lj1g_row<PREC, ENERGY, GENERAL, TPA>(L, c, A, B, g.row, g.sub, n, ai, T::load(A, ai), acc, e);
   acc.template reduce<TPA>();
   if (ENERGY) e.template reduce<TPA>();
   if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
@@ -132,6 +147,96 @@ void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const L
               <<<grid, 256, 0, s>>>(L, P, A, B, ctl, eslot, ekey, E);
           ++g_kernel_launches;
         });
+      });
+    });
+  });
+}
+
+// All lj / lj1g lists in one launch, atom-major (see PairSet).  A warp holds
+// 32/TPA consecutive atoms and walks them in tiles over the grid; the atoms of a
+// warp may head different numbers of rows, so every thread loops to the warp's
+// largest task count and the shuffles of the reductions see the whole warp.
+// Energies (per interaction) and the chain's kinetic energy go through one
+// grid reduction; its last block stores the energies and updates the chain.
+template <bool PREC, bool ENERGY, int TPA>
+__global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
+                                                    double ts2, double ts3, double ts4) {
+  using T = RT<PREC>;
+  if (ctl->stop) return;
+  constexpr int RPW = 32 / TPA;
+  const int lane = threadIdx.x & 31, sub = lane / RPW;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarp = (gridDim.x * blockDim.x) >> 5;
+  double red[kMaxPairKeys + 1] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int base = warp * RPW; base < S.natoms; base += nwarp * RPW) {
+    const int a = base + lane % RPW;
+    const bool valid = a < S.natoms;
+    const int t0 = valid ? S.task_off[a] : 0, nt = valid ? S.task_off[a + 1] - t0 : 0;
+    int ntw = nt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ntw = max(ntw, __shfl_xor_sync(0xffffffffu, ntw, o));
+    Acc3<PREC> acc;
+    Acc1<PREC> e[kMaxPairKeys];
+    const auto pi = T::load(A, valid ? a : 0);
+    for (int t = 0; t < ntw; ++t) {
+      if (t >= nt) continue;
+      const int2 tk = S.task[t0 + t];
+      // the slot's list and constants into registers once per row
+      const PairSlot& sl = S.slots[tk.x];
+      const RowList L = sl.L;
+      const auto c = cst<PREC>(sl.P);
+      const int kind = sl.kind, general = sl.general, ekey = sl.ekey;
+      const int n = L.nnum[tk.y];
+      Acc1<PREC> et;
+      if (kind == 0)
+        lj_row<PREC, ENERGY, TPA>(L, c, A, B, tk.y, sub, n, pi, acc, et);
+      else if (general)
+        lj1g_row<PREC, ENERGY, true, TPA>(L, c, A, B, tk.y, sub, n, a, pi, acc, et);
+      else
+        lj1g_row<PREC, ENERGY, false, TPA>(L, c, A, B, tk.y, sub, n, a, pi, acc, et);
+      if (ENERGY && ekey >= 0) {
+#pragma unroll
+        for (int k = 0; k < kMaxPairKeys; ++k)
+          if (k == ekey) e[k].add(static_cast<typename T::R>(et.get()));
+      }
+    }
+    acc.template reduce<TPA>();
+    if (ENERGY) {
+#pragma unroll
+      for (int k = 0; k < kMaxPairKeys; ++k) e[k].template reduce<TPA>();
+    }
+    if (valid && sub == 0) {
+      finish_force(A, E, a, acc.get(0), acc.get(1), acc.get(2));
+      if (ENERGY) {
+#pragma unroll
+        for (int k = 0; k < kMaxPairKeys; ++k) red[k] += e[k].get();
+      }
+      if (chain >= 0 && (E.mflag[a] & 4)) red[kMaxPairKeys] += ke_of(A, a);
+    }
+  }
+  if (!ENERGY && chain < 0) return;
+  double out[kMaxPairKeys + 1];
+  if (!grid_sum<kMaxPairKeys + 1>(ctl, kPairSlot, red, out)) return;
+  if (ENERGY) {
+#pragma unroll
+    for (int k = 0; k < kMaxPairKeys; ++k)
+      if (k < S.nkey) ctl->e_inter[S.keys[k]] = out[k];
+  }
+  if (chain >= 0) nhc_chain_update(ctl->nhc[chain], out[kMaxPairKeys], ts2, ts3, ts4);
+}
+
+void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A, const Box& B, Ctl* ctl,
+                       cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4) {
+  if (S.natoms <= 0) return;
+  // at most 4096 blocks: their partials of the grid reduction fit Ctl::partial
+  const long long blocks = nblk((long long)S.natoms * S.tpa, 256);
+  const int grid = static_cast<int>(blocks < 4096 ? blocks : 4096);
+  with_bool(prec, [&](auto pr) {
+    with_bool(energy, [&](auto en) {
+      with_tpa(S.tpa, [&](auto t) {
+        k_pair_atoms<decltype(pr)::value, decltype(en)::value, decltype(t)::value>
+            <<<grid, 256, 0, s>>>(S, A, B, ctl, E, chain, ts2, ts3, ts4);
+        ++g_kernel_launches;
       });
     });
   });

@@ -12,7 +12,7 @@
 // multiplies by a per-atom 1/(m*mass_coef) to keep FP64 divides off the step.
 // Reductions are deterministic: block partials summed in block order by the
 // last block, which also performs the scalar updates (chain, temperature).
-#include "kernels.h"
+#include "forces.cuh"
 
 namespace pfmd {
 
@@ -279,52 +279,32 @@ void launch_step_begin_fused(Ctl* ctl, cudaStream_t s) {
   ++g_kernel_launches;
 }
 
-__device__ __forceinline__ double ke_of(const Atoms& A, int i) {
-  const double4_32a v = A.vel[i];
-  return A.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z) / 2 * c_mass_coef;
-}
 
 // integrate_nose_hoover_chain (md_integrators.f90:200-245) up to the velocity
-// scaling: kinetic energy of the chain's group, both half-updates of the chain and
-// the scale factor s (k_scale / k_kick_drift apply it).
+// scaling: kinetic energy of the chain's group, then nhc_chain_update in the last
+// block.  prescale: the velocities first get the chain's pending s (the scaling
+// of the chain's previous half, which the force kernel before it left to this
+// kernel), so the kinetic energy is that of the scaled velocities, as in the
+// reference.
 __global__ void __launch_bounds__(kRedThreads) k_nhc(int chain, GroupRef g, double ts2, double ts3, double ts4,
-                                                     Atoms A, Ctl* ctl) {
+                                                     Atoms A, Ctl* ctl, int prescale) {
   if (ctl->stop) return;
   const int n = ctl->group_n[g.g];
+  const double s0 = ctl->nhc[chain].s;
   double v[1] = {0.0}, out[1];
-  for (int ind = blockIdx.x * blockDim.x + threadIdx.x; ind < n; ind += gridDim.x * blockDim.x)
-    v[0] += ke_of(A, g.idx[ind]);
+  for (int ind = blockIdx.x * blockDim.x + threadIdx.x; ind < n; ind += gridDim.x * blockDim.x) {
+    const int i = g.idx[ind];
+    if (prescale) {
+      double4_32a u = A.vel[i];
+      u.x *= s0;
+      u.y *= s0;
+      u.z *= s0;
+      A.vel[i] = u;
+    }
+    v[0] += ke_of(A, i);
+  }
   if (!grid_sum<1>(ctl, 0, v, out)) return;
-  const double ke = out[0];
-  NHCDev& h = ctl->nhc[chain];
-  const double kt = c_kt_a_degree * h.T;
-  const int M = h.M;
-  double kedif = 2.0 * ke - 3.0 * h.L * kt;
-  double b = 0.0;
-  if (M == 1) {
-    h.v[0] = h.v[0] + kedif / h.q[0] * ts3;
-  } else {
-    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) / h.q[M - 1] * ts3;
-    for (int i = M - 2; i >= 1; --i) {
-      b = exp(-h.v[i + 1] * ts4);
-      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) / h.q[i] * ts3 * b;
-    }
-    b = exp(-h.v[1] * ts4);
-    h.v[0] = h.v[0] * (b * b) + kedif / h.q[0] * ts3 * b;
-  }
-  h.s = exp(-h.v[0] * ts2);
-  kedif = 2.0 * ke * (h.s * h.s) - 3.0 * h.L * kt;
-  for (int i = 0; i < M; ++i) h.x[i] = h.x[i] + h.v[i] * ts2;
-  if (M == 1) {
-    h.v[0] = h.v[0] + kedif / h.q[0] * ts3;
-  } else {
-    h.v[0] = h.v[0] * (b * b) + kedif / h.q[0] * ts3 * b;
-    for (int i = 1; i <= M - 2; ++i) {
-      b = exp(-h.v[i + 1] * ts4);
-      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) / h.q[i] * ts3 * b;
-    }
-    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) / h.q[M - 1] * ts3;
-  }
+  nhc_chain_update(ctl->nhc[chain], out[0], ts2, ts3, ts4);
 }
 
 // scale_velocities (md_general.f90:97-112) by the chain's s
@@ -518,8 +498,8 @@ void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_pos
   ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
-                cudaStream_t s) {
-  { k_nhc<<<red_grid(g.cap), kRedThreads, 0, s>>>(chain, g, ts2, ts3, ts4, A, ctl); ++g_kernel_launches; }
+                cudaStream_t s, int prescale) {
+  { k_nhc<<<red_grid(g.cap), kRedThreads, 0, s>>>(chain, g, ts2, ts3, ts4, A, ctl, prescale); ++g_kernel_launches; }
 }
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s) {
   if (g.cap > 0) { k_scale<<<nb(g.cap, 256), 256, 0, s>>>(chain, g, A, ctl); ++g_kernel_launches; }

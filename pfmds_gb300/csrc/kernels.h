@@ -210,6 +210,39 @@ void launch_lj(bool prec, bool energy, const ListDev& L, const LJPar& P, const A
 void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const LJPar& P, const Atoms& A,
                  const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s,
                  const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
+// All lj and lj1g lists of a system in one launch (k_pair_atoms): TPA threads
+// own an atom and gather over every list row the atom heads -- its tasks, as
+// (slot, row) pairs in slot order -- so each atom's force is formed in one
+// place and stored (no zero_forces), kicked (Epi::kick) and, for a
+// Nose-Hoover chain (mflag bit 4 marks its group), the chain's kinetic energy
+// is reduced and the chain updated by the last block.
+// The fields of one list that the pair row loops read.
+struct RowList {
+  const int* nnum;
+  const int* nlist;
+  const int* lessnnum;
+  const int* bnd;
+  const int* row_of;
+  int stride, sorted;
+};
+struct PairSlot {  // device memory, one per list
+  RowList L;
+  LJPar P;
+  int kind;     // 0: lj, 1: lj1g
+  int general;  // lj1g rows with half-list weights (group not in atom order)
+  int ekey;     // index into PairSet::keys of the energy this list adds to, or -1
+};
+constexpr int kMaxPairSlots = 6, kMaxPairKeys = 4;
+struct PairSet {
+  int nslot, nkey, natoms, tpa;
+  const PairSlot* slots;   // nslot, device memory
+  int keys[kMaxPairKeys];  // e_inter indexes
+  const int* task_off;     // natoms + 1
+  const int2* task;        // (slot, row)
+};
+void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A, const Box& B, Ctl* ctl,
+                       cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4);
+
 // Multi-kernel interactions take `parts`, a bit mask of their kernels (all by
 // default; single kernels are launched alone only for timing).
 // inv_eb: 1/Eb per atom (double[N] plain, float[N] precision); pair: the plain
@@ -256,7 +289,8 @@ void launch_step_begin_fused(Ctl* ctl, cudaStream_t s);
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
-                cudaStream_t s);
+                cudaStream_t s,
+                int prescale = 0);
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_ms(const GroupRef& g, bool xyz, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_zero_forces(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
