@@ -679,6 +679,46 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(name):
+    """One small run of a single kernel family's workload (for ncu captures of
+    that family): the bench slab, the binary LJ gas, the graphene/Cu moire, a
+    64-replica batch or a learned-form force evaluation, in the plain or
+    precision form."""
+    import pfmds_gb300 as pf
+    from pfmds_gb300 import configs
+    d = tempfile.mkdtemp()
+    form = "plain" if name.endswith("plain") else "precision"
+    if name.startswith("slab"):
+        configs.cu_slab(d, nx=32, ny=32, nz=16, steps=10 ** 6, log_period=10)
+        pf.Simulation(d, form=form, out_period=10 ** 9).advance(23)
+    elif name.startswith("gas"):
+        configs.lj_gas(d, log_period=10)
+        pf.Simulation(d, form=form, out_period=10 ** 9).advance(33)
+    elif name.startswith("moire"):
+        configs.gr_on_cu(d, rotation=(49, 3, 2), layers=6, fixed_layers=1, temperature=500.0, integrator="nvt",
+                         dt=0.5, steps=10 ** 8, log_period=10, coupling="morsec")
+        pf.Simulation(d, form=form, out_period=10 ** 9).advance(13)
+    elif name == "batch":
+        ln, _ = configs.batch_systems(d, n_rep=64, n_min=500, n_max=20000, steps=1000, log_period=100, seed=5)
+        b = pf.Batch(d, ln)
+        b.run(10)
+        b.run(200)
+    elif name == "learned":
+        configs.gr_on_cu(d, n_gx=64, n_gy=64, n_cx=61, n_cy=61, layers=4, temperature=600.0, integrator="nve",
+                         dt=0.5, steps=10 ** 7, log_period=100, tb_list=(32, 4.5))
+        m = os.path.join(d, "m.bin")
+        s = pf.Simulation(d, form="plain", out_period=10 ** 9)
+        s.learned_train(m, frames=2, stride=0, iters=1, lr=1e-3)
+        s.close()
+        s = pf.Simulation(d, form="precision", out_period=10 ** 9)
+        s.learned_use(m, check_period=0, tensor_cores=True)
+        for _ in range(4):
+            s.compute()
+    else:
+        raise SystemExit(f"unknown case {name}")
+    print(json.dumps({"case": name, "done": True}), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -727,6 +767,9 @@ def main():
     ap.add_argument("--learned-only", action="store_true",
                     help="the learned form's leg alone (prints its JSON), for profiling its kernels")
     ap.add_argument("--learned-frames", type=int, default=200, help="training frames per temperature")
+    ap.add_argument("--case", default=None,
+                    help="run one small workload for a kernel family and exit (ncu captures): slab_plain, "
+                         "slab_prec, gas_plain, gas_prec, moire_plain, moire_prec, batch, learned")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -739,7 +782,9 @@ def main():
         return
     import __graft_entry__
     __graft_entry__.build()
-    if args.learned_only:
+    if args.case:
+        run_case(args.case)
+    elif args.learned_only:
         with tempfile.TemporaryDirectory() as d:
             print(json.dumps(learned_config(d, 0, frames=args.learned_frames, run_steps=args.learned_steps)),
                   flush=True)

@@ -274,8 +274,8 @@ int pfmd_learned_status(const pfmd_ctx* ctx, int* active, int* checks, double* l
  * format: a count, then settings-file / output-prefix pairs).  These entry points
  * load every entry of such a list into one device state and advance all replicas
  * together in one persistent cooperative kernel (precision form).  A replica is a
- * binary LJ gas (lj1g, lj1g, lj) or an rjl slab integrated with nve; all replicas
- * share one list period. */
+ * binary LJ gas (lj1g, lj1g, lj) or an rjl slab integrated with nve, or with nvt
+ * under one Nose-Hoover chain; all replicas share one list period. */
 typedef struct pfmd_batch pfmd_batch;
 
 /* Reads input_path+list_file and every settings file it names (as md() reads
@@ -283,6 +283,16 @@ typedef struct pfmd_batch pfmd_batch;
  * *batch is set even on failure, for pfmd_batch_errmsg; destroy it. */
 int pfmd_batch_create(const char* input_path, const char* list_file, const pfmd_options* opt,
                       pfmd_batch** batch);
+/* The same from the list's entries given directly: n settings files and their
+ * output prefixes (the pairs of an -ilist file, run_md_simulation.f90:56-70). */
+int pfmd_batch_create_entries(const char* input_path, int n, const char* const* settings,
+                              const char* const* prefixes, const pfmd_options* opt, pfmd_batch** batch);
+/* Whether the batched kernel takes the settings file (PFMD_OK) or not (the code
+ * and, in why, the reason).  On PFMD_OK: its step count, list update period and
+ * zero_momentum_period, which every replica of one batch must share.  Host only;
+ * run_md_simulation -ilist -batch runs the entries it refuses one by one. */
+int pfmd_batch_accepts(const char* input_path, const char* settings, long long* steps, int* list_period,
+                       long long* zero_momentum_period, char* why, int why_len);
 void pfmd_batch_destroy(pfmd_batch* batch);
 const char* pfmd_batch_errmsg(const pfmd_batch* batch);
 /* Number of replicas, total atoms, MD steps done. */
@@ -310,8 +320,8 @@ int pfmd_batch_get_state(pfmd_batch* batch, int r, double* pos, double* vel, dou
 /* Potential and kinetic energy of every replica at the last energy step. */
 int pfmd_batch_energies(pfmd_batch* batch, double* e_pot, double* e_kin);
 /* A settings-list run (run_md_simulation -ilist, run_md_simulation.f90:40-66) on
- * the batched kernel: every entry advanced from step 0 to the end of its nve
- * stage together, and for each entry the files its own run writes, with prefix =
+ * the batched kernel: every entry advanced from step 0 to the end of its nve or
+ * nvt stage together, and for each entry the files its own run writes, with prefix =
  * out_path + the entry's prefix -- the log (lines at the log period, then the
  * closing record), snapshot_<step>.xyz, traj_<group>.xyz and final_<xyz> -- plus
  * its closing record as one line to all_out_fd when that is >= 0 (list order).
@@ -319,10 +329,11 @@ int pfmd_batch_energies(pfmd_batch* batch, double* e_pot, double* e_kin);
  * batch must be at step 0 (PFMD_E_STATE).  No per-step output block is written. */
 int pfmd_batch_run_list(pfmd_batch* b, const char* out_path, int all_out_fd, double* device_ms);
 
-/* Energy history: rows x replicas x 4 (the potential energies of the replica's
- * interactions -- LJ gas: lj1g A-A, lj1g B-B, lj A-B; rjl slab: rjl, 0, 0 -- and
- * the kinetic energy), one row per energy step from step 0; *rows and *period
- * (steps between rows) are returned; hist may be NULL to query the size. */
+/* Energy history: rows x replicas x 5 (the potential energies of the replica's
+ * interactions -- LJ gas: lj1g A-A, lj1g B-B, lj A-B; rjl slab: rjl, 0, 0 --
+ * the kinetic energy and the Nose-Hoover chain's energy, 0 under nve), one row
+ * per energy step from step 0; *rows and *period (steps between rows) are
+ * returned; hist may be NULL to query the size. */
 int pfmd_batch_energy_history(pfmd_batch* batch, double* hist, long long* rows, int* period);
 
 /* ---- rjl forces without device allocation ----------------------------------

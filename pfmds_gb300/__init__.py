@@ -36,7 +36,8 @@ EXPORTS = ("pfmd_default_options", "pfmd_create_from_files", "pfmd_destroy", "pf
            "pfmd_batch_replica", "pfmd_batch_run", "pfmd_batch_run_list", "pfmd_batch_graphs", "pfmd_batch_tune", "pfmd_batch_set_tpa", "pfmd_batch_get_state",
            "pfmd_batch_energies", "pfmd_batch_energy_history", "pfmd_learned_train", "pfmd_learned_use",
            "pfmd_learned_check", "pfmd_learned_status", "pfmd_learned_gradient", "pfmd_nlist_builds", "pfmd_rjl_forces_noalloc",
-           "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting", "pfmd_debug_waits")
+           "pfmd_gr_on_cu_analysis", "pfmd_run_gr_analysis", "pfmd_run_gr_moire_fitting", "pfmd_debug_waits",
+           "pfmd_batch_create_entries", "pfmd_batch_accepts")
 
 _LIB = None
 
@@ -121,6 +122,9 @@ def load(path=LIB_PATH):
     L.pfmd_learned_status.argtypes = [vp, ip, ip, dp, ip]
     # device buffers are passed as integer addresses (c_void_p)
     L.pfmd_debug_waits.argtypes = [C.c_uint, C.c_int]
+    L.pfmd_batch_create_entries.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                            C.POINTER(Options), C.POINTER(vp)]
+    L.pfmd_batch_accepts.argtypes = [C.c_char_p, C.c_char_p, llp, ip, llp, C.c_char_p, C.c_int]
     L.pfmd_rjl_forces_noalloc.argtypes = [C.c_int, vp, dp, dp, vp, vp, C.c_int, vp, vp, vp, C.c_char_p, C.c_int]
     _LIB = L
     return L
@@ -130,6 +134,17 @@ def debug_waits(spin_limit=0, stall=False):
     """Test hook of the bounded device waits (pfmd_debug_waits): a poll limit
     (0: built-in) and whether the next waits are made impossible."""
     load().pfmd_debug_waits(int(spin_limit), 1 if stall else 0)
+
+
+def batch_accepts(input_path, settings):
+    """(accepted, reason, (steps, list period, zero_momentum_period)) of one
+    settings file for the batched kernel (host only)."""
+    ip = input_path if (not input_path or input_path.endswith("/")) else input_path + "/"
+    st, per, zmp = C.c_longlong(), C.c_int(), C.c_longlong()
+    why = C.create_string_buffer(512)
+    rc = load().pfmd_batch_accepts(ip.encode(), settings.encode(), C.byref(st), C.byref(per), C.byref(zmp), why,
+                                   len(why))
+    return rc == PFMD_OK, why.value.decode(), (st.value, per.value, zmp.value)
 
 
 def strerror(code):
@@ -466,9 +481,15 @@ class Batch:
 
     def history4(self):
         """(rows, replicas, 4): the three interaction energies and the kinetic energy."""
+        h5, per = self.history5()
+        return h5[..., :4], per
+
+    def history5(self):
+        """(rows, replicas, 5): the three interaction energies, the kinetic energy
+        and the Nose-Hoover chain's energy (0 for nve replicas)."""
         rows, per = C.c_longlong(), C.c_int()
         self._check(load().pfmd_batch_energy_history(self._h, None, C.byref(rows), C.byref(per)))
-        h = np.zeros((max(rows.value, 0), self.n_replicas, 4))
+        h = np.zeros((max(rows.value, 0), self.n_replicas, 5))
         if rows.value:
             self._check(load().pfmd_batch_energy_history(self._h, _dp(h), C.byref(rows), C.byref(per)))
         return h, per.value

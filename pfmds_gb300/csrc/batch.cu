@@ -17,7 +17,11 @@
 // pair terms with compensated sums, FP64 positions, velocities and energies.
 // Supported replicas (the systems of the batched configuration): a binary LJ gas
 // (lj1g A-A, lj1g B-B, lj A-B, as LennardJones_1g.f90 / LennardJones.f90) or an
-// rjl slab (RosatoGuillopeLegrand.f90), integrated with nve.  The merged LJ list
+// rjl slab (RosatoGuillopeLegrand.f90), integrated with nve or with nvt under one
+// Nose-Hoover chain per replica (md_integrators.f90:182-260): each half of the
+// chain is a per-replica reduction of its group's kinetic energy (one warp per
+// replica over its tiles' partials) and a chain update, and the scaling it
+// implies rides on the next phase that touches the velocities.  The merged LJ list
 // holds every partner within r_cut; same-species pairs take the lj1g terms
 // (quintic switch, energy once per pair) and cross pairs the lj terms (cosine
 // switch, energy on the A rows, the reference's nl(1)), so the sums equal the
@@ -49,9 +53,9 @@
 namespace pfmd {
 namespace batch {
 
-static constexpr double kMassCoef = 1.6605389217 / 1.6021765654 * 100.0;  // md_integrators.f90:62
 static constexpr int kThreads = 256;
 static constexpr int kBuckets = 6;
+static constexpr int kHistCols = 5;  // energy history: 3 interaction classes, kinetic, chain
 enum Kind : int { KIND_LJ = 0, KIND_RJL = 1 };
 
 struct Rep {
@@ -63,6 +67,8 @@ struct Rep {
   float qs[3];
   double L[3], Ltol[3], qinv[3];
   double ts1, ts2;  // dt, dt/2
+  double ts3, ts4;  // dt/4, dt/8 (the chain's substeps)
+  int nvt;          // 1: the replica integrates nvt with one Nose-Hoover chain
 };
 struct LJSet {
   LJc<float> aa, bb, ab;
@@ -90,6 +96,10 @@ struct Dev {
   const RJLc<float>* rjl;
   const Tile* tile;
   double *tile_e, *tile_k, *e_pot, *e_kin, *hist;  // tile_e, e_pot: 3 interaction classes each
+  double* tile_kc;  // per tile: kinetic energy of the chain group's atoms (nvt replicas)
+  NHCDev* nhc;      // per replica: its chain (nvt replicas)
+  double* e_nhc;    // per replica: the chain's energy at the last energy step
+  int any_nvt;      // some replica integrates nvt
   unsigned int *bar_count, *bar_gen, *bar_flag;  // bar_flag: status when the last block arrived
   unsigned int spin_limit;                        // polls before a barrier gives up
   unsigned int bar_extra;                         // arrivals expected beyond the grid (0; 1 stalls)
@@ -167,7 +177,16 @@ __device__ __forceinline__ double wrap(double x, double L) {
 // (md_integrators.f90:7-97), FMA form; the fixed-point position follows.
 __device__ void phase_kick_drift(const Dev& D) {
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < D.N; a += gridDim.x * blockDim.x) {
-    if (!(D.moving[a] & 1)) continue;
+    const unsigned char mv = D.moving[a];
+    if (mv & 4) {  // the chain's first-half scaling (scale_velocities, md_general.f90:97-112)
+      const double sc = D.nhc[D.rep_of[a]].s;
+      double4_32a u = D.vel[a];
+      u.x *= sc;
+      u.y *= sc;
+      u.z *= sc;
+      D.vel[a] = u;
+    }
+    if (!(mv & 1)) continue;
     const Rep& R = D.rep[D.rep_of[a]];
     const double kt = D.kc[a] * R.ts2;
     const double4_32a f = D.frc[a];
@@ -420,7 +439,7 @@ __device__ void tile_density(const Dev& D, const Tile& t, bool energy, float& er
 // Energy classes: LJ replicas 0 = lj1g A-A, 1 = lj1g B-B, 2 = lj A-B; rjl replicas 0.
 template <int TPA>
 __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, float (&es)[3], float (&ec)[3],
-                           double& ke) {
+                           double& ke, double& kc) {
   constexpr int RPW = 32 / TPA;
   const int lane = threadIdx.x & 31;
   const int row = lane % RPW, sub = lane / RPW;
@@ -495,6 +514,7 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
 #pragma unroll
   for (int k = 0; k < 3; ++k) es[k] = ec[k] = 0.f;
   ke = 0.0;
+  kc = 0.0;
   if (valid && sub == 0) {
     const double4_32a f = make_double4_32a(acc.get(0), acc.get(1), acc.get(2), 0.0);
     D.frc[a] = f;
@@ -508,7 +528,9 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
         v.z = fma(f.z, kt, v.z);
         D.vel[a] = v;
       }
-      if (energy && (mv & 2)) ke = D.mass[a] * (v.x * v.x + v.y * v.y + v.z * v.z) / 2 * kMassCoef;
+      const double k2 = D.mass[a] * (v.x * v.x + v.y * v.y + v.z * v.z) / 2 * kMassCoef;
+      if (energy && (mv & 2)) ke = k2;
+      if (kick && (mv & 4)) kc = k2;  // the chain's second half needs it (nvt replicas)
     }
     if (energy && R.kind == KIND_LJ)
 #pragma unroll
@@ -523,11 +545,16 @@ template <int TPA>
 __device__ void run_tile(const Dev& D, int ti, int phase, bool kick, bool energy) {
   const Tile& t = D.tile[ti];
   float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
-  double ke = 0.0;
+  double ke = 0.0, kc = 0.0;
   if (phase == 0) {
     tile_density<TPA>(D, t, energy, s[0], c[0]);
   } else {
-    tile_force<TPA>(D, t, kick, energy, s, c, ke);
+    tile_force<TPA>(D, t, kick, energy, s, c, ke, kc);
+    if (kick && D.rep[t.rep].nvt) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) kc += __shfl_xor_sync(0xffffffffu, kc, o);
+      if ((threadIdx.x & 31) == 0) D.tile_kc[ti] = kc;
+    }
   }
   if (!energy) return;
   // the tile's rows sit in one warp: compensated FP32 merges of the row energies,
@@ -602,6 +629,58 @@ __device__ bool phase_zero_momentum(const Dev& D) {
   return true;
 }
 
+// One warp per nvt replica: the chain's kinetic energy from its tiles' partials
+// (a fixed order) and integrate_nose_hoover_chain's chain update
+// (md_integrators.f90:200-245); the scaling it implies is applied by the next
+// phase that touches the velocities.
+__device__ void phase_chain(const Dev& D) {
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < D.R; r += nw) {
+    const Rep& R = D.rep[r];
+    if (!R.nvt) continue;
+    double k = 0.0;
+    for (int t = lane; t < R.ntile; t += 32) k += D.tile_kc[R.tile0 + t];
+    k = warp_sum(k);
+    if (lane == 0) nhc_chain_update(D.nhc[r], k, R.ts2, R.ts3, R.ts4);
+  }
+}
+
+// The chain's second-half scaling of the nvt replicas' chain-group atoms, then
+// per tile the kinetic energy of the chain group (for the next step's first
+// half) and, at energy steps, of the temperature group -- both of the scaled
+// velocities.  scale = false at step 0, which only forms the partials.
+__device__ void phase_scale(const Dev& D, bool scale, bool energy) {
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int lane = threadIdx.x & 31;
+  for (int ti = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ti < D.T; ti += nw) {
+    const Tile& t = D.tile[ti];
+    if (!D.rep[t.rep].nvt) continue;
+    const double sc = D.nhc[t.rep].s;
+    double kc = 0.0, ke = 0.0;
+    if (lane < t.nrows) {
+      const int a = t.row0 + lane;
+      const unsigned char mv = D.moving[a];
+      double4_32a v = D.vel[a];
+      if (scale && (mv & 4)) {
+        v.x *= sc;
+        v.y *= sc;
+        v.z *= sc;
+        D.vel[a] = v;
+      }
+      const double k2 = D.mass[a] * (v.x * v.x + v.y * v.y + v.z * v.z) / 2 * kMassCoef;
+      if (mv & 4) kc = k2;
+      if (mv & 2) ke = k2;
+    }
+    kc = warp_sum(kc);
+    ke = warp_sum(ke);
+    if (lane == 0) {
+      D.tile_kc[ti] = kc;
+      if (energy) D.tile_k[ti] = ke;
+    }
+  }
+}
+
 // Per-replica totals in a fixed order: one warp per replica, lane-strided over its
 // tiles, then the warp tree.
 __device__ void phase_energy(const Dev& D, long long s) {
@@ -619,13 +698,23 @@ __device__ void phase_energy(const Dev& D, long long s) {
     if (lane == 0) {
       for (int k = 0; k < 3; ++k) D.e_pot[3 * r + k] = ep[k];
       D.e_kin[r] = ek;
+      // calculate_nose_hoover_chain_energy (md_integrators.f90:247-260)
+      double en = 0.0;
+      if (R.nvt) {
+        const NHCDev& h = D.nhc[r];
+        const double kt = kKtPerKelvin * h.T;
+        en = h.q[0] / 2 * (h.v[0] * h.v[0]) + 3.0 * h.L * kt * h.x[0];
+        for (int i = 1; i < h.M; ++i) en = en + h.q[i] / 2 * (h.v[i] * h.v[i]) + kt * h.x[i];
+      }
+      D.e_nhc[r] = en;
       const long long h = s / D.energy_period;
       if (s % D.energy_period == 0 && h < D.hist_cap) {
-        double* o = D.hist + (h * D.R + r) * 4;
+        double* o = D.hist + (h * D.R + r) * kHistCols;
         o[0] = ep[0];
         o[1] = ep[1];
         o[2] = ep[2];
         o[3] = ek;
+        o[4] = en;
       }
     }
   }
@@ -640,6 +729,10 @@ __global__ void __launch_bounds__(kThreads) k_batch(Dev D, int nsteps) {
   for (int it = 0; it < nsteps; ++it) {
     const long long s = s0 + it;
     if (s > 0) {
+      if (D.any_nvt) {  // the chain's first half (its scaling rides on the kick-drift)
+        phase_chain(D);
+        if (!barrier(D)) return;
+      }
       phase_kick_drift(D);
       if (!barrier(D)) return;
     }
@@ -677,10 +770,25 @@ __global__ void __launch_bounds__(kThreads) k_batch(Dev D, int nsteps) {
     if (!barrier(D)) return;
     phase_tiles(D, 1, s > 0, energy);
     if (!barrier(D)) return;
+    if (D.any_nvt) {  // the chain's second half, then its scaling
+      if (s > 0) {
+        phase_chain(D);
+        if (!barrier(D)) return;
+      }
+      phase_scale(D, s > 0, energy);
+      if (!barrier(D)) return;
+    }
     if (energy) phase_energy(D, s);
   }
   if (!barrier(D)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) *D.step = s0 + nsteps;
+}
+
+// The chain group's kinetic energy per tile of the nvt replicas from the current
+// velocities (the partials the next step's first chain half reads), after the
+// tiles changed.
+__global__ void k_tile_kc(Dev D) {
+  phase_scale(D, false, false);
 }
 
 __global__ void k_pack(Dev D) {
@@ -734,6 +842,11 @@ struct HostRep {
   std::string integ_name, log_file, xyz_file;
   long long snap_period = 1, traj_period = 1;
   int traj_group = 0, n_ke = 0, n_nhc = 0;
+  // nvt: the one Nose-Hoover chain (md_integrators.f90:165-198): length, target
+  // temperature, q1 and the atoms of its group
+  bool nvt = false;
+  int nhc_M = 0, nhc_L = 0;
+  double nhc_T = 0.0, nhc_q1 = 0.0;
   std::vector<int> all_idx, traj_idx;  // group members in the reference's order (type, then atom)
   std::vector<int> inter_class;        // energy class of each interaction, settings order
   std::vector<std::string> types;
@@ -780,7 +893,9 @@ struct Batch {
   std::vector<int> rep_of_h;
   Buf<double4_32a> pos, vel, frc;
   Buf<int4> posq, cposq;
-  Buf<double> mass, kc, tile_e, tile_k, e_pot, e_kin, hist, vcm;
+  Buf<double> mass, kc, tile_e, tile_k, tile_kc, e_pot, e_kin, e_nhc, hist, vcm;
+  Buf<NHCDev> nhc;
+  bool any_nvt = false;
   Buf<unsigned char> species, moving;
   Buf<int> rep_of, nnum, nlist, ccount, cstart, ccursor, cell_of, catom, scan_part, status;
   Buf<float2> pair;
@@ -833,8 +948,20 @@ struct Batch {
     std::vector<const pfmd_io::IntegratorSpec*> runs;
     for (const auto& is : S.integrators)
       if (is.l > 0) runs.push_back(&is);
-    if (runs.size() != 1 || fortio::trim(runs[0]->name) != "nve")
-      throw Error(PFMD_E_PARAM, r.settings + ": the batched form integrates one nve stage only");
+    const std::string stage = runs.size() == 1 ? fortio::trim(runs[0]->name) : "";
+    if (stage != "nve" && stage != "nvt")
+      throw Error(PFMD_E_PARAM, r.settings + ": the batched form integrates one nve or nvt stage only");
+    r.nvt = stage == "nvt";
+    if (r.nvt) {
+      if (S.nhc.size() != 1)
+        throw Error(PFMD_E_PARAM, r.settings + ": an nvt replica of the batched form has one Nose-Hoover chain");
+      const auto& h = S.nhc[0];
+      r.nhc_M = h.M;
+      r.nhc_T = h.temperature;
+      r.nhc_q1 = h.q1;
+      if (h.M < 1 || h.M > PFMD_MAX_CHAIN)
+        throw Error(PFMD_E_PARAM, r.settings + ": chain length out of range");
+    }
     if (S.new_velocities) throw Error(PFMD_E_PARAM, r.settings + ": the batched form takes velocities from the .xyz");
     if (!S.changes.empty() || S.invert_z_vel)
       throw Error(PFMD_E_PARAM, r.settings + ": the batched form has no group changes or z-velocity inversion");
@@ -920,7 +1047,9 @@ struct Batch {
       if (in_group(S, S.z_moving, t))
         throw Error(PFMD_E_PARAM, r.settings + ": the batched form has no z-only moving group");
       const bool mv = in_group(S, S.xyz_moving, t), ke = in_group(S, S.all_moving, t);
-      mv_h.push_back(static_cast<unsigned char>((mv ? 1 : 0) | (ke ? 2 : 0)));
+      const bool ch = r.nvt && in_group(S, S.nhc[0].group, t);
+      mv_h.push_back(static_cast<unsigned char>((mv ? 1 : 0) | (ke ? 2 : 0) | (ch ? 4 : 0)));
+      r.nhc_L += ch ? 1 : 0;
       r.nmove += mv ? 1 : 0;
       r.n_ke += ke ? 1 : 0;
       sp_h.push_back(sp[static_cast<size_t>(i)]);
@@ -950,19 +1079,38 @@ struct Batch {
       tile_e.alloc(3 * t.size());
       tile_k = Buf<double>();
       tile_k.alloc(t.size());
+      tile_kc = Buf<double>();
+      tile_kc.alloc(t.size());
+      BCK(cudaMemsetAsync(tile_kc.p, 0, tile_kc.n * sizeof(double), st));
       BCK(cudaMemsetAsync(tile_e.p, 0, tile_e.n * sizeof(double), st));  // 3 classes per tile
       BCK(cudaMemsetAsync(tile_k.p, 0, tile_k.n * sizeof(double), st));
     }
     ntile_used = static_cast<int>(t.size());
     tile.up(t, st);
     rep.up(rep_h, st);
+    if (any_nvt && nhc.p) {  // new tiles: their chain partials from the current velocities
+      k_tile_kc<<<(ntile_used + 7) / 8, 256, 0, st>>>(dev_view());
+      BCK(cudaGetLastError());
+    }
   }
   int ntile_used = 0;
 
-  void create(const std::string& input_path, const std::string& list_file, const pfmd_options& o) {
+  // entries: the list's (settings file, prefix) pairs when not read from list_file
+  void create(const std::string& input_path, const std::string& list_file, const pfmd_options& o,
+              const std::vector<std::pair<std::string, std::string>>* entries = nullptr) {
     BCK(cudaSetDevice(o.device));
     BCK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    load(input_path, list_file);
+    if (entries) {
+      if (entries->empty()) throw Error(PFMD_E_PARAM, "batch: empty settings list");
+      for (const auto& e : *entries) {
+        HostRep r;
+        r.settings = fortio::trim(e.first);
+        r.prefix = fortio::trim(e.second);
+        reps.push_back(r);
+      }
+    } else {
+      load(input_path, list_file);
+    }
     std::vector<double> pos_h, vel_h;
     std::vector<unsigned char> sp_h, mv_h;
     for (auto& r : reps) {
@@ -1022,6 +1170,10 @@ struct Batch {
       ncell += nc;
       d.ts1 = r.dt;
       d.ts2 = r.dt / 2;
+      d.ts3 = r.dt / 4;
+      d.ts4 = r.dt / 8;
+      d.nvt = r.nvt ? 1 : 0;
+      if (r.nvt && r.nhc_L < 1) throw Error(PFMD_E_PARAM, r.settings + ": wrong nhc parameters");
       if (r.kind == KIND_LJ) {
         d.par = static_cast<int>(ljs.size());
         ljs.push_back(LJSet{r.aa.f, r.bb.f, r.ab.f});
@@ -1056,6 +1208,27 @@ struct Batch {
     rjl.alloc(rjls.size());
     e_pot.alloc(3 * reps.size());
     e_kin.alloc(reps.size());
+    e_nhc.alloc(reps.size());
+    BCK(cudaMemsetAsync(e_nhc.p, 0, reps.size() * sizeof(double), st));
+    // the chains (set_nose_hoover_chain, md_integrators.f90:182-198)
+    {
+      std::vector<NHCDev> ch(reps.size());
+      for (size_t k = 0; k < reps.size(); ++k) {
+        NHCDev& h = ch[k];
+        std::memset(&h, 0, sizeof(h));
+        h.s = 1.0;
+        const HostRep& r = reps[k];
+        if (!r.nvt) continue;
+        any_nvt = true;
+        h.M = r.nhc_M;
+        h.L = r.nhc_L;
+        h.T = r.nhc_T;
+        h.q[0] = r.nhc_q1;
+        for (int i = 1; i < h.M; ++i) h.q[i] = h.q[0] / (3.0 * h.L);
+      }
+      nhc.alloc(reps.size());
+      nhc.up(ch, st);
+    }
     vcm.alloc(3 * reps.size());
     status.alloc(4);
     bar.alloc(3);
@@ -1086,7 +1259,7 @@ struct Batch {
     long long max_steps = 0;
     for (const auto& r : reps) max_steps = std::max(max_steps, r.steps);
     hist_cap = max_steps / energy_period + 2;
-    hist.alloc(static_cast<size_t>(hist_cap) * reps.size() * 4);
+    hist.alloc(static_cast<size_t>(hist_cap) * reps.size() * kHistCols);
     BCK(cudaMemsetAsync(hist.p, 0, hist.n * sizeof(double), st));
     // threads per row: a heuristic start (the autotuner refines it)
     for (int b = 0; b < kBuckets; ++b) tpa[b] = (b / 3 == KIND_RJL) ? 2 : 2;
@@ -1097,7 +1270,10 @@ struct Batch {
     BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kThreads, 0));
     if (per_sm < 1) throw Error(PFMD_E_CUDA, "batch: the persistent kernel does not fit on an SM");
-    grid = sms * per_sm;
+    // every co-resident block; a small batch takes one block per SM (its grid
+    // barriers are shorter, and every SM still gets work)
+    const long long want = std::max<long long>((N + kThreads - 1) / kThreads, sms);
+    grid = static_cast<int>(std::min<long long>(static_cast<long long>(sms) * per_sm, want));
     scan_part.alloc(static_cast<size_t>(grid));
     k_pack<<<(N + 255) / 256, 256, 0, st>>>(dev_view());
     BCK(cudaGetLastError());
@@ -1142,6 +1318,10 @@ struct Batch {
     D.tile = tile.p;
     D.tile_e = tile_e.p;
     D.tile_k = tile_k.p;
+    D.tile_kc = tile_kc.p;
+    D.nhc = nhc.p;
+    D.e_nhc = e_nhc.p;
+    D.any_nvt = any_nvt ? 1 : 0;
     D.e_pot = e_pot.p;
     D.e_kin = e_kin.p;
     D.hist = hist.p;
@@ -1259,8 +1439,12 @@ struct Batch {
     BCK(cudaMemcpyAsync(sv.p, vel.p, n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, st));
     BCK(cudaMemcpyAsync(sf.p, frc.p, n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, st));
     BCK(cudaMemcpyAsync(sq.p, posq.p, n * sizeof(int4), cudaMemcpyDeviceToDevice, st));
+    Buf<NHCDev> sh;
+    sh.alloc(reps.size());
+    BCK(cudaMemcpyAsync(sh.p, nhc.p, reps.size() * sizeof(NHCDev), cudaMemcpyDeviceToDevice, st));
     BCK(cudaStreamSynchronize(st));
     auto restore = [&]() {
+      BCK(cudaMemcpyAsync(nhc.p, sh.p, reps.size() * sizeof(NHCDev), cudaMemcpyDeviceToDevice, st));
       BCK(cudaMemcpyAsync(pos.p, sp.p, n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, st));
       BCK(cudaMemcpyAsync(vel.p, sv.p, n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, st));
       BCK(cudaMemcpyAsync(frc.p, sf.p, n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, st));
@@ -1268,6 +1452,10 @@ struct Batch {
       // restart at the list period so the trial run rebuilds its lists
       const long long s0 = step_saved - step_saved % rebuild_period;
       BCK(cudaMemcpyAsync(step.p, &s0, sizeof(long long), cudaMemcpyHostToDevice, st));
+      if (any_nvt) {  // the chain partials of the restored velocities
+        k_tile_kc<<<(ntile_used + 7) / 8, 256, 0, st>>>(dev_view());
+        BCK(cudaGetLastError());
+      }
       BCK(cudaStreamSynchronize(st));
     };
     const long long md_saved = md_step;
@@ -1373,7 +1561,7 @@ static void run_list(Batch& B, const std::string& out_path, int all_out_fd, doub
   fetch();
   // energies: the history rows and the last step's totals
   const long long rows = std::min<long long>(B.hist_cap, L / B.energy_period + 1);
-  std::vector<double> hist(static_cast<size_t>(rows) * R * 4), ep(3 * R), ek(R);
+  std::vector<double> hist(static_cast<size_t>(rows) * R * kHistCols), ep(3 * R), ek(R);
   BCK(cudaMemcpyAsync(hist.data(), B.hist.p, hist.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
   BCK(cudaMemcpyAsync(ep.data(), B.e_pot.p, ep.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
   BCK(cudaMemcpyAsync(ek.data(), B.e_kin.p, ek.size() * sizeof(double), cudaMemcpyDeviceToHost, B.st));
@@ -1399,14 +1587,16 @@ static void run_list(Batch& B, const std::string& out_path, int all_out_fd, doub
     for (long long s = 0; s <= L; ++s) {
       if (s != 0) sim_time = sim_time + r.dt;
       if (s % r.log_period != 0) continue;
-      const double* h = hist.data() + (static_cast<size_t>(s / B.energy_period) * R + k) * 4;
+      const double* h = hist.data() + (static_cast<size_t>(s / B.energy_period) * R + k) * kHistCols;
       energies(h, h[3], inter, pe, temp);
+      // the chain's energy (0 under nve, where md() leaves it at its initial 0)
+      const double en = r.nvt ? h[4] : 0.0;
       fortio::Rec q;
       q.a(fortio::trim(r.integ_name), 6).i(s, 9);
-      q.f(sim_time, 24, 6).f(pe + h[3], 24, 6).f(0.0, 24, 6).f(pe + h[3], 24, 6).f(pe, 24, 6);
+      q.f(sim_time, 24, 6).f(pe + h[3] + en, 24, 6).f(en, 24, 6).f(pe + h[3], 24, 6).f(pe, 24, 6);
       q.f(h[3], 24, 6).f(temp, 24, 6);
       for (double v : inter) q.f(v, 20, 9);
-      for (int j = 0; j < r.n_nhc; ++j) q.f(0.0, 20, 9);  // chain energies stay 0 under nve
+      for (int j = 0; j < r.n_nhc; ++j) q.f(j == 0 ? en : 0.0, 20, 9);
       log += q.s + "\n";
     }
     // the closing record holds the energies of the last energy step (md_simulation.f90:188)
@@ -1422,7 +1612,7 @@ static void run_list(Batch& B, const std::string& out_path, int all_out_fd, doub
       cls = ep.data() + 3 * k;
       ke = ek[k];
     } else {
-      const double* h = hist.data() + (static_cast<size_t>(last / B.energy_period) * R + k) * 4;
+      const double* h = hist.data() + (static_cast<size_t>(last / B.energy_period) * R + k) * kHistCols;
       cls = h;
       ke = h[3];
     }
@@ -1490,6 +1680,55 @@ int pfmd_batch_create(const char* input_path, const char* list_file, const pfmd_
     return PFMD_E_CUDA;
   }
   return bguard(c, [&] { c->b->create(input_path ? input_path : "", list_file ? list_file : "", o); });
+}
+
+int pfmd_batch_create_entries(const char* input_path, int n, const char* const* settings,
+                              const char* const* prefixes, const pfmd_options* opt, pfmd_batch** out) {
+  if (!out) return PFMD_E_PARAM;
+  auto* c = new pfmd_batch();
+  *out = c;
+  c->b.reset(new Batch());
+  if (n < 1 || !settings || !prefixes) {
+    c->msg = "batch: no entries";
+    return PFMD_E_PARAM;
+  }
+  pfmd_options o;
+  pfmd_default_options(&o);
+  if (opt) o = *opt;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    c->msg = "no CUDA device";
+    return PFMD_E_CUDA;
+  }
+  std::vector<std::pair<std::string, std::string>> e;
+  for (int k = 0; k < n; ++k) e.emplace_back(settings[k] ? settings[k] : "", prefixes[k] ? prefixes[k] : "");
+  return bguard(c, [&] { c->b->create(input_path ? input_path : "", "", o, &e); });
+}
+
+int pfmd_batch_accepts(const char* input_path, const char* settings, long long* steps, int* list_period,
+                       long long* zero_momentum_period, char* why, int why_len) {
+  if (why && why_len > 0) why[0] = '\0';
+  try {
+    pfmd_io::Settings S;
+    pfmd_io::read_settings(input_path ? input_path : "", settings ? settings : "", S);
+    Batch B;
+    pfmd::batch::HostRep r;
+    r.settings = settings ? settings : "";
+    std::vector<double> p, v;
+    std::vector<unsigned char> sp, mv;
+    B.add(r, S, p, v, sp, mv);
+    if (steps) *steps = r.steps;
+    if (list_period) *list_period = static_cast<int>(r.period);
+    if (zero_momentum_period) *zero_momentum_period = r.zmp;
+    return PFMD_OK;
+  } catch (const pfmd::batch::Error& e) {
+    if (why && why_len > 0) std::snprintf(why, static_cast<size_t>(why_len), "%s", e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    if (why && why_len > 0) std::snprintf(why, static_cast<size_t>(why_len), "%s", e.what());
+    return PFMD_E_IO;
+  }
 }
 
 void pfmd_batch_destroy(pfmd_batch* c) { delete c; }
@@ -1601,7 +1840,7 @@ int pfmd_batch_energy_history(pfmd_batch* c, double* hist, long long* rows, int*
     if (rows) *rows = avail;
     if (period) *period = B.energy_period;
     if (hist && avail > 0)
-      BCK(cudaMemcpyAsync(hist, B.hist.p, static_cast<size_t>(avail) * B.reps.size() * 4 * sizeof(double),
+      BCK(cudaMemcpyAsync(hist, B.hist.p, static_cast<size_t>(avail) * B.reps.size() * pfmd::batch::kHistCols * sizeof(double),
                           cudaMemcpyDeviceToHost, B.st));
     BCK(cudaStreamSynchronize(B.st));
   });

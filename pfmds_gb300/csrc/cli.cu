@@ -2,13 +2,16 @@
 // same options (-i -p -op -omp_n -ipath -ilist -opath -ofile), the same banner
 // lines and the same single-file and list modes.  Extra options of this
 // implementation: -form plain|precision (arithmetic form), -graphs 0|1,
-// -device n, and -batch, which runs a whole list as one batch on the batched
-// kernel (pfmd_batch_run_list: the same files per entry; no per-step output
-// blocks).
+// -device n, and -batch, which runs the entries of a list that the batched
+// kernel takes as batches on it (pfmd_batch_run_list: the same files per entry;
+// no per-step output blocks) and the others one by one, as list mode does.
 #include <unistd.h>
 
 #include <cstdio>
+#include <map>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "../../include/pfmd.h"
 #include "settings.h"
@@ -81,23 +84,100 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
   std::fflush(stdout);
   int rc = PFMD_OK;
   if (batched && !settings_files_list.empty()) {
+    // the entries the batched kernel takes run together, one batch per shared
+    // (steps, list period, zero_momentum_period); the others run one by one as
+    // in list mode.  Closing records go to all_out in list order.
+    fortio::ListReader lst;
+    if (!lst.open(input_path + settings_files_list)) {
+      std::fprintf(stderr, "cannot open %s\n", (input_path + settings_files_list).c_str());
+      return PFMD_E_IO;
+    }
+    std::vector<std::pair<std::string, std::string>> entries;
+    try {
+      const long long set_num = fortio::to_int(lst.read_items(1)[0].s);
+      for (long long k = 0; k < set_num; ++k) {
+        auto it = lst.read_items(2);
+        entries.emplace_back(fortio::trim(fortio::to_char(it[0].s, 128)), fortio::trim(fortio::to_char(it[1].s, 128)));
+      }
+    } catch (const std::exception& e) {
+      return PFMD_E_IO;
+    }
+    const size_t n = entries.size();
+    std::vector<std::string> recs(n);
+    std::map<std::tuple<long long, int, long long>, std::vector<size_t>> groups;
+    std::vector<size_t> single;
+    for (size_t k = 0; k < n; ++k) {
+      long long steps = 0, zmp = 0;
+      int per = 0;
+      char why[256];
+      if (pfmd_batch_accepts(input_path.c_str(), entries[k].first.c_str(), &steps, &per, &zmp, why, sizeof why) ==
+          PFMD_OK)
+        groups[std::make_tuple(steps, per, zmp)].push_back(k);
+      else
+        single.push_back(k);
+    }
+    auto read_back = [](FILE* f) {
+      std::string t;
+      std::rewind(f);
+      char buf[4096];
+      size_t m;
+      while ((m = std::fread(buf, 1, sizeof buf, f)) > 0) t.append(buf, m);
+      return t;
+    };
+    for (auto& g : groups) {
+      std::vector<const char*> sf, pf;
+      for (size_t k : g.second) {
+        sf.push_back(entries[k].first.c_str());
+        pf.push_back(entries[k].second.c_str());
+      }
+      FILE* tmp = std::tmpfile();
+      if (!tmp) return PFMD_E_IO;
+      pfmd_batch* b = nullptr;
+      rc = pfmd_batch_create_entries(input_path.c_str(), static_cast<int>(sf.size()), sf.data(), pf.data(), &o, &b);
+      double ms = 0.0;
+      if (rc == PFMD_OK) rc = pfmd_batch_run_list(b, out_path.c_str(), fileno(tmp), &ms);
+      if (rc == PFMD_OK) {
+        int reps = 0;
+        long long atoms = 0, steps = 0;
+        pfmd_batch_info(b, &reps, &atoms, &steps);
+        say(line);
+        say(Rec().a("BATCH: ").i(reps, 6).a(" entries").i(atoms, 12).a(" atoms").i(steps, 12).a(" steps").s);
+        say(Rec().a("DEVICE TIME: ", 24).f(ms / 1000.0, 10, 2).a(" S ").s);
+        std::fflush(tmp);
+        const std::string t = read_back(tmp);
+        size_t pos = 0;
+        for (size_t k : g.second) {  // one line per entry, in the batch's order
+          const size_t e = t.find('\n', pos);
+          recs[k] = t.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+          pos = e == std::string::npos ? t.size() : e + 1;
+        }
+      } else {
+        std::fprintf(stderr, "%s\n", pfmd_batch_errmsg(b));
+      }
+      pfmd_batch_destroy(b);
+      std::fclose(tmp);
+      if (rc != PFMD_OK) return rc;
+    }
+    for (size_t k : single) {
+      const std::string prefix = fortio::trim(out_path) + entries[k].second;
+      say(line);
+      say(Rec().i(static_cast<long long>(k + 1), 6).a("\t").a(entries[k].first, 32, 128).a(prefix, 32, 128).s);
+      std::fflush(stdout);
+      FILE* tmp = std::tmpfile();
+      if (!tmp) return PFMD_E_IO;
+      o.output_prefix = prefix.c_str();
+      o.all_out_fd = fileno(tmp);
+      rc = pfmd_md(input_path.c_str(), entries[k].first.c_str(), &o);
+      std::fflush(tmp);
+      recs[k] = read_back(tmp);
+      while (!recs[k].empty() && recs[k].back() == '\n') recs[k].pop_back();
+      std::fclose(tmp);
+      say(line);
+      if (rc != PFMD_OK) return rc;
+    }
     FILE* all_out = std::fopen((out_path + all_out_file).c_str(), "w");
     if (!all_out) return PFMD_E_IO;
-    pfmd_batch* b = nullptr;
-    rc = pfmd_batch_create(input_path.c_str(), settings_files_list.c_str(), &o, &b);
-    double ms = 0.0;
-    if (rc == PFMD_OK) rc = pfmd_batch_run_list(b, out_path.c_str(), fileno(all_out), &ms);
-    if (rc == PFMD_OK) {
-      int reps = 0;
-      long long atoms = 0, steps = 0;
-      pfmd_batch_info(b, &reps, &atoms, &steps);
-      say(line);
-      say(Rec().a("BATCH: ").i(reps, 6).a(" entries").i(atoms, 12).a(" atoms").i(steps, 12).a(" steps").s);
-      say(Rec().a("DEVICE TIME: ", 24).f(ms / 1000.0, 10, 2).a(" S ").s);
-    } else {
-      std::fprintf(stderr, "%s\n", pfmd_batch_errmsg(b));
-    }
-    pfmd_batch_destroy(b);
+    for (const auto& r : recs) std::fputs((r + "\n").c_str(), all_out);
     std::fclose(all_out);
   } else if (!settings_files_list.empty()) {
     fortio::ListReader lst;

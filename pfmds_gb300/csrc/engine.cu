@@ -1395,7 +1395,7 @@ void Engine::plan_pair_fusion() {
   mflag.alloc(static_cast<size_t>(std::max(N, 1)));
   refresh_mflag();
   // until tune_tpa measures the rows: half of each headed row's capacity
-  pair_tpa = auto_tpa(N, cap / N, prec);
+  pair_tpa = opt.threads_per_row > 0 ? opt.threads_per_row : auto_tpa(N, cap / N, prec);
   CK(cudaStreamSynchronize(st));
 }
 

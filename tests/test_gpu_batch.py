@@ -112,10 +112,11 @@ def test_list_overflow_names_the_replica(tmp_path, built):
 def test_unsupported_replica_is_rejected(tmp_path, built):
     ln, reps = _batch(tmp_path, n_rep=2, seed=4)
     sf = tmp_path / reps[0]["settings"]
-    sf.write_text(sf.read_text().replace(" nve ", " nvt "))
+    sf.write_text(sf.read_text().replace(" nve ", " nvms "))
+    assert not pf.batch_accepts(str(tmp_path), reps[0]["settings"])[0]
     with pytest.raises(pf.PfmdError) as ei:
         pf.Batch(str(tmp_path), ln)
-    assert ei.value.code == pf.PFMD_E_PARAM and "nve" in str(ei.value)
+    assert ei.value.code == pf.PFMD_E_PARAM and "nve or nvt" in str(ei.value)
 
 
 def _fields(line):
