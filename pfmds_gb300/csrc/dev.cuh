@@ -384,6 +384,14 @@ __device__ __forceinline__ bool grid_finish(Ctl* ctl, int slot, double (&v)[K], 
   return threadIdx.x == 0;
 }
 
+// Ctl::stop as one verdict for the whole block (it is a block barrier): a kernel
+// with block barriers after its stop test uses it, so that no warp of a block
+// returns while another goes on to a barrier after a thread of this grid set
+// the flag in between their reads.  Every thread of the block calls it.
+__device__ __forceinline__ bool block_stop(const Ctl* ctl) {
+  return __syncthreads_or(*reinterpret_cast<const volatile int*>(&ctl->stop) != 0) != 0;
+}
+
 // Records the first error (later ones are dropped) at md_step `step` and stops
 // the device step loop.
 __device__ __forceinline__ void set_error_at(Ctl* ctl, int code, int kind, int a, int b, int c, long long step) {

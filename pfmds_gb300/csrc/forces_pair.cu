@@ -152,24 +152,29 @@ void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const L
   });
 }
 
-// All lj / lj1g lists in one launch, atom-major (see PairSet).  A warp holds
-// 32/TPA consecutive atoms and walks them in tiles over the grid; the atoms of a
-// warp may head different numbers of rows, so every thread loops to the warp's
-// largest task count and the shuffles of the reductions see the whole warp.
-// Energies (per interaction) and the chain's kinetic energy go through one
-// grid reduction; its last block stores the energies and updates the chain.
+// All lj / lj1g lists in one launch, atom-major (see PairSet).  A block takes
+// (256 / 32) * (32 / TPA) consecutive atoms per pass, TPA threads per atom; the
+// atoms of a warp may head different numbers of rows, so every thread loops to
+// the warp's largest task count and the shuffles of the reductions see the
+// whole warp.  The per-atom epilogue (FP64 force store, kick, kinetic energy) is
+// the FP64 pipe's work, which is scarce on this GPU: the reduced forces go
+// through shared memory and the epilogue runs with one atom per thread, so a
+// warp's FP64 instructions serve 32 atoms instead of 32 / TPA.  Energies (per
+// interaction) and the chain's kinetic energy go through one grid reduction;
+// its last block stores the energies and updates the chain.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
                                                     double ts2, double ts3, double ts4) {
   using T = RT<PREC>;
-  if (ctl->stop) return;
-  constexpr int RPW = 32 / TPA;
-  const int lane = threadIdx.x & 31, sub = lane / RPW;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarp = (gridDim.x * blockDim.x) >> 5;
+  if (block_stop(ctl)) return;
+  constexpr int RPW = 32 / TPA, APB = 8 * RPW;  // atoms per warp, per block pass (256 threads)
+  __shared__ double s_f[3][APB];
+  __shared__ double s_e[ENERGY ? kMaxPairKeys : 1][APB];
+  const int lane = threadIdx.x & 31, sub = lane / RPW, w = threadIdx.x >> 5;
   double red[kMaxPairKeys + 1] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int base = warp * RPW; base < S.natoms; base += nwarp * RPW) {
-    const int a = base + lane % RPW;
+  for (int bbase = blockIdx.x * APB; bbase < S.natoms; bbase += gridDim.x * APB) {  // uniform over the block
+    const int slot = w * RPW + lane % RPW;
+    const int a = bbase + slot;
     const bool valid = a < S.natoms;
     const int t0 = valid ? S.task_off[a] : 0, nt = valid ? S.task_off[a + 1] - t0 : 0;
     int ntw = nt;
@@ -205,14 +210,28 @@ __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, C
 #pragma unroll
       for (int k = 0; k < kMaxPairKeys; ++k) e[k].template reduce<TPA>();
     }
-    if (valid && sub == 0) {
-      finish_force(A, E, a, acc.get(0), acc.get(1), acc.get(2));
+    if (sub == 0) {
+      s_f[0][slot] = acc.get(0);
+      s_f[1][slot] = acc.get(1);
+      s_f[2][slot] = acc.get(2);
       if (ENERGY) {
 #pragma unroll
-        for (int k = 0; k < kMaxPairKeys; ++k) red[k] += e[k].get();
+        for (int k = 0; k < kMaxPairKeys; ++k) s_e[k][slot] = e[k].get();
       }
-      if (chain >= 0 && (E.mflag[a] & 4)) red[kMaxPairKeys] += ke_of(A, a);
     }
+    __syncthreads();
+    if (threadIdx.x < APB) {
+      const int ae = bbase + threadIdx.x;
+      if (ae < S.natoms) {
+        finish_force(A, E, ae, s_f[0][threadIdx.x], s_f[1][threadIdx.x], s_f[2][threadIdx.x]);
+        if (ENERGY) {
+#pragma unroll
+          for (int k = 0; k < kMaxPairKeys; ++k) red[k] += s_e[k][threadIdx.x];
+        }
+        if (chain >= 0 && (E.mflag[ae] & 4)) red[kMaxPairKeys] += ke_of(A, ae);
+      }
+    }
+    __syncthreads();  // s_f is rewritten by the next pass
   }
   if (!ENERGY && chain < 0) return;
   double out[kMaxPairKeys + 1];
@@ -229,7 +248,7 @@ void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A,
                        cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4) {
   if (S.natoms <= 0) return;
   // at most 4096 blocks: their partials of the grid reduction fit Ctl::partial
-  const long long blocks = nblk((long long)S.natoms * S.tpa, 256);
+  const long long blocks = nblk((long long)S.natoms * S.tpa, 256);  // 256 threads = 8 * 32 / TPA atoms
   const int grid = static_cast<int>(blocks < 4096 ? blocks : 4096);
   with_bool(prec, [&](auto pr) {
     with_bool(energy, [&](auto en) {

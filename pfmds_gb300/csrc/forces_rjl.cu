@@ -135,15 +135,22 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
   }
 }
 
+// Blocks of 32 rows (32 x TPA threads): the row sums go through shared memory to
+// one full warp, which runs the FP64 epilogue (force store, kick, the next
+// step's kick and drift) with all 32 lanes busy.  Finishing each row on its own
+// sub-0 lane instead keeps TPA - 1 of every TPA lanes idle on the FP64 pipe, which
+// is what held the kernel at 2 threads per row.
 template <bool PREC, int TPA>
-__global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A, Box B, const void* inv_eb,
-                                                   const double2* pair, Ctl* ctl, Epi E) {
+__global__ void __launch_bounds__(32 * TPA) k_rjl_force(ListDev L, RJLPar P, Atoms A, Box B, const void* inv_eb,
+                                                        const double2* pair, Ctl* ctl, Epi E) {
   asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
   using T = RT<PREC>;
   using R = typename T::R;
   using IE = typename std::conditional<PREC, float, double>::type;
+  constexpr int RPW = 32 / TPA;
+  __shared__ double s_f[3][32];
   const IE* ieb = static_cast<const IE*>(inv_eb);
-  if (ctl->stop) return;
+  if (block_stop(ctl)) return;
   const Grp<TPA> g;
   const bool valid = g.row < L.rows;
   const int n = valid ? L.nnum[g.row] : 0;
@@ -157,9 +164,7 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
       ieb_i = __int_as_float(pi.w);
     else
       ieb_i = ieb[ai];
-    // unroll 2: measured faster than 4 or 8 on the 65,536-atom slab (fewer live
-    // registers, more resident warps for the gather latency); the partner index is
-    // loaded one iteration ahead, as in the density pass
+    // the partner index is loaded one iteration ahead, as in the density pass
     int aj = g.sub < n ? ent(L, g.row, g.sub) : ai;
 #pragma unroll 2
     for (int p = g.sub; p < n; p += TPA) {
@@ -182,11 +187,24 @@ __global__ void __launch_bounds__(256) k_rjl_force(ListDev L, RJLPar P, Atoms A,
     }
   }
   acc.template reduce<TPA>();
-  if (valid && (n > 0 || E.store || E.kick) && g.sub == 0) {
-    if constexpr (PREC)
-      finish_force_drift(A, E, B, ctl, ai, acc.get(0), acc.get(1), acc.get(2));
-    else
-      finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
+  const int lane = threadIdx.x & 31, slot = (threadIdx.x >> 5) * RPW + lane % RPW;
+  if (g.sub == 0) {
+    s_f[0][slot] = acc.get(0);
+    s_f[1][slot] = acc.get(1);
+    s_f[2][slot] = acc.get(2);
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int r = blockIdx.x * 32 + threadIdx.x;
+    if (r < L.rows) {
+      const int ar = L.pidx[r];
+      if (L.nnum[r] > 0 || E.store || E.kick) {
+        if constexpr (PREC)
+          finish_force_drift(A, E, B, ctl, ar, s_f[0][threadIdx.x], s_f[1][threadIdx.x], s_f[2][threadIdx.x]);
+        else
+          finish_force(A, E, ar, s_f[0][threadIdx.x], s_f[1][threadIdx.x], s_f[2][threadIdx.x]);
+      }
+    }
   }
 }
 
@@ -214,12 +232,12 @@ void launch_rjl(bool prec, bool energy, const ListDev& L, const RJLPar& P, const
       });
     }
     if (parts & 2) {
-      // 128-thread blocks: 2x as many blocks spread more evenly over the SMs
-      const int grid = nblk((long long)L.rows * L.tpa, 128);
+      // 32 rows per block
+      const int grid = nblk(L.rows, 32);
       with_tpa(L.tpa, [&](auto t) {
         constexpr int TP = decltype(t)::value;
-        launch_dependent(k_rjl_force<PR, TP>, grid, 128, s, L, P, A, B, (const void*)Eb, (const double2*)pair, ctl,
-                         E);
+        launch_dependent(k_rjl_force<PR, TP>, grid, 32 * TP, s, L, P, A, B, (const void*)Eb, (const double2*)pair,
+                         ctl, E);
         ++g_kernel_launches;
       });
     }

@@ -179,7 +179,7 @@ __device__ int collect_ang(const ListDev& L, int row, int n, const int4& pi, con
 // reduced over the warp at the end (a fixed order).
 __global__ void __launch_bounds__(32 * kWarps) k_desc(ListDev L, const DescPar* __restrict__ Dp, Atoms A, Box B,
                                                       float* G, Ctl* ctl) {
-  if (ctl->stop) return;
+  if (block_stop(ctl)) return;
   __shared__ AngW s_ang[kWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int row = blockIdx.x * kWarps + w;

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(int rows, const float* __rest
   unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   TcSmem& S = *reinterpret_cast<TcSmem*>(base);
   const int t = threadIdx.x, w = t >> 5;
-  if (ctl->stop) return;
+  if (block_stop(ctl)) return;
   // weights into the core-matrix layout (BF16), padded K / N to 64
   for (int i = t; i < TC_N * TC_K; i += blockDim.x) {
     const int n = i / TC_K, k = i % TC_K;

@@ -614,7 +614,7 @@ __device__ __forceinline__ void skin_decide(Ctl* ctl, int id, float half_skin, f
 
 __global__ void k_skin_check(ListDev L, Atoms A, Box B, const int4* xref, int4* xprev, const int4* xout, int both,
                              float half_skin, float half_margin, Ctl* ctl) {
-  if (ctl->stop) return;
+  if (block_stop(ctl)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nr = ctl->group_n[L.row_group], nc = ctl->group_n[L.col_group];
   int a = -1;
@@ -665,7 +665,7 @@ __global__ void k_skin_decide(int id, float half_skin, float half_margin, int ou
 // (and a rebuilt outer list's, the outer reference); the last block to finish
 // clears the flags (every block has read them by then).
 __global__ void k_skin_commit(ListDev L, Atoms A, int4* xref, int4* xout, Ctl* ctl) {
-  if (ctl->stop) return;
+  if (block_stop(ctl)) return;
   __shared__ int need, oneed;
   if (threadIdx.x == 0) {
     need = ctl->list_need[L.skin];
