@@ -101,8 +101,49 @@ def atom_energies(G, model):
     return a2 @ w["w3"] + w["b3"]
 
 
+# the close-contact wall the library adds to each network's energy (learned.h:
+# kCoreK, core_radius): (k/2) (r_core - r)^2 per atom and partner below r_core
+CORE_K = 20.0
+CORE_R = {0: 1.15, 1: 2.2}
+
+
+def core_row_energies(pos, box, idx, kind):
+    """The wall's energy of each atom of idx (its own partners' share)."""
+    p = pos[idx]
+    box = np.asarray(box, float)
+    e = np.zeros(len(idx))
+    for a in range(len(idx)):
+        d = p - p[a]
+        d -= box * np.round(d / box)
+        r = np.sqrt((d * d).sum(1))
+        r[a] = np.inf
+        x = CORE_R[kind] - r[r < CORE_R[kind]]
+        e[a] = 0.5 * CORE_K * (x * x).sum()
+    return e
+
+
+def core_energy(pos, box, idx, kind):
+    return float(core_row_energies(pos, box, idx, kind).sum())
+
+
+def core_forces(pos, box, idx, kind, n_atoms):
+    """-d(wall energy)/dx (n_atoms x 3): 2 k (r_core - r) along the pair, apart."""
+    p = pos[idx]
+    box = np.asarray(box, float)
+    f = np.zeros((n_atoms, 3))
+    for a in range(len(idx)):
+        d = p - p[a]
+        d -= box * np.round(d / box)
+        r = np.sqrt((d * d).sum(1))
+        r[a] = np.inf
+        m = r < CORE_R[kind]
+        f[idx[a]] -= ((2.0 * CORE_K * (CORE_R[kind] - r[m]) / r[m])[:, None] * d[m]).sum(0)
+    return f
+
+
 def energy(pos, box, idx, model):
-    return float(atom_energies(descriptors(pos, box, idx, model["desc"]), model).sum())
+    return (float(atom_energies(descriptors(pos, box, idx, model["desc"]), model).sum())
+            + core_energy(pos, box, idx, model["kind"]))
 
 
 def forces_fd(pos, box, idx, model, atoms, h=1e-4):
@@ -236,13 +277,19 @@ def energies_and_dEdG(G, model):
     return E, (gz1 @ w["W1"]) * d["inv_std"]
 
 
-def training_loss(model, G, J, targets, f_ref, w_energy=1.0, w_force=1.0):
+def training_loss(model, G, J, targets, f_ref, w_energy=1.0, w_force=1.0, e_core=None, f_core=None):
     """L(W) at a configuration: G, J from descriptors_jacobian, per-row energy
-    targets and reference forces (N x 3)."""
+    targets and reference forces (N x 3).  The model's energies and forces are
+    the network's plus the close-contact wall's (e_core per row, f_core per atom;
+    constants of the weights)."""
     E, g = energies_and_dEdG(G, model)
+    if e_core is not None:
+        E = E + e_core
     loss = w_energy * np.mean((E - targets) ** 2)
     if w_force:
         F = -np.einsum("rf,rfac->ac", g, J)
+        if f_core is not None:
+            F = F + f_core
         loss += w_force * ((F - f_ref) ** 2).sum() / (3 * len(f_ref))
     return loss
 

@@ -82,6 +82,9 @@ struct Ctl {
   int group_n[PFMD_MAX_GROUPS];
   // Nose-Hoover chains
   NHCDev nhc[PFMD_MAX_NHC];
+  // chain 0's second-half scale when the pair kernel also ran the next step's
+  // first half: the next kick-drift applies it, then nhc[0].s
+  double nhc_sa;
   // small reduction results
   double red[PFMD_RED_SLOTS];
   int maxnnum[PFMD_MAX_LISTS];

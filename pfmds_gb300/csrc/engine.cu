@@ -256,6 +256,10 @@ struct StepPlan {
   // nvt with the pair kernel's fused chain: the chain's second-half scaling is
   // left to the next step's k_nhc (same segment, no energy or output step)
   bool nhc_defer = false;
+  // the same, with the pair kernel also running the next step's first
+  // half-update (nhc_ahead); the next step (nhc_done) launches no k_nhc for the
+  // chain, and its kick-drift opens the step and applies both scales
+  bool nhc_ahead = false, nhc_done = false;
 };
 
 // Snapshot and trajectory files (md_read_write.f90:65-107) are formatted and
@@ -413,6 +417,7 @@ class Engine {
   DBuf<PairSlot> pair_slots;
   bool nhc_fused = false;    // the pair kernel reduces chain 0's kinetic energy and updates it
   bool nhc_pending = false;  // chain 0's last scaling still to be applied (by the next k_nhc)
+  bool nhc_ahead = false;    // the pair launch being enqueued also runs the next first half-update
   void plan_pair_fusion();
   PairSet pair_set() const;
   bool need_check_all = true;
@@ -1422,7 +1427,8 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
     // and, under nvt, reduces and updates chain 0
     Epi e{1, kick ? 1 : 0, prec ? 0 : 1, ts[1], mflag.p, eatom_out};
     const int chain = (kick && nhc_fused && integ == I_NVT) ? 0 : -1;
-    launch_pair_atoms(prec, energy, pair_set(), A, box, ctl, st, e, chain, ts[1], ts[2], ts[3]);
+    launch_pair_atoms(prec, energy, pair_set(), A, box, ctl, st, e, chain, ts[1], ts[2], ts[3],
+                      chain == 0 && nhc_ahead);
     return;
   }
   // which launch is the first / last force writer
@@ -1453,7 +1459,7 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
       else
         learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
       learned::launch_force(L1, M.d.p, M.g.p, M.e.p, M.leg.p, M.cforce.p, energy, A, box, ctl, eslot, key, st,
-                            epi(first, last));
+                            epi(first, last), learned::core_radius(M.model.kind));
       continue;
     }
     switch (I.spec.kind) {
@@ -1489,7 +1495,10 @@ void Engine::enqueue_step(const StepPlan& p) {
   const bool nvms = integ == I_NVMS, nvt = integ == I_NVT;
   if (p.check_all) launch_check_all(A, box, ctl, st);
   // an nve step without group changes lets the kick-drift kernel open the step
-  const bool fused_begin = !p.first && integ == I_NVE && changes.empty() && !S.invert_z_vel && fuse_kick_drift &&
+  // (nvt too when the previous step ran this step's chain half-update: then the
+  // kick-drift is the step's first kernel)
+  const bool fused_begin = !p.first && (integ == I_NVE || (nvt && p.nhc_done)) && changes.empty() &&
+                           !S.invert_z_vel && fuse_kick_drift &&
                            groups[static_cast<size_t>(S.xyz_moving - 1)].idx.size() > 0;
   // a drifted step (its kick and drift ran in the previous step's force kernel)
   // that launches nothing before a single rjl interaction opens in that
@@ -1516,6 +1525,10 @@ void Engine::enqueue_step(const StepPlan& p) {
     if (nvt)
       for (size_t c = 0; c < S.nhc.size(); ++c) {
         const GroupRef gc = gref(S.nhc[c].group);
+        if (c == 0 && p.nhc_done) {  // updated by the previous step's pair kernel
+          scale_chain = 1;
+          continue;
+        }
         // a pending scaling of chain 0 (the previous step's second half) comes first
         launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st, (c == 0 && nhc_pending) ? 1 : 0);
         if (c == 0) nhc_pending = false;
@@ -1527,7 +1540,7 @@ void Engine::enqueue_step(const StepPlan& p) {
     if (p.drifted) {
       // (done)
     } else if (fuse_kick_drift) {
-      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st, fused_begin);
+      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st, fused_begin, p.nhc_done);
       if (gz.cap > 0) {
         launch_kick(gz, false, ts[1], !prec, A, ctl, st);
         launch_drift(gz, false, ts[0], true, A, box, ctl, st);
@@ -1543,7 +1556,9 @@ void Engine::enqueue_step(const StepPlan& p) {
   const GroupRef gall = gref(S.all_atoms);
   if (p.zero_mom) launch_zero_momentum(gall, A, ctl, st);
   if (!store_first) launch_zero_forces(gall, A, ctl, st);
+  nhc_ahead = p.nhc_ahead;
   enqueue_forces(p.energy, !p.first, p.drift_next, begin_in_forces);
+  nhc_ahead = false;
   if (p.drift_next) flip_posq();  // the next step reads the positions written by this one
   if (!p.first) {
     if (!kick_last) {
@@ -1555,7 +1570,9 @@ void Engine::enqueue_step(const StepPlan& p) {
         const GroupRef gc = gref(S.nhc[c].group);
         if (c == 0 && nhc_fused && pair_fused && !learned_active) {
           // the pair kernel reduced the kinetic energy and updated the chain
-          if (p.nhc_defer)
+          if (p.nhc_ahead)
+            ;  // and the next step's first half: the next kick-drift scales
+          else if (p.nhc_defer)
             nhc_pending = true;
           else
             launch_scale(0, gc, A, ctl, st);
@@ -1584,7 +1601,9 @@ static std::string plan_key(const StepPlan& p) {
   k.reserve(8 + p.rebuild.size());
   k.push_back(static_cast<char>('A' + (p.first ? 1 : 0) + 2 * (p.energy ? 1 : 0) + 4 * (p.out ? 1 : 0) +
                                 8 * (p.zero_mom ? 1 : 0) + 16 * (p.check_all ? 1 : 0)));
-  k.push_back(static_cast<char>('a' + (p.drift_next ? 1 : 0) + 2 * (p.drifted ? 1 : 0) + 4 * (p.nhc_defer ? 1 : 0)));
+  k.push_back(static_cast<char>('a' + (p.drift_next ? 1 : 0) + 2 * (p.drifted ? 1 : 0) + 4 * (p.nhc_defer ? 1 : 0) +
+                                8 * (p.nhc_ahead ? 1 : 0)));
+  k.push_back(p.nhc_done ? 'd' : '-');
   for (char r : p.rebuild) k.push_back(r ? '1' : '0');
   k.push_back('|');
   return k;
@@ -1846,6 +1865,12 @@ void Engine::advance(long long max_steps, int* fin) {
       for (size_t i = 0; i + 1 < plans.size(); ++i) {
         StepPlan& a = plans[i];
         if (!a.first && !a.energy && !a.out) a.nhc_defer = true;
+        // with chain 0's scaling in the kick-drift, the pair kernel runs the next
+        // step's first half-update as well
+        if (a.nhc_defer && fused_nhc_chain == 0) {
+          a.nhc_ahead = true;
+          plans[i + 1].nhc_done = true;
+        }
       }
     run_plans(plans);
     read_ctl();
@@ -2126,6 +2151,7 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
       const ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
       const int rows = L.d.rows;
       learned::launch_gather_rows(L.d, eatom.p, M.t.p, st);
+      learned::launch_core_sub(L.d, A, box, learned::core_radius(M.model.kind), M.t.p, st);
       if (fresh && f == 0) {
         // descriptor normalisation and the energy offset from the first frame
         for (int q = 0; q < learned::NG; ++q) {

@@ -385,6 +385,20 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
+// 1/sqrt(x) by the rsqrt.approx instruction, denormals flushed (list distances
+// are never denormal).
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// sin and cos of x by the sin.approx / cos.approx instructions (absolute error
+// about 2^-21 for |x| <= pi, the range the cosine switch uses).
+__device__ __forceinline__ void sincos_approx(float x, float& s, float& c) {
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(x));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(x));
+}
+
 // Calls F with an integral_constant for the list's threads-per-row.
 template <class F>
 static inline void with_tpa(int tpa, F f) {

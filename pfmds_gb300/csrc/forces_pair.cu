@@ -164,7 +164,7 @@ void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const L
 // its last block stores the energies and updates the chain.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
-                                                    double ts2, double ts3, double ts4) {
+                                                    double ts2, double ts3, double ts4, int ahead) {
   using T = RT<PREC>;
   if (block_stop(ctl)) return;
   constexpr int RPW = 32 / TPA, APB = 8 * RPW;  // atoms per warp, per block pass (256 threads)
@@ -241,11 +241,21 @@ __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, C
     for (int k = 0; k < kMaxPairKeys; ++k)
       if (k < S.nkey) ctl->e_inter[S.keys[k]] = out[k];
   }
-  if (chain >= 0) nhc_chain_update(ctl->nhc[chain], out[kMaxPairKeys], ts2, ts3, ts4);
+  if (chain >= 0) {
+    nhc_chain_update(ctl->nhc[chain], out[kMaxPairKeys], ts2, ts3, ts4);
+    if (ahead) {
+      // the next step's first half-update: its kinetic energy is this one's after
+      // the scaling, s^2 ke (the form the chain's own second part uses); the next
+      // kick-drift applies s_a, then the new s, to the velocities
+      const double sa = ctl->nhc[chain].s;
+      ctl->nhc_sa = sa;
+      nhc_chain_update(ctl->nhc[chain], out[kMaxPairKeys] * (sa * sa), ts2, ts3, ts4);
+    }
+  }
 }
 
 void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A, const Box& B, Ctl* ctl,
-                       cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4) {
+                       cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4, bool ahead) {
   if (S.natoms <= 0) return;
   // at most 4096 blocks: their partials of the grid reduction fit Ctl::partial
   const long long blocks = nblk((long long)S.natoms * S.tpa, 256);  // 256 threads = 8 * 32 / TPA atoms
@@ -254,7 +264,7 @@ void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A,
     with_bool(energy, [&](auto en) {
       with_tpa(S.tpa, [&](auto t) {
         k_pair_atoms<decltype(pr)::value, decltype(en)::value, decltype(t)::value>
-            <<<grid, 256, 0, s>>>(S, A, B, ctl, E, chain, ts2, ts3, ts4);
+            <<<grid, 256, 0, s>>>(S, A, B, ctl, E, chain, ts2, ts3, ts4, ahead ? 1 : 0);
         ++g_kernel_launches;
       });
     });

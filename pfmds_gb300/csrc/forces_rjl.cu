@@ -73,13 +73,13 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
       aj = aj_next;
       if constexpr (PREC) {
         // r and 1/r from one reciprocal square root
-        const float ir = rsqrtf(r2), r = r2 * ir;
+        const float ir = rsqrt_approx(r2), r = r2 * ir;
         // the cosine switch without branches: t is 0 below R1 and 1 from R2 on; entries
         // beyond R2 (about a fifth of the 5.5 A list) are masked, not skipped, so the
         // warp stays converged
         const float t = __saturatef(fmaf(r, c.inv_w, c.tb));
         float sn, cs;
-        __sincosf(3.14159265358979f * t, &sn, &cs);
+        sincos_approx(3.14159265358979f * t, sn, cs);  // argument in [0, pi]
         const float in = r <= c.R2 ? 1.f : 0.f;
         const float fc = (0.5f + 0.5f * cs) * in;
         const float rdfc = sn * c.dsw * in;

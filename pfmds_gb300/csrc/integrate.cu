@@ -148,8 +148,8 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
 // block is read (any index below the group's capacity names a valid atom), so
 // those loads overlap instead of forming a chain of dependent round trips.
 template <bool EXACT>
-__global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, int begin, Atoms A,
-                             Box B, Ctl* ctl) {
+__global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, int begin,
+                             int nhc_pre, Atoms A, Box B, Ctl* ctl) {
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   const bool have = ind < g.cap;
   const int i = have ? g.idx[ind] : 0;
@@ -175,6 +175,12 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   }
   if (ind >= ctl->group_n[g.g]) return;
   if (nhc_scale) {
+    if (nhc_pre) {  // the previous step's second-half scaling, in its own order
+      const double sa = ctl->nhc_sa;
+      v.x *= sa;
+      v.y *= sa;
+      v.z *= sa;
+    }
     const double s = ctl->nhc[nhc_scale - 1].s;
     v.x *= s;
     v.y *= s;
@@ -487,14 +493,14 @@ void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, cons
   if (g.cap > 0) { k_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts1, write_posq ? 1 : 0, A, B, ctl); ++g_kernel_launches; }
 }
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
-                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin) {
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin, bool nhc_pre) {
   if (g.cap <= 0) return;
   if (exact)
-    k_kick_drift<true><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0, A,
-                                                      B, ctl);
+    k_kick_drift<true><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0,
+                                                      nhc_pre ? 1 : 0, A, B, ctl);
   else
     k_kick_drift<false><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0,
-                                                       A, B, ctl);
+                                                       nhc_pre ? 1 : 0, A, B, ctl);
   ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,

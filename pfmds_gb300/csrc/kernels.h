@@ -240,8 +240,11 @@ struct PairSet {
   const int* task_off;     // natoms + 1
   const int2* task;        // (slot, row)
 };
+// chain >= 0: the chain's kinetic energy is reduced and its second half-update
+// run by the last block; with ahead, also the next step's first half-update
+// (Ctl::nhc_sa keeps the second half's scale for the next kick-drift).
 void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A, const Box& B, Ctl* ctl,
-                       cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4);
+                       cudaStream_t s, const Epi& E, int chain, double ts2, double ts3, double ts4, bool ahead = false);
 
 // Multi-kernel interactions take `parts`, a bit mask of their kernels (all by
 // default; single kernels are launched alone only for timing).
@@ -286,8 +289,11 @@ void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, cons
 // The step-begin bookkeeping of a step whose kick and drift ran in the previous
 // step's force kernel: the step counter and the previous potential energy.
 void launch_step_begin_fused(Ctl* ctl, cudaStream_t s);
+// nhc_scale = chain + 1 scales the velocities by that chain's s first (nhc_pre:
+// by Ctl::nhc_sa, then s); begin opens the step (counter, previous energy).
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
-                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false);
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false,
+                       bool nhc_pre = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s,
                 int prescale = 0);

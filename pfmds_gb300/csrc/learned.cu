@@ -410,17 +410,37 @@ __global__ void __launch_bounds__(32 * kWarps) k_lcenter(ListDev L, const DescPa
   if (lane == 0) cforce[row] = make_float4(fx, fy, fz, 0.f);
 }
 
+// Slots of atom ai in list rows ra (na entries) and rb (nb entries; 0: none), -1
+// where absent: both rows 64 entries a round, their four coalesced loads issued
+// together, then ballots (warp-uniform results).
+__device__ __forceinline__ void find_slot2(const ListDev& L, int ra, int na, int rb, int nb, int ai, int lane,
+                                           int& sa, int& sb) {
+  sa = -1;
+  sb = -1;
+  const int nm = max(na, nb);
+  for (int b = 0; b < nm && (sa < 0 || (nb > 0 && sb < 0)); b += 64) {
+    const int a0 = (sa < 0 && b + lane < na) ? ent(L, ra, b + lane) : -1;
+    const int a1 = (sa < 0 && b + 32 + lane < na) ? ent(L, ra, b + 32 + lane) : -1;
+    const int b0 = (sb < 0 && b + lane < nb) ? ent(L, rb, b + lane) : -1;
+    const int b1 = (sb < 0 && b + 32 + lane < nb) ? ent(L, rb, b + 32 + lane) : -1;
+    const unsigned ha0 = __ballot_sync(0xffffffffu, a0 == ai), ha1 = __ballot_sync(0xffffffffu, a1 == ai);
+    const unsigned hb0 = __ballot_sync(0xffffffffu, b0 == ai), hb1 = __ballot_sync(0xffffffffu, b1 == ai);
+    if (sa < 0) sa = ha0 ? b + __ffs(ha0) - 1 : (ha1 ? b + 32 + __ffs(ha1) - 1 : -1);
+    if (sb < 0) sb = hb0 ? b + __ffs(hb0) - 1 : (hb1 ? b + 32 + __ffs(hb1) - 1 : -1);
+  }
+}
+
 __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar* __restrict__ Dp,
                                                         const float* __restrict__ g, const float* __restrict__ erow,
                                                         const float4* __restrict__ leg,
                                                         const float4* __restrict__ cforce, int energy, Atoms A, Box B,
-                                                        Ctl* ctl, int eslot, int ekey, Epi E) {
+                                                        Ctl* ctl, int eslot, int ekey, Epi E, float rcore) {
   if (ctl->stop) return;
   const int lane = threadIdx.x & 31;
   const int r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
   const DescPar& d = *Dp;
   const float rs = d.rs[lane], er = d.eta_r[lane];
-  float mfx = 0.f, mfy = 0.f, mfz = 0.f;  // lane rr keeps row r0 + rr
+  float mfx = 0.f, mfy = 0.f, mfz = 0.f, mec = 0.f;  // lane rr keeps row r0 + rr
   for (int rr = 0; rr < 32; ++rr) {
     const int row = r0 + rr;
     if (row >= L.rows) break;  // uniform over the warp
@@ -428,45 +448,76 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
     const int4 pi = A.posq[ai];
     const int n = L.nnum[row];
     const float gi = g[(size_t)row * NG + lane];
-    float fx = 0.f, fy = 0.f, fz = 0.f;
+    float fx = 0.f, fy = 0.f, fz = 0.f, ec = 0.f;
     for (int base = 0; base < n; base += 32) {
       const int p = base + lane;
       float dr[3] = {0.f, 0.f, 0.f}, r = 3.4e38f, fc = 0.f, dfc = 0.f;
-      int rj = 0;
+      int rj = 0, nj = 0;
       if (p < n) {
         const int aj = ent(L, row, p);
         r = sqrtf(mi_q(pi, A.posq[aj], B, dr));
         rj = L.row_of[aj];
+        if (r < d.rc_ang) nj = L.nnum[rj];
       }
       if (r < d.rc_rad) fcut_d(r, d.rc_rad, fc, dfc);
       const int m = min(32, n - base);
-      for (int q = 0; q < m; ++q) {
-        const float rq = __shfl_sync(0xffffffffu, r, q);
-        const int rjq = __shfl_sync(0xffffffffu, rj, q);
-        const float dx = __shfl_sync(0xffffffffu, dr[0], q), dy = __shfl_sync(0xffffffffu, dr[1], q),
-                    dz = __shfl_sync(0xffffffffu, dr[2], q);
-        if (rq < d.rc_rad) {
+      // radial terms, four partners a round: their dE/dG rows are loaded together
+      // (lane = radial function); q0 <= 28, so q stays a lane index
+      for (int q0 = 0; q0 < m; q0 += 4) {
+        float gq[4], cq[4], dq[4][3];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int q = q0 + u;
+          const float rq = __shfl_sync(0xffffffffu, r, q);
+          const int rjq = __shfl_sync(0xffffffffu, rj, q);
           const float fq = __shfl_sync(0xffffffffu, fc, q), dfq = __shfl_sync(0xffffffffu, dfc, q);
+          dq[u][0] = __shfl_sync(0xffffffffu, dr[0], q);
+          dq[u][1] = __shfl_sync(0xffffffffu, dr[1], q);
+          dq[u][2] = __shfl_sync(0xffffffffu, dr[2], q);
+          const bool on = q < m && rq < d.rc_rad;
+          gq[u] = on ? g[(size_t)rjq * NG + lane] : 0.f;
           const float t = rq - rs;
-          const float c = (gi + g[(size_t)rjq * NG + lane]) * __expf(-er * t * t) * (-2.f * er * t * fq + dfq) / rq;
-          fx += c * dx;
-          fy += c * dy;
-          fz += c * dz;
-        }
-        if (rq < d.rc_ang) {  // i is an angular partner of j: j's centre pass holds i's leg term
-          const int nj = L.nnum[rjq];
-          int slot = -1;
-          for (int b2 = 0; b2 < nj && slot < 0; b2 += 32) {
-            const unsigned hit = __ballot_sync(0xffffffffu, b2 + lane < nj && ent(L, rjq, b2 + lane) == ai);
-            if (hit) slot = b2 + __ffs(hit) - 1;
-          }
-          if (slot >= 0 && lane == 0) {
-            const float4 lg = leg[(size_t)slot * L.stride + rjq];
-            fx -= lg.x;
-            fy -= lg.y;
-            fz -= lg.z;
+          cq[u] = on ? __expf(-er * t * t) * (-2.f * er * t * fq + dfq) / rq : 0.f;
+          if (q < m && rq < rcore && lane == 0) {  // the close-contact wall (learned.h)
+            const float x = rcore - rq;
+            const float c = -2.f * kCoreK * x / rq;  // both rows' (k/2) x^2 depend on this atom
+            fx += c * dq[u][0];
+            fy += c * dq[u][1];
+            fz += c * dq[u][2];
+            ec += 0.5f * kCoreK * x * x;
           }
         }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float c = (gi + gq[u]) * cq[u];
+          fx += c * dq[u][0];
+          fy += c * dq[u][1];
+          fz += c * dq[u][2];
+        }
+      }
+      // angular legs: the row's atom is an angular partner of each j within
+      // rc_ang, whose centre pass holds its leg term in the slot of this atom in
+      // j's row; two partners' rows are searched a round, and each lane then
+      // gathers the leg term of its own partner
+      int myslot = -1;
+      unsigned ang = __ballot_sync(0xffffffffu, r < d.rc_ang);
+      while (ang) {
+        const int qa = __ffs(ang) - 1;
+        ang &= ang - 1;
+        const int qb = ang ? __ffs(ang) - 1 : qa;
+        if (ang) ang &= ang - 1;
+        const int ra = __shfl_sync(0xffffffffu, rj, qa), na = __shfl_sync(0xffffffffu, nj, qa);
+        const int rb = __shfl_sync(0xffffffffu, rj, qb), nb = qb != qa ? __shfl_sync(0xffffffffu, nj, qb) : 0;
+        int sa, sb;
+        find_slot2(L, ra, na, rb, nb, ai, lane, sa, sb);
+        if (lane == qa) myslot = sa;
+        if (qb != qa && lane == qb) myslot = sb;
+      }
+      if (myslot >= 0) {
+        const float4 lg = leg[(size_t)myslot * L.stride + rj];
+        fx -= lg.x;
+        fy -= lg.y;
+        fz -= lg.z;
       }
     }
     if (lane == 0) {
@@ -478,31 +529,33 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
     fx = warp_sum_f(fx);
     fy = warp_sum_f(fy);
     fz = warp_sum_f(fz);
+    ec = __shfl_sync(0xffffffffu, ec, 0);
     if (lane == rr) {
       mfx = fx;
       mfy = fy;
       mfz = fz;
+      mec = ec;
     }
   }
   const int row = r0 + lane;
   float ei = 0.f;
   if (row < L.rows) {
     finish_force(A, E, L.pidx[row], mfx, mfy, mfz);
-    ei = erow[row];
+    ei = erow[row] + mec;
   }
   if (energy) energy_reduce_f(ctl, eslot, ekey, ei);
 }
 
 void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, float4* leg, float4* cforce,
                   bool energy, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s,
-                  const Epi& E) {
+                  const Epi& E, float rcore) {
   if (L.rows == 0) {
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
   }
   k_lcenter<<<nblk(L.rows, kWarps), 32 * kWarps, 0, s>>>(L, d, g, A, B, leg, cforce, ctl);
   k_lforce<<<nblk(nblk(L.rows, 32), kWarps), 32 * kWarps, 0, s>>>(L, d, g, e, leg, cforce, energy ? 1 : 0, A, B,
-                                                                  ctl, eslot, ekey, E);
+                                                                  ctl, eslot, ekey, E, rcore);
   g_kernel_launches += 2;
 }
 
@@ -829,6 +882,24 @@ void launch_adam(Net* net, TrainBuf& T, int step, float lr, cudaStream_t s) {
 __global__ void k_gather_rows(ListDev L, const double* eatom, double* t) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row < L.rows) t[row] = eatom[L.pidx[row]];
+}
+__global__ void k_core_sub(ListDev L, Atoms A, Box B, float rcore, double* t) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= L.rows) return;
+  const int n = L.nnum[row];
+  const int4 pi = A.posq[L.pidx[row]];
+  float e = 0.f;
+  for (int p = 0; p < n; ++p) {
+    float dr[3];
+    const float r = sqrtf(mi_q(pi, A.posq[ent(L, row, p)], B, dr));
+    if (r < rcore) e += 0.5f * kCoreK * (rcore - r) * (rcore - r);
+  }
+  t[row] -= (double)e;
+}
+void launch_core_sub(const ListDev& L, const Atoms& A, const Box& B, float rcore, double* t, cudaStream_t s) {
+  if (L.rows <= 0) return;
+  k_core_sub<<<nblk(L.rows, 128), 128, 0, s>>>(L, A, B, rcore, t);
+  ++g_kernel_launches;
 }
 void launch_gather_rows(const ListDev& L, const double* eatom, double* t, cudaStream_t s) {
   if (L.rows == 0) return;

@@ -22,6 +22,18 @@ namespace learned {
 constexpr int NR = 32, NA = 16, NG = NR + NA, NH = 64;
 constexpr int MAX_ANG = 32;  // angular partners per atom kept in registers
 
+// A close-contact wall added to each network's energy: (k/2) (r_core - r)^2 per
+// list entry below r_core (each pair sits in both atoms' rows, so a pair's wall
+// is k (r_core - r)^2).  r_core is 1.15 A for the tb (C) network and 2.2 A for
+// the rjl (Cu) one, in the lower tail of the nearest-neighbour distances that the
+// training runs visit; the networks are trained on the classical energies and
+// forces minus the wall's, so the wall is part of the model in training and in
+// use.  It keeps the dynamics out of the close-contact region that no training
+// frame covers, where a network extrapolates freely (without it, an rjl network
+// let Cu pairs close to 1.3 A within 900 steps of a 600 K run).
+constexpr float kCoreK = 20.f;  // eV/A^2
+inline float core_radius(int kind) { return kind == 0 ? 1.15f : 2.2f; }
+
 struct DescPar {
   float rc_rad, rc_ang;
   float rs[NR], eta_r[NR];
@@ -57,9 +69,10 @@ void launch_mlp_tc(int rows, const float* G, const DescPar* d, const Net* net, f
 // Forces of the learned energy (store/add and kick per Epi) and, at energy steps,
 // the interaction's energy into ctl->e_inter[ekey].  Needs L.row_of.
 // leg (nmax x stride, slot-major) and cforce (rows) are scratch of the two passes.
+// rcore: the wall's radius (core_radius of the model's kind).
 void launch_force(const ListDev& L, const DescPar* d, const float* g, const float* e, float4* leg, float4* cforce,
                   bool energy, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey, cudaStream_t s,
-                  const Epi& E);
+                  const Epi& E, float rcore);
 
 // Training on per-atom energy targets (mean squared error): gradients of one frame
 // into grad (sizeof(Net)/4 floats), reduced over rows in a fixed order; *loss_sum
@@ -94,6 +107,8 @@ int train_blocks(int rows);
 
 // Per-row gather of per-atom targets: t[row] = eatom[pidx[row]].
 void launch_gather_rows(const ListDev& L, const double* eatom, double* t, cudaStream_t s);
+// t[row] -= the row's close-contact wall energy (the network's share of the target).
+void launch_core_sub(const ListDev& L, const Atoms& A, const Box& B, float rcore, double* t, cudaStream_t s);
 // Sum over atoms of |f - f_ref|^2 and |f_ref|^2 (deterministic) into out[0..1].
 void launch_force_diff(int n, const double4_32a* f, const double4_32a* fref, double* part, double* out,
                        cudaStream_t s);

@@ -96,6 +96,41 @@ def test_learned_forces_match_cpu_reference_gradient(tmp_path, built):
     s.close()
 
 
+def test_close_contact_wall_matches_cpu_reference(tmp_path, built):
+    # two Cu atoms pushed to 1.8 A, inside the rjl network's 2.2 A wall: the
+    # library's energy and forces (network plus wall) against the FP64 CPU
+    # reference's energy and its central differences
+    configs.cu_slab(str(tmp_path), nx=3, ny=3, nz=3, steps=10 ** 6, log_period=10, temperature=300.0)
+    m = str(tmp_path / "m.bin")
+    s = pf.Simulation(str(tmp_path), form="plain", out_period=10 ** 9)
+    s.learned_train(m, frames=4, stride=2, iters=2, lr=2e-3)
+    s.close()
+    s = pf.Simulation(str(tmp_path), form="precision", out_period=10 ** 9)
+    s.learned_use(m, check_period=0)
+    s.compute()
+    p, _, _ = s.state()
+    box = configs.fcc_slab(3, 3, 3, 3.615, vacuum=25.0)[1]
+    d = p - p[40]
+    d -= box * np.round(d / box)
+    r = np.sqrt((d * d).sum(1))
+    r[40] = np.inf
+    j = int(np.argmin(r))
+    p[j] = p[40] + d[j] / r[j] * 1.8
+    s.set_state(p)
+    e = s.compute()
+    _, _, f = s.state()
+    model = learned_ref.load_models(m)[0]
+    idx = np.arange(len(p))
+    assert learned_ref.core_energy(p, box, idx, 1) >= 20.0 * 0.4 ** 2 * (1 - 1e-9)
+    fc = learned_ref.core_forces(p, box, idx, 1, len(p))
+    assert np.abs(fc[40]).max() > 10.0  # 2 k (r_core - r) = 16 eV/A
+    assert e[0] == pytest.approx(learned_ref.energy(p, box, idx, model), abs=2e-5 * len(p))
+    ref = learned_ref.forces_fd(p, box, idx, model, [40, j], h=1e-4)
+    scale = np.abs(ref).max()
+    assert np.abs(f[[40, j]] - ref).max() < 2e-3 * max(scale, 1.0), (f[[40, j]], ref)
+    s.close()
+
+
 def test_checked_run_stays_within_the_bound(tmp_path, built):
     # every 10 steps the classical kernels judge the network: the run either stays
     # learned with the force RMSE under the bound or falls back at the first check
@@ -223,11 +258,14 @@ def test_training_gradient_matches_fp64_loss(tmp_path, built):
     t = learned_ref.rjl_atom_energies(pos, box, idx, par)
     v0 = learned_ref.net_vector(model)
 
+    ec = learned_ref.core_row_energies(pos, box, idx, 1)
+    fc = learned_ref.core_forces(pos, box, idx, 1, len(pos))
+
     def loss(v):
-        return learned_ref.training_loss(learned_ref.with_net_vector(model, v), G, J, t, f_ref)
+        return learned_ref.training_loss(learned_ref.with_net_vector(model, v), G, J, t, f_ref, e_core=ec, f_core=fc)
 
     E, _ = learned_ref.energies_and_dEdG(G, model)
-    assert loss32[0] == pytest.approx(((E - t) ** 2).sum(), rel=2e-3)
+    assert loss32[0] == pytest.approx(((E + ec - t) ** 2).sum(), rel=2e-3)
     blocks = {"W1": (0, 3072), "b1": (3072, 3136), "W2": (3136, 7232), "b2": (7232, 7296), "w3": (7296, 7360),
               "b3": (7360, 7361), "all": (0, learned_ref.NET_FLOATS)}
     rng = np.random.default_rng(7)

@@ -85,3 +85,25 @@ def test_rjl_atom_energies_sum_to_the_oracle(tmp_path):
     par = [float(x) for x in open(tmp_path / "parameters_RJL_Cu.txt").read().split()]
     e = lr.rjl_atom_energies(pos, box, np.arange(len(pos)), par)
     assert e.sum() == pytest.approx(o.energies()["inter"][0], rel=1e-12)
+
+
+def test_core_wall_forces_are_its_gradient():
+    # a cluster with pairs inside both walls: the wall forces against central
+    # differences of the wall energy, and the pair energy k (r_core - r)^2
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0.0, 4.0, size=(12, 3))
+    box = np.array([30.0, 30.0, 30.0])
+    idx = np.arange(12)
+    for kind in (0, 1):
+        f = lr.core_forces(pos, box, idx, kind, 12)
+        assert np.abs(f).max() > 0.0
+        h = 1e-6
+        for a in (0, 5, 11):
+            for c in range(3):
+                pp, pm = pos.copy(), pos.copy()
+                pp[a, c] += h
+                pm[a, c] -= h
+                fd = -(lr.core_energy(pp, box, idx, kind) - lr.core_energy(pm, box, idx, kind)) / (2 * h)
+                assert f[a, c] == pytest.approx(fd, rel=1e-6, abs=1e-6)
+    two = np.array([[1.0, 1.0, 1.0], [2.8, 1.0, 1.0]])
+    assert lr.core_energy(two, box, np.arange(2), 1) == pytest.approx(lr.CORE_K * (lr.CORE_R[1] - 1.8) ** 2)
