@@ -336,7 +336,9 @@ def learned_config(root, device, frames=500, run_steps=20000):
     t0 = time.perf_counter()
     for T, lr in ((300.0, 2e-3), (700.0, 1e-3), (1200.0, 5e-4)):
         dT = os.path.join(root, f"learn_T{int(T)}")
-        configs.gr_on_cu(dT, n_gx=16, n_gy=10, n_cx=15, n_cy=8, layers=4, temperature=T, integrator="nve", dt=0.5,
+        # 6,400 atoms: a cell of the large system's proportions (the same lattice
+        # stretch), 5.5x smaller in x and y
+        configs.gr_on_cu(dT, n_gx=32, n_gy=20, n_cx=30, n_cy=16, layers=4, temperature=T, integrator="nve", dt=0.5,
                          steps=10 ** 7, log_period=10, tb_list=(32, 4.5))
         s = pf.Simulation(dT, form="plain", out_period=10 ** 9, device=device)
         out = os.path.join(root, f"learned_{int(T)}.bin")
@@ -347,7 +349,7 @@ def learned_config(root, device, frames=500, run_steps=20000):
         model = out
         s.close()
     t_train = time.perf_counter() - t0
-    # 11 x the training cell in x and y, 6 Cu layers: 77,440 C + 174,240 Cu = 251,680 atoms
+    # 5.5 x the training cell in x and y, 6 Cu layers: 77,440 C + 174,240 Cu = 251,680 atoms
     dbig = os.path.join(root, "learn_big")
     configs.gr_on_cu(dbig, n_gx=176, n_gy=110, n_cx=165, n_cy=88, layers=6, temperature=600.0, integrator="nvt",
                      dt=0.5, steps=10 ** 7, log_period=100, tb_list=(32, 4.5))

@@ -435,14 +435,19 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
                                                         const float4* __restrict__ leg,
                                                         const float4* __restrict__ cforce, int energy, Atoms A, Box B,
                                                         Ctl* ctl, int eslot, int ekey, Epi E, float rcore) {
-  if (ctl->stop) return;
-  const int lane = threadIdx.x & 31;
-  const int r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  if (block_stop(ctl)) return;
+  // a block takes 32 rows, each warp 4 of them; the row sums meet in shared
+  // memory and warp 0 finishes the 32 rows, one per lane (FP64 epilogue on full
+  // warps, as in the pair kernels)
+  constexpr int kRowsPerWarp = 32 / kWarps;
+  __shared__ float s_f[4][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int b0 = blockIdx.x * 32;
   const DescPar& d = *Dp;
   const float rs = d.rs[lane], er = d.eta_r[lane];
-  float mfx = 0.f, mfy = 0.f, mfz = 0.f, mec = 0.f;  // lane rr keeps row r0 + rr
-  for (int rr = 0; rr < 32; ++rr) {
-    const int row = r0 + rr;
+  for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+    const int slot = w * kRowsPerWarp + rr;
+    const int row = b0 + slot;
     if (row >= L.rows) break;  // uniform over the warp
     const int ai = L.pidx[row];
     const int4 pi = A.posq[ai];
@@ -530,18 +535,19 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
     fy = warp_sum_f(fy);
     fz = warp_sum_f(fz);
     ec = __shfl_sync(0xffffffffu, ec, 0);
-    if (lane == rr) {
-      mfx = fx;
-      mfy = fy;
-      mfz = fz;
-      mec = ec;
+    if (lane == 0) {
+      s_f[0][slot] = fx;
+      s_f[1][slot] = fy;
+      s_f[2][slot] = fz;
+      s_f[3][slot] = ec;
     }
   }
-  const int row = r0 + lane;
+  __syncthreads();
+  const int row = b0 + lane;
   float ei = 0.f;
-  if (row < L.rows) {
-    finish_force(A, E, L.pidx[row], mfx, mfy, mfz);
-    ei = erow[row] + mec;
+  if (w == 0 && row < L.rows) {
+    finish_force(A, E, L.pidx[row], s_f[0][lane], s_f[1][lane], s_f[2][lane]);
+    ei = erow[row] + s_f[3][lane];
   }
   if (energy) energy_reduce_f(ctl, eslot, ekey, ei);
 }
@@ -554,8 +560,8 @@ void launch_force(const ListDev& L, const DescPar* d, const float* g, const floa
     return;
   }
   k_lcenter<<<nblk(L.rows, kWarps), 32 * kWarps, 0, s>>>(L, d, g, A, B, leg, cforce, ctl);
-  k_lforce<<<nblk(nblk(L.rows, 32), kWarps), 32 * kWarps, 0, s>>>(L, d, g, e, leg, cforce, energy ? 1 : 0, A, B,
-                                                                  ctl, eslot, ekey, E, rcore);
+  k_lforce<<<nblk(L.rows, 32), 32 * kWarps, 0, s>>>(L, d, g, e, leg, cforce, energy ? 1 : 0, A, B, ctl, eslot, ekey, E,
+                                                   rcore);
   g_kernel_launches += 2;
 }
 
