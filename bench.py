@@ -351,8 +351,11 @@ def learned_config(root, device, frames=500, run_steps=20000):
     t_train = time.perf_counter() - t0
     # 5.5 x the training cell in x and y, 6 Cu layers: 77,440 C + 174,240 Cu = 251,680 atoms
     dbig = os.path.join(root, "learn_big")
+    # Cu rows hold up to 96 entries: the check every 100 steps, not the list
+    # capacity, judges the networks (a denser Cu shell than the 64 of the
+    # classical runs is what a drifting network produces first)
     configs.gr_on_cu(dbig, n_gx=176, n_gy=110, n_cx=165, n_cy=88, layers=6, temperature=600.0, integrator="nvt",
-                     dt=0.5, steps=10 ** 7, log_period=100, tb_list=(32, 4.5))
+                     dt=0.5, steps=10 ** 7, log_period=100, tb_list=(32, 4.5), cu_nmax=96)
     # force evaluations (all interactions, the step's dominant cost) on the large
     # system: classical precision, learned FP32, learned BF16 tensor cores, plain
     res = {}

@@ -15,13 +15,13 @@ its own energy.
 import numpy as np
 
 NR, NA, NG, NH = 32, 16, 48, 64
-DESC_FLOATS = 2 + NR + NR + 2 + 4 + 2 + NG + NG
+DESC_FLOATS = 2 + NR + NR + 2 + 4 + 2 + NG + NG + 5
 NET_FLOATS = NH * NG + NH + NH * NH + NH + NH + 1
 
 
 def load_models(path):
     raw = open(path, "rb").read()
-    assert raw[:8] == b"PFMDMLP1", "not a learned-potential file"
+    assert raw[:8] == b"PFMDMLP2", "not a learned-potential file"
     n = int(np.frombuffer(raw, np.int32, 1, 8)[0])
     off, out = 12, []
     for _ in range(n):
@@ -39,7 +39,8 @@ def load_models(path):
             k += m
             return v
         desc = dict(rc_rad=take(1)[0], rc_ang=take(1)[0], rs=take(NR), eta_r=take(NR), eta_a=take(2),
-                    zeta=take(4), lam=take(2), mean=take(NG), inv_std=take(NG))
+                    zeta=take(4), lam=take(2), mean=take(NG), inv_std=take(NG), bA=take(1)[0], bp=take(1)[0],
+                    br0=take(1)[0], bR1=take(1)[0], bR2=take(1)[0])
         k = 0
 
         def tw(m):
@@ -101,49 +102,75 @@ def atom_energies(G, model):
     return a2 @ w["w3"] + w["b3"]
 
 
-# the close-contact wall the library adds to each network's energy (learned.h:
-# kCoreK, core_radius): (k/2) (r_core - r)^2 per atom and partner below r_core
+# the model's pair terms besides the network (learned.h): the close-contact wall
+# (k/2) (r_core - r)^2 per atom and partner below r_core (kCoreK, core_radius)
+# and, for rjl networks, the baseline bA sum_j exp(-bp (r/br0 - 1)) fc(r) of each
+# atom (the rjl repulsion, RosatoGuillopeLegrand.f90:23-49, with the cosine
+# switch of cut_off_function.f90:6-28)
 CORE_K = 20.0
 CORE_R = {0: 1.15, 1: 2.2}
 
 
-def core_row_energies(pos, box, idx, kind):
-    """The wall's energy of each atom of idx (its own partners' share)."""
+def _pairs_of(p, box, a):
+    d = p - p[a]
+    d -= box * np.round(d / box)
+    r = np.sqrt((d * d).sum(1))
+    r[a] = np.inf
+    return d, r
+
+
+def _base_phi(desc, r):
+    """phi(r) and dphi/dr of the baseline (zero when bA = 0)."""
+    if desc["bA"] <= 0.0:
+        return np.zeros_like(r), np.zeros_like(r)
+    R1, R2 = desc["bR1"], desc["bR2"]
+    k = 3.14159265358979 / (R2 - R1)
+    x = np.clip(r - R1, 0.0, None)
+    fc = np.where(r <= R1, 1.0, np.where(r < R2, 0.5 * (1.0 + np.cos(k * x)), 0.0))
+    dfc = np.where((r > R1) & (r < R2), -0.5 * k * np.sin(k * x), 0.0)
+    e = np.exp(-desc["bp"] * (r / desc["br0"] - 1.0))
+    return e * fc, e * (dfc - desc["bp"] / desc["br0"] * fc)
+
+
+def pair_row_energies(pos, box, idx, model):
+    """Wall and baseline energy of each atom of idx (its own partners' share)."""
     p = pos[idx]
     box = np.asarray(box, float)
+    rc, d = CORE_R[model["kind"]], model["desc"]
     e = np.zeros(len(idx))
     for a in range(len(idx)):
-        d = p - p[a]
-        d -= box * np.round(d / box)
-        r = np.sqrt((d * d).sum(1))
-        r[a] = np.inf
-        x = CORE_R[kind] - r[r < CORE_R[kind]]
+        _, r = _pairs_of(p, box, a)
+        x = rc - r[r < rc]
         e[a] = 0.5 * CORE_K * (x * x).sum()
+        m = r < max(d["bR2"], 0.0)
+        e[a] += d["bA"] * _base_phi(d, r[m])[0].sum()
     return e
 
 
-def core_energy(pos, box, idx, kind):
-    return float(core_row_energies(pos, box, idx, kind).sum())
+def core_energy(pos, box, idx, model):
+    return float(pair_row_energies(pos, box, idx, model).sum())
 
 
-def core_forces(pos, box, idx, kind, n_atoms):
-    """-d(wall energy)/dx (n_atoms x 3): 2 k (r_core - r) along the pair, apart."""
+def pair_forces(pos, box, idx, model, n_atoms):
+    """-d(wall + baseline energy)/dx (n_atoms x 3)."""
     p = pos[idx]
     box = np.asarray(box, float)
+    rc, d = CORE_R[model["kind"]], model["desc"]
     f = np.zeros((n_atoms, 3))
     for a in range(len(idx)):
-        d = p - p[a]
-        d -= box * np.round(d / box)
-        r = np.sqrt((d * d).sum(1))
-        r[a] = np.inf
-        m = r < CORE_R[kind]
-        f[idx[a]] -= ((2.0 * CORE_K * (CORE_R[kind] - r[m]) / r[m])[:, None] * d[m]).sum(0)
+        dv, r = _pairs_of(p, box, a)
+        m = r < rc
+        f[idx[a]] -= ((2.0 * CORE_K * (rc - r[m]) / r[m])[:, None] * dv[m]).sum(0)
+        m = r < max(d["bR2"], 0.0)
+        if d["bA"] > 0.0 and m.any():
+            _, dph = _base_phi(d, r[m])
+            f[idx[a]] += ((2.0 * d["bA"] * dph / r[m])[:, None] * dv[m]).sum(0)
     return f
 
 
 def energy(pos, box, idx, model):
     return (float(atom_energies(descriptors(pos, box, idx, model["desc"]), model).sum())
-            + core_energy(pos, box, idx, model["kind"]))
+            + core_energy(pos, box, idx, model))
 
 
 def forces_fd(pos, box, idx, model, atoms, h=1e-4):

@@ -462,7 +462,7 @@ def gr_on_cu(d, n_gx=10, n_gy=6, n_cx=9, n_cy=5, layers=4, fixed_layers=1, a_cu=
              seed=7, temperature=300.0, disp=0.02, coupling="morsec", simplified=False, dt=0.5, steps=100,
              log_period=10, integrator="nvt", period=10, rotation=None, nhc_tau=100.0, xyz_name="gr_cu.xyz",
              morse=(0.1, 2.2, 1.7, 2.0), morse_r12=(7.0, 8.0), ljc=(0.0168, 2.2, 2.0), ljc_r12=(7.0, 8.0),
-             list_skin=0.5, tb_list=(4, 2.0), settings_name="md_run_settings.txt", carbon="tb"):
+             list_skin=0.5, tb_list=(4, 2.0), settings_name="md_run_settings.txt", carbon="tb", cu_nmax=64):
     """Graphene sheet (tb) on a Cu(111) slab (rjl), coupled by morsec or ljc.
 
     Without `rotation` the sheet has n_gx x n_gy rectangular cells and the Cu
@@ -518,7 +518,7 @@ def gr_on_cu(d, n_gx=10, n_gy=6, n_cx=9, n_cy=5, layers=4, fixed_layers=1, a_cu=
         nhc=[(4, temperature, 3, q1)], t0=temperature,
         interactions=[(carbon, "parameters_TB_C.txt" if carbon == "tb" else "parameters_REBO_C.txt",
                        [(1, 1, tb_list[0], tb_list[1], period)]),
-                      ("rjl", "parameters_RJL_Cu.txt", [(2, 2, 64, 5.5, period)]),
+                      ("rjl", "parameters_RJL_Cu.txt", [(2, 2, cu_nmax, 5.5, period)]),
                       (coupling, "parameters_coupling.txt", [(1, 2, 160, rc_c, period), (2, 1, 160, rc_c, period),
                                                              (1, 1, 3, 1.8, period)])])
     _write(d, settings_name, text)

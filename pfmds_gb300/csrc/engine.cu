@@ -2086,7 +2086,16 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
   if (fresh) {
     for (const auto& I : inters) {
       if (I.spec.kind == pfmd_io::K_TB) ms.push_back(learned::default_model(0, static_cast<unsigned>(opt.rand_seed)));
-      if (I.spec.kind == pfmd_io::K_RJL) ms.push_back(learned::default_model(1, static_cast<unsigned>(opt.rand_seed)));
+      if (I.spec.kind == pfmd_io::K_RJL) {
+        // the rjl repulsion is the model's baseline; the network learns the rest
+        learned::Model m = learned::default_model(1, static_cast<unsigned>(opt.rand_seed));
+        m.d.bA = static_cast<float>(I.rjl.A0);
+        m.d.bp = static_cast<float>(I.rjl.p);
+        m.d.br0 = static_cast<float>(I.rjl.r0);
+        m.d.bR1 = static_cast<float>(I.rjl.R1);
+        m.d.bR2 = static_cast<float>(I.rjl.R2);
+        ms.push_back(m);
+      }
     }
   } else {
     ms = learned::load_models(model_in);
@@ -2151,7 +2160,7 @@ void Engine::learned_train(const std::string& model_in, const std::string& model
       const ListH& L = lists[static_cast<size_t>(inters[k].lists[0])];
       const int rows = L.d.rows;
       learned::launch_gather_rows(L.d, eatom.p, M.t.p, st);
-      learned::launch_core_sub(L.d, A, box, learned::core_radius(M.model.kind), M.t.p, st);
+      learned::launch_core_sub(L.d, M.d.p, A, box, learned::core_radius(M.model.kind), M.t.p, st);
       if (fresh && f == 0) {
         // descriptor normalisation and the energy offset from the first frame
         for (int q = 0; q < learned::NG; ++q) {

@@ -28,6 +28,7 @@ Model default_model(int kind, unsigned seed) {
   }
   d.eta_a[0] = 0.0f;
   d.eta_a[1] = kind == 0 ? 0.1f : 0.2f;
+  d.bA = d.bp = d.br0 = d.bR1 = d.bR2 = 0.f;  // set from the interaction when trained
   const float z[4] = {1.f, 2.f, 4.f, 8.f};
   for (int k = 0; k < 4; ++k) d.zeta[k] = z[k];
   d.lambda[0] = 1.f;
@@ -52,7 +53,8 @@ Model default_model(int kind, unsigned seed) {
   return m;
 }
 
-static const char kMagic[8] = {'P', 'F', 'M', 'D', 'M', 'L', 'P', '1'};
+// version 2: the descriptor set carries the pair baseline
+static const char kMagic[8] = {'P', 'F', 'M', 'D', 'M', 'L', 'P', '2'};
 
 void save_models(const std::string& path, const std::vector<Model>& ms) {
   FILE* f = std::fopen(path.c_str(), "wb");
@@ -214,8 +216,14 @@ __global__ void __launch_bounds__(32 * kWarps) k_desc(ListDev L, const DescPar* 
   float ga[NA];
 #pragma unroll
   for (int f = 0; f < NA; ++f) ga[f] = 0.f;
-  for (int a = 0; a < na; ++a)
-    for (int c = a + 1 + lane; c < na; c += 32) {
+  // the pairs (a, c > a) in row-major order of the upper triangle, lane-strided:
+  // pair k = lane + 32 i; (a, rem) walks to it (row a holds na - 1 - a pairs)
+  const int npair = na * (na - 1) / 2;
+  int a = 0, rem = lane;
+  while (a < na - 1 && rem >= na - 1 - a) rem -= na - 1 - a++;
+  for (int k = lane; k < npair; k += 32) {
+    const int c = a + 1 + rem;
+    {
       const float cs = (sm.ux[a] * sm.ux[c] + sm.uy[a] * sm.uy[c] + sm.uz[a] * sm.uz[c]) / (sm.r[a] * sm.r[c]);
       const float C = sm.f[a] * sm.f[c];
       const float rr = sm.r[a] * sm.r[a] + sm.r[c] * sm.r[c];
@@ -233,6 +241,9 @@ __global__ void __launch_bounds__(32 * kWarps) k_desc(ListDev L, const DescPar* 
           for (int ie = 0; ie < 2; ++ie) ga[(il * 4 + iz) * 2 + ie] += tz[iz] * Bq[ie];
       }
     }
+    rem += 32;
+    while (a < na - 1 && rem >= na - 1 - a) rem -= na - 1 - a++;
+  }
   float mine = 0.f;  // lane f < NA keeps angular function f
 #pragma unroll
   for (int f = 0; f < NA; ++f) {
@@ -388,11 +399,15 @@ __global__ void __launch_bounds__(32 * kWarps) k_lcenter(ListDev L, const DescPa
     const int4 pj = A.posq[L.pidx[row]];
     const int na = collect_ang(L, row, n, pj, A, B, d.rc_ang, sm, ctl);
     const float* gj = g + (size_t)row * NG + NR;
-    if (lane < na) {
-      const float u[3] = {sm.ux[lane], sm.uy[lane], sm.uz[lane]};
-      const float ru = sm.r[lane], fu = sm.f[lane], dfu = sm.df[lane];
-      for (int c = 0; c < na; ++c) {
-        if (c == lane) continue;
+    // K lanes per partner: lane = u + na h (h < K) takes the partners c = h,
+    // h + K, ...; the K partial legs of u are then added into lane u in order
+    const int K = na > 0 ? max(1, 32 / na) : 1;
+    const int u_ = na > 0 ? lane % na : 0, h = na > 0 ? lane / na : K;
+    if (h < K) {
+      const float u[3] = {sm.ux[u_], sm.uy[u_], sm.uz[u_]};
+      const float ru = sm.r[u_], fu = sm.f[u_], dfu = sm.df[u_];
+      for (int c = h; c < na; c += K) {
+        if (c == u_) continue;
         const float v[3] = {sm.ux[c], sm.uy[c], sm.uz[c]};
         const float rv = sm.r[c];
         const float cs = (u[0] * v[0] + u[1] * v[1] + u[2] * v[2]) / (ru * rv);
@@ -403,11 +418,64 @@ __global__ void __launch_bounds__(32 * kWarps) k_lcenter(ListDev L, const DescPa
         ly += tu[1];
         lz += tu[2];
       }
+    }
+    for (int q = 1; q < K; ++q) {  // K is uniform over the warp
+      const int src = min(lane + na * q, 31);
+      const float x = __shfl_sync(0xffffffffu, lx, src), y = __shfl_sync(0xffffffffu, ly, src),
+                  z = __shfl_sync(0xffffffffu, lz, src);
+      if (lane < na) {
+        lx += x;
+        ly += y;
+        lz += z;
+      }
+    }
+    if (lane < na) {
       leg[(size_t)sm.slot[lane] * L.stride + row] = make_float4(lx, ly, lz, 0.f);
+    } else {
+      lx = ly = lz = 0.f;  // partials already in their partner's lane
     }
   }
   const float fx = warp_sum_f(lx), fy = warp_sum_f(ly), fz = warp_sum_f(lz);
   if (lane == 0) cforce[row] = make_float4(fx, fy, fz, 0.f);
+}
+
+// The baseline's pair function phi(r) = exp(-bp (r/br0 - 1)) fc(r) and dphi/dr,
+// fc the reference's cosine switch between bR1 and bR2 (cut_off_function.f90:6-28,
+// its truncated pi).
+__device__ __forceinline__ void base_phi(const DescPar& d, float r, float& phi, float& dphi) {
+  phi = dphi = 0.f;
+  if (r >= d.bR2) return;
+  const float e = __expf(-d.bp * (r / d.br0 - 1.f));
+  float fc = 1.f, dfc = 0.f;
+  if (r > d.bR1) {
+    const float k = 3.14159265358979f / (d.bR2 - d.bR1);
+    float sn, cs;
+    __sincosf(k * (r - d.bR1), &sn, &cs);
+    fc = 0.5f * (1.f + cs);
+    dfc = -0.5f * k * sn;
+  }
+  phi = e * fc;
+  dphi = e * (dfc - d.bp / d.br0 * fc);
+}
+
+// The model's pair terms of one list entry at distance r (separation dr, from
+// the row atom to the partner): the close-contact wall and the baseline.  Adds
+// the row's share of their energy to e and returns c with F_row += c dr; each
+// pair sits in both atoms' rows, so c carries both rows' derivatives.
+__device__ __forceinline__ float pair_terms(const DescPar& d, float rcore, float r, float& e) {
+  float c = 0.f;
+  if (r < rcore) {  // (k/2) (rcore - r)^2 per entry
+    const float x = rcore - r;
+    c -= 2.f * kCoreK * x / r;
+    e += 0.5f * kCoreK * x * x;
+  }
+  if (d.bA > 0.f) {  // bA phi(r) per entry (the rjl repulsion is a full-row sum)
+    float ph, dph;
+    base_phi(d, r, ph, dph);
+    c += 2.f * d.bA * dph / r;
+    e += d.bA * ph;
+  }
+  return c;
 }
 
 // Slots of atom ai in list rows ra (na entries) and rb (nb entries; 0: none), -1
@@ -463,6 +531,10 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
         r = sqrtf(mi_q(pi, A.posq[aj], B, dr));
         rj = L.row_of[aj];
         if (r < d.rc_ang) nj = L.nnum[rj];
+        const float c = pair_terms(d, rcore, r, ec);  // this lane's entry
+        fx += c * dr[0];
+        fy += c * dr[1];
+        fz += c * dr[2];
       }
       if (r < d.rc_rad) fcut_d(r, d.rc_rad, fc, dfc);
       const int m = min(32, n - base);
@@ -483,14 +555,6 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
           gq[u] = on ? g[(size_t)rjq * NG + lane] : 0.f;
           const float t = rq - rs;
           cq[u] = on ? __expf(-er * t * t) * (-2.f * er * t * fq + dfq) / rq : 0.f;
-          if (q < m && rq < rcore && lane == 0) {  // the close-contact wall (learned.h)
-            const float x = rcore - rq;
-            const float c = -2.f * kCoreK * x / rq;  // both rows' (k/2) x^2 depend on this atom
-            fx += c * dq[u][0];
-            fy += c * dq[u][1];
-            fz += c * dq[u][2];
-            ec += 0.5f * kCoreK * x * x;
-          }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -534,7 +598,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar
     fx = warp_sum_f(fx);
     fy = warp_sum_f(fy);
     fz = warp_sum_f(fz);
-    ec = __shfl_sync(0xffffffffu, ec, 0);
+    ec = warp_sum_f(ec);
     if (lane == 0) {
       s_f[0][slot] = fx;
       s_f[1][slot] = fy;
@@ -889,22 +953,24 @@ __global__ void k_gather_rows(ListDev L, const double* eatom, double* t) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row < L.rows) t[row] = eatom[L.pidx[row]];
 }
-__global__ void k_core_sub(ListDev L, Atoms A, Box B, float rcore, double* t) {
+__global__ void k_core_sub(ListDev L, const DescPar* __restrict__ Dp, Atoms A, Box B, float rcore, double* t) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= L.rows) return;
+  const DescPar& d = *Dp;
   const int n = L.nnum[row];
   const int4 pi = A.posq[L.pidx[row]];
   float e = 0.f;
   for (int p = 0; p < n; ++p) {
     float dr[3];
     const float r = sqrtf(mi_q(pi, A.posq[ent(L, row, p)], B, dr));
-    if (r < rcore) e += 0.5f * kCoreK * (rcore - r) * (rcore - r);
+    pair_terms(d, rcore, r, e);
   }
   t[row] -= (double)e;
 }
-void launch_core_sub(const ListDev& L, const Atoms& A, const Box& B, float rcore, double* t, cudaStream_t s) {
+void launch_core_sub(const ListDev& L, const DescPar* d, const Atoms& A, const Box& B, float rcore, double* t,
+                     cudaStream_t s) {
   if (L.rows <= 0) return;
-  k_core_sub<<<nblk(L.rows, 128), 128, 0, s>>>(L, A, B, rcore, t);
+  k_core_sub<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, A, B, rcore, t);
   ++g_kernel_launches;
 }
 void launch_gather_rows(const ListDev& L, const double* eatom, double* t, cudaStream_t s) {

@@ -22,7 +22,7 @@ namespace learned {
 constexpr int NR = 32, NA = 16, NG = NR + NA, NH = 64;
 constexpr int MAX_ANG = 32;  // angular partners per atom kept in registers
 
-// A close-contact wall added to each network's energy: (k/2) (r_core - r)^2 per
+// Besides the baseline (DescPar), a close-contact wall is added to each network's energy: (k/2) (r_core - r)^2 per
 // list entry below r_core (each pair sits in both atoms' rows, so a pair's wall
 // is k (r_core - r)^2).  r_core is 1.15 A for the tb (C) network and 2.2 A for
 // the rjl (Cu) one, in the lower tail of the nearest-neighbour distances that the
@@ -39,6 +39,11 @@ struct DescPar {
   float rs[NR], eta_r[NR];
   float eta_a[2], zeta[4], lambda[2];  // angular function a = (il*4 + iz)*2 + ie
   float mean[NG], inv_std[NG];
+  // pair baseline (rjl networks): the rjl repulsion bA sum_j exp(-bp (r/br0 - 1))
+  // fc(r) of each atom, with the reference's cosine switch between bR1 and bR2
+  // (RosatoGuillopeLegrand.f90:23-49), is part of the model's energy; the
+  // network learns the rest (the embedding term).  bA = 0: no baseline.
+  float bA, bp, br0, bR1, bR2;
 };
 struct Net {
   float W1[NH * NG], b1[NH];
@@ -107,8 +112,9 @@ int train_blocks(int rows);
 
 // Per-row gather of per-atom targets: t[row] = eatom[pidx[row]].
 void launch_gather_rows(const ListDev& L, const double* eatom, double* t, cudaStream_t s);
-// t[row] -= the row's close-contact wall energy (the network's share of the target).
-void launch_core_sub(const ListDev& L, const Atoms& A, const Box& B, float rcore, double* t, cudaStream_t s);
+// t[row] -= the row's wall and baseline energy (the network's share of the target).
+void launch_core_sub(const ListDev& L, const DescPar* d, const Atoms& A, const Box& B, float rcore, double* t,
+                     cudaStream_t s);
 // Sum over atoms of |f - f_ref|^2 and |f_ref|^2 (deterministic) into out[0..1].
 void launch_force_diff(int n, const double4_32a* f, const double4_32a* fref, double* part, double* out,
                        cudaStream_t s);

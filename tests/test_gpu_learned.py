@@ -121,9 +121,9 @@ def test_close_contact_wall_matches_cpu_reference(tmp_path, built):
     _, _, f = s.state()
     model = learned_ref.load_models(m)[0]
     idx = np.arange(len(p))
-    assert learned_ref.core_energy(p, box, idx, 1) >= 20.0 * 0.4 ** 2 * (1 - 1e-9)
-    fc = learned_ref.core_forces(p, box, idx, 1, len(p))
-    assert np.abs(fc[40]).max() > 10.0  # 2 k (r_core - r) = 16 eV/A
+    assert model["desc"]["bA"] > 0.0  # the rjl repulsion as the baseline
+    fc = learned_ref.pair_forces(p, box, idx, model, len(p))
+    assert np.abs(fc[40]).max() > 10.0  # the wall alone: 2 k (r_core - r) = 16 eV/A
     assert e[0] == pytest.approx(learned_ref.energy(p, box, idx, model), abs=2e-5 * len(p))
     ref = learned_ref.forces_fd(p, box, idx, model, [40, j], h=1e-4)
     scale = np.abs(ref).max()
@@ -213,6 +213,11 @@ def test_tensor_core_training_gradient_matches_fp32(tmp_path, built):
     for k in range(2):
         for a, b in zip(cuts[:-1], cuts[1:]):
             x, y = gtc[k, a:b].astype(np.float64), g32[k, a:b].astype(np.float64)
+            if b - a == 1:
+                # b3: twice the mean energy residual, which training drives towards
+                # zero; BF16 moves each row's energy by up to about 2e-3 eV
+                assert abs(x[0] - y[0]) < 4e-3 + 5e-2 * abs(y[0]), (k, x, y)
+                continue
             rel = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-30)
             assert rel < 5e-2, (k, a, b, rel)
 
@@ -258,8 +263,8 @@ def test_training_gradient_matches_fp64_loss(tmp_path, built):
     t = learned_ref.rjl_atom_energies(pos, box, idx, par)
     v0 = learned_ref.net_vector(model)
 
-    ec = learned_ref.core_row_energies(pos, box, idx, 1)
-    fc = learned_ref.core_forces(pos, box, idx, 1, len(pos))
+    ec = learned_ref.pair_row_energies(pos, box, idx, model)
+    fc = learned_ref.pair_forces(pos, box, idx, model, len(pos))
 
     def loss(v):
         return learned_ref.training_loss(learned_ref.with_net_vector(model, v), G, J, t, f_ref, e_core=ec, f_core=fc)

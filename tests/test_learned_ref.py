@@ -87,23 +87,27 @@ def test_rjl_atom_energies_sum_to_the_oracle(tmp_path):
     assert e.sum() == pytest.approx(o.energies()["inter"][0], rel=1e-12)
 
 
-def test_core_wall_forces_are_its_gradient():
-    # a cluster with pairs inside both walls: the wall forces against central
-    # differences of the wall energy, and the pair energy k (r_core - r)^2
+def test_pair_terms_forces_are_their_gradient():
+    # a cluster with pairs inside both walls and within the baseline's range:
+    # the wall and baseline forces against central differences of their energy
     rng = np.random.default_rng(3)
-    pos = rng.uniform(0.0, 4.0, size=(12, 3))
+    pos = rng.uniform(0.0, 5.0, size=(14, 3))
     box = np.array([30.0, 30.0, 30.0])
-    idx = np.arange(12)
-    for kind in (0, 1):
-        f = lr.core_forces(pos, box, idx, kind, 12)
+    idx = np.arange(14)
+    m = _model()
+    for kind, base in ((0, 0.0), (1, 0.0855)):
+        mk = dict(m, kind=kind, desc=dict(m["desc"], bA=base, bp=10.96, br0=2.556, bR1=4.0, bR2=5.0))
+        f = lr.pair_forces(pos, box, idx, mk, 14)
         assert np.abs(f).max() > 0.0
         h = 1e-6
-        for a in (0, 5, 11):
+        for a in (0, 5, 13):
             for c in range(3):
                 pp, pm = pos.copy(), pos.copy()
                 pp[a, c] += h
                 pm[a, c] -= h
-                fd = -(lr.core_energy(pp, box, idx, kind) - lr.core_energy(pm, box, idx, kind)) / (2 * h)
+                fd = -(lr.core_energy(pp, box, idx, mk) - lr.core_energy(pm, box, idx, mk)) / (2 * h)
                 assert f[a, c] == pytest.approx(fd, rel=1e-6, abs=1e-6)
     two = np.array([[1.0, 1.0, 1.0], [2.8, 1.0, 1.0]])
-    assert lr.core_energy(two, box, np.arange(2), 1) == pytest.approx(lr.CORE_K * (lr.CORE_R[1] - 1.8) ** 2)
+    mk = dict(m, kind=1, desc=dict(m["desc"], bA=0.0855, bp=10.96, br0=2.556, bR1=4.0, bR2=5.0))
+    expect = lr.CORE_K * (lr.CORE_R[1] - 1.8) ** 2 + 2 * 0.0855 * np.exp(-10.96 * (1.8 / 2.556 - 1.0))
+    assert lr.core_energy(two, box, np.arange(2), mk) == pytest.approx(expect)
