@@ -234,19 +234,22 @@ def other_configs(root, device):
     return out
 
 
-def batched_config(root, device, steps, n_rep=512):
+def batched_config(root, device, steps, n_rep=512, window=5000):
     """The batched form on its configuration: n_rep replicas (LJ gases and Cu rjl
     slabs of 500-20,000 atoms at 100-1,200 K, nve) stepped together by one persistent
     kernel, after the autotuner picked threads per row per size bucket.  Beside it:
     the same replicas run one at a time through the single-system library (plain
     and precision forms, on a sample of 8), the force error against the plain form
-    at the final positions, and each replica's NVE drift from its energy history."""
+    at the final positions, and each replica's NVE drift from its energy history:
+    over the timed run, which starts cold, and over a further `window` steps
+    after it, with the plain FP64 form from the same states beside it."""
     import numpy as np
     import pfmds_gb300 as pf
     from pfmds_gb300 import configs
     d = os.path.join(root, "batch")
     t0 = time.perf_counter()
-    ln, reps = configs.batch_systems(d, n_rep=n_rep, steps=steps, log_period=100, workers=os.cpu_count() or 1)
+    ln, reps = configs.batch_systems(d, n_rep=n_rep, steps=steps + window, log_period=100,
+                                     workers=os.cpu_count() or 1)
     t_gen = time.perf_counter() - t0
     b = pf.Batch(d, ln, device=device)
     R, n_all, _ = b.info()
@@ -285,7 +288,34 @@ def batched_config(root, device, steps, n_rep=512):
             s.close()
     one = {k: v[0] / v[1] for k, v in t_one.items()}
     graphs = b.graphs()
+    # the drift window: every replica equilibrated by the timed run, `window`
+    # more steps; the plain FP64 form runs the same window from the same state on
+    # one replica of each kind
+    wpick = [next((k for k in sample if reps[k]["kind"] == kind), None) for kind in ("lj", "rjl")]
+    w0 = {r: b.state(r)[:2] for r in wpick if r is not None}
+    hw0 = h.shape[0]
+    if window > 0:
+        b.run(window)
+    hw, _ = b.history()
     b.close()
+    totw = (hw[hw0 - 1:, :, 0] + hw[hw0 - 1:, :, 1]) / ns[None, :]
+    rows_w = np.arange(totw.shape[0], dtype=float) * per
+    dw = np.array([np.polyfit(rows_w * dts[r], totw[:, r], 1)[0] * 1e6 for r in range(R)]) if window > 0 else None
+    win_plain = []
+    for r, (p0, v0) in w0.items():
+        if window <= 0:
+            break
+        s = pf.Simulation(d, settings=reps[r]["settings"], form="plain", out_period=10 ** 9, device=device)
+        s.set_state(p0, v0)
+        e = []
+        for k in range(totw.shape[0]):
+            s.advance(1 if k == 0 else per)
+            en = s.energies()
+            e.append((en["pe"] + en["ke"]) / reps[r]["n"])
+        s.close()
+        win_plain.append({"replica": r, "kind": reps[r]["kind"], "atoms": reps[r]["n"],
+                          "plain_fp64": float(np.polyfit(rows_w * dts[r], np.array(e), 1)[0] * 1e6),
+                          "batched": float(dw[r])})
     # the plain FP64 form on two of the sampled replicas (one of each kind), same
     # start, same steps, energies every 100 steps: its drift is the integrator's
     plain_drift = []
@@ -319,6 +349,11 @@ def batched_config(root, device, steps, n_rep=512):
                                          "fraction_below_1e-5": float((np.abs(drift) < 1e-5).mean()),
                                          "window_fs": "steps x dt (0.5 fs LJ, 1 fs Cu), energies every 100 steps",
                                          "against_plain_fp64": plain_drift},
+        "nve_drift_equilibrated": None if dw is None else {
+            "window_steps": window, "after": f"the timed {steps}-step run",
+            "median_abs": float(np.median(np.abs(dw))), "max_abs": float(np.abs(dw).max()),
+            "fraction_below_1e-5": float((np.abs(dw) < 1e-5).mean()),
+            "unit": "eV/atom/ns", "against_plain_fp64": win_plain},
         "input_generation_s": t_gen}
 
 
@@ -562,7 +597,9 @@ def run_ours(args):
         cands = {}
         per_list = builds / (K * S) if builds >= 0 else 1.0 / 10  # rebuilds per MD step in the timed region
         for name, per_md in (("rjl_force", 1.0), ("rjl_density", 1.0), ("lists", per_list)):
-            ms, b = sim.time_kernel(name, reps=50)
+            # the fastest of three 50-launch loops: single loops scattered by up to
+            # 18% between boxes while the step time did not move
+            ms, b = min((sim.time_kernel(name, reps=50) for _ in range(3)), key=lambda t: t[0])
             cands[name] = (ms, b, ms * per_md)
         dom = max(("rjl_force", "rjl_density"), key=lambda k: cands[k][2])
         ms, b_impl, _ = cands[dom]
