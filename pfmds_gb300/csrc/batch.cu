@@ -1225,6 +1225,7 @@ struct Batch {
         h.T = r.nhc_T;
         h.q[0] = r.nhc_q1;
         for (int i = 1; i < h.M; ++i) h.q[i] = h.q[0] / (3.0 * h.L);
+        for (int i = 0; i < h.M; ++i) h.iq[i] = 1.0 / h.q[i];
       }
       nhc.alloc(reps.size());
       nhc.up(ch, st);

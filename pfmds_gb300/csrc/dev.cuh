@@ -55,6 +55,7 @@ struct NHCDev {
   int M, L;
   double T, s, e;
   double x[PFMD_MAX_CHAIN], v[PFMD_MAX_CHAIN], q[PFMD_MAX_CHAIN];
+  double iq[PFMD_MAX_CHAIN];  // 1/q, formed on the host
 };
 
 // Control block in device memory.  The host reads it back after a segment.

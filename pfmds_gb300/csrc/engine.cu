@@ -967,6 +967,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     d.e = 0.0;
     d.q[0] = h.q1;
     for (int i = 1; i < d.M; ++i) d.q[i] = d.q[0] / (3.0 * d.L);
+    for (int i = 0; i < d.M; ++i) d.iq[i] = 1.0 / d.q[i];
   }
   CK(cudaMemcpyAsync(ctl, hctl, ctl_head, cudaMemcpyHostToDevice, st));
   launch_pack_posq(A, box, ctl, st);

@@ -286,36 +286,40 @@ __device__ __forceinline__ double ke_of(const Atoms& A, int i) {
 
 // The chain part of integrate_nose_hoover_chain (md_integrators.f90:200-245)
 // for the group's kinetic energy ke: both half-updates of the chain and the
-// scale factor s (k_scale / k_kick_drift apply it).  One thread.
+// scale factor s (k_scale / k_kick_drift apply it).  One thread.  GB300's FP64
+// pipe makes every FP64 instruction of this one thread cost a full warp's issue,
+// so the update uses the host-formed 1/q instead of dividing, and the second
+// sweep reuses the first sweep's factors b_i = exp(-v_{i+1} ts4): v_{i+1} is not
+// touched between the two, so they are the same numbers the reference forms
+// again (the divisions become multiplications by 1/q, a last-bit difference).
 __device__ __forceinline__ void nhc_chain_update(NHCDev& hd, double ke, double ts2, double ts3, double ts4) {
   NHCDev h = hd;  // one set of independent loads, not a chain of dependent ones
   const double kt = kKtPerKelvin * h.T;
   const int M = h.M;
   double kedif = 2.0 * ke - 3.0 * h.L * kt;
-  double b = 0.0;
+  double bb[PFMD_MAX_CHAIN];
   if (M == 1) {
-    h.v[0] = h.v[0] + kedif / h.q[0] * ts3;
+    h.v[0] = h.v[0] + kedif * h.iq[0] * ts3;
   } else {
-    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) / h.q[M - 1] * ts3;
+    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) * h.iq[M - 1] * ts3;
     for (int i = M - 2; i >= 1; --i) {
-      b = exp(-h.v[i + 1] * ts4);
-      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) / h.q[i] * ts3 * b;
+      const double b = exp(-h.v[i + 1] * ts4);
+      bb[i] = b;
+      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) * h.iq[i] * ts3 * b;
     }
-    b = exp(-h.v[1] * ts4);
-    h.v[0] = h.v[0] * (b * b) + kedif / h.q[0] * ts3 * b;
+    bb[0] = exp(-h.v[1] * ts4);
+    h.v[0] = h.v[0] * (bb[0] * bb[0]) + kedif * h.iq[0] * ts3 * bb[0];
   }
   h.s = exp(-h.v[0] * ts2);
   kedif = 2.0 * ke * (h.s * h.s) - 3.0 * h.L * kt;
   for (int i = 0; i < M; ++i) h.x[i] = h.x[i] + h.v[i] * ts2;
   if (M == 1) {
-    h.v[0] = h.v[0] + kedif / h.q[0] * ts3;
+    h.v[0] = h.v[0] + kedif * h.iq[0] * ts3;
   } else {
-    h.v[0] = h.v[0] * (b * b) + kedif / h.q[0] * ts3 * b;
-    for (int i = 1; i <= M - 2; ++i) {
-      b = exp(-h.v[i + 1] * ts4);
-      h.v[i] = h.v[i] * (b * b) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) / h.q[i] * ts3 * b;
-    }
-    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) / h.q[M - 1] * ts3;
+    h.v[0] = h.v[0] * (bb[0] * bb[0]) + kedif * h.iq[0] * ts3 * bb[0];
+    for (int i = 1; i <= M - 2; ++i)
+      h.v[i] = h.v[i] * (bb[i] * bb[i]) + (h.q[i - 1] * (h.v[i - 1] * h.v[i - 1]) - kt) * h.iq[i] * ts3 * bb[i];
+    h.v[M - 1] = h.v[M - 1] + (h.q[M - 2] * (h.v[M - 2] * h.v[M - 2]) - kt) * h.iq[M - 1] * ts3;
   }
   hd = h;
 }

@@ -234,8 +234,32 @@ __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, C
     __syncthreads();  // s_f is rewritten by the next pass
   }
   if (!ENERGY && chain < 0) return;
+  // only the epilogue threads (the first APB of the block) hold sums: the
+  // block total is their warps' sum, with no FP64 shuffles in the other warps
+  // (each FP64 instruction costs a full warp's issue on this GPU's FP64 pipe)
+  constexpr int EW = (APB + 31) / 32;
+  if (w < EW) {
+#pragma unroll
+    for (int k = 0; k <= kMaxPairKeys; ++k) red[k] = warp_sum(red[k]);
+  }
+  if constexpr (EW > 1) {
+    __shared__ double s_red[kMaxPairKeys + 1][EW];
+    if (w < EW && lane == 0) {
+#pragma unroll
+      for (int k = 0; k <= kMaxPairKeys; ++k) s_red[k][w] = red[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k <= kMaxPairKeys; ++k) {
+        double t = s_red[k][0];
+        for (int q = 1; q < EW; ++q) t += s_red[k][q];
+        red[k] = t;
+      }
+    }
+  }
   double out[kMaxPairKeys + 1];
-  if (!grid_sum<kMaxPairKeys + 1>(ctl, kPairSlot, red, out)) return;
+  if (!grid_finish<kMaxPairKeys + 1>(ctl, kPairSlot, red, out)) return;
   if (ENERGY) {
 #pragma unroll
     for (int k = 0; k < kMaxPairKeys; ++k)
