@@ -129,136 +129,81 @@ __device__ __forceinline__ void ang_sums(const DescPar& d, const float* w, float
 }
 
 // ---------------------------------------------------------------------------
-// descriptors and forces: warp-cooperative.  NR = 32 radial functions and
-// MAX_ANG = 32 angular partners match the warp: lane k owns radial function k,
-// lane a owns angular partner a.
+// descriptors: one thread per row
 // ---------------------------------------------------------------------------
-constexpr int kWarps = 8;  // warps per block of the warp-cooperative kernels
-
-struct AngW {  // one warp's angular partners of its current row, in slot order
-  float ux[MAX_ANG], uy[MAX_ANG], uz[MAX_ANG], r[MAX_ANG], f[MAX_ANG], df[MAX_ANG];
-  int slot[MAX_ANG];
-};
-
-// The row's angular partners (r < rc_ang) into sm, in slot order: each chunk of
-// 32 entries is compacted with one ballot.  More than MAX_ANG records the error
-// (ST_PARAM) and keeps the first MAX_ANG, as one thread per row did.
-__device__ int collect_ang(const ListDev& L, int row, int n, const int4& pi, const Atoms& A, const Box& B,
-                           float rc_ang, AngW& sm, Ctl* ctl) {
-  const int lane = threadIdx.x & 31;
-  int na = 0;
-  for (int base = 0; base < n; base += 32) {
-    const int p = base + lane;
-    float dr[3] = {0.f, 0.f, 0.f}, r = 3.4e38f;
-    if (p < n) r = sqrtf(mi_q(pi, A.posq[ent(L, row, p)], B, dr));
-    const bool hit = p < n && r < rc_ang;
-    const unsigned m = __ballot_sync(0xffffffffu, hit);
-    const int k = na + __popc(m & ((1u << lane) - 1u));
-    if (hit && k < MAX_ANG) {
-      float fc, dfc;
-      fcut_d(r, rc_ang, fc, dfc);
-      sm.ux[k] = dr[0];
-      sm.uy[k] = dr[1];
-      sm.uz[k] = dr[2];
-      sm.r[k] = r;
-      sm.f[k] = fc;
-      sm.df[k] = dfc;
-      sm.slot[k] = p;
-    }
-    na += __popc(m);
-  }
-  __syncwarp();
-  if (na > MAX_ANG) {
-    if (lane == 0) set_error(ctl, ST_PARAM, EK_NONE, row + 1, na, MAX_ANG);
-    na = MAX_ANG;
-  }
-  return na;
-}
-
-// G of one row per warp.  Radial: each lane forms one entry's distance per chunk
-// of 32 entries, then every lane adds that entry's Gaussian of its own function.
-// Angular: for each partner a, lanes take the pairs (a, c > a); the 16 sums are
-// reduced over the warp at the end (a fixed order).
-__global__ void __launch_bounds__(32 * kWarps) k_desc(ListDev L, const DescPar* __restrict__ Dp, Atoms A, Box B,
-                                                      float* G, Ctl* ctl) {
-  if (block_stop(ctl)) return;
-  __shared__ AngW s_ang[kWarps];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int row = blockIdx.x * kWarps + w;
-  if (row >= L.rows) return;  // the whole warp
+__global__ void __launch_bounds__(128) k_desc(ListDev L, const DescPar* __restrict__ Dp, Atoms A, Box B, float* G,
+                                              Ctl* ctl) {
+  if (ctl->stop) return;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= L.rows) return;
   const DescPar& d = *Dp;
-  AngW& sm = s_ang[w];
+  float g[NG];
+#pragma unroll
+  for (int f = 0; f < NG; ++f) g[f] = 0.f;
+  float ux[MAX_ANG], uy[MAX_ANG], uz[MAX_ANG], ur[MAX_ANG], uf[MAX_ANG];
+  int na = 0;
   const int n = L.nnum[row];
-  const int4 pi = A.posq[L.pidx[row]];
-  const float rs = d.rs[lane], er = d.eta_r[lane];
-  float gk = 0.f;
-  for (int base = 0; base < n; base += 32) {
-    const int p = base + lane;
-    float r = 3.4e38f, fc = 0.f;
-    if (p < n) {
+  if (n > 0) {
+    const int4 pi = A.posq[L.pidx[row]];
+    for (int p = 0; p < n; ++p) {
       float dr[3];
-      r = sqrtf(mi_q(pi, A.posq[ent(L, row, p)], B, dr));
-    }
-    if (r < d.rc_rad) {
-      float dfc;
-      fcut_d(r, d.rc_rad, fc, dfc);
-    }
-    const int m = min(32, n - base);
-    for (int q = 0; q < m; ++q) {
-      const float rq = __shfl_sync(0xffffffffu, r, q), fq = __shfl_sync(0xffffffffu, fc, q);
-      if (rq < d.rc_rad) {
-        const float t = rq - rs;
-        gk += __expf(-er * t * t) * fq;
+      const float r2 = mi_q(pi, A.posq[ent(L, row, p)], B, dr);
+      const float r = sqrtf(r2);
+      if (r < d.rc_rad) {
+        float fc, dfc;
+        fcut_d(r, d.rc_rad, fc, dfc);
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+          const float t = r - d.rs[k];
+          g[k] += __expf(-d.eta_r[k] * t * t) * fc;
+        }
+      }
+      if (r < d.rc_ang) {
+        if (na < MAX_ANG) {
+          float fc, dfc;
+          fcut_d(r, d.rc_ang, fc, dfc);
+          ux[na] = dr[0];
+          uy[na] = dr[1];
+          uz[na] = dr[2];
+          ur[na] = r;
+          uf[na] = fc;
+        }
+        ++na;
       }
     }
-  }
-  const int na = collect_ang(L, row, n, pi, A, B, d.rc_ang, sm, ctl);
-  float ga[NA];
-#pragma unroll
-  for (int f = 0; f < NA; ++f) ga[f] = 0.f;
-  // the pairs (a, c > a) in row-major order of the upper triangle, lane-strided:
-  // pair k = lane + 32 i; (a, rem) walks to it (row a holds na - 1 - a pairs)
-  const int npair = na * (na - 1) / 2;
-  int a = 0, rem = lane;
-  while (a < na - 1 && rem >= na - 1 - a) rem -= na - 1 - a++;
-  for (int k = lane; k < npair; k += 32) {
-    const int c = a + 1 + rem;
-    {
-      const float cs = (sm.ux[a] * sm.ux[c] + sm.uy[a] * sm.uy[c] + sm.uz[a] * sm.uz[c]) / (sm.r[a] * sm.r[c]);
-      const float C = sm.f[a] * sm.f[c];
-      const float rr = sm.r[a] * sm.r[a] + sm.r[c] * sm.r[c];
-      float Bq[2];
-#pragma unroll
-      for (int ie = 0; ie < 2; ++ie) Bq[ie] = __expf(-d.eta_a[ie] * rr) * C;
-#pragma unroll
-      for (int il = 0; il < 2; ++il) {
-        const float t = fmaxf(1.f + d.lambda[il] * cs, 0.f);
-        const float t2 = t * t, t4 = t2 * t2;
-        const float tz[4] = {t, 0.5f * t2, 0.125f * t4, 0.0078125f * t4 * t4};
-#pragma unroll
-        for (int iz = 0; iz < 4; ++iz)
-#pragma unroll
-          for (int ie = 0; ie < 2; ++ie) ga[(il * 4 + iz) * 2 + ie] += tz[iz] * Bq[ie];
-      }
+    if (na > MAX_ANG) {
+      set_error(ctl, ST_PARAM, EK_NONE, row + 1, na, MAX_ANG);
+      na = MAX_ANG;
     }
-    rem += 32;
-    while (a < na - 1 && rem >= na - 1 - a) rem -= na - 1 - a++;
-  }
-  float mine = 0.f;  // lane f < NA keeps angular function f
+    for (int j = 0; j < na; ++j)
+      for (int k = j + 1; k < na; ++k) {
+        const float cs = (ux[j] * ux[k] + uy[j] * uy[k] + uz[j] * uz[k]) / (ur[j] * ur[k]);
+        const float C = uf[j] * uf[k];
+        const float rr = ur[j] * ur[j] + ur[k] * ur[k];
+        float Bq[2];
 #pragma unroll
-  for (int f = 0; f < NA; ++f) {
-    const float v = warp_sum_f(ga[f]);
-    if (lane == f) mine = v;
+        for (int ie = 0; ie < 2; ++ie) Bq[ie] = __expf(-d.eta_a[ie] * rr) * C;
+#pragma unroll
+        for (int il = 0; il < 2; ++il) {
+          const float t = fmaxf(1.f + d.lambda[il] * cs, 0.f);
+          const float t2 = t * t, t4 = t2 * t2;
+          const float tz[4] = {t, 0.5f * t2, 0.125f * t4, 0.0078125f * t4 * t4};
+#pragma unroll
+          for (int iz = 0; iz < 4; ++iz)
+#pragma unroll
+            for (int ie = 0; ie < 2; ++ie) g[NR + (il * 4 + iz) * 2 + ie] += tz[iz] * Bq[ie];
+        }
+      }
   }
   float* out = G + (size_t)row * NG;
-  out[lane] = (gk - d.mean[lane]) * d.inv_std[lane];
-  if (lane < NA) out[NR + lane] = (mine - d.mean[NR + lane]) * d.inv_std[NR + lane];
+#pragma unroll
+  for (int f = 0; f < NG; ++f) out[f] = (g[f] - d.mean[f]) * d.inv_std[f];
 }
 
 void launch_desc(const ListDev& L, const DescPar* d, const Atoms& A, const Box& B, float* G, Ctl* ctl,
                  cudaStream_t s) {
   if (L.rows == 0) return;
-  k_desc<<<nblk(L.rows, kWarps), 32 * kWarps, 0, s>>>(L, d, A, B, G, ctl);
+  k_desc<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, A, B, G, ctl);
   ++g_kernel_launches;
 }
 
@@ -374,69 +319,64 @@ __device__ __forceinline__ void dT_du(const float* u, float ru, const float* v, 
   }
 }
 
-// Angular terms in two passes.  Centre pass, one warp per row j: lane a owns j's
-// angular partner a and sums, over the other partners c, the derivative of the
-// pair's angular terms with respect to u_a -- the leg gradient, stored per
-// partner slot in leg[slot][j]; j's own term is the sum of its legs.  (Each pair
-// is evaluated by both of its lanes, so no two lanes add to one value and the
-// sums are deterministic.)  Gather pass, 32 rows per warp: for every row i the
-// radial terms (lanes over the radial functions), i's centre term and -leg[q][j]
-// for every angular neighbour j, q being i's slot in j's row (a warp search of
-// j's row); the FP64 epilogue then runs with one row per lane.
-__global__ void __launch_bounds__(32 * kWarps) k_lcenter(ListDev L, const DescPar* __restrict__ Dp,
-                                                         const float* __restrict__ g, Atoms A, Box B, float4* leg,
-                                                         float4* cforce, Ctl* ctl) {
+// Angular terms in two passes, each triplet evaluated once.  Centre pass, one
+// thread per row j: for every pair (p, k) of j's angular partners the weighted
+// sums and dT/du, dT/dv give j's own force term (dT/du + dT/dv) and the legs'
+// gradients, summed per partner slot into leg[p][j].  Gather pass, one thread per
+// row i: radial terms, i's centre term, and -leg[q][j] for every angular
+// neighbour j, q being i's slot in j's row.
+__global__ void __launch_bounds__(128) k_lcenter(ListDev L, const DescPar* __restrict__ Dp,
+                                                 const float* __restrict__ g, Atoms A, Box B, float4* leg,
+                                                 float4* cforce, Ctl* ctl) {
   if (ctl->stop) return;
-  __shared__ AngW s_ang[kWarps];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int row = blockIdx.x * kWarps + w;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= L.rows) return;
   const DescPar& d = *Dp;
-  AngW& sm = s_ang[w];
   const int n = L.nnum[row];
-  float lx = 0.f, ly = 0.f, lz = 0.f;
+  float ux[MAX_ANG], uy[MAX_ANG], uz[MAX_ANG], ur[MAX_ANG], uf[MAX_ANG], udf[MAX_ANG];
+  float lx[MAX_ANG], ly[MAX_ANG], lz[MAX_ANG];
+  int sl[MAX_ANG];
+  int na = 0;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
   if (n > 0) {
     const int4 pj = A.posq[L.pidx[row]];
-    const int na = collect_ang(L, row, n, pj, A, B, d.rc_ang, sm, ctl);
+    for (int p = 0; p < n && na < MAX_ANG; ++p) {
+      float dr[3];
+      const float r = sqrtf(mi_q(pj, A.posq[ent(L, row, p)], B, dr));
+      if (r < d.rc_ang) {
+        fcut_d(r, d.rc_ang, uf[na], udf[na]);
+        ux[na] = dr[0];
+        uy[na] = dr[1];
+        uz[na] = dr[2];
+        ur[na] = r;
+        lx[na] = ly[na] = lz[na] = 0.f;
+        sl[na] = p;
+        ++na;
+      }
+    }
     const float* gj = g + (size_t)row * NG + NR;
-    // K lanes per partner: lane = u + na h (h < K) takes the partners c = h,
-    // h + K, ...; the K partial legs of u are then added into lane u in order
-    const int K = na > 0 ? max(1, 32 / na) : 1;
-    const int u_ = na > 0 ? lane % na : 0, h = na > 0 ? lane / na : K;
-    if (h < K) {
-      const float u[3] = {sm.ux[u_], sm.uy[u_], sm.uz[u_]};
-      const float ru = sm.r[u_], fu = sm.f[u_], dfu = sm.df[u_];
-      for (int c = h; c < na; c += K) {
-        if (c == u_) continue;
-        const float v[3] = {sm.ux[c], sm.uy[c], sm.uz[c]};
-        const float rv = sm.r[c];
-        const float cs = (u[0] * v[0] + u[1] * v[1] + u[2] * v[2]) / (ru * rv);
-        float SA, SdA, Se, tu[3];
-        ang_sums(d, gj, cs, ru * ru, rv * rv, SA, SdA, Se);
-        dT_du(u, ru, v, rv, cs, SA, SdA, Se, fu, dfu, sm.f[c], tu);
-        lx += tu[0];
-        ly += tu[1];
-        lz += tu[2];
+    for (int a = 0; a < na; ++a)
+      for (int c = a + 1; c < na; ++c) {
+        const float u[3] = {ux[a], uy[a], uz[a]}, v[3] = {ux[c], uy[c], uz[c]};
+        const float cs = (u[0] * v[0] + u[1] * v[1] + u[2] * v[2]) / (ur[a] * ur[c]);
+        float SA, SdA, Se;
+        ang_sums(d, gj, cs, ur[a] * ur[a], ur[c] * ur[c], SA, SdA, Se);
+        float tu[3], tv[3];
+        dT_du(u, ur[a], v, ur[c], cs, SA, SdA, Se, uf[a], udf[a], uf[c], tu);
+        dT_du(v, ur[c], u, ur[a], cs, SA, SdA, Se, uf[c], udf[c], uf[a], tv);
+        fx += tu[0] + tv[0];
+        fy += tu[1] + tv[1];
+        fz += tu[2] + tv[2];
+        lx[a] += tu[0];
+        ly[a] += tu[1];
+        lz[a] += tu[2];
+        lx[c] += tv[0];
+        ly[c] += tv[1];
+        lz[c] += tv[2];
       }
-    }
-    for (int q = 1; q < K; ++q) {  // K is uniform over the warp
-      const int src = min(lane + na * q, 31);
-      const float x = __shfl_sync(0xffffffffu, lx, src), y = __shfl_sync(0xffffffffu, ly, src),
-                  z = __shfl_sync(0xffffffffu, lz, src);
-      if (lane < na) {
-        lx += x;
-        ly += y;
-        lz += z;
-      }
-    }
-    if (lane < na) {
-      leg[(size_t)sm.slot[lane] * L.stride + row] = make_float4(lx, ly, lz, 0.f);
-    } else {
-      lx = ly = lz = 0.f;  // partials already in their partner's lane
-    }
+    for (int a = 0; a < na; ++a) leg[(size_t)sl[a] * L.stride + row] = make_float4(lx[a], ly[a], lz[a], 0.f);
   }
-  const float fx = warp_sum_f(lx), fy = warp_sum_f(ly), fz = warp_sum_f(lz);
-  if (lane == 0) cforce[row] = make_float4(fx, fy, fz, 0.f);
+  cforce[row] = make_float4(fx, fy, fz, 0.f);
 }
 
 // The baseline's pair function phi(r) = exp(-bp (r/br0 - 1)) fc(r) and dphi/dr,
@@ -478,140 +418,59 @@ __device__ __forceinline__ float pair_terms(const DescPar& d, float rcore, float
   return c;
 }
 
-// Slots of atom ai in list rows ra (na entries) and rb (nb entries; 0: none), -1
-// where absent: both rows 64 entries a round, their four coalesced loads issued
-// together, then ballots (warp-uniform results).
-__device__ __forceinline__ void find_slot2(const ListDev& L, int ra, int na, int rb, int nb, int ai, int lane,
-                                           int& sa, int& sb) {
-  sa = -1;
-  sb = -1;
-  const int nm = max(na, nb);
-  for (int b = 0; b < nm && (sa < 0 || (nb > 0 && sb < 0)); b += 64) {
-    const int a0 = (sa < 0 && b + lane < na) ? ent(L, ra, b + lane) : -1;
-    const int a1 = (sa < 0 && b + 32 + lane < na) ? ent(L, ra, b + 32 + lane) : -1;
-    const int b0 = (sb < 0 && b + lane < nb) ? ent(L, rb, b + lane) : -1;
-    const int b1 = (sb < 0 && b + 32 + lane < nb) ? ent(L, rb, b + 32 + lane) : -1;
-    const unsigned ha0 = __ballot_sync(0xffffffffu, a0 == ai), ha1 = __ballot_sync(0xffffffffu, a1 == ai);
-    const unsigned hb0 = __ballot_sync(0xffffffffu, b0 == ai), hb1 = __ballot_sync(0xffffffffu, b1 == ai);
-    if (sa < 0) sa = ha0 ? b + __ffs(ha0) - 1 : (ha1 ? b + 32 + __ffs(ha1) - 1 : -1);
-    if (sb < 0) sb = hb0 ? b + __ffs(hb0) - 1 : (hb1 ? b + 32 + __ffs(hb1) - 1 : -1);
-  }
-}
-
-__global__ void __launch_bounds__(32 * kWarps) k_lforce(ListDev L, const DescPar* __restrict__ Dp,
-                                                        const float* __restrict__ g, const float* __restrict__ erow,
-                                                        const float4* __restrict__ leg,
-                                                        const float4* __restrict__ cforce, int energy, Atoms A, Box B,
-                                                        Ctl* ctl, int eslot, int ekey, Epi E, float rcore) {
-  if (block_stop(ctl)) return;
-  // a block takes 32 rows, each warp 4 of them; the row sums meet in shared
-  // memory and warp 0 finishes the 32 rows, one per lane (FP64 epilogue on full
-  // warps, as in the pair kernels)
-  constexpr int kRowsPerWarp = 32 / kWarps;
-  __shared__ float s_f[4][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int b0 = blockIdx.x * 32;
+__global__ void __launch_bounds__(128) k_lforce(ListDev L, const DescPar* __restrict__ Dp, const float* __restrict__ g,
+                                                const float* __restrict__ erow, const float4* __restrict__ leg,
+                                                const float4* __restrict__ cforce, int energy, Atoms A, Box B, Ctl* ctl,
+                                                int eslot, int ekey, Epi E, float rcore) {
+  if (ctl->stop) return;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = row < L.rows;
   const DescPar& d = *Dp;
-  const float rs = d.rs[lane], er = d.eta_r[lane];
-  for (int rr = 0; rr < kRowsPerWarp; ++rr) {
-    const int slot = w * kRowsPerWarp + rr;
-    const int row = b0 + slot;
-    if (row >= L.rows) break;  // uniform over the warp
+  Acc3<true> acc;
+  float ei = 0.f, ep = 0.f;
+  const int n = valid ? L.nnum[row] : 0;
+  if (valid) {
+    ei = erow[row];
     const int ai = L.pidx[row];
     const int4 pi = A.posq[ai];
-    const int n = L.nnum[row];
-    const float gi = g[(size_t)row * NG + lane];
-    float fx = 0.f, fy = 0.f, fz = 0.f, ec = 0.f;
-    for (int base = 0; base < n; base += 32) {
-      const int p = base + lane;
-      float dr[3] = {0.f, 0.f, 0.f}, r = 3.4e38f, fc = 0.f, dfc = 0.f;
-      int rj = 0, nj = 0;
-      if (p < n) {
-        const int aj = ent(L, row, p);
-        r = sqrtf(mi_q(pi, A.posq[aj], B, dr));
-        rj = L.row_of[aj];
-        if (r < d.rc_ang) nj = L.nnum[rj];
-        const float c = pair_terms(d, rcore, r, ec);  // this lane's entry
-        fx += c * dr[0];
-        fy += c * dr[1];
-        fz += c * dr[2];
+    const float* gi = g + (size_t)row * NG;
+    const float4 cf = cforce[row];
+    acc.add(cf.x, cf.y, cf.z);
+    for (int p = 0; p < n; ++p) {
+      const int aj = ent(L, row, p);
+      float dr[3];
+      const float r = sqrtf(mi_q(pi, A.posq[aj], B, dr));
+      {  // the model's pair terms besides the network: the wall and the baseline
+        const float c = pair_terms(d, rcore, r, ep);
+        acc.add(c * dr[0], c * dr[1], c * dr[2]);
       }
-      if (r < d.rc_rad) fcut_d(r, d.rc_rad, fc, dfc);
-      const int m = min(32, n - base);
-      // radial terms, four partners a round: their dE/dG rows are loaded together
-      // (lane = radial function); q0 <= 28, so q stays a lane index
-      for (int q0 = 0; q0 < m; q0 += 4) {
-        float gq[4], cq[4], dq[4][3];
+      if (r < d.rc_rad) {
+        const float* gj = g + (size_t)L.row_of[aj] * NG;
+        float fc, dfc;
+        fcut_d(r, d.rc_rad, fc, dfc);
+        float c = 0.f;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int q = q0 + u;
-          const float rq = __shfl_sync(0xffffffffu, r, q);
-          const int rjq = __shfl_sync(0xffffffffu, rj, q);
-          const float fq = __shfl_sync(0xffffffffu, fc, q), dfq = __shfl_sync(0xffffffffu, dfc, q);
-          dq[u][0] = __shfl_sync(0xffffffffu, dr[0], q);
-          dq[u][1] = __shfl_sync(0xffffffffu, dr[1], q);
-          dq[u][2] = __shfl_sync(0xffffffffu, dr[2], q);
-          const bool on = q < m && rq < d.rc_rad;
-          gq[u] = on ? g[(size_t)rjq * NG + lane] : 0.f;
-          const float t = rq - rs;
-          cq[u] = on ? __expf(-er * t * t) * (-2.f * er * t * fq + dfq) / rq : 0.f;
+        for (int k = 0; k < NR; ++k) {
+          const float t = r - d.rs[k];
+          const float ex = __expf(-d.eta_r[k] * t * t);
+          c += (gi[k] + gj[k]) * ex * (-2.f * d.eta_r[k] * t * fc + dfc);
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const float c = (gi + gq[u]) * cq[u];
-          fx += c * dq[u][0];
-          fy += c * dq[u][1];
-          fz += c * dq[u][2];
-        }
+        const float ir = 1.f / r;
+        acc.add(c * dr[0] * ir, c * dr[1] * ir, c * dr[2] * ir);
       }
-      // angular legs: the row's atom is an angular partner of each j within
-      // rc_ang, whose centre pass holds its leg term in the slot of this atom in
-      // j's row; two partners' rows are searched a round, and each lane then
-      // gathers the leg term of its own partner
-      int myslot = -1;
-      unsigned ang = __ballot_sync(0xffffffffu, r < d.rc_ang);
-      while (ang) {
-        const int qa = __ffs(ang) - 1;
-        ang &= ang - 1;
-        const int qb = ang ? __ffs(ang) - 1 : qa;
-        if (ang) ang &= ang - 1;
-        const int ra = __shfl_sync(0xffffffffu, rj, qa), na = __shfl_sync(0xffffffffu, nj, qa);
-        const int rb = __shfl_sync(0xffffffffu, rj, qb), nb = qb != qa ? __shfl_sync(0xffffffffu, nj, qb) : 0;
-        int sa, sb;
-        find_slot2(L, ra, na, rb, nb, ai, lane, sa, sb);
-        if (lane == qa) myslot = sa;
-        if (qb != qa && lane == qb) myslot = sb;
-      }
-      if (myslot >= 0) {
-        const float4 lg = leg[(size_t)myslot * L.stride + rj];
-        fx -= lg.x;
-        fy -= lg.y;
-        fz -= lg.z;
+      if (r < d.rc_ang) {  // i is an angular partner of j: j's centre pass holds i's leg term
+        const int rj = L.row_of[aj];
+        const int nj = L.nnum[rj];
+        for (int q = 0; q < nj; ++q)
+          if (ent(L, rj, q) == ai) {
+            const float4 lg = leg[(size_t)q * L.stride + rj];
+            acc.add(-lg.x, -lg.y, -lg.z);
+            break;
+          }
       }
     }
-    if (lane == 0) {
-      const float4 cf = cforce[row];
-      fx += cf.x;
-      fy += cf.y;
-      fz += cf.z;
-    }
-    fx = warp_sum_f(fx);
-    fy = warp_sum_f(fy);
-    fz = warp_sum_f(fz);
-    ec = warp_sum_f(ec);
-    if (lane == 0) {
-      s_f[0][slot] = fx;
-      s_f[1][slot] = fy;
-      s_f[2][slot] = fz;
-      s_f[3][slot] = ec;
-    }
-  }
-  __syncthreads();
-  const int row = b0 + lane;
-  float ei = 0.f;
-  if (w == 0 && row < L.rows) {
-    finish_force(A, E, L.pidx[row], s_f[0][lane], s_f[1][lane], s_f[2][lane]);
-    ei = erow[row] + s_f[3][lane];
+    finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
+    ei += ep;
   }
   if (energy) energy_reduce_f(ctl, eslot, ekey, ei);
 }
@@ -623,9 +482,9 @@ void launch_force(const ListDev& L, const DescPar* d, const float* g, const floa
     if (energy) cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
     return;
   }
-  k_lcenter<<<nblk(L.rows, kWarps), 32 * kWarps, 0, s>>>(L, d, g, A, B, leg, cforce, ctl);
-  k_lforce<<<nblk(L.rows, 32), 32 * kWarps, 0, s>>>(L, d, g, e, leg, cforce, energy ? 1 : 0, A, B, ctl, eslot, ekey, E,
-                                                   rcore);
+  k_lcenter<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, g, A, B, leg, cforce, ctl);
+  k_lforce<<<nblk(L.rows, 128), 128, 0, s>>>(L, d, g, e, leg, cforce, energy ? 1 : 0, A, B, ctl, eslot, ekey, E,
+                                             rcore);
   g_kernel_launches += 2;
 }
 
