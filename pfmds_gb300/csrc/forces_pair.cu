@@ -166,6 +166,7 @@ template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
                                                     double ts2, double ts3, double ts4, int ahead) {
   using T = RT<PREC>;
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
   if (block_stop(ctl)) return;
   constexpr int RPW = 32 / TPA, APB = 8 * RPW;  // atoms per warp, per block pass (256 threads)
   __shared__ double s_f[3][APB];
@@ -233,6 +234,7 @@ __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, C
     }
     __syncthreads();  // s_f is rewritten by the next pass
   }
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   if (!ENERGY && chain < 0) return;
   // only the epilogue threads (the first APB of the block) hold sums: the
   // block total is their warps' sum, with no FP64 shuffles in the other warps
@@ -287,8 +289,8 @@ void launch_pair_atoms(bool prec, bool energy, const PairSet& S, const Atoms& A,
   with_bool(prec, [&](auto pr) {
     with_bool(energy, [&](auto en) {
       with_tpa(S.tpa, [&](auto t) {
-        k_pair_atoms<decltype(pr)::value, decltype(en)::value, decltype(t)::value>
-            <<<grid, 256, 0, s>>>(S, A, B, ctl, E, chain, ts2, ts3, ts4, ahead ? 1 : 0);
+        launch_dependent(k_pair_atoms<decltype(pr)::value, decltype(en)::value, decltype(t)::value>, grid, 256, s, S,
+                         A, B, ctl, E, chain, ts2, ts3, ts4, ahead ? 1 : 0);
         ++g_kernel_launches;
       });
     });

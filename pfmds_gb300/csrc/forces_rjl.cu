@@ -16,27 +16,6 @@
 
 namespace pfmd {
 
-// Launches with programmatic stream serialisation: the grid is set up while the
-// previous kernel on the stream drains, and waits in griddepcontrol.wait (first
-// statement of both rjl kernels) until that kernel has completed and its writes
-// are visible.  Neither kernel triggers its dependents early: an early trigger
-// let the next grid's blocks take SM slots from the running one (38.3 us per
-// MD step against 32.1 on the 65,536-atom slab).
-template <class K, class... Args>
-static void launch_dependent(K kern, int grid, int block, cudaStream_t s, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
 // inv_eb holds 1/Eb per atom: double for the plain form, float for the precision form.
 template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms A, Box B, void* inv_eb,

@@ -150,6 +150,7 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
 template <bool EXACT>
 __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, int begin,
                              int nhc_pre, Atoms A, Box B, Ctl* ctl) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent (forces.cuh)
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   const bool have = ind < g.cap;
   const int i = have ? g.idx[ind] : 0;
@@ -496,11 +497,11 @@ void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_pos
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin, bool nhc_pre) {
   if (g.cap <= 0) return;
   if (exact)
-    k_kick_drift<true><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0,
-                                                      nhc_pre ? 1 : 0, A, B, ctl);
+    launch_dependent(k_kick_drift<true>, nb(g.cap, 256), 256, s, g, ts1, ts2, write_posq ? 1 : 0, nhc_scale,
+                     begin ? 1 : 0, nhc_pre ? 1 : 0, A, B, ctl);
   else
-    k_kick_drift<false><<<nb(g.cap, 256), 256, 0, s>>>(g, ts1, ts2, write_posq ? 1 : 0, nhc_scale, begin ? 1 : 0,
-                                                       nhc_pre ? 1 : 0, A, B, ctl);
+    launch_dependent(k_kick_drift<false>, nb(g.cap, 256), 256, s, g, ts1, ts2, write_posq ? 1 : 0, nhc_scale,
+                     begin ? 1 : 0, nhc_pre ? 1 : 0, A, B, ctl);
   ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
