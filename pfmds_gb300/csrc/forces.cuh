@@ -273,6 +273,69 @@ __device__ __forceinline__ void finish_force_drift(const Atoms& A, const Epi& E,
   }
 }
 
+// Grid sum of K values held as float-float pairs (value = s - c, the form gmerge
+// merges): every block's thread 0 passes its block totals, which go to
+// Ctl::partial as two floats per value; the last block to arrive merges all
+// partials with FP32 TwoSum steps in a fixed order (threads over blocks, then a
+// warp and block tree) and returns the totals in FP64 in thread 0.  No FP64
+// arithmetic runs in the tree: on this GPU's narrow FP64 pipe each FP64
+// instruction of a warp costs a full warp's issue.  Every thread of every block
+// calls it; the relative error is about 2^-46.
+template <int K>
+__device__ __forceinline__ bool grid_finish_ff(Ctl* ctl, int slot, const float (&s)[K], const float (&c)[K],
+                                               double (&out)[K]) {
+  __shared__ bool last;
+  __shared__ float ss[K][32], sc[K][32];
+  float2* part = reinterpret_cast<float2*>(ctl->partial);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) part[(size_t)blockIdx.x * K + k] = make_float2(s[k], c[k]);
+    __threadfence();
+    const unsigned int t = atomicAdd(&ctl->counter[slot], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  float ws[K], wc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) ws[k] = wc[k] = 0.f;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float2 p = __ldcg(&part[(size_t)b * K + k]);  // written by other blocks: from L2
+      float s2 = p.x, c2 = p.y;  // merge (s2, c2) into (ws, wc)
+      const float t = ws[k] + s2, bb = t - ws[k];
+      const float e = (ws[k] - (t - bb)) + (s2 - bb);
+      wc[k] = (wc[k] + c2) - e;
+      ws[k] = t;
+    }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    gmerge<32>(ws[k], wc[k]);
+    if (lane == 0) {
+      ss[k][w] = ws[k];
+      sc[k][w] = wc[k];
+    }
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      ws[k] = lane < nw ? ss[k][lane] : 0.f;
+      wc[k] = lane < nw ? sc[k][lane] : 0.f;
+      gmerge<32>(ws[k], wc[k]);
+    }
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = (double)ws[k] - (double)wc[k];
+    ctl->counter[slot] = 0u;
+  }
+  return threadIdx.x == 0;
+}
+
 // Reduction slot (Ctl::counter) of the all-pairs kernel k_pair_atoms.
 constexpr int kPairSlot = 20;
 constexpr double kMassCoef = 1.6605389217 / 1.6021765654 * 100.0;  // amu A^2/fs^2 -> eV (md_integrators.f90:62)

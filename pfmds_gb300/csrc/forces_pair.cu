@@ -236,32 +236,45 @@ __global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, C
   }
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   if (!ENERGY && chain < 0) return;
-  // only the epilogue threads (the first APB of the block) hold sums: the
-  // block total is their warps' sum, with no FP64 shuffles in the other warps
-  // (each FP64 instruction costs a full warp's issue on this GPU's FP64 pipe)
+  // only the epilogue threads (the first APB of the block) hold sums: each
+  // splits its FP64 sums into float-float pairs, and their warps merge them in
+  // FP32 (no FP64 shuffles; each FP64 instruction costs a full warp's issue on
+  // this GPU's FP64 pipe), then the grid sum runs in float-float as well
   constexpr int EW = (APB + 31) / 32;
+  float fs[kMaxPairKeys + 1], fcmp[kMaxPairKeys + 1];
+#pragma unroll
+  for (int k = 0; k <= kMaxPairKeys; ++k) {
+    fs[k] = (float)red[k];
+    fcmp[k] = (float)((double)fs[k] - red[k]);  // value = fs - fcmp
+  }
   if (w < EW) {
 #pragma unroll
-    for (int k = 0; k <= kMaxPairKeys; ++k) red[k] = warp_sum(red[k]);
+    for (int k = 0; k <= kMaxPairKeys; ++k) gmerge<32>(fs[k], fcmp[k]);
   }
   if constexpr (EW > 1) {
-    __shared__ double s_red[kMaxPairKeys + 1][EW];
+    __shared__ float s_rs[kMaxPairKeys + 1][EW], s_rc[kMaxPairKeys + 1][EW];
     if (w < EW && lane == 0) {
 #pragma unroll
-      for (int k = 0; k <= kMaxPairKeys; ++k) s_red[k][w] = red[k];
+      for (int k = 0; k <= kMaxPairKeys; ++k) {
+        s_rs[k][w] = fs[k];
+        s_rc[k][w] = fcmp[k];
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-      for (int k = 0; k <= kMaxPairKeys; ++k) {
-        double t = s_red[k][0];
-        for (int q = 1; q < EW; ++q) t += s_red[k][q];
-        red[k] = t;
-      }
+      for (int k = 0; k <= kMaxPairKeys; ++k)
+        for (int q = 1; q < EW; ++q) {
+          const float s2 = s_rs[k][q], c2 = s_rc[k][q];
+          const float t = fs[k] + s2, bb = t - fs[k];
+          const float e = (fs[k] - (t - bb)) + (s2 - bb);
+          fcmp[k] = (fcmp[k] + c2) - e;
+          fs[k] = t;
+        }
     }
   }
   double out[kMaxPairKeys + 1];
-  if (!grid_finish<kMaxPairKeys + 1>(ctl, kPairSlot, red, out)) return;
+  if (!grid_finish_ff<kMaxPairKeys + 1>(ctl, kPairSlot, fs, fcmp, out)) return;
   if (ENERGY) {
 #pragma unroll
     for (int k = 0; k < kMaxPairKeys; ++k)
