@@ -106,6 +106,11 @@ static int auto_tpa(int rows, double mean_entries, bool prec) {
   else
     while (t < want && t < 32) t <<= 1;
   while (t > 1 && t > mean_entries / 2.0) t >>= 1;
+  // long rows: at most 32 entries per thread, so a thread's chain of dependent
+  // gathers stays short (the graphene side of morsec, about 150 Cu partners per
+  // row over 20,456 rows: 4 -> 8 threads per row took the moire step from 337 to
+  // 274 us with every list at 8)
+  while (t < 32 && mean_entries / t > 32.0) t <<= 1;
   return t;
 }
 

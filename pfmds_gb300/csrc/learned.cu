@@ -461,12 +461,21 @@ __global__ void __launch_bounds__(128) k_lforce(ListDev L, const DescPar* __rest
       if (r < d.rc_ang) {  // i is an angular partner of j: j's centre pass holds i's leg term
         const int rj = L.row_of[aj];
         const int nj = L.nnum[rj];
-        for (int q = 0; q < nj; ++q)
-          if (ent(L, rj, q) == ai) {
-            const float4 lg = leg[(size_t)q * L.stride + rj];
-            acc.add(-lg.x, -lg.y, -lg.z);
-            break;
-          }
+        // this atom's slot in j's row: eight entries a round, their loads issued
+        // together (each is its own cache line in the slot-major list)
+        int slot = -1;
+        for (int q0 = 0; q0 < nj && slot < 0; q0 += 8) {
+          int e[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) e[u] = q0 + u < nj ? ent(L, rj, q0 + u) : -1;
+#pragma unroll
+          for (int u = 7; u >= 0; --u)
+            if (e[u] == ai) slot = q0 + u;  // the first match of the round wins
+        }
+        if (slot >= 0) {
+          const float4 lg = leg[(size_t)slot * L.stride + rj];
+          acc.add(-lg.x, -lg.y, -lg.z);
+        }
       }
     }
     finish_force(A, E, ai, acc.get(0), acc.get(1), acc.get(2));
