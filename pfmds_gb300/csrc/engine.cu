@@ -99,17 +99,18 @@ static constexpr double kOuterTol = 1e-3;
 static int auto_tpa(int rows, double mean_entries, bool prec) {
   const double want = 152.0 * 32 * 32 / std::max(rows, 1);
   int t = 1;
-  // FP32 kernels are latency bound: the largest power of two within the target;
-  // FP64 kernels hide pipe latency with more threads: the smallest above it
+  // FP32 kernels: the power of two nearest the target (in ratio): 2 for the
+  // 65,536-row slab (target 2.4), 8 for the 20,456 graphene rows of the moire's
+  // morsec lists (target 7.6; every list at 8 took that step from 337 to 274 us,
+  // against 4); FP64 kernels hide pipe latency with more threads: the smallest
+  // power of two above the target
   if (prec)
-    while (2 * t <= want && t < 32) t <<= 1;
+    while (t < 32 && t * 1.4142135623730951 < want) t <<= 1;
   else
     while (t < want && t < 32) t <<= 1;
   while (t > 1 && t > mean_entries / 2.0) t >>= 1;
   // long rows: at most 32 entries per thread, so a thread's chain of dependent
-  // gathers stays short (the graphene side of morsec, about 150 Cu partners per
-  // row over 20,456 rows: 4 -> 8 threads per row took the moire step from 337 to
-  // 274 us with every list at 8)
+  // gathers stays short
   while (t < 32 && mean_entries / t > 32.0) t <<= 1;
   return t;
 }
