@@ -1008,10 +1008,18 @@ void Engine::tune_tpa() {
     std::vector<int> n(static_cast<size_t>(L.d.rows));
     CK(cudaMemcpyAsync(n.data(), L.nnum.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    // the mean over the rows that have entries: in a coupling list most rows
+    // can be empty (the Cu atoms below the surface layer of the moire) while
+    // the rest hold about 150 partners each
     double tot = 0;
-    for (int v : n) tot += v;
-    const int t = auto_tpa(L.d.rows, tot / static_cast<double>(n.size()), prec);
-    const int t1 = pass1_tpa(t, tot / static_cast<double>(n.size()), prec);
+    int filled = 0;
+    for (int v : n) {
+      tot += v;
+      filled += v > 0 ? 1 : 0;
+    }
+    const double mean = tot / std::max(filled, 1);
+    const int t = auto_tpa(L.d.rows, mean, prec);
+    const int t1 = pass1_tpa(t, mean, prec);
     if (t != L.d.tpa || t1 != L.d.tpa1) {
       L.d.tpa = t;
       L.d.tpa1 = t1;
