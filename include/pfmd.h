@@ -228,7 +228,7 @@ int pfmd_flush_l2(pfmd_ctx* ctx, long long bytes);
  * No reference counterpart: a per-atom network potential (32 radial + 16 angular
  * Behler-Parrinello symmetry functions, 48-64-64-1 with SiLU) standing in for the
  * tb and rjl interactions, trained on what the plain kernels compute; the
- * classical kernels remain its fallback and the judge of its error. */
+ * classical kernels remain its fallback and the check on its error. */
 
 /* Trains on frames of this context's own run (plain form only): `frames` times it
  * advances `stride` steps (md()'s loop), takes the per-atom tb and rjl energies and
