@@ -14,9 +14,17 @@ __device__ __forceinline__ void lj_row(const LT& L, const LJc<typename RT<PREC>:
 #pragma unroll 4
   for (int p = sub; p < n; p += TPA) {
     R dr[3];
-    const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, row, p)), B, dr));
+    const R r2 = T::d2(pi, T::load(A, ent(L, row, p)), B, dr);
+    // plain: r and 1/r from one reciprocal square root (no FP64 divide)
+    R r, ir;
+    if constexpr (PREC) {
+      r = xsqrt<PREC>(r2);
+      ir = xrcp<PREC>(r);
+    } else {
+      ir = rsqrt(r2);
+      r = r2 * ir;
+    }
     if (r < c.R2) {
-      const R ir = xrcp<PREC>(r);
       const R x = c.sig * ir, x2 = x * x, V = x2 * x2 * x2;
       R fc, dfc;
       fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
@@ -40,11 +48,18 @@ __device__ __forceinline__ void lj1g_row(const LT& L, const LJc<typename RT<PREC
     const int aj = ent(L, row, p);
     R dr[3];
     const R r2 = T::d2(pi, T::load(A, aj), B, dr);
-    const R r = xsqrt<PREC>(r2);
+    R r, invr2;
+    if constexpr (PREC) {
+      r = xsqrt<PREC>(r2);
+    } else {  // r and 1/r^2 from one reciprocal square root (no FP64 divide)
+      const R ir = rsqrt(r2);
+      r = r2 * ir;
+      invr2 = ir * ir;
+    }
     if (r < c.R2) {  // beyond R2 the clamped switch makes force and energy exactly zero
       R w = R(1);
       if (GENERAL) w = R((p < less ? 1 : 0) + (row < L.bnd[L.row_of[aj]] ? 1 : 0));
-      const R invr2 = xrcp<PREC>(r2);
+      if constexpr (PREC) invr2 = xrcp<PREC>(r2);
       const R U = invr2 * invr2 * invr2;
       R fcut, dfr;
       f_dfr_cut<R>(r, c.R1, c.R2, fcut, dfr);

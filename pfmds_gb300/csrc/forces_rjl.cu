@@ -71,7 +71,9 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
         ab.y = c.xi * (c.qr0 * fc - 0.5f * rdfc) * eq * ir;
         reinterpret_cast<float2*>(pair)[(size_t)p * L.stride + g.row] = ab;
       } else {
-        const R r = sqrt(r2);
+        // r and 1/r from one reciprocal square root (no FP64 divide: each FP64
+        // instruction costs a full warp's issue on this GPU's FP64 pipe)
+        const R ir = rsqrt(r2), r = r2 * ir;
         double2 ab = make_double2(0.0, 0.0);
         if (r <= c.R2) {
           R fc, dfc;
@@ -80,7 +82,6 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
           const R eq = xexp<PREC>(c.m2q * x), ep = xexp<PREC>(c.mp * x);
           eb2.add(eq * fc);
           if (ENERGY) er.add(ep * fc);
-          const R ir = xrcp<PREC>(r);
           ab.x = c.a2 * (c.pr0 * fc - dfc * r) * ep * ir;
           ab.y = c.xi * (c.qr0 * fc - dfc * R(0.5) * r) * eq * ir;
         }
