@@ -266,6 +266,9 @@ struct StepPlan {
   // half-update (nhc_ahead); the next step (nhc_done) launches no k_nhc for the
   // chain, and its kick-drift opens the step and applies both scales
   bool nhc_ahead = false, nhc_done = false;
+  // a log step inside the segment: its record's row in the device log ring,
+  // turned into the log line at the segment's end (-1: none)
+  int log_row = -1;
 };
 
 // Snapshot and trajectory files (md_read_write.f90:65-107) are formatted and
@@ -403,6 +406,10 @@ class Engine {
   void ensure_lists();
   Ctl* ctl = nullptr;
   Ctl* hctl = nullptr;  // pinned host copy (header part)
+  // log records of the log steps inside a segment (kLogCols doubles each)
+  DBuf<double> log_ring;
+  double* hlog = nullptr;  // pinned host copy
+  size_t log_cap = 0;      // rows
   size_t ctl_head = 0;
   // hctl equals the device's header: set by read_ctl, cleared when an API call
   // that may launch work starts (energies reads the copy while it holds)
@@ -497,7 +504,10 @@ class Engine {
   void plan_fusion();
   void refresh_mflag();
   void run_plans(const std::vector<StepPlan>& plans);
-  void host_events(const StepPlan& p);
+  void host_events(const StepPlan& p, bool log_line = true);
+  bool log_step(const StepPlan& p) const;
+  bool hard_event(const StepPlan& p) const;
+  void write_log_line(long long s, double t, const double* row);
   void get_state_host(std::vector<double>& p, std::vector<double>& v, std::vector<double>* f);
   void get_state_to(double* p, double* v, double* f);
   std::unique_ptr<FileWriter> writer;  // snapshot / trajectory files (opt.async_io)
@@ -515,6 +525,7 @@ Engine::~Engine() {
   if (log) std::fclose(log);
   if (ctl) cudaFree(ctl);
   if (hctl) cudaFreeHost(hctl);
+  if (hlog) cudaFreeHost(hlog);
   if (st) cudaStreamDestroy(st);
 }
 
@@ -1219,10 +1230,19 @@ StepPlan Engine::plan(long long s) const {
   return p;
 }
 
-bool Engine::is_event(const StepPlan& p) const {
+bool Engine::is_event(const StepPlan& p) const { return log_step(p) || hard_event(p); }
+
+bool Engine::log_step(const StepPlan& p) const {
+  const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
+  return log && p.step % I.period_log == 0;
+}
+
+// Events that need the host between steps (output block, files, the learned
+// form's check).  A log line does not: log steps record their values on the
+// device and the lines are written at the segment's end, in step order.
+bool Engine::hard_event(const StepPlan& p) const {
   const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
   if (learned_active && check_period > 0 && p.step > 0 && p.step % check_period == 0) return true;
-  if (log && p.step % I.period_log == 0) return true;
   if (p.out) return true;
   if (opt.write_files && p.step % I.period_snapshot == 0 && p.step != 0) return true;
   if (opt.write_files && p.step % S.period_traj == 0) return true;
@@ -1604,6 +1624,7 @@ void Engine::enqueue_step(const StepPlan& p) {
   if (p.energy)
     launch_energy_finalize(gref(S.all_moving), static_cast<int>(inters.size()), static_cast<int>(S.nhc.size()),
                            nvt ? 1 : 0, A, ctl, st);
+  if (p.log_row >= 0) launch_log_row(ctl, log_ring.p + static_cast<size_t>(p.log_row) * kLogCols, st);
   if (p.out) {
     launch_out_reduce(gall, A, ctl, st);
     CK(cudaMemsetAsync(ctl->maxnnum, 0, sizeof(int) * PFMD_MAX_LISTS, st));
@@ -1619,6 +1640,9 @@ static std::string plan_key(const StepPlan& p) {
   k.push_back(static_cast<char>('a' + (p.drift_next ? 1 : 0) + 2 * (p.drifted ? 1 : 0) + 4 * (p.nhc_defer ? 1 : 0) +
                                 8 * (p.nhc_ahead ? 1 : 0)));
   k.push_back(p.nhc_done ? 'd' : '-');
+  // (a log step's row is its rank among the segment's log steps, which the
+  // key's earlier steps fix)
+  k.push_back(p.log_row >= 0 ? 'L' : '-');
   for (char r : p.rebuild) k.push_back(r ? '1' : '0');
   k.push_back('|');
   return k;
@@ -1758,19 +1782,34 @@ std::string Engine::nlists_load_text() {  // md_interactions.f90:427-444
 
 // Host work after an event step: log line, output block, snapshot, trajectory
 // (md_simulation.f90:204-241).
-void Engine::host_events(const StepPlan& p) {
+// The log line (A6,i9,7f24.6 then the interactions' and chains' energies,
+// md_simulation.f90:204-207) of step s at simulation time t from a log record.
+void Engine::write_log_line(long long s, double t, const double* row) {
+  fortio::Rec r;
+  r.a(fortio::trim(integrator_name), 6).i(s, 9);
+  r.f(t, 24, 6).f(row[0], 24, 6).f(row[1], 24, 6).f(row[2], 24, 6).f(row[3], 24, 6);
+  r.f(row[4], 24, 6).f(row[5], 24, 6);
+  for (size_t k = 0; k < inters.size(); ++k) r.f(row[6 + k], 20, 9);
+  for (size_t k = 0; k < S.nhc.size(); ++k) r.f(row[6 + kLogInter + k], 20, 9);
+  std::string line = r.s + "\n";
+  std::fputs(line.c_str(), log);
+}
+
+void Engine::host_events(const StepPlan& p, bool log_line) {
   const long long s = p.step;
   const auto& I = S.integrators[static_cast<size_t>(integrator_index - 1)];
   const Ctl& c = *hctl;
-  if (log && s % I.period_log == 0) {
-    fortio::Rec r;
-    r.a(fortio::trim(integrator_name), 6).i(s, 9);
-    r.f(sim_time, 24, 6).f(c.conserved, 24, 6).f(c.e_nhc, 24, 6).f(c.total, 24, 6).f(c.pe_last, 24, 6);
-    r.f(c.ke, 24, 6).f(c.temperature, 24, 6);
-    for (size_t k = 0; k < inters.size(); ++k) r.f(c.e_inter[k], 20, 9);
-    for (size_t k = 0; k < S.nhc.size(); ++k) r.f(c.nhc[k].e, 20, 9);
-    std::string line = r.s + "\n";
-    std::fputs(line.c_str(), log);
+  if (log_line && log && s % I.period_log == 0) {
+    double row[kLogCols];
+    row[0] = c.conserved;
+    row[1] = c.e_nhc;
+    row[2] = c.total;
+    row[3] = c.pe_last;
+    row[4] = c.ke;
+    row[5] = c.temperature;
+    for (int k = 0; k < kLogInter; ++k) row[6 + k] = c.e_inter[k];
+    for (int k = 0; k < kLogChains; ++k) row[6 + kLogInter + k] = c.nhc[k].e;
+    write_log_line(s, sim_time, row);
   }
   if (p.out) {
     const double fs = std::sqrt(c.red[0] * c.red[0] + c.red[1] * c.red[1] + c.red[2] * c.red[2]);
@@ -1861,8 +1900,21 @@ void Engine::advance(long long max_steps, int* fin) {
       if (t != s && switch_needed(t)) break;
       plans.push_back(plan(t));
       need_check_all = false;  // only the first planned step runs the full check
-      if (is_event(plans.back()) || plans.size() >= seg_cap || done + static_cast<long long>(plans.size()) >= max_steps)
+      if (hard_event(plans.back()) || plans.size() >= seg_cap ||
+          done + static_cast<long long>(plans.size()) >= max_steps)
         break;
+    }
+    // log steps record their values on the device; the lines follow at the end
+    int log_rows = 0;
+    for (auto& p : plans)
+      if (log_step(p)) p.log_row = log_rows++;
+    if (static_cast<size_t>(log_rows) > log_cap) {
+      log_cap = static_cast<size_t>(log_rows);
+      log_ring.alloc(log_cap * kLogCols);
+      clear_graphs();  // captured segments hold the old ring's address
+      if (hlog) cudaFreeHost(hlog);
+      hlog = nullptr;
+      CK(cudaMallocHost(&hlog, sizeof(double) * log_cap * kLogCols));
     }
     need_check_all = plans.front().check_all;
     // each force kernel also runs the next step's kick and drift when both steps
@@ -1888,7 +1940,21 @@ void Engine::advance(long long max_steps, int* fin) {
         }
       }
     run_plans(plans);
+    if (log_rows > 0)
+      CK(cudaMemcpyAsync(hlog, log_ring.p, sizeof(double) * static_cast<size_t>(log_rows) * kLogCols,
+                         cudaMemcpyDeviceToHost, st));
     read_ctl();
+    if (log_rows > 0) {
+      // the log lines of the steps that completed (a stop inside the segment
+      // ends it at err_step), with the simulation time of each
+      const long long done_to = (hctl->error || hctl->converged) ? hctl->err_step : plans.back().step + 1;
+      double t = sim_time;
+      for (const auto& p : plans) {
+        if (p.step >= done_to) break;
+        if (p.step != 0) t = t + ts[0];
+        if (p.log_row >= 0) write_log_line(p.step, t, hlog + static_cast<size_t>(p.log_row) * kLogCols);
+      }
+    }
     if (hctl->error) raise_device_error();
     if (!tpa_tuned) tune_tpa();
     const long long executed_to = hctl->converged ? hctl->err_step : plans.back().step + 1;
@@ -1903,8 +1969,8 @@ void Engine::advance(long long max_steps, int* fin) {
     }
     md_step = plans.back().step + 1;
     done += static_cast<long long>(plans.size());
-    if (is_event(plans.back())) {
-      host_events(plans.back());
+    if (hard_event(plans.back())) {
+      host_events(plans.back(), plans.back().log_row < 0);
       const long long ls = plans.back().step;
       if (learned_active && check_period > 0 && ls > 0 && ls % check_period == 0) learned_check(true);
     }

@@ -521,6 +521,23 @@ void launch_zero_momentum(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStrea
   { k_momentum<<<red_grid(g.cap), kRedThreads, 0, s>>>(g, A, ctl); ++g_kernel_launches; }
   if (g.cap > 0) { k_sub_velocity<<<nb(g.cap, 256), 256, 0, s>>>(g, A, ctl); ++g_kernel_launches; }
 }
+__global__ void k_log_row(const Ctl* ctl, double* row) {
+  const int t = threadIdx.x;
+  if (t < kLogInter) row[6 + t] = ctl->e_inter[t];
+  if (t < kLogChains) row[6 + kLogInter + t] = ctl->nhc[t].e;
+  if (t == 0) {
+    row[0] = ctl->conserved;
+    row[1] = ctl->e_nhc;
+    row[2] = ctl->total;
+    row[3] = ctl->pe_last;
+    row[4] = ctl->ke;
+    row[5] = ctl->temperature;
+  }
+}
+void launch_log_row(const Ctl* ctl, double* row, cudaStream_t s) {
+  k_log_row<<<1, 32, 0, s>>>(ctl, row);
+  ++g_kernel_launches;
+}
 void launch_energy_finalize(const GroupRef& moving, int n_inter, int n_nhc, int nvt, const Atoms& A, Ctl* ctl,
                             cudaStream_t s) {
   { k_energy_finalize<<<red_grid(moving.cap), kRedThreads, 0, s>>>(moving, n_inter, n_nhc, nvt, A, ctl); ++g_kernel_launches; }

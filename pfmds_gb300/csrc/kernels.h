@@ -303,6 +303,13 @@ void launch_zero_forces(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_
 void launch_zero_momentum(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
 // energies at log/out/nvms steps: KE and temperature of the all-moving group,
 // Nose-Hoover energies (when nvt), potential/total/conserved sums
+// One log record's values (the log line of md_simulation.f90:204-207) copied
+// from the control block into row: conserved, chain energy, total, potential,
+// kinetic, temperature, the interactions' energies (kLogInter), the chains'
+// energies (kLogChains).  Log steps inside a segment write rows that the host
+// turns into log lines at the segment's end.
+constexpr int kLogInter = PFMD_MAX_INTER, kLogChains = PFMD_MAX_NHC, kLogCols = 6 + kLogInter + kLogChains;
+void launch_log_row(const Ctl* ctl, double* row, cudaStream_t s);
 void launch_energy_finalize(const GroupRef& moving, int n_inter, int n_nhc, int nvt, const Atoms& A,
                             Ctl* ctl, cudaStream_t s);
 // output-block sums: force sum, mass-weighted position and velocity sums and the
