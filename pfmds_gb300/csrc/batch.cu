@@ -724,7 +724,11 @@ __device__ void phase_energy(const Dev& D, long long s) {
 // rebuild when s % period == 0; rjl density; forces and (s > 0) the second
 // half-kick; energies when s % energy_period == 0 (history rows) and at the
 // launch's last step (e_pot / e_kin only).
-__global__ void __launch_bounds__(kThreads) k_batch(Dev D, int nsteps) {
+// Four blocks per SM: the register cap this implies (64) holds the kernel
+// without spills, where the compiler's own choice (80 registers, 140 bytes of
+// spills, three blocks per SM) ran the 512-replica batch at 5.3-5.5 ms per MD
+// step against 4.4-4.5.
+__global__ void __launch_bounds__(kThreads, 4) k_batch(Dev D, int nsteps) {
   const long long s0 = *D.step;
   for (int it = 0; it < nsteps; ++it) {
     const long long s = s0 + it;

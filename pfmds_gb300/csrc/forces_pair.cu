@@ -177,8 +177,12 @@ void launch_lj1g(bool prec, bool energy, bool general, const ListDev& L, const L
 // warp's FP64 instructions serve 32 atoms instead of 32 / TPA.  Energies (per
 // interaction) and the chain's kinetic energy go through one grid reduction;
 // its last block stores the energies and updates the chain.
+// Register budgets by resident blocks per SM: the precision variants at three
+// (80 registers, no spills, where the compiler's own choice of 64 registers
+// spilled 536 bytes: the 4,000-atom gas step 34.3 us against 32.8), the plain
+// variants at two (at most 128 registers, as the 106 they took before).
 template <bool PREC, bool ENERGY, int TPA>
-__global__ void __launch_bounds__(256) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
+__global__ void __launch_bounds__(256, PREC ? 3 : 2) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
                                                     double ts2, double ts3, double ts4, int ahead) {
   using T = RT<PREC>;
   asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
