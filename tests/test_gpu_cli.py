@@ -120,3 +120,22 @@ def test_precision_switches(tmp_path, built):
             _same_text(keep(out), keep(out0), name + " stdout", **tol)
         for f in files:
             _same_text(open(d / f).read(), open(d0 / f).read(), name + " " + f, **tol)
+
+
+def test_log_lines_written_at_segment_end_match(tmp_path, built):
+    # log steps inside a device segment record their values on the device and
+    # the lines are written when the segment ends; here no other event ends a
+    # segment before the nvms exit, so the log of nvt, nve and the nvms stage up
+    # to its exit comes from those records
+    a, b = tmp_path / "gpu", tmp_path / "cpu"
+    configs.lj_gas(str(a), n_a=60, n_b=60, box=18.0, min_sep=2.8, ms_de=1e-2,
+                   integrators=[("nvt", 0.5, 30, 10 ** 8, 5), ("nve", 0.5, 30, 10 ** 8, 5),
+                                ("nvms", 0.5, 200, 10 ** 8, 5)])
+    shutil.copytree(a, b)
+    args = ["-i", "md_run_settings.txt", "-op", "1000000", "-omp_n", "4"]
+    out_a = _run(pf.EXE_PATH, a, args)
+    out_b = _run(ORACLE_EXE, b, args)
+    _same_text(out_a, out_b, "stdout")
+    la, lb = open(a / "md_run.log").read(), open(b / "md_run.log").read()
+    assert la.count("\n") > 12  # log lines of all three stages
+    _same_text(la, lb, "md_run.log", atol=2e-6, rtol=0)
