@@ -357,6 +357,68 @@ def batched_config(root, device, steps, n_rep=512, window=5000):
         "input_generation_s": t_gen}
 
 
+def gr_cu_list_config(root, device, n_entries=16, steps=2000, streams=16):
+    """A settings list of graphene/Cu systems (tb, rjl, morsec; 600-3,360 atoms,
+    nvt), the kind of entry the persistent batched kernel does not take, through
+    run_md_simulation -ilist -batch: one entry at a time (-streams 1) and
+    `streams` entries at a time, each an independent md() on its own host thread,
+    stream and graphs.  Wall-clock time of the whole list run, set-up, file
+    reading and writing included; the two runs' all_out records and log files
+    must be identical."""
+    import pfmds_gb300 as pf
+    from pfmds_gb300 import configs
+    d = os.path.join(root, "grlist")
+    os.makedirs(d, exist_ok=True)
+    sizes = [(10, 6, 9, 5), (16, 10, 14, 8), (20, 12, 18, 10), (24, 14, 21, 12)]
+    names, atoms = [], 0
+    for k in range(n_entries):
+        gx, gy, cx, cy = sizes[k % len(sizes)]
+        xyz, sname = f"gr{k}.xyz", f"s_gr{k}.txt"
+        configs.gr_on_cu(d, n_gx=gx, n_gy=gy, n_cx=cx, n_cy=cy, seed=100 + k, steps=steps, log_period=1000,
+                         integrator="nvt", xyz_name=xyz, settings_name=sname)
+        with open(os.path.join(d, xyz)) as f:
+            atoms += int(f.readline())
+        names.append(sname)
+    with open(os.path.join(d, "list.txt"), "w") as f:
+        f.write(f"{len(names)}\n")
+        for k, n in enumerate(names):
+            f.write(f"{n} p{k + 1}_\n")
+    out = {}
+    for s in (1, streams):
+        o = os.path.join(d, f"out{s}") + "/"
+        os.makedirs(o, exist_ok=True)
+        args = ["-ipath", d + "/", "-ilist", "list.txt", "-opath", o, "-ofile", "all_out.txt", "-batch",
+                "-form", "precision", "-device", str(device), "-streams", str(s)]
+        sys.stdout.flush()
+        saved = os.dup(1)
+        null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(null, 1)  # the command line's own banner and per-entry blocks
+        try:
+            t0 = time.perf_counter()
+            rc = pf.run_md_simulation(args)
+            wall = time.perf_counter() - t0
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+            os.close(null)
+        if rc != 0:
+            raise RuntimeError(f"list run with -streams {s} returned {rc}")
+        files = {}
+        for fn in sorted(os.listdir(o)):
+            if fn == "all_out.txt" or fn.endswith("md_run.log"):
+                with open(os.path.join(o, fn)) as f:
+                    files[fn] = f.read().replace(o, "")  # all_out's records name the output prefix
+        out[s] = (wall, files)
+    w1, f1 = out[1]
+    wn, fn_ = out[streams]
+    return {"workload": f"{n_entries} graphene/Cu entries (tb, rjl, morsec; 600-3,360 atoms, nvt), {atoms} atoms, "
+                        f"{steps} steps each, run_md_simulation -ilist -batch, precision form",
+            "unit": "atom-steps/s (wall clock of the whole list run)",
+            "one_at_a_time": {"value": atoms * steps / w1, "wall_s": w1},
+            "concurrent": {"streams": streams, "value": atoms * steps / wn, "wall_s": wn},
+            "speedup": w1 / wn, "identical_outputs": f1 == fn_ and len(f1) == n_entries + 1}
+
+
 def learned_config(root, device, frames=500, run_steps=20000):
     """The learned form: networks for the tb (C) and rjl (Cu) interactions trained
     online on plain-form runs of a graphene/Cu(111) system at 300, 700, 1,200 and
@@ -695,6 +757,8 @@ def run_ours(args):
         extra = other_configs(d, device) if (rank == 0 and not args.no_extra) else None
         if extra is not None and args.batch_steps > 0:
             extra["batched_512"] = batched_config(d, device, args.batch_steps)
+        if extra is not None:
+            extra["gr_cu_list"] = gr_cu_list_config(d, device)
         if extra is not None and args.learned_steps > 0:
             extra["learned"] = learned_config(d, device, frames=args.learned_frames, run_steps=args.learned_steps)
 

@@ -4,12 +4,18 @@
 // implementation: -form plain|precision (arithmetic form), -graphs 0|1,
 // -device n, and -batch, which runs the entries of a list that the batched
 // kernel takes as batches on it (pfmd_batch_run_list: the same files per entry;
-// no per-step output blocks) and the others one by one, as list mode does.
+// no per-step output blocks) and the others (graphene/Cu, nvms, several chains)
+// as independent md() runs, -streams n of them at a time (default 16), each on
+// its own host thread with its own stream and graphs; their standard output is
+// held and written in list order, as list mode writes it.
 #include <unistd.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <map>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -26,6 +32,7 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
   std::string settings_files_list, settings_filename = "md_run_settings.txt", all_out_file = "all_out.txt",
                                    output_prefix, input_path, out_path;
   bool batched = false;
+  int streams = 16;
   std::string banner;
   auto say = [&](const std::string& s) {
     std::fputs((s + "\n").c_str(), stdout);
@@ -75,6 +82,9 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
         o.async_io = static_cast<int>(fortio::to_int(next()));
       } else if (arg == "-batch") {
         batched = true;
+      } else if (arg == "-streams") {
+        streams = static_cast<int>(fortio::to_int(next()));
+        if (streams < 1) streams = 1;
       }
     } catch (const std::exception& e) {
       std::fprintf(stderr, "%s\n", e.what());
@@ -158,22 +168,61 @@ extern "C" int pfmd_run_md_simulation(int argc, const char* const* argv) {
       std::fclose(tmp);
       if (rc != PFMD_OK) return rc;
     }
-    for (size_t k : single) {
-      const std::string prefix = fortio::trim(out_path) + entries[k].second;
+    // The other entries are independent md() runs (run_md_simulation_mpi.f90:74-85
+    // gives each its own rank): up to `streams` at a time, each on a host thread
+    // with its own engine, stream and graphs, so that small systems fill the GPU
+    // together.  No new entry starts after one has failed; the output stops at
+    // the first failed entry in list order, as in a one-by-one run.
+    struct Single {
+      std::string prefix, text;
+      int rc = PFMD_OK;
+      bool ran = false;
+    };
+    std::vector<Single> sg(single.size());
+    std::atomic<size_t> next_j{0};
+    std::atomic<bool> failed{false};
+    auto worker = [&] {
+      for (size_t j; !failed.load() && (j = next_j.fetch_add(1)) < single.size();) {
+        const size_t k = single[j];
+        Single& s = sg[j];
+        s.ran = true;
+        s.prefix = fortio::trim(out_path) + entries[k].second;
+        FILE* cap = std::tmpfile();
+        FILE* rec = std::tmpfile();
+        if (cap && rec) {
+          pfmd_options oj = o;
+          oj.output_prefix = s.prefix.c_str();
+          oj.out_fd = fileno(cap);
+          oj.all_out_fd = fileno(rec);
+          s.rc = pfmd_md(input_path.c_str(), entries[k].first.c_str(), &oj);
+          std::fflush(cap);
+          std::fflush(rec);
+          s.text = read_back(cap);
+          recs[k] = read_back(rec);
+          while (!recs[k].empty() && recs[k].back() == '\n') recs[k].pop_back();
+        } else {
+          s.rc = PFMD_E_IO;
+        }
+        if (cap) std::fclose(cap);
+        if (rec) std::fclose(rec);
+        if (s.rc != PFMD_OK) failed.store(true);
+      }
+    };
+    {
+      std::vector<std::thread> th;
+      const size_t nt = std::min(single.size(), static_cast<size_t>(streams));
+      for (size_t t = 0; t < nt; ++t) th.emplace_back(worker);
+      for (auto& t : th) t.join();
+    }
+    for (size_t j = 0; j < single.size(); ++j) {
+      const size_t k = single[j];
+      const Single& s = sg[j];
+      if (!s.ran) return PFMD_E_IO;  // not started: an earlier entry failed
       say(line);
-      say(Rec().i(static_cast<long long>(k + 1), 6).a("\t").a(entries[k].first, 32, 128).a(prefix, 32, 128).s);
-      std::fflush(stdout);
-      FILE* tmp = std::tmpfile();
-      if (!tmp) return PFMD_E_IO;
-      o.output_prefix = prefix.c_str();
-      o.all_out_fd = fileno(tmp);
-      rc = pfmd_md(input_path.c_str(), entries[k].first.c_str(), &o);
-      std::fflush(tmp);
-      recs[k] = read_back(tmp);
-      while (!recs[k].empty() && recs[k].back() == '\n') recs[k].pop_back();
-      std::fclose(tmp);
+      say(Rec().i(static_cast<long long>(k + 1), 6).a("\t").a(entries[k].first, 32, 128).a(s.prefix, 32, 128).s);
+      std::fputs(s.text.c_str(), stdout);
       say(line);
-      if (rc != PFMD_OK) return rc;
+      if (s.rc != PFMD_OK) return s.rc;
     }
     FILE* all_out = std::fopen((out_path + all_out_file).c_str(), "w");
     if (!all_out) return PFMD_E_IO;

@@ -5,10 +5,12 @@ entry of a settings list through md(); the oracle runs them one by one in FP64).
   with one Nose-Hoover chain each, stepped together by the persistent kernel,
   against the oracle's run of each settings file: positions, velocities, the
   energies and the chain's energy after 60 steps.
-* run_md_simulation -ilist -batch on a mixed list -- those four entries plus a
-  graphene/Cu entry (tb, rjl, morsec) that the batched kernel does not take and
-  that runs on its own -- against the oracle's -ilist run: every log record,
-  the closing records in all_out and the final .xyz files, field by field.
+* run_md_simulation -ilist -batch on a mixed list -- those four entries plus
+  two graphene/Cu entries (tb, rjl, morsec; nvt and nve) that the batched kernel
+  does not take and that run as concurrent md() calls -- against the oracle's
+  -ilist run: every log record, the closing records in all_out and the final
+  .xyz files, field by field; and against the same list run with -streams 1
+  (one entry at a time), byte for byte.
 The precision form's FP32 pair terms set the tolerances."""
 import os
 import re
@@ -99,18 +101,29 @@ def test_mixed_list_cli_matches_oracle(tmp_path, built, monkeypatch):
     names = _entries(d)
     configs.gr_on_cu(d, n_gx=6, n_gy=4, n_cx=6, n_cy=3, layers=3, steps=STEPS, log_period=10, integrator="nvt",
                      xyz_name="gr.xyz", settings_name="s_gr.txt")
+    configs.gr_on_cu(d, n_gx=8, n_gy=4, n_cx=7, n_cy=3, layers=3, seed=9, steps=STEPS, log_period=10,
+                     integrator="nve", xyz_name="gr2.xyz", settings_name="s_gr2.txt")
     names.insert(2, "s_gr.txt")
-    assert not pf.batch_accepts(d, "s_gr.txt")[0]
+    names.append("s_gr2.txt")
+    assert not pf.batch_accepts(d, "s_gr.txt")[0] and not pf.batch_accepts(d, "s_gr2.txt")[0]
     lst = _write_list(d, names)
     outs = {}
-    for who in ("gpu", "oracle"):
+    for who in ("gpu", "gpu_one_stream", "oracle"):
         o = str(tmp_path / who)
         os.makedirs(o)
-        monkeypatch.chdir(o)  # the same output prefixes in both all_out files
+        monkeypatch.chdir(o)  # the same output prefixes in every all_out file
         args = ["-ipath", d + "/", "-ilist", lst, "-ofile", "all_out.txt"]
-        rc = pf.run_md_simulation(args + ["-batch", "-form", "precision"]) if who == "gpu" else oracle_cli(args)
+        if who == "oracle":
+            rc = oracle_cli(args)
+        else:
+            rc = pf.run_md_simulation(args + ["-batch", "-form", "precision"] +
+                                      (["-streams", "1"] if who == "gpu_one_stream" else []))
         assert rc == 0, who
         outs[who] = o
+    for f in sorted(os.listdir(outs["gpu_one_stream"])):
+        if f.endswith((".txt", ".log", ".xyz")):
+            assert open(os.path.join(outs["gpu"], f)).read() == \
+                open(os.path.join(outs["gpu_one_stream"], f)).read(), f
     _compare_text(open(os.path.join(outs["gpu"], "all_out.txt")).read(),
                   open(os.path.join(outs["oracle"], "all_out.txt")).read(), "all_out")
     for k, n in enumerate(names):
