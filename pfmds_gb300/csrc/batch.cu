@@ -488,7 +488,7 @@ __device__ void tile_force(const Dev& D, const Tile& t, bool kick, bool energy, 
           if (r < c.R2) {
             const float invr2 = ir * ir, U = invr2 * invr2 * invr2;
             float fcut, dfr;
-            f_dfr_cut<float>(r, c.R1, c.R2, fcut, dfr);
+            f_dfr_cut<float>(r, c.R1, c.R2, c.inv_w, fcut, dfr);
             const float F = U * invr2 * ((c.c12t12 * U - c.c6t6) * fcut - (c.c12 * U - c.c6) * dfr);
             acc.add(-F * dr[0], -F * dr[1], -F * dr[2]);
             if (energy && aj < a) e[si].add(U * (c.c12 * U - c.c6) * fcut);

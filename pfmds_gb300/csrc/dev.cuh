@@ -253,6 +253,33 @@ __device__ __forceinline__ void fdfcut_cos(double r, double R1, double R2, doubl
     df = 0.0;
   }
 }
+// The same switch for the FP64 kernels without FP64 divides (each a
+// multi-instruction sequence on this GPU's narrow FP64 pipe): the argument as
+// (r - R1) inv_w with inv_w = 1/(R2 - R1) formed on the host, f'/r through the
+// caller's 1/r, and sin and cos of pi_t x as sincospi of x pi_t/pi (its
+// reduction is exact).  The results differ from the divided form in the last
+// bits only.
+constexpr double kPiTruncOverPi = PFMD_PI_TRUNC / 3.14159265358979323846;
+__device__ __forceinline__ double fcut_cos_w(double r, double R1, double R2, double inv_w) {
+  if (r < R1) return 1.0;
+  if (r < R2) return (1.0 + cospi((r - R1) * inv_w * kPiTruncOverPi)) * 0.5;
+  return 0.0;
+}
+__device__ __forceinline__ void fdfcut_cos_w(double r, double ir, double R1, double R2, double inv_w, double& f,
+                                             double& df) {
+  if (r < R1) {
+    f = 1.0;
+    df = 0.0;
+  } else if (r < R2) {
+    double s, c;
+    sincospi((r - R1) * inv_w * kPiTruncOverPi, &s, &c);
+    f = (1.0 + c) * 0.5;
+    df = -s * (0.5 * PFMD_PI_TRUNC) * inv_w * ir;
+  } else {
+    f = 0.0;
+    df = 0.0;
+  }
+}
 __device__ __forceinline__ void fdfcut_cos_f(float r, float R1, float R2, float inv_w, float& f, float& df) {
   if (r < R1) {
     f = 1.0f;
@@ -292,12 +319,13 @@ __device__ __forceinline__ double fcut_poly(double r, double R1, double R2) {
   if (r <= R1) return 1.0;
   return 0.0;
 }
-// cut_off_poly.f90:30-43 (dfr lacks 1/(R2-R1), as in the reference)
+// cut_off_poly.f90:30-43 (dfr lacks 1/(R2-R1), as in the reference); x as
+// (t - R1) inv_w with inv_w = 1/(R2 - R1) formed on the host (no divide)
 template <class T>
-__device__ __forceinline__ void f_dfr_cut(T r, T R1, T R2, T& f, T& dfr) {
+__device__ __forceinline__ void f_dfr_cut(T r, T R1, T R2, T inv_w, T& f, T& dfr) {
   T t = r < R1 ? R1 : r;
   t = t > R2 ? R2 : t;
-  T x = (t - R1) / (R2 - R1);
+  T x = (t - R1) * inv_w;
   T x2 = x * x;
   f = T(1) + x2 * x * (T(-10) + T(15) * x - T(6) * x2);
   dfr = t * x2 * (T(-30) + T(60) * x - T(30) * x2);

@@ -145,7 +145,17 @@ __device__ __forceinline__ void fdfc(typename RT<PREC>::R r, typename RT<PREC>::
   if constexpr (PREC)
     fdfcut_cos_f(r, R1, R2, inv_w, f, df);
   else
-    fdfcut_cos(r, R1, R2, f, df);
+    fdfcut_cos_w(r, 1.0 / r, R1, R2, inv_w, f, df);
+}
+// The same with the caller's 1/r (the FP64 form then divides nowhere).
+template <bool PREC>
+__device__ __forceinline__ void fdfc(typename RT<PREC>::R r, typename RT<PREC>::R ir, typename RT<PREC>::R R1,
+                                     typename RT<PREC>::R R2, typename RT<PREC>::R inv_w, typename RT<PREC>::R& f,
+                                     typename RT<PREC>::R& df) {
+  if constexpr (PREC)
+    fdfcut_cos_f(r, R1, R2, inv_w, f, df);
+  else
+    fdfcut_cos_w(r, ir, R1, R2, inv_w, f, df);
 }
 template <bool PREC>
 __device__ __forceinline__ typename RT<PREC>::R fc_only(typename RT<PREC>::R r, typename RT<PREC>::R R1,
@@ -155,7 +165,7 @@ __device__ __forceinline__ typename RT<PREC>::R fc_only(typename RT<PREC>::R r, 
     if (r < R2) return (1.0f + __cosf(3.14159265358979f * (r - R1) * inv_w)) * 0.5f;
     return 0.0f;
   } else {
-    return fcut_cos(r, R1, R2);
+    return fcut_cos_w(r, R1, R2, inv_w);
   }
 }
 template <bool PREC>

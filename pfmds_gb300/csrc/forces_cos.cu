@@ -16,10 +16,10 @@ __device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r
   const auto& c = cst<PREC>(P);
   const R R1 = c.R1, R2 = c.R2, delt = c.delt, inv_w = c.inv_w;
   const R nd = nv[0] * dr[0] + nv[1] * dr[1] + nv[2] * dr[2];
+  const R ir = xrcp<PREC>(r);  // the one divide of the pair (FP64 divides are long sequences)
   R fc, dfc;
-  fdfc<PREC>(r, R1, R2, inv_w, fc, dfc);
+  fdfc<PREC>(r, ir, R1, R2, inv_w, fc, dfc);
   if (!MORSE) {
-    const R ir = xrcp<PREC>(r);
     const R x = c.sig * ir, x2 = x * x, V2 = x2 * x2 * x2, V1 = V2 * V2;
     const R V3 = xpow<PREC>(fabs(nd) * ir, delt);
     X = (R(12) * V1 - (R(6) + delt) * V2 * V3) * (ir * ir) * fc - (V1 - V2 * V3) * dfc;
@@ -28,8 +28,8 @@ __device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r
   } else {
     const R a = c.a;
     const R V2 = xexp<PREC>(-a * (r - c.r0)), V1 = V2 * V2;
-    const R V3 = xpow<PREC>(metal ? fabs(nd) / (nnorm * r) : fabs(nd) / r, delt);
-    X = R(2) * (a * V1 - (a + delt / r) * V2 * V3) / r * fc - (V1 - R(2) * V2 * V3) * dfc;
+    const R V3 = xpow<PREC>(metal ? fabs(nd) * ir / nnorm : fabs(nd) * ir, delt);
+    X = R(2) * (a * V1 - (a + delt * ir) * V2 * V3) * ir * fc - (V1 - R(2) * V2 * V3) * dfc;
     Y = R(2) * delt * V2 * V3 / nd * fc;
     E = (V1 - R(2) * V2 * V3) * fc;
   }

@@ -27,7 +27,7 @@ __device__ __forceinline__ void lj_row(const LT& L, const LJc<typename RT<PREC>:
     if (r < c.R2) {
       const R x = c.sig * ir, x2 = x * x, V = x2 * x2 * x2;
       R fc, dfc;
-      fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
+      fdfc<PREC>(r, ir, c.R1, c.R2, c.inv_w, fc, dfc);
       const R k = c.eps4 * (V * (R(12) * V - R(6)) * (ir * ir) * fc - V * (V - R(1)) * dfc);
       acc.add(-k * dr[0], -k * dr[1], -k * dr[2]);
       if (ENERGY) e.add(c.eps4 * V * (V - R(1)) * fc);
@@ -62,7 +62,7 @@ __device__ __forceinline__ void lj1g_row(const LT& L, const LJc<typename RT<PREC
       if constexpr (PREC) invr2 = xrcp<PREC>(r2);
       const R U = invr2 * invr2 * invr2;
       R fcut, dfr;
-      f_dfr_cut<R>(r, c.R1, c.R2, fcut, dfr);
+      f_dfr_cut<R>(r, c.R1, c.R2, c.inv_w, fcut, dfr);
       const R F = w * (U * invr2 * ((c.c12t12 * U - c.c6t6) * fcut - (c.c12 * U - c.c6) * dfr));
       acc.add(-F * dr[0], -F * dr[1], -F * dr[2]);
       // the half list p <= lessnnum(i); in a row kept in cell order (groups in

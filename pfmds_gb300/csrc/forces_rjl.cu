@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) k_rjl_density(ListDev L, RJLPar P, Atoms 
         double2 ab = make_double2(0.0, 0.0);
         if (r <= c.R2) {
           R fc, dfc;
-          fdfc<PREC>(r, c.R1, c.R2, c.inv_w, fc, dfc);
+          fdfc<PREC>(r, ir, c.R1, c.R2, c.inv_w, fc, dfc);
           const R x = r * c.inv_r0 - R(1);
           const R eq = xexp<PREC>(c.m2q * x), ep = xexp<PREC>(c.mp * x);
           eb2.add(eq * fc);
