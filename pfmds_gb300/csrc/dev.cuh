@@ -164,12 +164,21 @@ struct Box {
 // ---------------------------------------------------------------------------
 // minimum image
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double sgn1(double x) { return copysign(1.0, x); }
 
-// d - h*(sign(1,d-h)+sign(1,d+h)), rounded exactly as written.
+// d - h*(sign(1,d-h)+sign(1,d+h)), rounded exactly as written.  The sum of
+// signs is 2 when d >= h, -2 when d < -h and 0 otherwise (a rounded d -+ h is
+// zero only when exactly zero, and otherwise keeps its sign), and h*2 is exact,
+// so the expression is d - 2h, d + 2h or d itself, bit for bit.  The two
+// comparisons run on the doubles' bit patterns as integers (h > 0: the order of
+// non-negative doubles is that of their patterns), which leaves one FP64 add per
+// axis on this GPU's narrow FP64 pipe instead of five operations.
 __device__ __forceinline__ double mi_axis_exact(double d, double h) {
-  double s = __dadd_rn(sgn1(__dsub_rn(d, h)), sgn1(__dadd_rn(d, h)));
-  return __dsub_rn(d, __dmul_rn(h, s));
+  const long long bd = __double_as_longlong(d), bh = __double_as_longlong(h);
+  const bool up = bd >= bh;                                    // d >= h
+  const bool dn = bd < 0 && (bd & 0x7FFFFFFFFFFFFFFFLL) > bh;  // d < -h
+  const double w = up ? -(h + h) : (h + h);
+  const double r = __dadd_rn(d, w);
+  return (up || dn) ? r : d;
 }
 // dr = b - a with the minimum image; returns dr.dr evaluated as
 // (dx*dx + dy*dy) + dz*dz without contraction.
