@@ -150,6 +150,7 @@ static void fill_cos(Cosc<R>& c, const CosPar& P, bool morse) {
   c.R2 = (R)P.R2;
   c.inv_w = (R)(1.0 / (P.R2 - P.R1));
   c.pref = (R)(morse ? P.D : 4.0 * P.eps);
+  c.idelt = P.delt == 2.0 ? 2 : 0;
 }
 void derive(CosPar& P, bool morse) {
   fill_cos(P.d, P, morse);

@@ -468,6 +468,11 @@ template <bool PREC>
 __device__ __forceinline__ const TBc<typename RT<PREC>::R>& cst(const TBPar& p) {
   if constexpr (PREC) return p.f; else return p.dd;
 }
+// 1/sqrt(x): the FP64 reciprocal square root (no divide) or rsqrtf
+template <bool PREC>
+__device__ __forceinline__ typename RT<PREC>::R xrsqrt(typename RT<PREC>::R x) {
+  if constexpr (PREC) return rsqrtf(x); else return rsqrt(x);
+}
 // 1/x: one divide per pair in FP64 (the plain form), the fast reciprocal in FP32
 template <bool PREC>
 __device__ __forceinline__ typename RT<PREC>::R xrcp(typename RT<PREC>::R x) {

@@ -8,29 +8,54 @@
 
 namespace pfmd {
 
+// The cosine power V3 = (|n.d| / (|n| r))^delta (|n| only where `scaled`:
+// morsec's metal side) and V3 / (n.d).  For delta = 2, the parameter files'
+// value (Cosc::idelt), both are products (no FP64 divide, no pow); otherwise pow
+// and a divide as written.  (At n.d = 0 the written quotient is 0/0 where the
+// product gives 0: the partner would lie in the plane through the atom normal
+// to n, which a sheet coupled to a slab never forms.)
+template <bool PREC>
+__device__ __forceinline__ void cos_v3(const Cosc<typename RT<PREC>::R>& c, typename RT<PREC>::R nd,
+                                       typename RT<PREC>::R ir, typename RT<PREC>::R inn2, bool scaled,
+                                       typename RT<PREC>::R& V3, typename RT<PREC>::R& V3n) {
+  using R = typename RT<PREC>::R;
+  if (c.idelt == 2) {
+    const R u = nd * ir, s = scaled ? inn2 : R(1);
+    V3 = u * u * s;
+    V3n = u * ir * s;
+  } else {
+    const R x = fabs(nd) * ir;
+    V3 = xpow<PREC>(scaled ? x * xsqrt<PREC>(inn2) : x, c.delt);
+    V3n = V3 / nd;
+  }
+}
+
+// One pair (r, its reciprocal ir, dr, the normal nv; inn2 = 1/|nv|^2 on morsec's
+// metal side): X, Y with F = pref (X dr + Y nv), and the energy E.
 template <bool PREC, bool MORSE>
-__device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r, const typename RT<PREC>::R* dr,
-                                         const typename RT<PREC>::R* nv, typename RT<PREC>::R nnorm, bool metal,
-                                         typename RT<PREC>::R& X, typename RT<PREC>::R& Y, typename RT<PREC>::R& E) {
+__device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r, typename RT<PREC>::R ir,
+                                         const typename RT<PREC>::R* dr, const typename RT<PREC>::R* nv,
+                                         typename RT<PREC>::R inn2, bool metal, typename RT<PREC>::R& X,
+                                         typename RT<PREC>::R& Y, typename RT<PREC>::R& E) {
   using R = typename RT<PREC>::R;
   const auto& c = cst<PREC>(P);
   const R R1 = c.R1, R2 = c.R2, delt = c.delt, inv_w = c.inv_w;
   const R nd = nv[0] * dr[0] + nv[1] * dr[1] + nv[2] * dr[2];
-  const R ir = xrcp<PREC>(r);  // the one divide of the pair (FP64 divides are long sequences)
   R fc, dfc;
   fdfc<PREC>(r, ir, R1, R2, inv_w, fc, dfc);
+  R V3, V3n;
   if (!MORSE) {
     const R x = c.sig * ir, x2 = x * x, V2 = x2 * x2 * x2, V1 = V2 * V2;
-    const R V3 = xpow<PREC>(fabs(nd) * ir, delt);
+    cos_v3<PREC>(c, nd, ir, R(1), false, V3, V3n);
     X = (R(12) * V1 - (R(6) + delt) * V2 * V3) * (ir * ir) * fc - (V1 - V2 * V3) * dfc;
-    Y = delt * V2 * V3 / nd * fc;
+    Y = delt * V2 * V3n * fc;
     E = (V1 - V2 * V3) * fc;
   } else {
     const R a = c.a;
     const R V2 = xexp<PREC>(-a * (r - c.r0)), V1 = V2 * V2;
-    const R V3 = xpow<PREC>(metal ? fabs(nd) * ir / nnorm : fabs(nd) * ir, delt);
+    cos_v3<PREC>(c, nd, ir, inn2, metal, V3, V3n);
     X = R(2) * (a * V1 - (a + delt * ir) * V2 * V3) * ir * fc - (V1 - R(2) * V2 * V3) * dfc;
-    Y = R(2) * delt * V2 * V3 / nd * fc;
+    Y = R(2) * delt * V2 * V3n * fc;
     E = (V1 - R(2) * V2 * V3) * fc;
   }
 }
@@ -57,10 +82,11 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
     const int n = nl.nnum[i];
     for (int p = g.sub; p < n; p += TPA) {
       R dr[3];
-      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, ent(nl, i, p)), B, dr));
+      const R r2 = T::d2(pi, T::load(A, ent(nl, i, p)), B, dr);
+      const R ir = xrsqrt<PREC>(r2), r = r2 * ir;
       if (r < R2) {
         R X, Y, E;
-        cos_pair<PREC, MORSE>(P, r, dr, nv, R(1), false, X, Y, E);
+        cos_pair<PREC, MORSE>(P, r, ir, dr, nv, R(1), false, X, Y, E);
         acc.add(-pref * (X * dr[0] + Y * nv[0]), -pref * (X * dr[1] + Y * nv[1]), -pref * (X * dr[2] + Y * nv[2]));
         if (ENERGY) e.add(pref * E);
       }
@@ -95,6 +121,7 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
           d23[k] = dl[l3][k] - dl[l2][k];
         }
         const R Aa = dot3<PREC>(d12, d12) * dot3<PREC>(d31, d31) - dot3<PREC>(d12, d31) * dot3<PREC>(d12, d31);
+        const R iAa = R(1) / Aa;  // once per neighbour j, not per partner
         const R s2331 = dot3<PREC>(d23, d31), s2312 = dot3<PREC>(d23, d12);
         R w[3];
 #pragma unroll
@@ -106,20 +133,22 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
         const int m = nl.nnum[j];
         for (int p = g.sub; p < m; p += TPA) {
           R dr[3];
-          const R r = xsqrt<PREC>(T::d2(pg, T::load(A, ent(nl, j, p)), B, dr));
+          const R r2 = T::d2(pg, T::load(A, ent(nl, j, p)), B, dr);
+          const R ir = xrsqrt<PREC>(r2), r = r2 * ir;
           if (r < R2) {
             const R nd = nj[0] * dr[0] + nj[1] * dr[1] + nj[2] * dr[2];
-            const R V3 = xpow<PREC>(fabs(nd) / r, delt);
+            R V3, V3n;
+            cos_v3<PREC>(c, nd, ir, R(1), false, V3, V3n);
             const R fc = fc_only<PREC>(r, R1, R2, inv_w);
             R V2;
             if (MORSE)
               V2 = xexp<PREC>(-c.a * (r - c.r0));
             else {
-              const R x = c.sig / r, x2 = x * x;
+              const R x = c.sig * ir, x2 = x * x;
               V2 = x2 * x2 * x2;
             }
             const R C = dr[0] * w[0] + dr[1] * w[1] + dr[2] * w[2];
-            const R coef = (MORSE ? R(2) * pref : pref) * delt * V2 * V3 * fc / Aa / nd;
+            const R coef = (MORSE ? R(2) * pref : pref) * delt * V2 * V3n * fc * iAa;
             acc.add(-coef * nj[0] * C, -coef * nj[1] * C, -coef * nj[2] * C);
           }
         }
@@ -150,13 +179,14 @@ __global__ void __launch_bounds__(256) k_cos_metal(ListDev nl, CosPar P, const d
     for (int p = g.sub; p < n; p += TPA) {
       const int aj = ent(nl, g.row, p);
       R dr[3];
-      const R r = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dr));
+      const R r2 = T::d2(pi, T::load(A, aj), B, dr);
+      const R ir = xrsqrt<PREC>(r2), r = r2 * ir;
       if (r < R2) {
         const double4_32a gn = norm[aj];
         const R nv[3] = {(R)gn.x, (R)gn.y, (R)gn.z};
-        const R nn = xsqrt<PREC>(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        const R inn2 = MORSE ? xrcp<PREC>(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]) : R(1);
         R X, Y, E;
-        cos_pair<PREC, MORSE>(P, r, dr, nv, nn, true, X, Y, E);
+        cos_pair<PREC, MORSE>(P, r, ir, dr, nv, inn2, true, X, Y, E);
         acc.add(-pref * (X * dr[0] + Y * nv[0]), -pref * (X * dr[1] + Y * nv[1]), -pref * (X * dr[2] + Y * nv[2]));
       }
     }

@@ -106,7 +106,8 @@ struct LJPar {
 template <class R>
 struct Cosc {
   R sig, delt, a, r0, R1, R2, inv_w;
-  R pref;  // 4 eps (ljc) or D (morsec)
+  R pref;     // 4 eps (ljc) or D (morsec)
+  int idelt;  // 2 when delta is exactly 2 (the cosine power then runs as products), else 0
 };
 struct CosPar {  // ljc: eps sig delt; morsec: D r0 a delt
   double eps, sig, delt, D, r0, a, R1, R2;

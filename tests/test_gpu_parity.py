@@ -34,7 +34,10 @@ def _gr(d, **kw):
 
 SYSTEMS = {"lj": _lj, "cu": _cu, "gr_morsec": _gr,
            "gr_ljc": lambda d: _gr(d, coupling="ljc"),
-           "gr_simplified": lambda d: _gr(d, simplified=True)}
+           "gr_simplified": lambda d: _gr(d, simplified=True),
+           # a cosine power other than 2 (pow instead of the product form)
+           "gr_morsec_delta1.5": lambda d: _gr(d, morse=(0.1, 2.2, 1.7, 1.5)),
+           "gr_ljc_delta1.5": lambda d: _gr(d, coupling="ljc", ljc=(0.0168, 2.2, 1.5))}
 
 
 def _compare_lists(s, o):
