@@ -1614,6 +1614,10 @@ void Engine::enqueue_step(const StepPlan& p) {
             launch_scale(0, gc, A, ctl, st);
           continue;
         }
+        if (c == 0 && p.nhc_ahead) {  // with the next first half; the next kick-drift scales
+          launch_nhc(0, gc, ts[1], ts[2], ts[3], A, ctl, st, 0, 1);
+          continue;
+        }
         launch_nhc(static_cast<int>(c), gc, ts[1], ts[2], ts[3], A, ctl, st);
         launch_scale(static_cast<int>(c), gc, A, ctl, st);
       }
@@ -1939,6 +1943,16 @@ void Engine::advance(long long max_steps, int* fin) {
           a.nhc_ahead = true;
           plans[i + 1].nhc_done = true;
         }
+      }
+    // other interactions: the second half's k_nhc runs the next first half too,
+    // and the next kick-drift applies both scalings (no k_scale, no k_nhc there)
+    if (!pair_fused && S.nhc.size() == 1 && !S.invert_z_vel && integ == I_NVT && !learned_active &&
+        fused_nhc_chain == 0 && changes.empty())
+      for (size_t i = 0; i + 1 < plans.size(); ++i) {
+        StepPlan& a = plans[i];
+        if (a.first || a.energy || a.out || plans[i + 1].first) continue;
+        a.nhc_ahead = true;
+        plans[i + 1].nhc_done = true;
       }
     run_plans(plans);
     if (log_rows > 0)

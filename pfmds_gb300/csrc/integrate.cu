@@ -292,9 +292,13 @@ void launch_step_begin_fused(Ctl* ctl, cudaStream_t s) {
 // block.  prescale: the velocities first get the chain's pending s (the scaling
 // of the chain's previous half, which the force kernel before it left to this
 // kernel), so the kinetic energy is that of the scaled velocities, as in the
-// reference.
+// reference.  ahead (a step's second half when the next step's first half
+// follows with nothing between that changes velocities): the last block also
+// runs that first half-update on the kinetic energy after this half's scaling,
+// s^2 ke, and leaves both scalings to the next step's kick-drift (Ctl::nhc_sa
+// holds this half's s), so neither k_scale nor the next step's k_nhc runs.
 __global__ void __launch_bounds__(kRedThreads) k_nhc(int chain, GroupRef g, double ts2, double ts3, double ts4,
-                                                     Atoms A, Ctl* ctl, int prescale) {
+                                                     Atoms A, Ctl* ctl, int prescale, int ahead) {
   if (ctl->stop) return;
   const int n = ctl->group_n[g.g];
   const double s0 = ctl->nhc[chain].s;
@@ -312,6 +316,11 @@ __global__ void __launch_bounds__(kRedThreads) k_nhc(int chain, GroupRef g, doub
   }
   if (!grid_sum<1>(ctl, 0, v, out)) return;
   nhc_chain_update(ctl->nhc[chain], out[0], ts2, ts3, ts4);
+  if (ahead) {
+    const double sa = ctl->nhc[chain].s;
+    ctl->nhc_sa = sa;
+    nhc_chain_update(ctl->nhc[chain], out[0] * (sa * sa), ts2, ts3, ts4);
+  }
 }
 
 // scale_velocities (md_general.f90:97-112) by the chain's s
@@ -505,8 +514,11 @@ void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_pos
   ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
-                cudaStream_t s, int prescale) {
-  { k_nhc<<<red_grid(g.cap), kRedThreads, 0, s>>>(chain, g, ts2, ts3, ts4, A, ctl, prescale); ++g_kernel_launches; }
+                cudaStream_t s, int prescale, int ahead) {
+  {
+    k_nhc<<<red_grid(g.cap), kRedThreads, 0, s>>>(chain, g, ts2, ts3, ts4, A, ctl, prescale, ahead);
+    ++g_kernel_launches;
+  }
 }
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s) {
   if (g.cap > 0) { k_scale<<<nb(g.cap, 256), 256, 0, s>>>(chain, g, A, ctl); ++g_kernel_launches; }

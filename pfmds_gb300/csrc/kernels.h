@@ -296,8 +296,7 @@ void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_pos
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false,
                        bool nhc_pre = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
-                cudaStream_t s,
-                int prescale = 0);
+                cudaStream_t s, int prescale = 0, int ahead = 0);
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_ms(const GroupRef& g, bool xyz, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_zero_forces(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
