@@ -249,6 +249,7 @@ struct InterH {
   DBuf<double> scratch;  // rjl 1/Eb, tb bond orders
   DBuf<double2> pair;    // rjl plain form: per-slot force coefficients
   DBuf<double4_32a> norm;    // ljc / morsec graphene normals
+  DBuf<double4_32a> gsum;    // ljc / morsec: per graphene row, the sum the normal-derivative term reads
   int tb_inter = -1;     // ljc / morsec: the first tb interaction
   double rc_nn = 0.0;
 };
@@ -887,6 +888,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
     if (I.lists[2] >= 0) {
       I.norm.alloc(static_cast<size_t>(std::max(N, 1)));  // normals per atom
       I.norm.zero(st);
+      I.gsum.alloc(static_cast<size_t>(std::max(N, 1)));  // at most one graphene row per atom
+      I.gsum.zero(st);
     }
     // lj1g in a group that is not in atom order needs lessnnum in the reference's order
     if (I.spec.kind == pfmd_io::K_LJ1G && I.general) lists[static_cast<size_t>(I.lists[0])].d.sorted = 1;
@@ -1520,7 +1523,7 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
       case pfmd_io::K_LJC:
       case pfmd_io::K_MORSEC:
         launch_cos(prec, energy, I.spec.kind == pfmd_io::K_MORSEC, L1, lists[static_cast<size_t>(I.lists[1])].d,
-                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, A, box, ctl, eslot, key, st);
+                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, I.gsum.p, A, box, ctl, eslot, key, st);
         break;
     }
   }
@@ -2550,7 +2553,7 @@ double Engine::time_kernel(const std::string& name, int reps, double* bytes) {
       }
       if ((kind == pfmd_io::K_LJC || kind == pfmd_io::K_MORSEC) && (name == "cos_graphene" || name == "cos_metal")) {
         launch_cos(prec, false, kind == pfmd_io::K_MORSEC, L1, lists[static_cast<size_t>(I.lists[1])].d,
-                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, A, box, ctl, eslot, 0, st,
+                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, I.gsum.p, A, box, ctl, eslot, 0, st,
                    name == "cos_graphene" ? 1 : 2);
         return true;
       }

@@ -60,16 +60,22 @@ __device__ __forceinline__ void cos_pair(const CosPar& P, typename RT<PREC>::R r
   }
 }
 
+// Graphene side, the pair terms.  Unless `simplified`, each row also stores
+// G_i = sum_p pref Y_ip dr_ip (Y the pair's normal coefficient, dr to partner p):
+// the normal-derivative term of every row i' with i among its three nearest
+// neighbours is a function of G_i and of the geometry of i's three neighbours
+// only (k_cos_nderiv), so the partners are visited once instead of four times.
 template <bool PREC, bool ENERGY, bool MORSE, int TPA>
-__global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, CosPar P, const double4_32a* norm,
-                                                      Atoms A, Box B, Ctl* ctl, int eslot, int ekey) {
+__global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, CosPar P, const double4_32a* norm,
+                                                      double4_32a* gsum, Atoms A, Box B, Ctl* ctl, int eslot,
+                                                      int ekey) {
   using T = RT<PREC>;
   using R = typename T::R;
   if (ctl->stop) return;
   const Grp<TPA> g;
   const bool valid = g.row < nl.rows;
   const int i = g.row;
-  Acc3<PREC> acc;
+  Acc3<PREC> acc, gacc;
   Acc1<PREC> e;
   const int ai = valid ? nl.pidx[i] : 0;
   const auto& c = cst<PREC>(P);
@@ -88,77 +94,80 @@ __global__ void __launch_bounds__(256) k_cos_graphene(ListDev nl, ListDev nn, Co
         R X, Y, E;
         cos_pair<PREC, MORSE>(P, r, ir, dr, nv, R(1), false, X, Y, E);
         acc.add(-pref * (X * dr[0] + Y * nv[0]), -pref * (X * dr[1] + Y * nv[1]), -pref * (X * dr[2] + Y * nv[2]));
+        const R py = pref * Y;
+        gacc.add(py * dr[0], py * dr[1], py * dr[2]);
         if (ENERGY) e.add(pref * E);
-      }
-    }
-    if (!P.simplified) {
-      const R R1 = c.R1, delt = c.delt, inv_w = c.inv_w;
-      for (int q = 0; q < 3; ++q) {
-        const int j = ent(nn, i, q);
-        if (j < 0 || j >= nn.rows || j >= nl.rows || j >= nn.row_cap) {
-          // a neighbour outside the graphene rows (groups 5/6 of the list differ)
-          if (g.sub == 0) set_error(ctl, ST_PARAM, EK_NONE, i + 1, j + 1, 0);
-          break;
-        }
-        int l1 = 0;
-        for (; l1 < 3; ++l1)
-          if (ent(nn, j, l1) == i) break;
-        if (l1 >= 3) {
-          if (g.sub == 0) set_error(ctl, ST_GR_NN, EK_L1, i + 1, j + 1, 0);
-          break;
-        }
-        const int l2 = (l1 + 1) % 3, l3 = (l1 + 2) % 3;
-        const int aj = nn.row_idx[j];
-        const auto pj = T::load(A, aj);
-        R dl[3][3];
-#pragma unroll
-        for (int l = 0; l < 3; ++l) T::d2(pj, T::load(A, nn.col_idx[ent(nn, j, l)]), B, dl[l]);
-        R d12[3], d31[3], d23[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          d12[k] = dl[l2][k] - dl[l1][k];
-          d31[k] = dl[l1][k] - dl[l3][k];
-          d23[k] = dl[l3][k] - dl[l2][k];
-        }
-        const R Aa = dot3<PREC>(d12, d12) * dot3<PREC>(d31, d31) - dot3<PREC>(d12, d31) * dot3<PREC>(d12, d31);
-        const R iAa = R(1) / Aa;  // once per neighbour j, not per partner
-        const R s2331 = dot3<PREC>(d23, d31), s2312 = dot3<PREC>(d23, d12);
-        R w[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) w[k] = d12[k] * s2331 - d31[k] * s2312;
-        const int ag = nl.pidx[j];
-        const double4_32a nj4 = norm[ag];
-        const R nj[3] = {(R)nj4.x, (R)nj4.y, (R)nj4.z};
-        const auto pg = T::load(A, ag);
-        const int m = nl.nnum[j];
-        for (int p = g.sub; p < m; p += TPA) {
-          R dr[3];
-          const R r2 = T::d2(pg, T::load(A, ent(nl, j, p)), B, dr);
-          const R ir = xrsqrt<PREC>(r2), r = r2 * ir;
-          if (r < R2) {
-            const R nd = nj[0] * dr[0] + nj[1] * dr[1] + nj[2] * dr[2];
-            R V3, V3n;
-            cos_v3<PREC>(c, nd, ir, R(1), false, V3, V3n);
-            const R fc = fc_only<PREC>(r, R1, R2, inv_w);
-            R V2;
-            if (MORSE)
-              V2 = xexp<PREC>(-c.a * (r - c.r0));
-            else {
-              const R x = c.sig * ir, x2 = x * x;
-              V2 = x2 * x2 * x2;
-            }
-            const R C = dr[0] * w[0] + dr[1] * w[1] + dr[2] * w[2];
-            const R coef = (MORSE ? R(2) * pref : pref) * delt * V2 * V3n * fc * iAa;
-            acc.add(-coef * nj[0] * C, -coef * nj[1] * C, -coef * nj[2] * C);
-          }
-        }
       }
     }
   }
   acc.template reduce<TPA>();
+  if (!P.simplified) gacc.template reduce<TPA>();
   if (ENERGY) e.template reduce<TPA>();
-  if (valid && g.sub == 0) add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+  if (valid && g.sub == 0) {
+    add_force(A, ai, acc.get(0), acc.get(1), acc.get(2));
+    if (!P.simplified) gsum[i] = double4_32a{gacc.get(0), gacc.get(1), gacc.get(2), 0.0};
+  }
   if (ENERGY) energy_reduce(ctl, eslot, ekey, (valid && g.sub == 0) ? e.get() : 0.0);
+}
+
+// The normal-derivative term of the graphene side (the dn_j/dr_i part of
+// LennardJonesCosine.f90 / MorseCosine.f90 when not simplified).  For each of
+// row i's three nearest neighbours j, j's partners p contribute
+// -(pref Y_jp / A_ij) (dr_jp . w_ij) n_j, with A_ij and w_ij formed from the
+// positions of j's three neighbours (i among them); A_ij and w_ij do not depend
+// on p, so the sum over p is -((w_ij . G_j) / A_ij) n_j with k_cos_graphene's
+// G_j.  One thread per row; the force adds to the pair terms'.
+template <bool PREC>
+__global__ void __launch_bounds__(256) k_cos_nderiv(ListDev nl, ListDev nn, const double4_32a* norm,
+                                                    const double4_32a* gsum, Atoms A, Box B, Ctl* ctl) {
+  using T = RT<PREC>;
+  using R = typename T::R;
+  if (ctl->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nl.rows) return;
+  const int ai = nl.pidx[i];
+  double f[3] = {0.0, 0.0, 0.0};
+  for (int q = 0; q < 3; ++q) {
+    const int j = ent(nn, i, q);
+    if (j < 0 || j >= nn.rows || j >= nl.rows || j >= nn.row_cap) {
+      // a neighbour outside the graphene rows (groups 5/6 of the list differ)
+      set_error(ctl, ST_PARAM, EK_NONE, i + 1, j + 1, 0);
+      break;
+    }
+    int l1 = 0;
+    for (; l1 < 3; ++l1)
+      if (ent(nn, j, l1) == i) break;
+    if (l1 >= 3) {
+      set_error(ctl, ST_GR_NN, EK_L1, i + 1, j + 1, 0);
+      break;
+    }
+    const int l2 = (l1 + 1) % 3, l3 = (l1 + 2) % 3;
+    const int aj = nn.row_idx[j];
+    const auto pj = T::load(A, aj);
+    R dl[3][3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) T::d2(pj, T::load(A, nn.col_idx[ent(nn, j, l)]), B, dl[l]);
+    R d12[3], d31[3], d23[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      d12[k] = dl[l2][k] - dl[l1][k];
+      d31[k] = dl[l1][k] - dl[l3][k];
+      d23[k] = dl[l3][k] - dl[l2][k];
+    }
+    const R Aa = dot3<PREC>(d12, d12) * dot3<PREC>(d31, d31) - dot3<PREC>(d12, d31) * dot3<PREC>(d12, d31);
+    const R s2331 = dot3<PREC>(d23, d31), s2312 = dot3<PREC>(d23, d12);
+    const double4_32a G = gsum[j];
+    double wg = 0.0;
+    wg += (double)(d12[0] * s2331 - d31[0] * s2312) * G.x;
+    wg += (double)(d12[1] * s2331 - d31[1] * s2312) * G.y;
+    wg += (double)(d12[2] * s2331 - d31[2] * s2312) * G.z;
+    const double k = wg / (double)Aa;
+    const double4_32a nj = norm[nl.pidx[j]];
+    f[0] -= k * (double)(R)nj.x;
+    f[1] -= k * (double)(R)nj.y;
+    f[2] -= k * (double)(R)nj.z;
+  }
+  add_force(A, ai, f[0], f[1], f[2]);
 }
 
 template <bool PREC, bool MORSE, int TPA>
@@ -196,8 +205,8 @@ __global__ void __launch_bounds__(256) k_cos_metal(ListDev nl, CosPar P, const d
 }
 
 void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
-                const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot, int ekey,
-                cudaStream_t s, int parts) {
+                const CosPar& P, const double4_32a* norm, double4_32a* gsum, const Atoms& A, const Box& B, Ctl* ctl,
+                int eslot, int ekey, cudaStream_t s, int parts) {
   with_bool(prec, [&](auto pr) {
     with_bool(morse, [&](auto mo) {
       constexpr bool PR = decltype(pr)::value, MO = decltype(mo)::value;
@@ -207,11 +216,15 @@ void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const Li
           with_tpa(nl1.tpa, [&](auto t) {
             constexpr int TP = decltype(t)::value;
             if (energy)
-              k_cos_graphene<PR, true, MO, TP><<<grid, 256, 0, s>>>(nl1, nn, P, norm, A, B, ctl, eslot, ekey);
+              k_cos_graphene<PR, true, MO, TP><<<grid, 256, 0, s>>>(nl1, P, norm, gsum, A, B, ctl, eslot, ekey);
             else
-              k_cos_graphene<PR, false, MO, TP><<<grid, 256, 0, s>>>(nl1, nn, P, norm, A, B, ctl, eslot, ekey);
+              k_cos_graphene<PR, false, MO, TP><<<grid, 256, 0, s>>>(nl1, P, norm, gsum, A, B, ctl, eslot, ekey);
             ++g_kernel_launches;
           });
+          if (!P.simplified) {
+            k_cos_nderiv<PR><<<nblk(nl1.rows, 256), 256, 0, s>>>(nl1, nn, norm, gsum, A, B, ctl);
+            ++g_kernel_launches;
+          }
         } else if (energy) {
           cudaMemsetAsync(&ctl->e_inter[ekey], 0, sizeof(double), s);
         }

@@ -264,9 +264,11 @@ void launch_tb(bool prec, bool energy, const ListDev& L, const TBPar& P, const A
 void launch_rebo(bool energy, const ListDev& L, const REBOPar& P, const Atoms& A, const Box& B, double* S3, Ctl* ctl,
                  int eslot, int ekey, cudaStream_t s, int parts = 3, const Epi& E = Epi{0, 0, 0, 0.0, nullptr});
 // parts: 1 graphene side, 2 metal side
+// gsum: one record per graphene row (the per-row sums the normal-derivative
+// term reads), unused when P.simplified
 void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const ListDev& nl2, const ListDev& nn,
-                const CosPar& P, const double4_32a* norm, const Atoms& A, const Box& B, Ctl* ctl, int eslot,
-                int ekey, cudaStream_t s, int parts = 3);
+                const CosPar& P, const double4_32a* norm, double4_32a* gsum, const Atoms& A, const Box& B, Ctl* ctl,
+                int eslot, int ekey, cudaStream_t s, int parts = 3);
 
 // ---------------- state transfer (integrate.cu) ----------------
 // xyz-interleaved doubles (the reference's (3,N) arrays, as the host passes them)
