@@ -1600,11 +1600,18 @@ void Engine::enqueue_step(const StepPlan& p) {
   nhc_ahead = false;
   if (p.drift_next) flip_posq();  // the next step reads the positions written by this one
   if (!p.first) {
-    if (!kick_last) {
+    // the chain's group is the kicked one and nothing else is kicked: the kick
+    // and the chain's half-update run as one kernel
+    const bool kick_nhc = !kick_last && nvt && fused_nhc_chain == 0 && gz.cap == 0 &&
+                          !(nhc_fused && pair_fused && !learned_active);
+    if (kick_nhc) {
+      launch_kick_nhc(gx, ts[1], !prec, 0, ts[1], ts[2], ts[3], p.nhc_ahead, A, ctl, st);
+      if (!p.nhc_ahead) launch_scale(0, gx, A, ctl, st);
+    } else if (!kick_last) {
       launch_kick(gx, true, ts[1], !prec, A, ctl, st);
       if (gz.cap > 0) launch_kick(gz, false, ts[1], !prec, A, ctl, st);
     }
-    if (nvt)
+    if (nvt && !kick_nhc)
       for (size_t c = 0; c < S.nhc.size(); ++c) {
         const GroupRef gc = gref(S.nhc[c].group);
         if (c == 0 && nhc_fused && pair_fused && !learned_active) {

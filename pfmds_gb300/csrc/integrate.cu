@@ -323,6 +323,45 @@ __global__ void __launch_bounds__(kRedThreads) k_nhc(int chain, GroupRef g, doub
   }
 }
 
+// The second half-kick of the xyz-moving group (md_integrators.f90:58-97) fused
+// with the Nose-Hoover half-update of the chain over that same group
+// (md_integrators.f90:200-245): each thread kicks its atoms and adds their
+// kinetic energy after the kick, in k_nhc's grid and order, and the last block
+// updates the chain (with ahead, also the next step's first half, as k_nhc).
+// One pass over the velocities and one launch instead of two.
+template <bool EXACT>
+__global__ void __launch_bounds__(kRedThreads) k_kick_nhc(GroupRef g, double kts2, int chain, double ts2, double ts3,
+                                                          double ts4, int ahead, Atoms A, Ctl* ctl) {
+  if (ctl->stop) return;
+  const int n = ctl->group_n[g.g];
+  double v[1] = {0.0}, out[1];
+  for (int ind = blockIdx.x * blockDim.x + threadIdx.x; ind < n; ind += gridDim.x * blockDim.x) {
+    const int i = g.idx[ind];
+    const double4_32a f = A.frc[i];
+    double4_32a u = A.vel[i];
+    if (EXACT) {
+      const double m = A.mass[i];
+      u.x = kick1(u.x, f.x, m, kts2);
+      u.y = kick1(u.y, f.y, m, kts2);
+      u.z = kick1(u.z, f.z, m, kts2);
+    } else {
+      const double kt = A.kc[i] * kts2;
+      u.x = kick1_fast(u.x, f.x, kt);
+      u.y = kick1_fast(u.y, f.y, kt);
+      u.z = kick1_fast(u.z, f.z, kt);
+    }
+    A.vel[i] = u;
+    v[0] += ke_of(A, i);
+  }
+  if (!grid_sum<1>(ctl, 0, v, out)) return;
+  nhc_chain_update(ctl->nhc[chain], out[0], ts2, ts3, ts4);
+  if (ahead) {
+    const double sa = ctl->nhc[chain].s;
+    ctl->nhc_sa = sa;
+    nhc_chain_update(ctl->nhc[chain], out[0] * (sa * sa), ts2, ts3, ts4);
+  }
+}
+
 // scale_velocities (md_general.f90:97-112) by the chain's s
 __global__ void k_scale(int chain, GroupRef g, Atoms A, Ctl* ctl) {
   if (ctl->stop) return;
@@ -519,6 +558,14 @@ void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4
     k_nhc<<<red_grid(g.cap), kRedThreads, 0, s>>>(chain, g, ts2, ts3, ts4, A, ctl, prescale, ahead);
     ++g_kernel_launches;
   }
+}
+void launch_kick_nhc(const GroupRef& g, double kts2, bool exact, int chain, double ts2, double ts3, double ts4,
+                     bool ahead, const Atoms& A, Ctl* ctl, cudaStream_t s) {
+  if (exact)
+    k_kick_nhc<true><<<red_grid(g.cap), kRedThreads, 0, s>>>(g, kts2, chain, ts2, ts3, ts4, ahead ? 1 : 0, A, ctl);
+  else
+    k_kick_nhc<false><<<red_grid(g.cap), kRedThreads, 0, s>>>(g, kts2, chain, ts2, ts3, ts4, ahead ? 1 : 0, A, ctl);
+  ++g_kernel_launches;
 }
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s) {
   if (g.cap > 0) { k_scale<<<nb(g.cap, 256), 256, 0, s>>>(chain, g, A, ctl); ++g_kernel_launches; }

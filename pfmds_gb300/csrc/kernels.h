@@ -299,6 +299,10 @@ void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_pos
                        bool nhc_pre = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s, int prescale = 0, int ahead = 0);
+// the xyz-moving group's second half-kick with the half-update of the chain over
+// the same group (ahead: and the next step's first half, as launch_nhc)
+void launch_kick_nhc(const GroupRef& g, double kts2, bool exact, int chain, double ts2, double ts3, double ts4,
+                     bool ahead, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_scale(int chain, const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_ms(const GroupRef& g, bool xyz, const Atoms& A, Ctl* ctl, cudaStream_t s);
 void launch_zero_forces(const GroupRef& g, const Atoms& A, Ctl* ctl, cudaStream_t s);
