@@ -199,6 +199,7 @@ static void fill_tb(TBc<R>& c, const TBPar& P) {
   c.sq2os = (R)std::sqrt(2.0 / P.s);
   c.pre_e = (R)(P.d / (P.s - 1.0));
   c.c02d02 = (R)(P.c02 / P.d02);
+  c.is = (R)(1.0 / P.s);
 }
 void derive(TBPar& P) {
   fill_tb(P.dd, P);
@@ -882,7 +883,8 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
       I.pair.alloc(std::max<size_t>(prec ? (slots + 1) / 2 : slots, 1));
     }
     if (I.spec.kind == pfmd_io::K_TB)
-      I.scratch.alloc(std::max<size_t>(static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));  // B per list slot
+      // B and B^(1/delta + 1) per list slot
+      I.scratch.alloc(std::max<size_t>(2 * static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));
     if (I.spec.kind == pfmd_io::K_REBOSC)  // bsp, dbsp/dS and bdh per list slot
       I.scratch.alloc(std::max<size_t>(3 * static_cast<size_t>(L1.d.nmax) * L1.d.stride, 1));
     if (I.lists[2] >= 0) {

@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(256) k_cos_metal(ListDev nl, CosPar P, const d
       if (r < R2) {
         const double4_32a gn = norm[aj];
         const R nv[3] = {(R)gn.x, (R)gn.y, (R)gn.z};
-        const R inn2 = MORSE ? xrcp<PREC>(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]) : R(1);
+        const R inn2 = MORSE ? (R)gn.w : R(1);  // 1/|n|^2, formed with the normal
         R X, Y, E;
         cos_pair<PREC, MORSE>(P, r, ir, dr, nv, inn2, true, X, Y, E);
         acc.add(-pref * (X * dr[0] + Y * nv[0]), -pref * (X * dr[1] + Y * nv[1]), -pref * (X * dr[2] + Y * nv[2]));

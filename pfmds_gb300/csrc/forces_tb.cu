@@ -7,6 +7,10 @@
 
 namespace pfmd {
 
+// Pass 1: B(p,i) = (1 + a0 sum_q fc(r_q) g(cos))^-delta for every bond of row i,
+// and beside it (at slot nmax + p) B^(1/delta + 1) = B / (1 + a0 sum), the power
+// of B the force pass takes (no pow there).  Distances through one reciprocal
+// square root per bond (no FP64 divide but the angular term's).
 template <bool PREC>
 __global__ void __launch_bounds__(128) k_tb_bond(ListDev L, TBPar P, Atoms A, Box B, double* Bb, Ctl* ctl) {
   using T = RT<PREC>;
@@ -19,23 +23,29 @@ __global__ void __launch_bounds__(128) k_tb_bond(ListDev L, TBPar P, Atoms A, Bo
   const auto pi = T::load(A, ai);
   const auto& c = cst<PREC>(P);
   const R R1 = c.R1, R2 = c.R2, a0 = c.a0, c02 = c.c02, d02 = c.d02, delt = c.delt, inv_w = c.inv_w;
+  const size_t ex_off = (size_t)L.nmax * L.stride;
   for (int p = 0; p < n; ++p) {
     R dp[3];
-    const R rp = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, p)), B, dp));
-    R b = R(0);
+    const R r2p = T::d2(pi, T::load(A, ent(L, i, p)), B, dp);
+    const R irp = xrsqrt<PREC>(r2p), rp = r2p * irp;
+    R b = R(0), bex = R(0);
     if (rp < R2) {
       for (int q = 0; q < n; ++q) {
         if (q == p) continue;
         R dq[3];
-        const R rq = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, q)), B, dq));
+        const R r2q = T::d2(pi, T::load(A, ent(L, i, q)), B, dq);
+        const R irq = xrsqrt<PREC>(r2q), rq = r2q * irq;
         if (rq < R2) {
-          const R cs = dot3<PREC>(dp, dq) / (rp * rq);
+          const R cs = dot3<PREC>(dp, dq) * (irp * irq);
           b += fc_only<PREC>(rq, R1, R2, inv_w) * (R(1) + c.c02d02 - c02 / (d02 + (R(1) + cs) * (R(1) + cs)));
         }
       }
-      b = xpow<PREC>(R(1) + a0 * b, -delt);
+      const R base = R(1) + a0 * b;
+      b = xpow<PREC>(base, -delt);
+      bex = b / base;
     }
     Bb[(size_t)p * L.stride + i] = (double)b;
+    Bb[ex_off + (size_t)p * L.stride + i] = (double)bex;
   }
 }
 
@@ -52,8 +62,9 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
     const int ai = L.pidx[i];
     const auto pi = T::load(A, ai);
     const auto& c = cst<PREC>(P);
-    const R R1 = c.R1, R2 = c.R2, a0 = c.a0, c02 = c.c02, d02 = c.d02, delt = c.delt, d = c.d, s = c.s, bb = c.b,
-            r0 = c.r0, inv_w = c.inv_w, ex = c.ex, sq2s = c.sq2s, sq2os = c.sq2os, pre_e = c.pre_e;
+    const R R1 = c.R1, R2 = c.R2, a0 = c.a0, c02 = c.c02, d02 = c.d02, delt = c.delt, s = c.s, bb = c.b,
+            r0 = c.r0, inv_w = c.inv_w, sq2s = c.sq2s, sq2os = c.sq2os, pre_e = c.pre_e, is = c.is;
+    const size_t ex_off = (size_t)L.nmax * L.stride;
     Acc3<PREC> acc;
     Acc1<PREC> e, eh;
     // Entries at or beyond R2 contribute exactly zero (every term carries fc or
@@ -62,28 +73,32 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
     for (int p = 0; p < n; ++p) {
       const int aj = ent(L, i, p);
       R dp[3];
-      const R rp = xsqrt<PREC>(T::d2(pi, T::load(A, aj), B, dp));
+      const R r2p = T::d2(pi, T::load(A, aj), B, dp);
+      const R irp = xrsqrt<PREC>(r2p), rp = r2p * irp;
       if (!(rp < R2)) continue;
+      const R irp2 = irp * irp;
       const int j = L.row_of[aj];
       R dB[3] = {R(0), R(0), R(0)};
       for (int q = 0; q < n; ++q) {
         if (q == p) continue;
         R dq[3];
-        const R rq = xsqrt<PREC>(T::d2(pi, T::load(A, ent(L, i, q)), B, dq));
+        const R r2q = T::d2(pi, T::load(A, ent(L, i, q)), B, dq);
+        const R irq = xrsqrt<PREC>(r2q), rq = r2q * irq;
         if (!(rq < R2)) continue;
-        const R rr = R(1) / rp / rq;
+        const R rr = irp * irq;
         const R cosi = dot3<PREC>(dp, dq) * rr;
-        const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
+        const R it = R(1) / (d02 + (R(1) + cosi) * (R(1) + cosi));
         R fq, dfq;
-        fdfc<PREC>(rq, R1, R2, inv_w, fq, dfq);
-        const R g1 = fq * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
-        const R g2 = dfq * a0 * (R(1) + c.c02d02 - c02 / t);
+        fdfc<PREC>(rq, irq, R1, R2, inv_w, fq, dfq);
+        const R g1 = fq * R(2) * a0 * c02 * (R(1) + cosi) * (it * it);
+        const R g2 = dfq * a0 * (R(1) + c.c02d02 - c02 * it);
+        const R irq2 = irq * irq;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-          dB[k] += g1 * ((dp[k] + dq[k]) * rr - cosi * (dp[k] / (rp * rp) + dq[k] / (rq * rq))) + g2 * dq[k];
+          dB[k] += g1 * ((dp[k] + dq[k]) * rr - cosi * (dp[k] * irp2 + dq[k] * irq2)) + g2 * dq[k];
       }
       const R Bpi = (R)Bb[(size_t)p * L.stride + i];
-      const R bpe = xpow<PREC>(Bpi, ex);
+      const R bpe = (R)Bb[ex_off + (size_t)p * L.stride + i];
 #pragma unroll
       for (int k = 0; k < 3; ++k) dB[k] *= bpe;
       // i's slot l in j's row, and j's environment
@@ -93,34 +108,38 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
       for (; l < nj; ++l)
         if (ent(L, j, l) == ai) break;
       R dl[3] = {R(0), R(0), R(0)};
-      R rl = R(0), Blj = R(0);
+      R rl = R(0), irl = R(0), Blj = R(0), blpe = R(0);
       if (l < nj) {
-        rl = xsqrt<PREC>(T::d2(pj, pi, B, dl));
+        const R r2l = T::d2(pj, pi, B, dl);
+        irl = xrsqrt<PREC>(r2l);
+        rl = r2l * irl;
         Blj = (R)Bb[(size_t)l * L.stride + j];
+        blpe = (R)Bb[ex_off + (size_t)l * L.stride + j];
       }
-      const R blpe = xpow<PREC>(Blj, ex);
+      const R irl2 = irl * irl;
       for (int q = 0; q < nj && l < nj; ++q) {
         if (q == l) continue;
         R dq[3];
-        const R rq = xsqrt<PREC>(T::d2(pj, T::load(A, ent(L, j, q)), B, dq));
+        const R r2q = T::d2(pj, T::load(A, ent(L, j, q)), B, dq);
+        const R irq = xrsqrt<PREC>(r2q), rq = r2q * irq;
         if (!(rq < R2)) continue;
-        const R rr = R(1) / rl / rq;
+        const R rr = irl * irq;
         const R cosi = dot3<PREC>(dl, dq) * rr;
-        const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
-        const R g = blpe * fc_only<PREC>(rq, R1, R2, inv_w) * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
+        const R it = R(1) / (d02 + (R(1) + cosi) * (R(1) + cosi));
+        const R g = blpe * fc_only<PREC>(rq, R1, R2, inv_w) * R(2) * a0 * c02 * (R(1) + cosi) * (it * it);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) dB[k] += g * (-dq[k] * rr + cosi * dl[k] / (rl * rl));
+        for (int k = 0; k < 3; ++k) dB[k] += g * (-dq[k] * rr + cosi * dl[k] * irl2);
       }
 #pragma unroll
       for (int k = 0; k < 3; ++k) dB[k] = dB[k] * (-delt) * R(0.5);
-      if (rp < R2) {
+      {
         R fc, dfc;
-        fdfc<PREC>(rp, R1, R2, inv_w, fc, dfc);
+        fdfc<PREC>(rp, irp, R1, R2, inv_w, fc, dfc);
         const R dff = dfc / fc;
         const R a = -sq2s * bb * (rp - r0);
-        const R ea = xexp<PREC>(a), eas = xexp<PREC>(a / s);
-        const R c1 = sq2s * bb / rp, c2 = sq2os * bb / rp;
-        const R pre = fc * d / (s - R(1));
+        const R ea = xexp<PREC>(a), eas = xexp<PREC>(a * is);
+        const R c1 = sq2s * bb * irp, c2 = sq2os * bb * irp;
+        const R pre = fc * pre_e;  // fc d / (s - 1)
         const R bavg = (Bpi + Blj) * R(0.5);
         R f[3];
 #pragma unroll
@@ -132,22 +151,23 @@ __global__ void __launch_bounds__(128) k_tb_force(ListDev L, TBPar P, Atoms A, B
       }
       if (l < nj) {
         R fl, dfl;
-        fdfc<PREC>(rl, R1, R2, inv_w, fl, dfl);
+        fdfc<PREC>(rl, irl, R1, R2, inv_w, fl, dfl);
         for (int q = 0; q < nj; ++q) {
           if (q == l) continue;
           R dq[3];
-          const R rq = xsqrt<PREC>(T::d2(pj, T::load(A, ent(L, j, q)), B, dq));
+          const R r2q = T::d2(pj, T::load(A, ent(L, j, q)), B, dq);
+          const R irq = xrsqrt<PREC>(r2q), rq = r2q * irq;
           if (!(rq < R2)) continue;
-          const R rr = R(1) / rl / rq;
+          const R rr = irl * irq;
           const R cosi = dot3<PREC>(dl, dq) * rr;
-          const R t = d02 + (R(1) + cosi) * (R(1) + cosi);
-          const R t1 = fl * R(2) * a0 * c02 * (R(1) + cosi) / (t * t);
-          const R t2 = dfl * a0 * (R(1) + c.c02d02 - c02 / t);
-          const R pre = delt * R(0.5) * xpow<PREC>((R)Bb[(size_t)q * L.stride + j], ex);
-          const R post = fc_only<PREC>(rq, R1, R2, inv_w) * d / (s - R(1)) * s * xexp<PREC>(-sq2s * bb * (rq - r0) / s);
+          const R it = R(1) / (d02 + (R(1) + cosi) * (R(1) + cosi));
+          const R t1 = fl * R(2) * a0 * c02 * (R(1) + cosi) * (it * it);
+          const R t2 = dfl * a0 * (R(1) + c.c02d02 - c02 * it);
+          const R pre = delt * R(0.5) * (R)Bb[ex_off + (size_t)q * L.stride + j];
+          const R post = fc_only<PREC>(rq, R1, R2, inv_w) * pre_e * s * xexp<PREC>(-sq2s * bb * (rq - r0) * is);
           R f[3];
 #pragma unroll
-          for (int k = 0; k < 3; ++k) f[k] = pre * (t1 * (-dq[k] * rr + cosi * dl[k] / (rl * rl)) + dp[k] * t2) * post;
+          for (int k = 0; k < 3; ++k) f[k] = pre * (t1 * (-dq[k] * rr + cosi * dl[k] * irl2) + dp[k] * t2) * post;
           acc.add(f[0], f[1], f[2]);
         }
       }

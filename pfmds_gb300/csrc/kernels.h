@@ -132,6 +132,7 @@ struct RJLPar {
 template <class R>
 struct TBc {
   R d, s, b, r0, delt, a0, c02, d02, R1, R2, inv_w, ex, sq2s, sq2os, pre_e, c02d02;
+  R is;  // 1/s
 };
 struct TBPar {
   double d, s, b, r0, delt, a0, c0, d0, R1, R2, c02, d02;

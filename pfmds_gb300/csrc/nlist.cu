@@ -525,7 +525,7 @@ __global__ void k_normals(ListDev nn, double4_32a* norm, int simplified, Atoms A
   if (i >= nn.rows || i >= nn.row_cap) return;  // rows past the row group have no atom
   const int ai = nn.row_idx[i];
   if (simplified) {
-    norm[ai] = make_double4_32a(0.0, 0.0, 1.0, 0.0);
+    norm[ai] = make_double4_32a(0.0, 0.0, 1.0, 1.0);
     return;
   }
   const int cnt = nn.nnum[i];
@@ -561,7 +561,10 @@ __global__ void k_normals(ListDev nn, double4_32a* norm, int simplified, Atoms A
     g2 = -g2;
   }
   const double nr = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
-  norm[ai] = make_double4_32a(g0 / nr, g1 / nr, g2 / nr, 0.0);
+  const double nx = g0 / nr, ny = g1 / nr, nz = g2 / nr;
+  // w: 1/|n|^2 of the stored components (1 up to rounding), which morsec's metal
+  // side divides by for every pair (MorseCosine.f90:127)
+  norm[ai] = make_double4_32a(nx, ny, nz, 1.0 / (nx * nx + ny * ny + nz * nz));
 }
 
 __global__ void k_nnum_max(ListDev L, Ctl* ctl) {

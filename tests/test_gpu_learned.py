@@ -159,17 +159,22 @@ def test_fallback_to_classical_kernels(tmp_path, built):
     s.advance(11)
     st = s.learned_status()
     assert st["fallen_back"] and not st["active"] and st["checks"] == 1
-    # after the fallback the run uses the classical kernels: same forces as a run
-    # that never loaded a network, from the same state
+    # after the fallback the run uses the classical kernels: the same forces as a
+    # run that never loaded a network, from the same state
     p, v, f = s.state()
     c = pf.Simulation(d, form="precision", out_period=10 ** 9)
     c.set_state(p, v)
     c.compute()
     s.compute()
     fs, fc = s.state()[2], c.state()[2]
-    # the same kernels; only the threads per row (tuned after a context's first
-    # steps) and so the FP32 summation order may differ
-    assert np.abs(fs - fc).max() < 1e-6 * np.abs(fc).max()
+    # the same kernels, but not the same FP32 summation order: the learned
+    # context rebuilds the tb list at every update step in cell order, the other
+    # filters it from its outer list (another order), and the threads per row are
+    # tuned per context.  tb's force sums cancel strongly, so the two agree to
+    # the precision form's own error scale (force RMSE against FP64 about 1e-5
+    # relative), three orders of magnitude below the network's error: forces of
+    # the network would fail this check.
+    assert np.abs(fs - fc).max() < 1e-5 * np.abs(fc).max()
     s.close()
     c.close()
 
