@@ -1581,7 +1581,10 @@ void Engine::enqueue_step(const StepPlan& p) {
     if (p.drifted) {
       // (done)
     } else if (fuse_kick_drift) {
-      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st, fused_begin, p.nhc_done);
+      // the fused pair kernel may start early: it reads its static tables while
+      // this one runs (a kernel between them is an ordinary launch and waits)
+      launch_kick_drift(gx, ts[0], ts[1], true, scale_chain, !prec, A, box, ctl, st, fused_begin, p.nhc_done,
+                        pair_fused && !learned_active);
       if (gz.cap > 0) {
         launch_kick(gz, false, ts[1], !prec, A, ctl, st);
         launch_drift(gz, false, ts[0], true, A, box, ctl, st);

@@ -185,18 +185,34 @@ template <bool PREC, bool ENERGY, int TPA>
 __global__ void __launch_bounds__(256, PREC ? 3 : 2) k_pair_atoms(PairSet S, Atoms A, Box B, Ctl* ctl, Epi E, int chain,
                                                     double ts2, double ts3, double ts4, int ahead) {
   using T = RT<PREC>;
-  asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
-  if (block_stop(ctl)) return;
   constexpr int RPW = 32 / TPA, APB = 8 * RPW;  // atoms per warp, per block pass (256 threads)
   __shared__ double s_f[3][APB];
   __shared__ double s_e[ENERGY ? kMaxPairKeys : 1][APB];
+  __shared__ PairSlot s_slot[kMaxPairSlots];
   const int lane = threadIdx.x & 31, sub = lane / RPW, w = threadIdx.x >> 5;
+  const int slot = w * RPW + lane % RPW;
+  // The slot table and the atoms' task ranges are set up once per system and
+  // written by no kernel of the step: they are read before the wait on the
+  // previous kernel, whose tail they then overlap.
+  {
+    constexpr int W = sizeof(PairSlot) / sizeof(int);
+    static_assert(sizeof(PairSlot) % sizeof(int) == 0, "PairSlot copies as ints");
+    const int* src = reinterpret_cast<const int*>(S.slots);
+    int* dst = reinterpret_cast<int*>(s_slot);
+    for (int k = threadIdx.x; k < S.nslot * W; k += blockDim.x) dst[k] = src[k];
+  }
+  const int a_first = blockIdx.x * APB + slot;
+  const int t0_first = a_first < S.natoms ? S.task_off[a_first] : 0;
+  const int t1_first = a_first < S.natoms ? S.task_off[a_first + 1] : 0;
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent
+  if (block_stop(ctl)) return;  // (its barrier also publishes s_slot)
   double red[kMaxPairKeys + 1] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int bbase = blockIdx.x * APB; bbase < S.natoms; bbase += gridDim.x * APB) {  // uniform over the block
-    const int slot = w * RPW + lane % RPW;
     const int a = bbase + slot;
     const bool valid = a < S.natoms;
-    const int t0 = valid ? S.task_off[a] : 0, nt = valid ? S.task_off[a + 1] - t0 : 0;
+    const bool first = bbase == blockIdx.x * APB;
+    const int t0 = first ? t0_first : (valid ? S.task_off[a] : 0);
+    const int nt = first ? t1_first - t0_first : (valid ? S.task_off[a + 1] - t0 : 0);
     int ntw = nt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ntw = max(ntw, __shfl_xor_sync(0xffffffffu, ntw, o));
@@ -207,7 +223,7 @@ __global__ void __launch_bounds__(256, PREC ? 3 : 2) k_pair_atoms(PairSet S, Ato
       if (t >= nt) continue;
       const int2 tk = S.task[t0 + t];
       // the slot's list and constants into registers once per row
-      const PairSlot& sl = S.slots[tk.x];
+      const PairSlot& sl = s_slot[tk.x];
       const RowList L = sl.L;
       const auto c = cst<PREC>(sl.P);
       const int kind = sl.kind, general = sl.general, ekey = sl.ekey;

@@ -149,8 +149,11 @@ __global__ void k_drift(GroupRef g, int xyz, double ts1, int write_posq, Atoms A
 // those loads overlap instead of forming a chain of dependent round trips.
 template <bool EXACT>
 __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq, int nhc_scale, int begin,
-                             int nhc_pre, Atoms A, Box B, Ctl* ctl) {
+                             int nhc_pre, int early, Atoms A, Box B, Ctl* ctl) {
   asm volatile("griddepcontrol.wait;" ::: "memory");  // see launch_dependent (forces.cuh)
+  // early: the next kernel (the fused pair kernel) may start now; it reads its
+  // static tables, then waits for this grid to complete
+  if (early) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const int ind = blockIdx.x * blockDim.x + threadIdx.x;
   const bool have = ind < g.cap;
   const int i = have ? g.idx[ind] : 0;
@@ -542,14 +545,14 @@ void launch_drift(const GroupRef& g, bool xyz, double ts1, bool write_posq, cons
   if (g.cap > 0) { k_drift<<<nb(g.cap, 256), 256, 0, s>>>(g, xyz ? 1 : 0, ts1, write_posq ? 1 : 0, A, B, ctl); ++g_kernel_launches; }
 }
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
-                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin, bool nhc_pre) {
+                       const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin, bool nhc_pre, bool early) {
   if (g.cap <= 0) return;
   if (exact)
     launch_dependent(k_kick_drift<true>, nb(g.cap, 256), 256, s, g, ts1, ts2, write_posq ? 1 : 0, nhc_scale,
-                     begin ? 1 : 0, nhc_pre ? 1 : 0, A, B, ctl);
+                     begin ? 1 : 0, nhc_pre ? 1 : 0, early ? 1 : 0, A, B, ctl);
   else
     launch_dependent(k_kick_drift<false>, nb(g.cap, 256), 256, s, g, ts1, ts2, write_posq ? 1 : 0, nhc_scale,
-                     begin ? 1 : 0, nhc_pre ? 1 : 0, A, B, ctl);
+                     begin ? 1 : 0, nhc_pre ? 1 : 0, early ? 1 : 0, A, B, ctl);
   ++g_kernel_launches;
 }
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,

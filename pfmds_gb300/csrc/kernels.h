@@ -297,7 +297,7 @@ void launch_step_begin_fused(Ctl* ctl, cudaStream_t s);
 // by Ctl::nhc_sa, then s); begin opens the step (counter, previous energy).
 void launch_kick_drift(const GroupRef& g, double ts1, double ts2, bool write_posq, int nhc_scale, bool exact,
                        const Atoms& A, const Box& B, Ctl* ctl, cudaStream_t s, bool begin = false,
-                       bool nhc_pre = false);
+                       bool nhc_pre = false, bool early = false);
 void launch_nhc(int chain, const GroupRef& g, double ts2, double ts3, double ts4, const Atoms& A, Ctl* ctl,
                 cudaStream_t s, int prescale = 0, int ahead = 0);
 // the xyz-moving group's second half-kick with the half-update of the chain over
