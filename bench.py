@@ -385,7 +385,8 @@ def gr_cu_list_config(root, device, n_entries=16, steps=2000, streams=16):
             f.write(f"{n} p{k + 1}_\n")
     out = {}
     for s in (1, streams):
-        o = os.path.join(d, f"out{s}") + "/"
+        # output folders of one name length: all_out pads each entry's prefix
+        o = os.path.join(d, "out_one" if s == 1 else "out_all") + "/"
         os.makedirs(o, exist_ok=True)
         args = ["-ipath", d + "/", "-ilist", "list.txt", "-opath", o, "-ofile", "all_out.txt", "-batch",
                 "-form", "precision", "-device", str(device), "-streams", str(s)]
@@ -407,7 +408,7 @@ def gr_cu_list_config(root, device, n_entries=16, steps=2000, streams=16):
         for fn in sorted(os.listdir(o)):
             if fn == "all_out.txt" or fn.endswith("md_run.log"):
                 with open(os.path.join(o, fn)) as f:
-                    files[fn] = f.read().replace(o, "")  # all_out's records name the output prefix
+                    files[fn] = f.read().replace(o, "<out>/")  # all_out's records name the output prefix
         out[s] = (wall, files)
     w1, f1 = out[1]
     wn, fn_ = out[streams]
