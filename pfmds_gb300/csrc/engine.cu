@@ -435,6 +435,16 @@ class Engine {
   bool nhc_pending = false;  // chain 0's last scaling still to be applied (by the next k_nhc)
   bool nhc_ahead = false;    // the pair launch being enqueued also runs the next first half-update
   void plan_pair_fusion();
+  // Forces on two streams: with one ljc / morsec coupling whose two sides' rows
+  // are disjoint atom sets, and every other interaction's rows inside one side
+  // (tb on the sheet, rjl in the slab), the kernels that write one side's atoms
+  // run on st and the others on st2 (non-energy steps: the energy variants share
+  // the grid-reduction scratch).  Every force kernel writes only its own rows.
+  void plan_force_split();
+  bool force_split = false;
+  std::vector<int> force_side;  // per interaction: 1 (st), 2 (st2), 3 (the coupling: both)
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   PairSet pair_set() const;
   bool need_check_all = true;
 
@@ -523,6 +533,9 @@ Engine::~Engine() {
   writer.reset();  // its queued jobs read this engine's groups and types
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (st2) cudaStreamDestroy(st2);
   for (auto& kv : graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   if (log) std::fclose(log);
@@ -959,6 +972,7 @@ void Engine::create(const std::string& ip, const std::string& sf, const pfmd_opt
   }
   plan_fusion();
   plan_pair_fusion();
+  plan_force_split();
   // the next step's kick and drift in the force kernel: precision form, one rjl
   // interaction whose rows are every atom and which kicks last, an xyz-moving group
   // and no z-moving one, no group changes or z-velocity inversion
@@ -1445,6 +1459,52 @@ void Engine::plan_pair_fusion() {
   CK(cudaStreamSynchronize(st));
 }
 
+void Engine::plan_force_split() {
+  force_split = false;
+  if (pair_fused || N == 0 || inters.size() < 2) return;
+  int cos = -1;
+  for (size_t k = 0; k < inters.size(); ++k) {
+    const int kind = inters[k].spec.kind;
+    if (kind == pfmd_io::K_LJC || kind == pfmd_io::K_MORSEC) {
+      if (cos >= 0) return;
+      cos = static_cast<int>(k);
+    } else if (kind != pfmd_io::K_RJL && kind != pfmd_io::K_TB && kind != pfmd_io::K_LJ1G) {
+      return;  // kernels not known to write only their own rows
+    }
+  }
+  if (cos < 0) return;
+  std::vector<char> side(static_cast<size_t>(N), 0);
+  auto mark = [&](int g, char s) {
+    for (int a : groups[static_cast<size_t>(g)].idx) {
+      if (side[static_cast<size_t>(a)] && side[static_cast<size_t>(a)] != s) return false;
+      side[static_cast<size_t>(a)] = s;
+    }
+    return true;
+  };
+  const InterH& C = inters[static_cast<size_t>(cos)];
+  if (!mark(lists[static_cast<size_t>(C.lists[0])].d.row_group, 1) ||
+      !mark(lists[static_cast<size_t>(C.lists[1])].d.row_group, 2))
+    return;
+  std::vector<int> fs(inters.size(), 0);
+  fs[static_cast<size_t>(cos)] = 3;
+  for (size_t k = 0; k < inters.size(); ++k) {
+    if (static_cast<int>(k) == cos) continue;
+    char s = 0;
+    for (int a : groups[static_cast<size_t>(lists[static_cast<size_t>(inters[k].lists[0])].d.row_group)].idx) {
+      const char t = side[static_cast<size_t>(a)];
+      if (t == 0 || (s != 0 && t != s)) return;
+      s = t;
+    }
+    if (s == 0) return;
+    fs[k] = s;
+  }
+  if (!st2) CK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+  if (!ev_fork) CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  if (!ev_join) CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  force_side = fs;
+  force_split = true;
+}
+
 PairSet Engine::pair_set() const {
   PairSet P{};
   P.natoms = N;
@@ -1486,12 +1546,18 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
     e.begin = (first && begin) ? 1 : 0;
     return e;
   };
+  const bool split = force_split && !energy && !learned_active;
+  if (split) {
+    CK(cudaEventRecord(ev_fork, st));
+    CK(cudaStreamWaitEvent(st2, ev_fork, 0));
+  }
   for (int k = 0; k < nint; ++k) {
     InterH& I = inters[static_cast<size_t>(k)];
     const int key = k;
     const int eslot = 4 + (k % 16);
     const bool first = k == 0, last = k == nint - 1;
     const ListDev& L1 = lists[static_cast<size_t>(I.lists[0])].d;
+    cudaStream_t sk = (split && force_side[static_cast<size_t>(k)] == 2) ? st2 : st;
     if (learned_active && k < static_cast<int>(lrn.size()) && lrn[static_cast<size_t>(k)].on) {
       Lrn& M = lrn[static_cast<size_t>(k)];
       learned::launch_desc(L1, M.d.p, A, box, M.G.p, ctl, st);
@@ -1510,24 +1576,36 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
                   epi(false, last));
         break;
       case pfmd_io::K_LJ1G:
-        launch_lj1g(prec, energy, I.general, L1, I.lj, A, box, ctl, eslot, key, st, epi(first, last));
+        launch_lj1g(prec, energy, I.general, L1, I.lj, A, box, ctl, eslot, key, sk, epi(first, last));
         break;
       case pfmd_io::K_RJL:
-        launch_rjl(prec, energy, L1, I.rjl, A, box, I.scratch.p, I.pair.p, ctl, eslot, key, st, 3,
+        launch_rjl(prec, energy, L1, I.rjl, A, box, I.scratch.p, I.pair.p, ctl, eslot, key, sk, 3,
                    epi(first, last));
         break;
       case pfmd_io::K_TB:
-        launch_tb(prec, energy, L1, I.tb, A, box, I.scratch.p, ctl, eslot, key, st, 3, epi(first, last));
+        launch_tb(prec, energy, L1, I.tb, A, box, I.scratch.p, ctl, eslot, key, sk, 3, epi(first, last));
         break;
       case pfmd_io::K_REBOSC:
         launch_rebo(energy, L1, I.rebo, A, box, I.scratch.p, ctl, eslot, key, st, 3, epi(first, last));
         break;
       case pfmd_io::K_LJC:
-      case pfmd_io::K_MORSEC:
-        launch_cos(prec, energy, I.spec.kind == pfmd_io::K_MORSEC, L1, lists[static_cast<size_t>(I.lists[1])].d,
-                   lists[static_cast<size_t>(I.lists[2])].d, I.cp, I.norm.p, I.gsum.p, A, box, ctl, eslot, key, st);
+      case pfmd_io::K_MORSEC: {
+        const bool morse = I.spec.kind == pfmd_io::K_MORSEC;
+        const ListDev& L2 = lists[static_cast<size_t>(I.lists[1])].d;
+        const ListDev& L3 = lists[static_cast<size_t>(I.lists[2])].d;
+        if (split) {  // the sheet's side on st, the metal's on st2
+          launch_cos(prec, energy, morse, L1, L2, L3, I.cp, I.norm.p, I.gsum.p, A, box, ctl, eslot, key, st, 1);
+          launch_cos(prec, energy, morse, L1, L2, L3, I.cp, I.norm.p, I.gsum.p, A, box, ctl, eslot, key, st2, 2);
+        } else {
+          launch_cos(prec, energy, morse, L1, L2, L3, I.cp, I.norm.p, I.gsum.p, A, box, ctl, eslot, key, st);
+        }
         break;
+      }
     }
+  }
+  if (split) {
+    CK(cudaEventRecord(ev_join, st2));
+    CK(cudaStreamWaitEvent(st, ev_join, 0));
   }
 }
 
