@@ -83,9 +83,10 @@ def load(path=LIB_PATH):
     L.pfmd_gr_on_cu_analysis.argtypes = [C.c_char_p, C.c_double, dp, dp]
     L.pfmd_natoms.argtypes = [vp, ip]
     L.pfmd_md_step.argtypes = [vp, llp, dp]
-    L.pfmd_get_state.argtypes = [vp, dp, dp, dp]
-    L.pfmd_set_state.argtypes = [vp, dp, dp]
-    L.pfmd_energies.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+    # the array arguments of the per-step calls as plain pointers (see _addr)
+    L.pfmd_get_state.argtypes = [vp, vp, vp, vp]
+    L.pfmd_set_state.argtypes = [vp, vp, vp]
+    L.pfmd_energies.argtypes = [vp, vp, dp, dp, dp, dp, dp]
     L.pfmd_compute.argtypes = [vp, C.c_int, dp]
     L.pfmd_ninteractions.argtypes = [vp, ip]
     L.pfmd_nlist_shape.argtypes = [vp, C.c_int, C.c_int, ip, ip]
@@ -162,6 +163,16 @@ def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
+def _addr(a):
+    """A C-contiguous array's data as a void* argument.  Through the buffer
+    protocol when the array is writable (a fraction of the cost of data_as,
+    which matters on the per-step calls), else by its address."""
+    try:
+        return C.byref(C.c_char.from_buffer(a))
+    except (TypeError, ValueError):
+        return C.c_void_p(a.__array_interface__["data"][0])
+
+
 def default_options(**kw):
     o = Options()
     load().pfmd_default_options(C.byref(o))
@@ -210,9 +221,11 @@ class Simulation:
             raise PfmdError(rc, load().pfmd_errmsg(self._h).decode())
 
     def advance(self, n):
-        f = C.c_int(0)
-        self._check(load().pfmd_advance(self._h, int(n), C.byref(f)))
-        self.finished = bool(f.value)
+        if getattr(self, "_fin", None) is None:
+            self._fin = C.c_int(0)
+            self._finref = C.byref(self._fin)
+        self._check(load().pfmd_advance(self._h, int(n), self._finref))
+        self.finished = bool(self._fin.value)
         return self.finished
 
     def finish(self):
@@ -220,9 +233,12 @@ class Simulation:
 
     @property
     def natoms(self):
-        n = C.c_int()
-        self._check(load().pfmd_natoms(self._h, C.byref(n)))
-        return n.value
+        n = getattr(self, "_natoms", None)
+        if n is None:  # fixed for the context's life
+            c = C.c_int()
+            self._check(load().pfmd_natoms(self._h, C.byref(c)))
+            n = self._natoms = c.value
+        return n
 
     @property
     def md_step(self):
@@ -244,26 +260,36 @@ class Simulation:
         for a in (p, v, f):
             if a.shape != (n, 3) or a.dtype != np.float64 or not a.flags.c_contiguous:
                 raise ValueError("state(): out arrays must be C-contiguous float64 of shape (natoms, 3)")
-        self._check(load().pfmd_get_state(self._h, _dp(p), _dp(v), _dp(f)))
+        self._check(load().pfmd_get_state(self._h, _addr(p), _addr(v), _addr(f)))
         return p, v, f
 
     def set_state(self, pos=None, vel=None):
+        n = self.natoms
         p = None if pos is None else np.ascontiguousarray(pos, dtype=np.float64)
         v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
-        self._check(load().pfmd_set_state(self._h, None if p is None else _dp(p), None if v is None else _dp(v)))
+        for a in (p, v):
+            if a is not None and a.size != 3 * n:
+                raise ValueError("set_state(): arrays must hold natoms x 3 values")
+        self._check(load().pfmd_set_state(self._h, None if p is None else _addr(p), None if v is None else _addr(v)))
 
     @property
     def n_interactions(self):
-        n = C.c_int()
-        self._check(load().pfmd_ninteractions(self._h, C.byref(n)))
-        return n.value
+        k = getattr(self, "_nint", None)
+        if k is None:  # fixed for the context's life
+            c = C.c_int()
+            self._check(load().pfmd_ninteractions(self._h, C.byref(c)))
+            k = self._nint = c.value
+        return k
 
     def energies(self):
-        e = np.zeros(max(1, self.n_interactions))
-        vals = [C.c_double() for _ in range(5)]
-        self._check(load().pfmd_energies(self._h, _dp(e), *[C.byref(v) for v in vals]))
-        pe, ke, t, enhc, econs = (v.value for v in vals)
-        return dict(inter=e[:self.n_interactions].copy(), pe=pe, ke=ke, temperature=t, nhc=enhc, conserved=econs)
+        ni = self.n_interactions
+        e = np.zeros(max(1, ni))
+        if getattr(self, "_evals", None) is None:
+            self._evals = [C.c_double() for _ in range(5)]
+            self._erefs = [C.byref(v) for v in self._evals]
+        self._check(load().pfmd_energies(self._h, _addr(e), *self._erefs))
+        pe, ke, t, enhc, econs = (v.value for v in self._evals)
+        return dict(inter=e[:ni].copy(), pe=pe, ke=ke, temperature=t, nhc=enhc, conserved=econs)
 
     def compute(self, rebuild=True):
         e = np.zeros(max(1, self.n_interactions))
