@@ -2810,7 +2810,6 @@ int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
     const size_t n3 = 3 * static_cast<size_t>(N);
     // read in place when page-locked, else copied as given; converted on the device
     const double* in[3] = {nullptr, nullptr, nullptr};
-    double4_32a* to[3] = {e.pos.p, e.vel.p, nullptr};
     const double* h[2] = {pos, vel};
     for (int k = 0; k < 2 && N; ++k) {
       if (!h[k]) continue;
@@ -2821,11 +2820,8 @@ int pfmd_set_state(pfmd_ctx* c, const double* pos, const double* vel) {
         in[k] = e.stage.p + k * n3;
       }
     }
-    pfmd::launch_xyz_to_d4(N, in, to, e.st);
-    if (pos && N) {
-      pfmd::launch_pack_posq(e.A, e.box, e.ctl, e.st);
-      e.need_check_all = true;  // also rebuilds the lists (skin-triggered ones if needed) at the next step
-    }
+    pfmd::launch_state_in(N, in[0], in[1], e.A, e.box, e.st);
+    if (pos && N) e.need_check_all = true;  // also rebuilds the lists (skin-triggered ones if needed) at the next step
     CK(cudaStreamSynchronize(e.st));
   });
 }

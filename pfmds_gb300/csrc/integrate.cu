@@ -220,31 +220,15 @@ __global__ void k_kick_drift(GroupRef g, double ts1, double ts2, int write_posq,
   if (out_of_cell(p.x, B.Ltol[0]) || out_of_cell(p.y, B.Ltol[1]) || out_of_cell(p.z, B.Ltol[2])) flag_oob(ctl, i);
 }
 
-// xyz-interleaved arrays <-> double4 records, up to three arrays per launch
+// double4 records -> xyz-interleaved arrays, up to three arrays per launch
 // (blockIdx.y picks one; null ones are skipped).  One thread per double of the
-// interleaved array, so a warp reads or writes 256 contiguous bytes of it: the
+// interleaved array, so a warp writes 256 contiguous bytes of it: the
 // interleaved side may be page-locked host memory reached over NVLink-C2C, where
 // whole-line accesses matter; the double4 side is device memory.
-struct XyzArrays {
-  const double* xyz[3];
-  double4_32a* d4[3];
-};
 struct D4Arrays {
   const double4_32a* d4[3];
   double* xyz[3];
 };
-__global__ void k_xyz_to_d4(long long n3, XyzArrays a) {
-  const int k = blockIdx.y;
-  const double* __restrict__ xyz = a.xyz[k];
-  if (!xyz) return;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n3) return;
-  const long long i = t / 3;
-  const int c = (int)(t - 3 * i);
-  double* r = reinterpret_cast<double*>(a.d4[k] + i);
-  r[c] = xyz[t];
-  if (c == 0) r[3] = 0.0;
-}
 __global__ void k_d4_to_xyz(long long n3, D4Arrays a) {
   const int k = blockIdx.y;
   double* xyz = a.xyz[k];
@@ -255,15 +239,33 @@ __global__ void k_d4_to_xyz(long long n3, D4Arrays a) {
   const int c = (int)(t - 3 * i);
   xyz[t] = reinterpret_cast<const double*>(a.d4[k] + i)[c];
 }
-void launch_xyz_to_d4(int n, const double* const xyz[3], double4_32a* const d4[3], cudaStream_t s) {
-  if (n <= 0) return;
-  XyzArrays a;
-  for (int k = 0; k < 3; ++k) {
-    a.xyz[k] = xyz[k];
-    a.d4[k] = d4[k];
+// pfmd_set_state's conversion in one launch: positions (blockIdx.y 0) and
+// velocities (1) from xyz-interleaved doubles, which may be page-locked host
+// memory read over the C2C link, into the device records; positions also into
+// the fixed-point records.  A block reads its 256 atoms' 768 doubles as three
+// coalesced sweeps into shared memory, then each thread writes its atom.
+__global__ void __launch_bounds__(256) k_state_in(int n, const double* __restrict__ pos,
+                                                  const double* __restrict__ vel, Atoms A, Box B) {
+  __shared__ double s[3 * 256];
+  const double* src = blockIdx.y == 0 ? pos : vel;
+  if (!src) return;
+  const long long base = (long long)blockIdx.x * 256;
+  const long long m = min(3LL * n - 3 * base, 3LL * 256);
+  for (int k = threadIdx.x; k < m; k += 256) s[k] = src[3 * base + k];
+  __syncthreads();
+  const long long i = base + threadIdx.x;
+  if (i >= n) return;
+  const double x = s[3 * threadIdx.x], y = s[3 * threadIdx.x + 1], z = s[3 * threadIdx.x + 2];
+  if (blockIdx.y == 0) {
+    A.pos[i] = make_double4_32a(x, y, z, 0.0);
+    A.posq[i] = make_int4(quantize(x, B.qinv[0]), quantize(y, B.qinv[1]), quantize(z, B.qinv[2]), 0);
+  } else {
+    A.vel[i] = make_double4_32a(x, y, z, 0.0);
   }
-  const long long n3 = 3LL * n;
-  k_xyz_to_d4<<<dim3((unsigned)((n3 + 255) / 256), 3), 256, 0, s>>>(n3, a);
+}
+void launch_state_in(int n, const double* pos, const double* vel, const Atoms& A, const Box& B, cudaStream_t s) {
+  if (n <= 0 || (!pos && !vel)) return;
+  k_state_in<<<dim3((unsigned)((n + 255) / 256), 2), 256, 0, s>>>(n, pos, vel, A, B);
   ++g_kernel_launches;
 }
 void launch_d4_to_xyz(int n, const double4_32a* const d4[3], double* const xyz[3], cudaStream_t s) {

@@ -276,7 +276,9 @@ void launch_cos(bool prec, bool energy, bool morse, const ListDev& nl1, const Li
 // to / from the device's 32-byte atom records, on the device.
 // xyz-interleaved <-> double4 records, up to three arrays in one launch (null
 // entries skipped)
-void launch_xyz_to_d4(int n, const double* const xyz[3], double4_32a* const d4[3], cudaStream_t s);
+// positions and velocities (either may be null) from xyz-interleaved doubles into
+// the records, positions also into the fixed-point records
+void launch_state_in(int n, const double* pos, const double* vel, const Atoms& A, const Box& B, cudaStream_t s);
 void launch_d4_to_xyz(int n, const double4_32a* const d4[3], double* const xyz[3], cudaStream_t s);
 
 // ---------------- integration and reductions (integrate.cu) ----------------
