@@ -99,3 +99,19 @@ def test_wrong_nhc_parameters_message(tmp_path, built):
 def test_strerror_names(built):
     assert pf.strerror(pf.PFMD_E_NLIST_OVERFLOW) == "PFMD_E_NLIST_OVERFLOW"
     assert pf.strerror(pf.PFMD_E_GR_NN) == "PFMD_E_GR_NN"
+
+
+def test_array_pointer_arguments():
+    """The per-step calls pass arrays as void* through the buffer protocol, and
+    by address when the array is read-only: both name the array's first double."""
+    import numpy as np
+    libc = C.CDLL(None)
+    libc.memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    libc.memcpy.restype = C.c_void_p
+    src = np.arange(6.0)
+    ro = src.copy()
+    ro.flags.writeable = False
+    for a in (src, ro):
+        dst = np.zeros(6)
+        libc.memcpy(pf._addr(dst), pf._addr(a), 48)
+        assert np.array_equal(dst, a)
