@@ -811,9 +811,9 @@ def run_ours(args):
 
 def run_case(name):
     """One small run of a single kernel family's workload (for ncu captures of
-    that family): the bench slab, the binary LJ gas, the graphene/Cu moire, a
-    64-replica batch or a learned-form force evaluation, in the plain or
-    precision form."""
+    that family): the bench slab, the binary LJ gas, the graphene/Cu moire, the
+    slab's state transfers, a 64-replica batch or a learned-form force
+    evaluation, in the plain or precision form."""
     import pfmds_gb300 as pf
     from pfmds_gb300 import configs
     d = tempfile.mkdtemp()
@@ -828,6 +828,17 @@ def run_case(name):
         configs.gr_on_cu(d, rotation=(49, 3, 2), layers=6, fixed_layers=1, temperature=500.0, integrator="nvt",
                          dt=0.5, steps=10 ** 8, log_period=10, coupling="morsec")
         pf.Simulation(d, form=form, out_period=10 ** 9).advance(13)
+    elif name == "state":
+        # the end-to-end leg's transfers: set_state from and state() into
+        # page-locked arrays, 10 of each after one step
+        make_workload(d)
+        s = pf.Simulation(d, form="precision", out_period=10 ** 9)
+        s.advance(1)
+        bufs, _ = pinned_arrays(s.natoms, 5)
+        s.state(out=(bufs[0], bufs[1], bufs[2]))
+        for _ in range(10):
+            s.set_state(bufs[0], bufs[1])
+            s.state(out=(bufs[2], bufs[3], bufs[4]))
     elif name == "batch":
         ln, _ = configs.batch_systems(d, n_rep=64, n_min=500, n_max=20000, steps=1000, log_period=100, seed=5)
         b = pf.Batch(d, ln)
@@ -899,7 +910,7 @@ def main():
     ap.add_argument("--learned-frames", type=int, default=500, help="training frames per temperature")
     ap.add_argument("--case", default=None,
                     help="run one small workload for a kernel family and exit (ncu captures): slab_plain, "
-                         "slab_prec, gas_plain, gas_prec, moire_plain, moire_prec, batch, learned")
+                         "slab_prec, gas_plain, gas_prec, moire_plain, moire_prec, state, batch, learned")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
