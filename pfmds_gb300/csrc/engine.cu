@@ -1546,7 +1546,7 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
     e.begin = (first && begin) ? 1 : 0;
     return e;
   };
-  const bool split = force_split && !energy && !learned_active;
+  const bool split = force_split && !energy;
   if (split) {
     CK(cudaEventRecord(ev_fork, st));
     CK(cudaStreamWaitEvent(st2, ev_fork, 0));
@@ -1560,12 +1560,13 @@ void Engine::enqueue_forces(bool energy, bool kick, bool drift_next, bool begin)
     cudaStream_t sk = (split && force_side[static_cast<size_t>(k)] == 2) ? st2 : st;
     if (learned_active && k < static_cast<int>(lrn.size()) && lrn[static_cast<size_t>(k)].on) {
       Lrn& M = lrn[static_cast<size_t>(k)];
-      learned::launch_desc(L1, M.d.p, A, box, M.G.p, ctl, st);
+      // (each model's kernels write its own buffers and its rows' forces only)
+      learned::launch_desc(L1, M.d.p, A, box, M.G.p, ctl, sk);
       if (M.tc)
-        learned::launch_mlp_tc(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
+        learned::launch_mlp_tc(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, sk);
       else
-        learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, st);
-      learned::launch_force(L1, M.d.p, M.g.p, M.e.p, M.leg.p, M.cforce.p, energy, A, box, ctl, eslot, key, st,
+        learned::launch_mlp(L1.rows, M.G.p, M.d.p, M.net.p, M.e.p, M.g.p, ctl, sk);
+      learned::launch_force(L1, M.d.p, M.g.p, M.e.p, M.leg.p, M.cforce.p, energy, A, box, ctl, eslot, key, sk,
                             epi(first, last), learned::core_radius(M.model.kind));
       continue;
     }
